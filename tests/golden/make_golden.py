@@ -1,0 +1,54 @@
+"""Regenerates the golden fixtures in this folder from the VOTCA-XTP test data.
+
+Run in a checkout that has the reference tree at REF (default /root/reference):
+    python tests/golden/make_golden.py [REF]
+
+Writes bse_operator_hqp.npz:
+  Hqp      17x17  xtp/src/tests/DataFiles/bse_operator/Hqp.mm   (operator input)
+  hqp_ref  20x20  xtp/src/tests/DataFiles/bse_operator/hqp_ref.mm
+           (HqpOperator * Identity for homo=4, vmin=0, cmax=8, qpmin=rpamin=0;
+            xtp/src/tests/test_bse_operator.cc:74-93, compared at isApprox 1e-3)
+  epsilon_inv 17  the screening vector hard-coded at test_bse_operator.cc:65-72
+Writes davidson_kat.npz: the lowest 10 eigenvalues of init_matrix(N, 0.01)
+(test_davidson.cc:42-56) for N = 100, 400, from a dense symmetric eigensolver,
+the reference value its Davidson tests check against at 1e-6.
+"""
+import os
+import sys
+
+import numpy as np
+
+
+def read_mm_array(path):
+    with open(path) as f:
+        lines = [l.strip() for l in f if l.strip() and not l.startswith("%")]
+    r, c = (int(x) for x in lines[0].split())
+    vals = np.array([float(x) for x in lines[1 : 1 + r * c]])
+    return vals.reshape(c, r).T.copy()  # column-major storage
+
+
+def main():
+    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    here = os.path.dirname(os.path.abspath(__file__))
+    d = os.path.join(ref, "xtp/src/tests/DataFiles/bse_operator")
+    eps_inv = np.array([
+        0.999807798016267, 0.994206065211371, 0.917916768047073, 0.902913813951883,
+        0.902913745974602, 0.902913584797742, 0.853352878674581, 0.853352727016914,
+        0.853352541699637, 0.79703468058566, 0.797034577207669, 0.797034400395582,
+        0.787701833916331, 0.518976361745313, 0.518975064844033, 0.518973712898761,
+        0.459286057710524])
+    np.savez(os.path.join(here, "bse_operator_hqp.npz"),
+             Hqp=read_mm_array(os.path.join(d, "Hqp.mm")),
+             hqp_ref=read_mm_array(os.path.join(d, "hqp_ref.mm")),
+             epsilon_inv=eps_inv)
+    sys.path.insert(0, os.path.join(here, "..", ".."))
+    from oracle.davidson_oracle import init_matrix
+    out = {}
+    for n in (100, 400):
+        out[f"evals_{n}"] = np.linalg.eigvalsh(init_matrix(n, 0.01))[:10]
+    np.savez(os.path.join(here, "davidson_kat.npz"), **out)
+    print("wrote fixtures to", here)
+
+
+if __name__ == "__main__":
+    main()
