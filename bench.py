@@ -1,0 +1,406 @@
+"""Benchmark of the BSE hot path on one GB300 (N GPUs run independent replicas).
+
+Workload: TDA singlet BSE at v=64 occupied, c=512 virtual (dim 32768),
+Naux=2048, Nmo=576, seeded synthetic inputs with the distributions of the
+VOTCA-XTP GW-BSE workload definition (Mmn N(0,1)*0.1/sqrt(Naux)*exp(-|m-n|/40),
+QP energies U[-20,-5] / U[0.5,30] eV, screening w = 1 - 1/lambda, lambda ~ U[1,10]).
+
+One step = one application of the singlet operator (Hqp + 2Hx - Hd) to k=30
+trial vectors (the Davidson block size at 20 roots, size_update = neigen + 10),
+with X and Y resident in HBM.  value = algorithmic matvec TFLOP/s,
+F = k [2 Naux vc (v+c) + 4 Naux vc + 2 vc].  The staged Mmn blocks (>5 GB)
+exceed the 129 MB L2, so no L2 flush is needed between steps.
+
+e2e: the same product through the host-pointer C ABI call (bse_op_matmul):
+X copied host->device and Y device->host inside every timed step.
+
+Also reported once, outside the timed steps: time-to-20-roots of the full
+Davidson solve (tolerance 1e-7) for each precision built.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|mixed]
+  python bench.py --impl reference ...   # the reference CPU path (oracle port)
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+V, C, NAUX, NMO, K, ROOTS = 64, 512, 2048, 576, 30, 20
+WORKLOAD = f"tda_singlet_v{V}_c{C}_naux{NAUX}_k{K}"
+
+
+def algorithmic_flops(v, c, naux, k, singlet=True):
+    vc = v * c
+    return k * (2.0 * naux * vc * (v + c) + (4.0 * naux * vc if singlet else 0.0) + 2.0 * vc)
+
+
+def hd_stage_a_flops(v, c, naux, k):
+    """c-contraction of Hd: S = Mcc X, 2 Naux v c^2 per vector."""
+    return 2.0 * naux * v * c * c * k
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def make_mmn(seed, naux, nmo):
+    """Seeded Mmn, layout (m, P, n) == the reference's slices laid end to end.
+    Each aux slice is a symmetric N(0,1) matrix ((G + G^T)/sqrt(2) off the
+    diagonal, G_mm on it) times 0.1/sqrt(Naux) exp(-|m-n|/40); drawn on the GPU
+    when one is present."""
+    import torch
+
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    g = torch.Generator(device=dev).manual_seed(seed)
+    m = torch.arange(nmo, dtype=torch.float64, device=dev)
+    decay = torch.exp(-(m[:, None] - m[None, :]).abs() / 40.0) * (0.1 / np.sqrt(naux))
+    out = torch.empty((nmo, naux, nmo), dtype=torch.float64)
+    chunk = 128
+    for p0 in range(0, naux, chunk):
+        p1 = min(naux, p0 + chunk)
+        G = torch.randn((p1 - p0, nmo, nmo), generator=g, dtype=torch.float64, device=dev)
+        M = (G + G.transpose(1, 2)) * (1.0 / np.sqrt(2.0))
+        M.diagonal(dim1=1, dim2=2).copy_(G.diagonal(dim1=1, dim2=2))
+        out[:, p0:p1, :] = (M * decay).permute(1, 0, 2).cpu()
+    return out.numpy()
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for i, nm in enumerate(names):
+                if len(r) > 5 + i and r[5 + i].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def cpu_baseline(mmn, w, hqp, seconds_target=20.0, full=False):
+    """The reference's CPU loop nest (oracle port of bse_operator.cc:39-119 with
+    the CPU branches of openmp_cuda.cc) on a bounded sample of one matvec:
+    a sub-range of c1 for the Hd/Hqp row stage and of v1 for the Hx block stage,
+    scaled to the full product by the share of work sampled (the work per c1 is
+    uniform; per v1 it is proportional to the number of v2 >= v1 pairs)."""
+    import oracle
+
+    nthreads = os.cpu_count() or 1
+    oracle.set_threads(nthreads)
+    prob = oracle.BSEProblem(mmn, w, hqp, V, C)
+    X = np.asfortranarray(np.random.default_rng(1).standard_normal((V * C, K)))
+    # Row stage: OpenMP over c1 as in the reference; one wave = one c1 per thread.
+    wave = min(C, nthreads)
+    t0 = time.perf_counter()
+    prob.matmul_ref(X, "singlet", c1_range=(0, wave), v1_range=(0, 0))
+    t_wave = time.perf_counter() - t0
+    waves = int(max(1, min(C // wave, (seconds_target * 0.6) // max(t_wave, 1e-3))))
+    n_c1 = wave * waves
+    if waves > 1:
+        t0 = time.perf_counter()
+        prob.matmul_ref(X, "singlet", c1_range=(0, n_c1), v1_range=(0, 0))
+        t_rows = time.perf_counter() - t0
+    else:
+        t_rows = t_wave
+    # Hx block stage: OpenMP over v1; v1 carries V - v1 pairs (v2 >= v1).
+    n_v1 = min(V, nthreads)
+    t0 = time.perf_counter()
+    prob.matmul_ref(X, "singlet", c1_range=(0, 0), v1_range=(0, n_v1))
+    t_hx = time.perf_counter() - t0
+    pairs_total = V * (V + 1) // 2
+    pairs_s = sum(V - v1 for v1 in range(n_v1))
+    t_full = t_rows * (C / n_c1) + t_hx * (pairs_total / pairs_s)
+    F = algorithmic_flops(V, C, NAUX, K)
+    return {
+        "value": F / t_full / 1e12, "unit": "TFLOP/s", "cores": nthreads, "kind": "port",
+        "sample": (f"reference loop nest (row-built Hd + v-pair Hx) on {n_c1}/{C} c1 rows and "
+                   f"{n_v1} of {V} v1 blocks ({pairs_s:.0f}/{pairs_total} pairs) of one k={K} singlet "
+                   f"matvec, extrapolated: {t_full:.1f} s per matvec"),
+        "seconds_per_matvec": t_full,
+    }
+
+
+def reference_arm(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from votca_gb300.synthetic import qp_energies, screening_w
+
+    mmn = make_mmn(1, NAUX, NMO)
+    w = screening_w(1, NAUX)
+    hqp = np.diag(qp_energies(1, V, C))
+    times = []
+    cb = None
+    for step in range(args.warmup + args.steps):
+        cb = cpu_baseline(mmn, w, hqp, seconds_target=8.0)
+        if step >= args.warmup:
+            times.append(cb["seconds_per_matvec"])
+    t = float(np.median(times)) if times else cb["seconds_per_matvec"]
+    F = algorithmic_flops(V, C, NAUX, K)
+    val = F / t / 1e12
+    line = {
+        "impl": "reference", "metric": "bse_matvec_tflops", "value": val, "unit": "TFLOP/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "v": V, "c": C, "naux": NAUX, "nmo": NMO, "k": K},
+        "cpu_baseline": {"value": val, "unit": "TFLOP/s", "cores": cb["cores"], "kind": cb["kind"],
+                         "sample": cb["sample"]},
+        "e2e": {"value": val, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
+    ap.add_argument("--no-roots", action="store_true", help="skip the time-to-roots solves")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--small", action="store_true", help="C0-sized workload (for profiling captures)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+
+    import torch
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from votca_gb300 import _lib
+    from votca_gb300 import bse_operator as bo
+    from votca_gb300.davidson import DavidsonSolver
+    from votca_gb300.synthetic import qp_energies, screening_w
+
+    global V, C, NAUX, NMO, WORKLOAD
+    if args.small:
+        V, C, NAUX, NMO = 8, 64, 256, 72
+        WORKLOAD = f"tda_singlet_v{V}_c{C}_naux{NAUX}_k{K}"
+    L = _lib.load()
+    seed = 1  # every replica solves the same seeded problem
+    mmn = make_mmn(seed, NAUX, NMO)
+    w = screening_w(seed, NAUX)
+    hqp = np.diag(qp_energies(seed, V, C))
+    Mmn = bo.TCMatrix_gwbse(mmn)
+    opt = bo.BSEOperator_Options(homo=V - 1, rpamin=0, qpmin=0, vmin=0, cmax=V + C - 1)
+    prec_name = args.precision
+    if prec_name == "auto":
+        prec_name = "fp64"
+    precision = bo.PRECISION_MIXED if prec_name == "mixed" else bo.PRECISION_FP64
+    t0 = time.perf_counter()
+    ctx = bo.GpuBSEContext(w, Mmn, hqp, opt, precision=precision)
+    staging_s = time.perf_counter() - t0
+    op = bo.SingletOperator_TDA(ctx)
+    dim = V * C
+
+    rng = np.random.default_rng(2)
+    Xh = torch.from_numpy(np.asfortranarray(rng.standard_normal((dim, K))).T.copy())  # (K, dim) row-major
+    dX = Xh.to("cuda")
+    dY = torch.empty_like(dX)
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def step():
+        op.matmul_device(dX.data_ptr(), dim, K, dY.data_ptr(), dim, stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    # per-stage device time (events on the launch stream) for the roofline figure
+    _lib.check(L.bse_op_profile(ctx.handle, 1))
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ms = e0.elapsed_time(e1) / args.steps
+    clk = clocks.stop()
+    import ctypes
+
+    stage_ms = (ctypes.c_double * 10)()
+    stage_calls = (ctypes.c_int64 * 10)()
+    _lib.check(L.bse_op_profile_read(ctx.handle, stage_ms, stage_calls, 10))
+    _lib.check(L.bse_op_profile(ctx.handle, 0))
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+
+    # e2e through the host-pointer C ABI call with pinned buffers
+    Xp = torch.empty((K, dim), dtype=torch.float64).pin_memory()
+    Xp.copy_(Xh)
+    Yp = torch.empty((K, dim), dtype=torch.float64).pin_memory()
+    Xptr = ctypes.cast(Xp.data_ptr(), _lib.c_dp)
+    Yptr = ctypes.cast(Yp.data_ptr(), _lib.c_dp)
+    for _ in range(1):
+        _lib.check(L.bse_op_matmul(ctx.handle, *op.coef, Xptr, dim, K, Yptr, dim))
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        _lib.check(L.bse_op_matmul(ctx.handle, *op.coef, Xptr, dim, K, Yptr, dim))
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    # consistency of the two paths
+    yd = dY.cpu().numpy()
+    rel = float(np.linalg.norm(Yp.numpy() - yd) / np.linalg.norm(yd))
+
+    F = algorithmic_flops(V, C, NAUX, K)
+    value = world * F / (ms * 1e-3) / 1e12
+    e2e_val = world * F / e2e_s / 1e12
+
+    # roofline of the dominant kernel
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    if precision == bo.PRECISION_FP64:
+        fp64 = ctypes.c_double()
+        _lib.check(L.bse_probe_fp64_tflops(ctypes.byref(fp64)))
+        st = 2  # BSE_STAGE_HD_A
+        per_launch_ms = stage_ms[st] / max(1, stage_calls[st])
+        launches_per_step = stage_calls[st] / max(1, args.steps)
+        achieved = hd_stage_a_flops(V, C, NAUX, K) / launches_per_step / (per_launch_ms * 1e-3) / 1e12
+        roofline = {"bound": "fp64", "kernel": "dgemm_kernel (Hd c-contraction, FP64 CUDA cores)",
+                    "achieved": achieved, "peak": fp64.value, "unit": "TFLOP/s",
+                    "frac": achieved / fp64.value,
+                    "peak_source": "measured in-run: FP64 FMA register loop (bse_probe_fp64_tflops)",
+                    "traffic": None}
+    else:
+        st = 6
+        per_launch_ms = stage_ms[st] / max(1, stage_calls[st])
+        launches_per_step = stage_calls[st] / max(1, args.steps)
+        achieved = 2.0 * NAUX * V * C * (V + C) * K / launches_per_step / (per_launch_ms * 1e-3) / 1e12
+        pk = peaks.get("bf16_tflops")
+        roofline = {"bound": "tensor", "kernel": "tcgen05 BF16x3 Hd", "achieved": achieved,
+                    "peak": pk / 3.0 if pk else None, "unit": "TFLOP/s (FP64-equivalent, 3 BF16 products each)",
+                    "frac": achieved / (pk / 3.0) if pk else None,
+                    "peak_source": "MEASURED_PEAKS.json bf16_tflops / 3 (of measured)", "traffic": None}
+    stages = {name: {"ms_per_step": stage_ms[i] / args.steps, "launches_per_step": stage_calls[i] / args.steps}
+              for i, name in enumerate(["hqp", "hx", "hd_a", "hd_b", "hd2_a", "hd2_b", "tc_hd", "tc_hx",
+                                        "tc_hd2", "tc_split"]) if stage_calls[i]}
+    gpu_launches = None
+    try:
+        gpu_launches = int(sum(stage_calls) / args.steps * args.steps)
+    except Exception:
+        pass
+
+    line = {
+        "metric": "bse_matvec_tflops", "value": value, "unit": "TFLOP/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if precision == bo.PRECISION_FP64 else "bf16x3/f64",
+        "data": "synthetic (seeded; distributions of the VOTCA GW-BSE workload definition)",
+        "config": {"workload": WORKLOAD, "v": V, "c": C, "naux": NAUX, "nmo": NMO, "k": K,
+                   "precision": prec_name, "parallelism": f"replicas{world}",
+                   "l2": "inputs larger than L2 (staged Mmn blocks > 5 GB)"},
+        "e2e": {"value": e2e_val, "unit": "TFLOP/s", "h2d_bytes_per_step": dim * K * 8,
+                "d2h_bytes_per_step": dim * K * 8, "matches_device_path_rel": rel},
+        "roofline": roofline,
+        "stages": stages,
+        "staging_seconds": staging_s,
+        "clocks": clk,
+        "gpu_launches": gpu_launches,
+    }
+    if rank == 0 and not args.no_roots:
+        roots = {}
+        for pname, pr in (("fp64", bo.PRECISION_FP64), ("mixed", bo.PRECISION_MIXED)):
+            try:
+                c2 = ctx if pr == precision else bo.GpuBSEContext(w, Mmn, hqp, opt, precision=pr)
+            except _lib.BSEError as e:
+                roots[pname] = {"unavailable": str(e)}
+                continue
+            ds = DavidsonSolver()
+            ds.set_tolerance(1e-7)
+            ds.set_max_search_space(10 * ROOTS)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            lam, _ = ds.solve(bo.SingletOperator_TDA(c2), ROOTS)
+            dt = time.perf_counter() - t0
+            roots[pname] = {"seconds": dt, "iterations": int(ds.num_iterations()), "info": ds.info(),
+                            "matvec_seconds": ds.result.seconds_matvec,
+                            "matvec_columns": int(ds.result.matvec_columns),
+                            "roots_eV": [round(float(x), 9) for x in lam]}
+            if c2 is not ctx:
+                c2.close()
+        if "lam" in roots.get("fp64", {}) and "roots_eV" in roots.get("mixed", {}):
+            pass
+        if "roots_eV" in roots.get("fp64", {}) and "roots_eV" in roots.get("mixed", {}):
+            d = np.abs(np.array(roots["fp64"]["roots_eV"]) - np.array(roots["mixed"]["roots_eV"])) * 1e3
+            roots["max_abs_diff_meV"] = float(d.max())
+        line["time_to_20_roots"] = roots
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cb = cpu_baseline(mmn, w, hqp)
+        cb.pop("seconds_per_matvec", None)
+        line["cpu_baseline"] = cb
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,206 @@
+/*
+ * votca_gb300_bse.h -- C ABI of the GB300-native BSE hot path.
+ *
+ * A drop-in for VOTCA-XTP's matrix-free BSE Hamiltonian product and the
+ * Davidson eigensolver that drives it.  Every entry point takes plain
+ * pointers and 64-bit sizes, returns an int status (0 = success, see
+ * bse_status) and never throws; bse_last_error() returns a thread-local
+ * message for the last failure on the calling thread.
+ *
+ * Conventions (identical to the reference):
+ *   - matrices are column-major FP64; sizes are int64 (votca::Index);
+ *   - the BSE pair index is I(v, c) = ctotal * v + c, virtual index fastest
+ *     (xtp/include/votca/xtp/vc2index.h:42-44);
+ *   - the operator applies  cqp*Hqp + cx*Hx - cd*Hd - cd2*Hd2
+ *     (BSE_OPERATOR<cqp,cx,cd,cd2>, xtp/include/votca/xtp/bse_operator.h:40-87);
+ *   - Mmn is the reference's TCMatrix_gwbse: msize() slices, slice m a
+ *     column-major [nsize() x auxsize()] matrix (threecenter.h:70-142).
+ *
+ * Threading: a handle may be used from one host thread at a time; every call
+ * is synchronous on return (host-pointer calls) or stream-ordered on the
+ * stream passed in (the *_device calls).
+ */
+#ifndef VOTCA_GB300_BSE_H
+#define VOTCA_GB300_BSE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum bse_status {
+  BSE_OK = 0,
+  BSE_ERR_ARGUMENT = 1,      /* shape / option error (the reference throws std::runtime_error) */
+  BSE_ERR_OUT_OF_MEMORY = 2, /* device allocation failed (CudaMatrix::throw_if_not_enough_memory_in_gpu) */
+  BSE_ERR_CUDA = 3,          /* CUDA runtime error */
+  BSE_ERR_TIMEOUT = 4,       /* a bounded device wait gave up */
+  BSE_ERR_NUMERICAL = 5,     /* small eigenproblem failed, Gram-Schmidt linear dependence, ... */
+  BSE_ERR_UNSUPPORTED = 6    /* option not available in this build */
+} bse_status;
+
+typedef enum bse_precision {
+  BSE_PRECISION_FP64 = 0,  /* every product in FP64 (the plain drop-in) */
+  BSE_PRECISION_MIXED = 1  /* Hx/Hd/Hd2 contractions as BF16x3 split products on
+                              tcgen05 tensor cores with FP32 accumulation;
+                              Hqp and all Davidson algebra in FP64 */
+} bse_precision;
+
+/* BSEOperator_Options, xtp/include/votca/xtp/bse_operator.h:32-38 (absolute MO indices). */
+typedef struct bse_options {
+  int64_t homo;
+  int64_t rpamin;
+  int64_t qpmin;
+  int64_t vmin;
+  int64_t cmax;
+} bse_options;
+
+/* Window of a TCMatrix_gwbse (TCMatrix_gwbse::Initialize, threecenter.cc:29-48). */
+typedef struct bse_mmn_desc {
+  int64_t auxsize; /* Naux */
+  int64_t mmin, mmax;
+  int64_t nmin, nmax;
+} bse_mmn_desc;
+
+typedef struct bse_handle bse_handle;
+
+/*
+ * Create a device-resident BSE operator from host data.  Replaces the
+ * construction of BSE_OPERATOR(epsilon_0_inv, Mmn, Hqp) + configure(opt)
+ * (bse_operator.h:44-48, bse_operator.cc:28-37).  The Mmn blocks the product
+ * needs (vv, vc, cv, cc in the BSE window) are staged into HBM once, here,
+ * instead of per matvec as the reference's CudaPipeline does
+ * (openmp_cuda.cc:299-407).
+ *   mmn_slices: msize pointers; slice m is column-major nsize x auxsize
+ *               (the data() of Mmn_[m]).
+ *   epsilon_0_inv: auxsize screening weights (BSE::epsilon_0_inv_).
+ *   hqp: column-major Hqp, leading dimension ldh >= hqp_size, occupied first;
+ *        its leading (vtotal+ctotal) window is used as by BSE_OPERATOR::Hqp_row.
+ */
+int bse_op_create(const bse_mmn_desc *mmn, const double *const *mmn_slices,
+                  const double *epsilon_0_inv, const double *hqp, int64_t ldh,
+                  int64_t hqp_size, const bse_options *opt, int32_t precision,
+                  bse_handle **out);
+
+/* Same, with a dense screening matrix W (auxsize x auxsize, symmetric) in place
+ * of the diagonal epsilon_0_inv: Hd = sum_PQ M^P W_PQ M^Q.  W is folded into
+ * the vv (and cv) blocks at staging. */
+int bse_op_create_dense_screening(const bse_mmn_desc *mmn,
+                                  const double *const *mmn_slices,
+                                  const double *W, const double *hqp,
+                                  int64_t ldh, int64_t hqp_size,
+                                  const bse_options *opt, int32_t precision,
+                                  bse_handle **out);
+
+/* A dense FP64 symmetric matrix as an operator (the reference tests'
+ * HermitianBlockOperator, test_davidson.cc:265-281).  b may be NULL; when
+ * given, bse_ham_* use [[a, b], [-b, -a]]. */
+int bse_dense_op_create(const double *a, const double *b, int64_t n,
+                        int64_t lda, bse_handle **out);
+
+int bse_op_destroy(bse_handle *h);
+
+/* rows() == cols() of the (TDA) operator: vtotal * ctotal (or n). */
+int bse_op_size(const bse_handle *h, int64_t *size);
+
+/* Y = H(cqp,cx,cd,cd2) * X, host pointers, X and Y column-major dim x k.
+ * Replaces BSE_OPERATOR::matmul (bse_operator.cc:39-119). */
+int bse_op_matmul(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd,
+                  int32_t cd2, const double *X, int64_t ldx, int64_t k,
+                  double *Y, int64_t ldy);
+
+/* Same on device pointers, stream-ordered on `stream` (a cudaStream_t, NULL =
+ * legacy default stream). */
+int bse_op_matmul_device(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd,
+                         int32_t cd2, const double *dX, int64_t ldx, int64_t k,
+                         double *dY, int64_t ldy, void *stream);
+
+/* D = diagonal of H(cqp,cx,cd,cd2), host pointer of length size.
+ * Replaces BSE_OPERATOR::diagonal (bse_operator.cc:133-175). */
+int bse_op_diagonal(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd,
+                    int32_t cd2, double *D);
+int bse_op_diagonal_device(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd,
+                           int32_t cd2, double *dD, void *stream);
+
+/* HamiltonianOperator<A,B> product [[A, B], [-B, -A]] * X, X and Y column-major
+ * (2*size) x k.  Replaces the product hook of bseoperator_btda.h:116-149. */
+int bse_ham_matmul(bse_handle *h, const int32_t a_coef[4],
+                   const int32_t b_coef[4], const double *X, int64_t ldx,
+                   int64_t k, double *Y, int64_t ldy);
+
+/* DavidsonSolver options (davidsonsolver.h:52-57, davidsonsolver.cc:101-170). */
+typedef struct bse_davidson_options {
+  int64_t iter_max;         /* set_iter_max (default 50) */
+  double tolerance;         /* residual-norm tolerance (presets 1e-3/1e-4/1e-5/1e-9) */
+  int64_t max_search_space; /* set_max_search_space (0 -> 5*neigen, as the reference) */
+  int32_t correction;       /* 0 = DPR, 1 = OLSEN */
+  int32_t update;           /* 0 = min, 1 = safe, 2 = max */
+  int32_t matrix_type;      /* 0 = SYMM (Ritz), 1 = HAM (harmonic Ritz) */
+  int32_t verbose;          /* print one line per iteration to stderr */
+} bse_davidson_options;
+
+typedef struct bse_davidson_result {
+  int64_t iterations;      /* num_iterations() */
+  int32_t info;            /* 0 = Success, 1 = NoConvergence (eigenpairs of unconverged roots zeroed) */
+  int32_t reserved;
+  int64_t matvec_columns;  /* operator columns applied during the solve */
+  double seconds_matvec;   /* device time in operator products */
+  double seconds_total;    /* wall time of the solve */
+} bse_davidson_result;
+
+/*
+ * DavidsonSolver::solve on the device (davidsonsolver.h:64-190): all vectors,
+ * projections, Gram-Schmidt, residuals and corrections stay in HBM in FP64.
+ *   SYMM: operator H(a_coef) (TDA singlet/triplet); b_coef ignored.
+ *   HAM:  HamiltonianOperator [[A, B], [-B, -A]] with A = H(a_coef), B = H(b_coef).
+ *   guess: NULL for the reference's unit-vector guess (2*neigen columns), else
+ *          column-major (op size) x guess_cols (the solve(A, neigen, guess) overload).
+ *   evals: neigen values; evecs: column-major (op size) x neigen, ldv >= op size
+ *          (op size = size for SYMM, 2*size for HAM).  Either may be NULL.
+ */
+int bse_davidson_solve(bse_handle *h, const int32_t a_coef[4],
+                       const int32_t b_coef[4],
+                       const bse_davidson_options *opt, int64_t neigen,
+                       const double *guess, int64_t guess_cols, double *evals,
+                       double *evecs, int64_t ldv, bse_davidson_result *result);
+
+/* ---- Diagnostics (no counterpart in the reference) ---- */
+
+/* Stage indices of bse_op_profile_read. */
+enum {
+  BSE_STAGE_HQP = 0,
+  BSE_STAGE_HX = 1,
+  BSE_STAGE_HD_A = 2,
+  BSE_STAGE_HD_B = 3,
+  BSE_STAGE_HD2_A = 4,
+  BSE_STAGE_HD2_B = 5,
+  BSE_STAGE_TC_HD = 6,
+  BSE_STAGE_TC_HX = 7,
+  BSE_STAGE_TC_HD2 = 8,
+  BSE_STAGE_TC_SPLIT = 9,
+  BSE_STAGE_COUNT = 10
+};
+
+/* enable != 0: record CUDA events around every stage of the product on its
+ * launch stream and reset the counters; enable == 0: stop recording. */
+int bse_op_profile(bse_handle *h, int32_t enable);
+/* Accumulated device milliseconds and launches per stage since the last
+ * bse_op_profile(h, 1); synchronises with the recorded events. */
+int bse_op_profile_read(bse_handle *h, double *stage_ms, int64_t *stage_calls,
+                        int32_t nstages);
+
+/* Measured FP64 FMA throughput of the current device (TFLOP/s) from a short
+ * register-resident FMA loop: the roofline denominator of the FP64 path. */
+int bse_probe_fp64_tflops(double *tflops);
+
+/* Thread-local text of the last error on this thread ("" if none). */
+const char *bse_last_error(void);
+
+/* Library version string. */
+const char *bse_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VOTCA_GB300_BSE_H */

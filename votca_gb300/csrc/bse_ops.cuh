@@ -1,0 +1,178 @@
+// Device-resident BSE operator: staged Mmn blocks + the matrix-free product.
+//
+// The reference (xtp/src/libxtp/gwbse/bse_operator.cc:39-119) builds every
+// row of Hd explicitly for each (c1, v1) pair and rebuilds every c x c block of
+// Hx for each v1 <= v2 pair, re-copying Mmn slices to the GPU for every row.
+// Here the blocks are staged into HBM once (at handle creation) in layouts
+// chosen for the contractions, and the product is factorised over the
+// auxiliary index:
+//   Hx  X : Z = Bvc^T X (Naux x k),   Y += cx Bvc Z
+//   Hd  X : S_{jP} = Mcc_P X_j (c x v),   Y_j -= cd sum_{P,v} S_{jP} G_P
+//   Hd2 X : U_{jP} = X_j^T Bvc_P (v x v), Y_j -= cd2 sum_{P,v} Mcv_P U_{jP}
+//   Hqp X : (e_c - e_v) X, or the two small GEMMs with off-diagonal Hqp
+// with the screening (diagonal w or dense W) folded into G and Mcv at staging.
+#pragma once
+
+#include <memory>
+#include <vector>
+
+#include "common.cuh"
+#include "dgemm.cuh"
+
+namespace vgb {
+
+struct Coef {
+  int cqp = 0, cx = 0, cd = 0, cd2 = 0;
+};
+
+// Per-stage device timing with CUDA events on the launch stream (off by default).
+enum Stage {
+  STAGE_HQP = 0,
+  STAGE_HX = 1,
+  STAGE_HD_A = 2,   // FP64 Hd: S = Mcc X (c-contraction)
+  STAGE_HD_B = 3,   // FP64 Hd: Y -= S G (v,P-contraction)
+  STAGE_HD2_A = 4,
+  STAGE_HD2_B = 5,
+  STAGE_TC_HD = 6,  // tensor-core Hd
+  STAGE_TC_HX = 7,
+  STAGE_TC_HD2 = 8,
+  STAGE_TC_SPLIT = 9,
+  STAGE_COUNT = 10
+};
+
+class StageTimer {
+ public:
+  ~StageTimer();
+  void enable(bool on);
+  bool on() const { return on_; }
+  void begin(int stage, cudaStream_t s);
+  void end(int stage, cudaStream_t s);
+  // accumulated milliseconds and call counts since enable(true)
+  void read(double *ms, int64_t *calls, int n);
+
+ private:
+  struct Rec { cudaEvent_t a, b; int stage; };
+  bool on_ = false;
+  std::vector<Rec> pending_;
+  std::vector<cudaEvent_t> pool_;
+  double ms_[STAGE_COUNT] = {0};
+  int64_t calls_[STAGE_COUNT] = {0};
+  cudaEvent_t get_();
+  void drain_();
+};
+
+// Linear operator on device vectors (what the Davidson driver needs).
+struct DeviceOperator {
+  virtual ~DeviceOperator() = default;
+  virtual int64_t size() const = 0;
+  // Y = Op X; X, Y device, column-major, size x k.
+  virtual void apply(const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy,
+                     cudaStream_t s) = 0;
+  virtual void diagonal(double *D, cudaStream_t s) = 0;
+};
+
+class MixedEngine;  // tensor-core contractions (tc_engine.cu)
+
+class BseOperator {
+ public:
+  int64_t vt = 0, ct = 0, naux = 0, dim = 0;
+  int precision = BSE_PRECISION_FP64;
+  bool hqp_diagonal = true;
+
+  // FP64 staged blocks (layouts documented in bse_ops.cu)
+  DeviceBuffer<double> Bvc, Mcc, Gvv, Mcv, dcc, dvv, Hcc, Hvv;
+  // scratch
+  DeviceBuffer<double> S, Z, Xc, Ttmp;
+  GemmWorkspace ws;
+  int64_t s_budget_bytes = 4LL << 30;
+  std::unique_ptr<MixedEngine> mixed;
+  StageTimer timer;
+
+  BseOperator();
+  ~BseOperator();
+
+  // Stage from host data (see bse_op_create).  W: diagonal (naux) when dense_w == false,
+  // else naux x naux column-major.
+  void stage(const bse_mmn_desc &desc, const double *const *slices, const double *w, bool dense_w,
+             const double *hqp, int64_t ldh, int64_t hqp_size, const bse_options &opt,
+             int prec, cudaStream_t s);
+
+  // Y = H(coef) X on device (ldx/ldy >= dim).
+  void matmul(const Coef &c, const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy,
+              cudaStream_t s);
+  void diagonal(const Coef &c, double *D, cudaStream_t s);
+  // [[A, B], [-B, -A]] X, X and Y (2 dim) x k
+  void ham_matmul(const Coef &a, const Coef &b, const double *X, int64_t ldx, int64_t k, double *Y,
+                  int64_t ldy, cudaStream_t s);
+
+  // FP64 stage entry points (also used by the mixed engine for checks)
+  void apply_hqp(double cqp, const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy,
+                 bool accumulate, cudaStream_t s);
+  void apply_hx_fp64(double cx, const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy,
+                     bool accumulate, cudaStream_t s);
+  void apply_hd_fp64(double alpha, const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy,
+                     bool accumulate, cudaStream_t s);
+  void apply_hd2_fp64(double alpha, const double *X, int64_t ldx, int64_t k, double *Y,
+                      int64_t ldy, bool accumulate, cudaStream_t s);
+
+ private:
+  DeviceBuffer<double> hamA_, hamB_, hamX_;
+};
+
+struct BseApply : DeviceOperator {
+  BseOperator *op;
+  Coef coef;
+  BseApply(BseOperator *o, Coef c) : op(o), coef(c) {}
+  int64_t size() const override { return op->dim; }
+  void apply(const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy,
+             cudaStream_t s) override {
+    op->matmul(coef, X, ldx, k, Y, ldy, s);
+  }
+  void diagonal(double *D, cudaStream_t s) override { op->diagonal(coef, D, s); }
+};
+
+struct BseHamApply : DeviceOperator {
+  BseOperator *op;
+  Coef a, b;
+  BseHamApply(BseOperator *o, Coef a_, Coef b_) : op(o), a(a_), b(b_) {}
+  int64_t size() const override { return 2 * op->dim; }
+  void apply(const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy,
+             cudaStream_t s) override {
+    op->ham_matmul(a, b, X, ldx, k, Y, ldy, s);
+  }
+  void diagonal(double *D, cudaStream_t s) override;
+};
+
+// Dense FP64 symmetric operator(s): A, optionally B for [[A, B], [-B, -A]].
+class DenseOperator {
+ public:
+  int64_t n = 0;
+  bool has_b = false;
+  DeviceBuffer<double> A, B, tmpA, tmpB, Xr;
+  GemmWorkspace ws;
+  void stage(const double *a, const double *b, int64_t n_, int64_t lda, cudaStream_t s);
+  void matmul(const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy, cudaStream_t s);
+  void diagonal(double *D, cudaStream_t s);
+  void ham_matmul(const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy, cudaStream_t s);
+};
+
+struct DenseApply : DeviceOperator {
+  DenseOperator *op;
+  bool ham;
+  DenseApply(DenseOperator *o, bool h) : op(o), ham(h) {}
+  int64_t size() const override { return ham ? 2 * op->n : op->n; }
+  void apply(const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy,
+             cudaStream_t s) override {
+    if (ham) op->ham_matmul(X, ldx, k, Y, ldy, s); else op->matmul(X, ldx, k, Y, ldy, s);
+  }
+  void diagonal(double *D, cudaStream_t s) override;
+};
+
+// Combine kernel for the HamiltonianOperator reshaping trick
+// (bseoperator_btda.h:136-148): TA = A [M1_0, M2_0, M1_1, ...], TB likewise.
+void ham_combine(const double *TA, const double *TB, int64_t dim, int64_t k, double *Y,
+                 int64_t ldy, cudaStream_t s);
+// D2 = [D; -D]
+void ham_diag(const double *D, int64_t dim, double *D2, cudaStream_t s);
+
+}  // namespace vgb

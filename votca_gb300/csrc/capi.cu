@@ -1,0 +1,284 @@
+// C ABI of the library (declarations and reference mapping: include/votca_gb300_bse.h).
+#include <cstring>
+#include <memory>
+#include <string>
+
+#include "bse_ops.cuh"
+#include "davidson.cuh"
+
+struct bse_handle {
+  int kind = 0;  // 0: BSE operator, 1: dense operator
+  std::unique_ptr<vgb::BseOperator> bse;
+  std::unique_ptr<vgb::DenseOperator> dense;
+  cudaStream_t stream = nullptr;
+  vgb::DeviceBuffer<double> dX, dY, dD;
+  int64_t size() const { return kind == 0 ? bse->dim : dense->n; }
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+template <typename F>
+int guarded(F &&f) {
+  try {
+    f();
+    g_last_error.clear();
+    return BSE_OK;
+  } catch (const vgb::Error &e) {
+    g_last_error = e.what();
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    g_last_error = "host allocation failed";
+    return BSE_ERR_OUT_OF_MEMORY;
+  } catch (const std::exception &e) {
+    g_last_error = e.what();
+    return BSE_ERR_ARGUMENT;
+  }
+}
+
+vgb::Coef coef(int32_t a, int32_t b, int32_t c, int32_t d) {
+  vgb::Coef k;
+  k.cqp = a; k.cx = b; k.cd = c; k.cd2 = d;
+  return k;
+}
+
+void require_handle(const bse_handle *h) { VGB_REQUIRE(h != nullptr, "null handle"); }
+
+void create_stream(bse_handle *h) {
+  VGB_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *bse_last_error(void) { return g_last_error.c_str(); }
+
+const char *bse_version(void) { return "votca_gb300 0.1 (sm_103a)"; }
+
+static int create_impl(const bse_mmn_desc *mmn, const double *const *slices, const double *w,
+                       bool dense_w, const double *hqp, int64_t ldh, int64_t hqp_size,
+                       const bse_options *opt, int32_t precision, bse_handle **out) {
+  return guarded([&] {
+    VGB_REQUIRE(mmn && slices && w && hqp && opt && out, "bse_op_create: null argument");
+    *out = nullptr;
+    std::unique_ptr<bse_handle> h(new bse_handle());
+    h->kind = 0;
+    create_stream(h.get());
+    h->bse.reset(new vgb::BseOperator());
+    try {
+      h->bse->stage(*mmn, slices, w, dense_w, hqp, ldh, hqp_size, *opt, precision, h->stream);
+    } catch (...) {
+      cudaStreamDestroy(h->stream);
+      h->stream = nullptr;
+      throw;
+    }
+    *out = h.release();
+  });
+}
+
+int bse_op_create(const bse_mmn_desc *mmn, const double *const *mmn_slices,
+                  const double *epsilon_0_inv, const double *hqp, int64_t ldh,
+                  int64_t hqp_size, const bse_options *opt, int32_t precision,
+                  bse_handle **out) {
+  return create_impl(mmn, mmn_slices, epsilon_0_inv, false, hqp, ldh, hqp_size, opt, precision, out);
+}
+
+int bse_op_create_dense_screening(const bse_mmn_desc *mmn, const double *const *mmn_slices,
+                                  const double *W, const double *hqp, int64_t ldh,
+                                  int64_t hqp_size, const bse_options *opt, int32_t precision,
+                                  bse_handle **out) {
+  return create_impl(mmn, mmn_slices, W, true, hqp, ldh, hqp_size, opt, precision, out);
+}
+
+int bse_dense_op_create(const double *a, const double *b, int64_t n, int64_t lda,
+                        bse_handle **out) {
+  return guarded([&] {
+    VGB_REQUIRE(out != nullptr, "bse_dense_op_create: null out");
+    *out = nullptr;
+    std::unique_ptr<bse_handle> h(new bse_handle());
+    h->kind = 1;
+    create_stream(h.get());
+    h->dense.reset(new vgb::DenseOperator());
+    h->dense->stage(a, b, n, lda, h->stream);
+    *out = h.release();
+  });
+}
+
+int bse_op_destroy(bse_handle *h) {
+  return guarded([&] {
+    if (!h) return;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    cudaStream_t s = h->stream;
+    delete h;
+    if (s) cudaStreamDestroy(s);
+  });
+}
+
+int bse_op_size(const bse_handle *h, int64_t *size) {
+  return guarded([&] {
+    require_handle(h);
+    VGB_REQUIRE(size != nullptr, "bse_op_size: null out");
+    *size = h->size();
+  });
+}
+
+int bse_op_matmul_device(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd, int32_t cd2,
+                         const double *dX, int64_t ldx, int64_t k, double *dY, int64_t ldy,
+                         void *stream) {
+  return guarded([&] {
+    require_handle(h);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (h->kind == 0) {
+      h->bse->matmul(coef(cqp, cx, cd, cd2), dX, ldx, k, dY, ldy, s);
+    } else {
+      h->dense->matmul(dX, ldx, k, dY, ldy, s);
+    }
+  });
+}
+
+int bse_op_matmul(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd, int32_t cd2,
+                  const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy) {
+  return guarded([&] {
+    require_handle(h);
+    const int64_t n = h->size();
+    VGB_REQUIRE(X && Y, "bse_op_matmul: null matrix");
+    VGB_REQUIRE(ldx >= n && ldy >= n && k >= 0, "bse_op_matmul: bad leading dimension or k");
+    if (k == 0) return;
+    h->dX.resize(n * k);
+    h->dY.resize(n * k);
+    cudaStream_t s = h->stream;
+    VGB_CUDA(cudaMemcpy2DAsync(h->dX.get(), n * sizeof(double), X, ldx * sizeof(double),
+                               n * sizeof(double), k, cudaMemcpyHostToDevice, s));
+    if (h->kind == 0)
+      h->bse->matmul(coef(cqp, cx, cd, cd2), h->dX.get(), n, k, h->dY.get(), n, s);
+    else
+      h->dense->matmul(h->dX.get(), n, k, h->dY.get(), n, s);
+    VGB_CUDA(cudaMemcpy2DAsync(Y, ldy * sizeof(double), h->dY.get(), n * sizeof(double),
+                               n * sizeof(double), k, cudaMemcpyDeviceToHost, s));
+    VGB_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int bse_op_diagonal_device(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd, int32_t cd2,
+                           double *dD, void *stream) {
+  return guarded([&] {
+    require_handle(h);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (h->kind == 0) h->bse->diagonal(coef(cqp, cx, cd, cd2), dD, s);
+    else h->dense->diagonal(dD, s);
+  });
+}
+
+int bse_op_diagonal(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd, int32_t cd2, double *D) {
+  return guarded([&] {
+    require_handle(h);
+    VGB_REQUIRE(D != nullptr, "bse_op_diagonal: null output");
+    const int64_t n = h->size();
+    h->dD.resize(n);
+    cudaStream_t s = h->stream;
+    if (h->kind == 0) h->bse->diagonal(coef(cqp, cx, cd, cd2), h->dD.get(), s);
+    else h->dense->diagonal(h->dD.get(), s);
+    VGB_CUDA(cudaMemcpyAsync(D, h->dD.get(), n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    VGB_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int bse_ham_matmul(bse_handle *h, const int32_t a_coef[4], const int32_t b_coef[4],
+                   const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy) {
+  return guarded([&] {
+    require_handle(h);
+    const int64_t n = 2 * h->size();
+    VGB_REQUIRE(X && Y, "bse_ham_matmul: null matrix");
+    VGB_REQUIRE(ldx >= n && ldy >= n && k >= 0, "bse_ham_matmul: bad leading dimension or k");
+    if (k == 0) return;
+    h->dX.resize(n * k);
+    h->dY.resize(n * k);
+    cudaStream_t s = h->stream;
+    VGB_CUDA(cudaMemcpy2DAsync(h->dX.get(), n * sizeof(double), X, ldx * sizeof(double),
+                               n * sizeof(double), k, cudaMemcpyHostToDevice, s));
+    if (h->kind == 0) {
+      VGB_REQUIRE(a_coef && b_coef, "bse_ham_matmul: null coefficients");
+      h->bse->ham_matmul(coef(a_coef[0], a_coef[1], a_coef[2], a_coef[3]),
+                         coef(b_coef[0], b_coef[1], b_coef[2], b_coef[3]), h->dX.get(), n, k,
+                         h->dY.get(), n, s);
+    } else {
+      h->dense->ham_matmul(h->dX.get(), n, k, h->dY.get(), n, s);
+    }
+    VGB_CUDA(cudaMemcpy2DAsync(Y, ldy * sizeof(double), h->dY.get(), n * sizeof(double),
+                               n * sizeof(double), k, cudaMemcpyDeviceToHost, s));
+    VGB_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int bse_davidson_solve(bse_handle *h, const int32_t a_coef[4], const int32_t b_coef[4],
+                       const bse_davidson_options *opt, int64_t neigen, const double *guess,
+                       int64_t guess_cols, double *evals, double *evecs, int64_t ldv,
+                       bse_davidson_result *result) {
+  return guarded([&] {
+    require_handle(h);
+    VGB_REQUIRE(opt != nullptr, "bse_davidson_solve: null options");
+    const bool ham = opt->matrix_type == 1;
+    std::unique_ptr<vgb::DeviceOperator> op;
+    if (h->kind == 0) {
+      VGB_REQUIRE(a_coef != nullptr, "bse_davidson_solve: null operator coefficients");
+      vgb::Coef a = coef(a_coef[0], a_coef[1], a_coef[2], a_coef[3]);
+      if (ham) {
+        VGB_REQUIRE(b_coef != nullptr, "bse_davidson_solve: HAM needs B coefficients");
+        op.reset(new vgb::BseHamApply(h->bse.get(), a, coef(b_coef[0], b_coef[1], b_coef[2], b_coef[3])));
+      } else {
+        op.reset(new vgb::BseApply(h->bse.get(), a));
+      }
+    } else {
+      VGB_REQUIRE(!ham || h->dense->has_b, "bse_davidson_solve: HAM needs a B block");
+      op.reset(new vgb::DenseApply(h->dense.get(), ham));
+    }
+    const int64_t n = op->size();
+    VGB_REQUIRE(evecs == nullptr || ldv >= n, "bse_davidson_solve: ldv smaller than the operator size");
+    vgb::DeviceBuffer<double> devecs;
+    if (evecs) devecs.resize(n * neigen);
+    vgb::DavidsonOutput o;
+    vgb::davidson_solve(*op, neigen, *opt, guess, guess_cols, evecs ? devecs.get() : nullptr, o,
+                        h->stream);
+    if (evals) std::memcpy(evals, o.evals.data(), neigen * sizeof(double));
+    if (evecs) {
+      VGB_CUDA(cudaMemcpy2DAsync(evecs, ldv * sizeof(double), devecs.get(), n * sizeof(double),
+                                 n * sizeof(double), neigen, cudaMemcpyDeviceToHost, h->stream));
+      VGB_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    if (result) {
+      result->iterations = o.iterations;
+      result->info = o.info;
+      result->reserved = 0;
+      result->matvec_columns = o.matvec_columns;
+      result->seconds_matvec = o.seconds_matvec;
+      result->seconds_total = o.seconds_total;
+    }
+  });
+}
+
+int bse_op_profile(bse_handle *h, int32_t enable) {
+  return guarded([&] {
+    require_handle(h);
+    VGB_REQUIRE(h->kind == 0, "bse_op_profile: not a BSE operator");
+    h->bse->timer.enable(enable != 0);
+  });
+}
+
+int bse_op_profile_read(bse_handle *h, double *stage_ms, int64_t *stage_calls, int32_t nstages) {
+  return guarded([&] {
+    require_handle(h);
+    VGB_REQUIRE(h->kind == 0, "bse_op_profile_read: not a BSE operator");
+    h->bse->timer.read(stage_ms, stage_calls, nstages);
+  });
+}
+
+int bse_probe_fp64_tflops(double *tflops) {
+  return guarded([&] {
+    VGB_REQUIRE(tflops != nullptr, "bse_probe_fp64_tflops: null out");
+    *tflops = vgb::probe_fp64_tflops();
+  });
+}
+
+}  // extern "C"

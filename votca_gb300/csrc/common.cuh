@@ -1,0 +1,76 @@
+// Shared host/device helpers of the GB300 BSE library.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+
+#include "../../include/votca_gb300_bse.h"
+
+namespace vgb {
+
+// Error carried from the C++ core to the C ABI (mapped to a bse_status code).
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string &msg) : std::runtime_error(msg), code(c) {}
+};
+
+[[noreturn]] inline void fail(int code, const std::string &msg) { throw Error(code, msg); }
+
+inline void cuda_check(cudaError_t e, const char *what, const char *file, int line) {
+  if (e != cudaSuccess) {
+    int code = (e == cudaErrorMemoryAllocation) ? BSE_ERR_OUT_OF_MEMORY : BSE_ERR_CUDA;
+    fail(code, std::string(what) + " failed at " + file + ":" + std::to_string(line) + ": " +
+                   cudaGetErrorString(e));
+  }
+}
+#define VGB_CUDA(x) ::vgb::cuda_check((x), #x, __FILE__, __LINE__)
+#define VGB_LAUNCH_CHECK() ::vgb::cuda_check(cudaGetLastError(), "kernel launch", __FILE__, __LINE__)
+#define VGB_REQUIRE(cond, msg)                                   \
+  do {                                                           \
+    if (!(cond)) ::vgb::fail(BSE_ERR_ARGUMENT, std::string(msg)); \
+  } while (0)
+
+// Owning device buffer.
+template <typename T>
+struct DeviceBuffer {
+  T *ptr = nullptr;
+  size_t count = 0;
+  DeviceBuffer() = default;
+  explicit DeviceBuffer(size_t n) { resize(n); }
+  DeviceBuffer(const DeviceBuffer &) = delete;
+  DeviceBuffer &operator=(const DeviceBuffer &) = delete;
+  DeviceBuffer(DeviceBuffer &&o) noexcept : ptr(o.ptr), count(o.count) { o.ptr = nullptr; o.count = 0; }
+  DeviceBuffer &operator=(DeviceBuffer &&o) noexcept {
+    if (this != &o) { release(); ptr = o.ptr; count = o.count; o.ptr = nullptr; o.count = 0; }
+    return *this;
+  }
+  ~DeviceBuffer() { release(); }
+  void resize(size_t n) {
+    if (n <= count && ptr) return;
+    release();
+    if (n == 0) return;
+    VGB_CUDA(cudaMalloc(&ptr, n * sizeof(T)));
+    count = n;
+  }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    count = 0;
+  }
+  T *get() const { return ptr; }
+  size_t bytes() const { return count * sizeof(T); }
+};
+
+__host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Number of SMs of the current device (152 on GB300).
+int sm_count();
+
+// Measured FP64 FMA throughput of the current device in TFLOP/s.
+double probe_fp64_tflops();
+
+}  // namespace vgb

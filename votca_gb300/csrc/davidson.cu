@@ -1,0 +1,671 @@
+// Block Davidson on the device.  Every dim-sized vector (search space V, A V,
+// Ritz vectors, residuals, corrections) lives in HBM; Gram-Schmidt, the
+// projections V^T A V, the Ritz vectors V U, the residuals A V U - q Lambda,
+// the residual norms and the DPR/Olsen corrections run as FP64 kernels.  Only
+// the projected matrices (<= a few hundred squared) and the norms cross to
+// the host, where the small eigenproblem is solved.
+//
+// Step-by-step correspondence with xtp/src/libxtp/davidsonsolver.cc:
+//   checkOptions :44-62, getSizeUpdate :149-170, setupInitialEigenvectors :180-206,
+//   getRitz :221-239, getHarmonicRitz :241-332, checkConvergence :347-352,
+//   extendProjection :354-378, computeCorrectionVector/dpr/olsen :389-436,
+//   gramschmidt :442-478, qr :480-488, restart :490-513, store* :515-555,
+// and updateProjection, davidsonsolver.h:239-280.
+#include "davidson.cuh"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <numeric>
+#include <cstdlib>
+
+#include "host_eig.hpp"
+
+namespace vgb {
+
+namespace {
+
+constexpr int kRedChunks = 64;
+
+unsigned blocks_for(int64_t n, int threads = 256) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, threads), 16LL * 152));
+}
+
+// partial[c * kRedChunks + b] = sum over chunk b of A[:, c] * B[:, c]
+__global__ void coldot_partial_kernel(const double *__restrict__ A, int64_t lda,
+                                      const double *__restrict__ B, int64_t ldb, int64_t n,
+                                      double *__restrict__ partial) {
+  const int64_t c = blockIdx.y;
+  const int64_t chunk = ceil_div(n, kRedChunks);
+  const int64_t r0 = blockIdx.x * chunk, r1 = min(n, r0 + chunk);
+  const double *a = A + c * lda, *b = B + c * ldb;
+  double s = 0.0;
+  for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) s = fma(a[r], b[r], s);
+  __shared__ double red[256];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[c * kRedChunks + blockIdx.x] = red[0];
+}
+
+__global__ void coldot_final_kernel(const double *__restrict__ partial, int64_t ncols, int take_sqrt,
+                                    double *__restrict__ out) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncols;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int b = 0; b < kRedChunks; ++b) s += partial[c * kRedChunks + b];
+    out[c] = take_sqrt ? sqrt(s) : s;
+  }
+}
+
+__global__ void set_unit_columns_kernel(double *V, int64_t ldv, const int64_t *rows, int64_t count) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < count;
+       j += (int64_t)gridDim.x * blockDim.x)
+    V[rows[j] + ldv * j] = 1.0;
+}
+
+// res[:, j] -= lam[j] * q[:, j]
+__global__ void residual_kernel(double *__restrict__ res, const double *__restrict__ q, int64_t n,
+                                int64_t ncols, const double *__restrict__ lam) {
+  const int64_t total = n * ncols;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = t / n;
+    res[t] -= lam[j] * q[t];
+  }
+}
+
+// out[:, kk] = -r_j / (D - lambda_j) for the listed roots (DPR, davidsonsolver.cc:416-422);
+// with olsen != 0 also dq[:, kk] = -q_j / (D - lambda_j).  clean != 0 zeroes
+// non-finite entries (computeCorrectionVector, :411-413).
+__global__ void dpr_kernel(double *__restrict__ out, int64_t ldo, const double *__restrict__ res,
+                           const double *__restrict__ q, int64_t n, const double *__restrict__ D,
+                           const int64_t *__restrict__ cols, const double *__restrict__ lams,
+                           int64_t count, int clean, double *__restrict__ dq) {
+  const int64_t total = n * count;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t % n, kk = t / n;
+    const int64_t j = cols[kk];
+    const double den = D[i] - lams[kk];
+    double v = -res[j * n + i] / den;
+    if (clean && !isfinite(v)) v = 0.0;
+    out[kk * ldo + i] = v;
+    if (dq) dq[kk * n + i] = -q[j * n + i] / den;
+  }
+}
+
+// Olsen: delta += (num/denom) q_j, then non-finite -> 0 (davidsonsolver.cc:424-436)
+__global__ void olsen_finish_kernel(double *__restrict__ out, int64_t ldo,
+                                    const double *__restrict__ q, int64_t n,
+                                    const int64_t *__restrict__ cols, const double *__restrict__ num,
+                                    const double *__restrict__ den, int64_t count) {
+  const int64_t total = n * count;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t % n, kk = t / n;
+    const double eps = (-num[kk]) / (-den[kk]);
+    double v = out[kk * ldo + i] + eps * q[cols[kk] * n + i];
+    if (!isfinite(v)) v = 0.0;
+    out[kk * ldo + i] = v;
+  }
+}
+
+// A[:, c] /= norm[c] where norm[c] > 0 (Eigen's normalize leaves zero columns alone)
+__global__ void scale_columns_kernel(double *A, int64_t lda, int64_t n, int64_t ncols,
+                                     const double *__restrict__ norm) {
+  const int64_t total = n * ncols;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t % n, c = t / n;
+    const double nv = norm[c];
+    if (nv > 0.0) A[c * lda + i] /= nv;
+  }
+}
+
+// Gram-Schmidt linear-dependence check of one column (davidsonsolver.cc:472-475)
+__global__ void gs_check_kernel(const double *norm, const double *norm0, int *flag) {
+  if (threadIdx.x == 0 && blockIdx.x == 0)
+    if (!(norm[0] > 1e-12 * norm0[0])) flag[0] = 1;
+}
+
+__global__ void copy_block_kernel(const double *src, int64_t lds, double *dst, int64_t ldd,
+                                  int64_t n, int64_t ncols) {
+  const int64_t total = n * ncols;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t % n, c = t / n;
+    dst[c * ldd + i] = src[c * lds + i];
+  }
+}
+
+}  // namespace
+
+namespace {
+
+struct Ctx {
+  cudaStream_t s;
+  int64_t n;
+  GemmWorkspace ws;
+  DeviceBuffer<double> red_partial, scal;
+
+  // out[c] = ||A[:, c]|| (or dot(A[:, c], B[:, c]) when B given), device
+  void coldots(const double *A, int64_t lda, const double *B, int64_t ldb, int64_t ncols,
+               double *out, bool sqrt_) {
+    if (ncols <= 0) return;
+    red_partial.resize(ncols * kRedChunks);
+    dim3 grid(kRedChunks, (unsigned)ncols);
+    coldot_partial_kernel<<<grid, 256, 0, s>>>(A, lda, B ? B : A, B ? ldb : lda, n,
+                                               red_partial.get());
+    VGB_LAUNCH_CHECK();
+    coldot_final_kernel<<<blocks_for(ncols, 128), 128, 0, s>>>(red_partial.get(), ncols,
+                                                               sqrt_ ? 1 : 0, out);
+    VGB_LAUNCH_CHECK();
+  }
+  void scale_cols(double *A, int64_t lda, int64_t ncols, const double *norms) {
+    if (ncols <= 0) return;
+    scale_columns_kernel<<<blocks_for(n * ncols), 256, 0, s>>>(A, lda, n, ncols, norms);
+    VGB_LAUNCH_CHECK();
+  }
+  // C (m x nc, ldc) = alpha * A[:, a0:a0+m]^T B[:, b0:b0+nc] + beta C
+  void gemm_tn(const double *A, int64_t lda, int64_t m, const double *B, int64_t ldb, int64_t nc,
+               double *C, int64_t ldc, double alpha, double beta) {
+    GemmDesc g;
+    g.M = m; g.N = nc; g.K = n;
+    g.a_colmajor(A, lda, true).b_colmajor(B, ldb, false).c_colmajor(C, ldc);
+    g.alpha = alpha; g.beta = beta;
+    dgemm(g, s, &ws);
+  }
+  // C (n x nc) = alpha * A (n x k) B (k x nc) + beta C
+  void gemm_nn(const double *A, int64_t lda, int64_t k, const double *B, int64_t ldb, int64_t nc,
+               double *C, int64_t ldc, double alpha, double beta) {
+    GemmDesc g;
+    g.M = n; g.N = nc; g.K = k;
+    g.a_colmajor(A, lda, false).b_colmajor(B, ldb, false).c_colmajor(C, ldc);
+    g.alpha = alpha; g.beta = beta;
+    dgemm(g, s, &ws);
+  }
+  void copy_cols(const double *src, int64_t lds, double *dst, int64_t ldd, int64_t ncols) {
+    if (ncols <= 0) return;
+    copy_block_kernel<<<blocks_for(n * ncols), 256, 0, s>>>(src, lds, dst, ldd, n, ncols);
+    VGB_LAUNCH_CHECK();
+  }
+};
+
+// DavidsonSolver::gramschmidt on columns [nstart, ncols) of Q (ld n).
+void gramschmidt(Ctx &x, double *Q, int64_t nstart, int64_t ncols, DeviceBuffer<double> &work,
+                 DeviceBuffer<int> &flag) {
+  const int64_t n = x.n, nupdate = ncols - nstart;
+  if (nupdate <= 0) return;
+  work.resize(3 * nupdate + std::max<int64_t>(nstart, 1) * nupdate + ncols + 8);
+  double *norms0 = work.get();            // initial norms of the new columns
+  double *norms = norms0 + nupdate;       // scratch norms
+  double *h = norms + nupdate + 8;        // projection coefficients
+  x.coldots(Q + nstart * n, n, nullptr, 0, nupdate, norms0, true);
+  VGB_CUDA(cudaMemsetAsync(flag.get(), 0, sizeof(int), x.s));
+  for (int pass = 0; pass < 2; ++pass) {
+    if (nstart > 0) {
+      // Q_new -= Q_old (Q_old^T Q_new); normalise
+      x.gemm_tn(Q, n, nstart, Q + nstart * n, n, nupdate, h, nstart, 1.0, 0.0);
+      x.gemm_nn(Q, n, nstart, h, nstart, nupdate, Q + nstart * n, n, -1.0, 1.0);
+      x.coldots(Q + nstart * n, n, nullptr, 0, nupdate, norms, true);
+      x.scale_cols(Q + nstart * n, n, nupdate, norms);
+    }
+    for (int64_t j = nstart + 1; j < ncols; ++j) {
+      const int64_t range = j - nstart;
+      double *qj = Q + j * n;
+      const double *M = Q + nstart * n;
+      x.gemm_tn(M, n, range, qj, n, 1, h, range, 1.0, 0.0);
+      x.gemm_nn(M, n, range, h, range, 1, qj, n, -1.0, 1.0);
+      x.coldots(qj, n, nullptr, 0, 1, norms, true);
+      if (pass == 1) {
+        gs_check_kernel<<<1, 32, 0, x.s>>>(norms, norms0 + range, flag.get());
+        VGB_LAUNCH_CHECK();
+      }
+      x.scale_cols(qj, n, 1, norms);
+    }
+  }
+  int hflag = 0;
+  VGB_CUDA(cudaMemcpyAsync(&hflag, flag.get(), sizeof(int), cudaMemcpyDeviceToHost, x.s));
+  VGB_CUDA(cudaStreamSynchronize(x.s));
+  if (hflag) fail(BSE_ERR_NUMERICAL, "Linear dependencies in Gram-Schmidt.");
+}
+
+// Householder QR, thin Q (m x r) of the m x r column-major matrix A (DavidsonSolver::qr)
+std::vector<double> thin_q(int64_t m, int64_t r, const std::vector<double> &A) {
+  std::vector<double> R(A), Q(m * r, 0.0);
+  std::vector<std::vector<double>> vs;
+  for (int64_t k = 0; k < r && k < m; ++k) {
+    std::vector<double> v(m, 0.0);
+    double nrm = 0.0;
+    for (int64_t i = k; i < m; ++i) nrm += R[i + m * k] * R[i + m * k];
+    nrm = std::sqrt(nrm);
+    if (nrm == 0.0) { vs.push_back(v); continue; }
+    const double alpha = R[k + m * k] >= 0 ? -nrm : nrm;
+    for (int64_t i = k; i < m; ++i) v[i] = R[i + m * k];
+    v[k] -= alpha;
+    double vn = 0.0;
+    for (int64_t i = k; i < m; ++i) vn += v[i] * v[i];
+    vn = std::sqrt(vn);
+    if (vn > 0)
+      for (int64_t i = k; i < m; ++i) v[i] /= vn;
+    for (int64_t c = k; c < r; ++c) {
+      double s = 0.0;
+      for (int64_t i = k; i < m; ++i) s += v[i] * R[i + m * c];
+      for (int64_t i = k; i < m; ++i) R[i + m * c] -= 2.0 * s * v[i];
+    }
+    vs.push_back(v);
+  }
+  for (int64_t c = 0; c < r; ++c) Q[c + m * c] = 1.0;
+  for (int64_t k = (int64_t)vs.size() - 1; k >= 0; --k) {
+    const auto &v = vs[k];
+    for (int64_t c = 0; c < r; ++c) {
+      double s = 0.0;
+      for (int64_t i = k; i < m; ++i) s += v[i] * Q[i + m * c];
+      for (int64_t i = k; i < m; ++i) Q[i + m * c] -= 2.0 * s * v[i];
+    }
+  }
+  return Q;
+}
+
+}  // namespace
+
+void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_options &opt,
+                    const double *host_guess, int64_t guess_cols, double *evecs_dev,
+                    DavidsonOutput &out, cudaStream_t s) {
+  const auto t_start = std::chrono::steady_clock::now();
+  const bool ham = opt.matrix_type == 1;
+  const bool debug = getenv("VGB_DAVIDSON_DEBUG") != nullptr;
+  const int64_t n = A.size();
+  VGB_REQUIRE(neigen >= 1 && neigen <= n, "DavidsonSolver: neigen out of range");
+  VGB_REQUIRE(opt.correction == 0 || opt.correction == 1, "not a valid Davidson correction method");
+  VGB_REQUIRE(opt.update >= 0 && opt.update <= 2, "not a valid Davidson update");
+  VGB_REQUIRE(opt.matrix_type == 0 || opt.matrix_type == 1, "not a valid Davidson matrix type");
+  const int64_t iter_max = opt.iter_max > 0 ? opt.iter_max : 50;
+  const double tol = opt.tolerance;
+  int64_t max_space = opt.max_search_space;
+  if (max_space < neigen) max_space = neigen * 5;
+  if (max_space > n) max_space = n;  // checkOptions
+  int64_t size_update;               // getSizeUpdate
+  if (opt.update == 0) size_update = neigen;
+  else if (opt.update == 1) size_update = neigen < 20 ? (int64_t)(1.5 * (double)neigen) : neigen + 10;
+  else size_update = 2 * neigen;
+
+  int64_t restart_size, ncols;
+  if (host_guess) {
+    VGB_REQUIRE(guess_cols >= neigen, "DavidsonSolver::solve initial_guess has fewer columns than neigen.");
+    restart_size = std::min(guess_cols, max_space);
+    ncols = guess_cols;
+  } else {
+    restart_size = 2 * neigen;
+    ncols = restart_size;
+  }
+  VGB_REQUIRE(ncols <= n, "DavidsonSolver: initial search space larger than the operator");
+  const int64_t cap = std::max(ncols, max_space) + 2 * size_update + restart_size + 2;
+  const int64_t capc = std::min(cap, n + 2 * size_update + restart_size + 2);
+
+  Ctx x;
+  x.s = s;
+  x.n = n;
+  DeviceBuffer<double> V(n * capc), AV(n * capc), AAV, D(n), q, res, Ud, tmp, lamd, work, cbuf;
+  DeviceBuffer<int64_t> colsd;
+  DeviceBuffer<int> flag(1);
+  if (ham) AAV.resize(n * capc);
+  VGB_CUDA(cudaMemsetAsync(V.get(), 0, n * capc * sizeof(double), s));
+
+  cudaEvent_t ev0, ev1;
+  VGB_CUDA(cudaEventCreate(&ev0));
+  VGB_CUDA(cudaEventCreate(&ev1));
+  double matvec_ms = 0.0;
+  auto apply = [&](const double *X, int64_t k, double *Y) {
+    if (k <= 0) return;
+    VGB_CUDA(cudaEventRecord(ev0, s));
+    A.apply(X, n, k, Y, n, s);
+    VGB_CUDA(cudaEventRecord(ev1, s));
+    VGB_CUDA(cudaEventSynchronize(ev1));
+    float ms = 0.f;
+    VGB_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+    matvec_ms += ms;
+    out.matvec_columns += k;
+  };
+
+  // diagonal of the operator
+  A.diagonal(D.get(), s);
+  std::vector<double> Dh(n);
+  VGB_CUDA(cudaMemcpyAsync(Dh.data(), D.get(), n * sizeof(double), cudaMemcpyDeviceToHost, s));
+  VGB_CUDA(cudaStreamSynchronize(s));
+
+  if (host_guess) {
+    VGB_CUDA(cudaMemcpyAsync(V.get(), host_guess, n * guess_cols * sizeof(double),
+                             cudaMemcpyHostToDevice, s));
+    gramschmidt(x, V.get(), 0, ncols, work, flag);
+  } else {
+    // setupInitialEigenvectors: unit vectors at the smallest diagonal entries
+    // (SYMM) or from the middle of the sorted diagonal (HAM)
+    std::vector<int64_t> idx(n);
+    std::iota(idx.begin(), idx.end(), 0);
+    std::stable_sort(idx.begin(), idx.end(), [&](int64_t a, int64_t b) { return Dh[a] < Dh[b]; });
+    const int64_t ind0 = ham ? n / 2 : 0;
+    VGB_REQUIRE(ind0 + ncols <= n, "DavidsonSolver: initial guess exceeds the operator size");
+    std::vector<int64_t> rows(idx.begin() + ind0, idx.begin() + ind0 + ncols);
+    colsd.resize(std::max<int64_t>(ncols, 64));
+    VGB_CUDA(cudaMemcpyAsync(colsd.get(), rows.data(), ncols * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    set_unit_columns_kernel<<<blocks_for(ncols), 256, 0, s>>>(V.get(), n, colsd.get(), ncols);
+    VGB_LAUNCH_CHECK();
+  }
+
+  std::vector<double> T(capc * capc, 0.0), Bm;  // host projected matrices, ld capc
+  if (ham) Bm.assign(capc * capc, 0.0);
+  const int64_t ldT = capc;
+  int64_t nav = 0;  // columns of AV
+  std::vector<double> lam, U, resn;
+  std::vector<char> conv(size_update, 0);
+  out.history_resnorm.clear();
+
+  for (int64_t it = 0; it < iter_max; ++it) {
+    out.iterations = it;
+    // ---- updateProjection ----
+    {
+      const int64_t old = (it == 0) ? 0 : nav, nvec = ncols - old;
+      apply(V.get() + old * n, nvec, AV.get() + old * n);
+      cbuf.resize(ncols * std::max<int64_t>(ncols, 1));
+      // T[:, old:ncols] = V^T AV_new
+      x.gemm_tn(V.get(), n, ncols, AV.get() + old * n, n, nvec, cbuf.get(), ncols, 1.0, 0.0);
+      std::vector<double> blk(ncols * nvec);
+      VGB_CUDA(cudaMemcpyAsync(blk.data(), cbuf.get(), blk.size() * sizeof(double),
+                               cudaMemcpyDeviceToHost, s));
+      VGB_CUDA(cudaStreamSynchronize(s));
+      for (int64_t c = 0; c < nvec; ++c)
+        for (int64_t r = 0; r < ncols; ++r) T[r + ldT * (old + c)] = blk[r + ncols * c];
+      if (!ham) {
+        for (int64_t c = 0; c < nvec; ++c)
+          for (int64_t r = 0; r < old; ++r) T[(old + c) + ldT * r] = T[r + ldT * (old + c)];
+      } else {
+        // T[old:, :old] = V_new^T AV_old;  AAV_new = A AV_new;  B likewise
+        if (old > 0) {
+          x.gemm_tn(V.get() + old * n, n, nvec, AV.get(), n, old, cbuf.get(), nvec, 1.0, 0.0);
+          std::vector<double> b2(nvec * old);
+          VGB_CUDA(cudaMemcpyAsync(b2.data(), cbuf.get(), b2.size() * sizeof(double),
+                                   cudaMemcpyDeviceToHost, s));
+          VGB_CUDA(cudaStreamSynchronize(s));
+          for (int64_t c = 0; c < old; ++c)
+            for (int64_t r = 0; r < nvec; ++r) T[(old + r) + ldT * c] = b2[r + nvec * c];
+        }
+        apply(AV.get() + old * n, nvec, AAV.get() + old * n);
+        x.gemm_tn(V.get(), n, ncols, AAV.get() + old * n, n, nvec, cbuf.get(), ncols, 1.0, 0.0);
+        VGB_CUDA(cudaMemcpyAsync(blk.data(), cbuf.get(), blk.size() * sizeof(double),
+                                 cudaMemcpyDeviceToHost, s));
+        VGB_CUDA(cudaStreamSynchronize(s));
+        for (int64_t c = 0; c < nvec; ++c)
+          for (int64_t r = 0; r < ncols; ++r) Bm[r + ldT * (old + c)] = blk[r + ncols * c];
+        if (old > 0) {
+          x.gemm_tn(V.get() + old * n, n, nvec, AAV.get(), n, old, cbuf.get(), nvec, 1.0, 0.0);
+          std::vector<double> b2(nvec * old);
+          VGB_CUDA(cudaMemcpyAsync(b2.data(), cbuf.get(), b2.size() * sizeof(double),
+                                   cudaMemcpyDeviceToHost, s));
+          VGB_CUDA(cudaStreamSynchronize(s));
+          for (int64_t c = 0; c < old; ++c)
+            for (int64_t r = 0; r < nvec; ++r) Bm[(old + r) + ldT * c] = b2[r + nvec * c];
+        }
+      }
+      nav = ncols;
+    }
+    const int64_t m = ncols;
+    std::vector<double> Tm(m * m);
+    for (int64_t c = 0; c < m; ++c)
+      for (int64_t r = 0; r < m; ++r) Tm[r + m * c] = T[r + ldT * c];
+    if (debug) {
+      fprintf(stderr, "[davidson-debug] iter %lld m %lld T diag:", (long long)it, (long long)m);
+      for (int64_t c = 0; c < std::min<int64_t>(m, 40); ++c) fprintf(stderr, " %.4f", Tm[c + m * c]);
+      fprintf(stderr, "\n");
+    }
+    const int64_t needed = std::min(m, std::max(restart_size, size_update));
+
+    // ---- getRitzEigenPairs (small problem on the host) ----
+    if (!ham) {
+      std::vector<double> ev, evec;
+      if (!sym_eig(m, Tm.data(), ev, evec))
+        fail(BSE_ERR_NUMERICAL, "Small hermitian eigenvalue problem failed.");
+      lam.assign(ev.begin(), ev.begin() + needed);
+      U.assign(evec.begin(), evec.begin() + m * needed);
+    } else {
+      std::vector<double> Bmm(m * m);
+      for (int64_t c = 0; c < m; ++c)
+        for (int64_t r = 0; r < m; ++r) Bmm[r + m * c] = Bm[r + ldT * c];
+      std::vector<double> wr, wi, vr;
+      if (!gen_eig(m, Tm.data(), Bmm.data(), wr, wi, vr))
+        fail(BSE_ERR_NUMERICAL, "Small generalized eigenvalue problem failed.");
+      // complex partners (davidsonsolver.cc:261-291)
+      std::vector<std::pair<int64_t, int64_t>> pairs;
+      for (int64_t i = 0; i < m; ++i) {
+        if (wi[i] != 0.0) {
+          bool found = false;
+          for (auto &p : pairs) {
+            if (p.second > -1) continue;
+            if (std::fabs(wr[p.first] - wr[i]) < 1e-9 && std::fabs(wi[p.first] + wi[i]) < 1e-9) {
+              p.second = i;
+              found = true;
+            }
+          }
+          if (!found) pairs.emplace_back(i, -1);
+        }
+      }
+      for (auto &p : pairs)
+        if (p.second < 0)
+          fail(BSE_ERR_NUMERICAL, "Eigenvalue:" + std::to_string(p.first) + " is complex but has no partner.");
+      std::vector<double> evals;
+      std::vector<double> evecs;
+      for (int64_t i = 0; i < m; ++i) {
+        bool second = false;
+        for (auto &p : pairs) if (p.second == i) second = true;
+        if (second) continue;
+        evals.push_back(wr[i]);
+        // real part of eigenvector i (LAPACK packing: pair (i, i+1) shares columns)
+        std::vector<double> col(m);
+        for (int64_t r = 0; r < m; ++r) col[r] = vr[r + m * i];
+        double nn = 0.0;
+        for (double v : col) nn += v * v;
+        nn = std::sqrt(nn);
+        if (nn > 0) for (double &v : col) v /= nn;
+        evecs.insert(evecs.end(), col.begin(), col.end());
+      }
+      std::vector<int64_t> idx(evals.size());
+      std::iota(idx.begin(), idx.end(), 0);
+      std::stable_sort(idx.begin(), idx.end(), [&](int64_t a, int64_t b) { return evals[a] < evals[b]; });
+      std::reverse(idx.begin(), idx.end());
+      U.assign(m * needed, 0.0);
+      for (int64_t c = 0; c < needed; ++c)
+        std::copy(evecs.begin() + m * idx[c], evecs.begin() + m * (idx[c] + 1), U.begin() + m * c);
+      // lambda = diag(U^T T U)
+      lam.assign(needed, 0.0);
+      for (int64_t c = 0; c < needed; ++c) {
+        double sacc = 0.0;
+        for (int64_t a = 0; a < m; ++a) {
+          double tu = 0.0;
+          for (int64_t b = 0; b < m; ++b) tu += Tm[a + m * b] * U[b + m * c];
+          sacc += U[a + m * c] * tu;
+        }
+        lam[c] = sacc;
+      }
+    }
+    // q = V U, res = AV U - q Lambda
+    Ud.resize(m * needed);
+    lamd.resize(needed);
+    q.resize(n * needed);
+    res.resize(n * needed);
+    VGB_CUDA(cudaMemcpyAsync(Ud.get(), U.data(), m * needed * sizeof(double), cudaMemcpyHostToDevice, s));
+    VGB_CUDA(cudaMemcpyAsync(lamd.get(), lam.data(), needed * sizeof(double), cudaMemcpyHostToDevice, s));
+    x.gemm_nn(V.get(), n, m, Ud.get(), m, needed, q.get(), n, 1.0, 0.0);
+    x.gemm_nn(AV.get(), n, m, Ud.get(), m, needed, res.get(), n, 1.0, 0.0);
+    residual_kernel<<<blocks_for(n * needed), 256, 0, s>>>(res.get(), q.get(), n, needed, lamd.get());
+    VGB_LAUNCH_CHECK();
+
+    // ---- checkConvergence ----
+    const int64_t nn_check = std::min(needed, size_update);
+    work.resize(std::max<int64_t>(needed, 1) + 8);
+    x.coldots(res.get(), n, nullptr, 0, nn_check, work.get(), true);
+    resn.assign(nn_check, 0.0);
+    VGB_CUDA(cudaMemcpyAsync(resn.data(), work.get(), nn_check * sizeof(double), cudaMemcpyDeviceToHost, s));
+    VGB_CUDA(cudaStreamSynchronize(s));
+    for (int64_t j = 0; j < size_update; ++j) conv[j] = (j < nn_check) ? (resn[j] < tol) : 0;
+    bool converged = true;
+    double maxres = 0.0;
+    for (int64_t j = 0; j < neigen; ++j) {
+      if (!conv[j]) converged = false;
+      if (j < nn_check) maxres = std::max(maxres, resn[j]);
+    }
+    out.history_resnorm.push_back(maxres);
+    if (opt.verbose)
+      fprintf(stderr, "[davidson] iter %4lld  search space %6lld  max residual %.3e\n",
+              (long long)it, (long long)ncols, maxres);
+    const bool last = it == iter_max - 1;
+    if (converged || last) {
+      // storeEigenPairs (+ zeroing of unconverged roots on the last iteration)
+      out.evals.assign(lam.begin(), lam.begin() + std::min(neigen, needed));
+      out.evals.resize(neigen, 0.0);
+      out.info = converged ? 0 : 1;
+      if (evecs_dev) {
+        const int64_t nc = std::min(neigen, needed);
+        x.copy_cols(q.get(), n, evecs_dev, n, nc);
+        x.coldots(evecs_dev, n, nullptr, 0, nc, work.get(), true);
+        x.scale_cols(evecs_dev, n, nc, work.get());
+        if (!converged)
+          for (int64_t j = 0; j < neigen; ++j)
+            if (j >= nc || !conv[j])
+              VGB_CUDA(cudaMemsetAsync(evecs_dev + j * n, 0, n * sizeof(double), s));
+      }
+      if (!converged)
+        for (int64_t j = 0; j < neigen; ++j)
+          if (!conv[j]) out.evals[j] = 0.0;
+      break;
+    }
+
+    // ---- extendProjection ----
+    std::vector<int64_t> upd;
+    std::vector<double> upd_lam;
+    for (int64_t j = 0; j < size_update; ++j)
+      if (!conv[j] && j < needed) { upd.push_back(j); upd_lam.push_back(lam[j]); }
+    const int64_t nupdate = (int64_t)upd.size();
+    VGB_REQUIRE(ncols + nupdate <= capc, "DavidsonSolver: search space capacity exceeded");
+    colsd.resize(std::max<int64_t>(nupdate, 64));
+    tmp.resize(2 * nupdate * n + 2 * nupdate + 8);
+    double *lamu = tmp.get();
+    double *numd = lamu + nupdate, *dend = numd + nupdate + 4;
+    double *dq = dend + nupdate + 4;
+    VGB_CUDA(cudaMemcpyAsync(colsd.get(), upd.data(), nupdate * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    VGB_CUDA(cudaMemcpyAsync(lamu, upd_lam.data(), nupdate * sizeof(double), cudaMemcpyHostToDevice, s));
+    double *Vnew = V.get() + ncols * n;
+    const bool olsen = opt.correction == 1;
+    dpr_kernel<<<blocks_for(n * nupdate), 256, 0, s>>>(Vnew, n, res.get(), q.get(), n, D.get(),
+                                                      colsd.get(), lamu, nupdate, olsen ? 0 : 1,
+                                                      olsen ? dq : nullptr);
+    VGB_LAUNCH_CHECK();
+    if (olsen) {
+      // num_k = q_j . delta_k ; den_k = q_j . dpr(q_j)   (signs applied in the finish kernel)
+      for (int64_t kk = 0; kk < nupdate; ++kk) {
+        x.coldots(q.get() + upd[kk] * n, n, Vnew + kk * n, n, 1, numd + kk, false);
+        x.coldots(q.get() + upd[kk] * n, n, dq + kk * n, n, 1, dend + kk, false);
+      }
+      olsen_finish_kernel<<<blocks_for(n * nupdate), 256, 0, s>>>(Vnew, n, q.get(), n, colsd.get(),
+                                                                 numd, dend, nupdate);
+      VGB_LAUNCH_CHECK();
+    }
+    // w.normalized()
+    work.resize(nupdate + 8);
+    x.coldots(Vnew, n, nullptr, 0, nupdate, work.get(), true);
+    x.scale_cols(Vnew, n, nupdate, work.get());
+    if (debug) {
+      std::vector<double> wn(nupdate);
+      VGB_CUDA(cudaMemcpyAsync(wn.data(), work.get(), nupdate * sizeof(double), cudaMemcpyDeviceToHost, s));
+      DeviceBuffer<double> G(nupdate * nupdate);
+      x.gemm_tn(Vnew, n, nupdate, Vnew, n, nupdate, G.get(), nupdate, 1.0, 0.0);
+      std::vector<double> Gh(nupdate * nupdate);
+      VGB_CUDA(cudaMemcpyAsync(Gh.data(), G.get(), Gh.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+      VGB_CUDA(cudaStreamSynchronize(s));
+      fprintf(stderr, "[davidson-debug] corrections: cols");
+      for (auto c : upd) fprintf(stderr, " %lld", (long long)c);
+      fprintf(stderr, "\n[davidson-debug] norms before normalise:");
+      for (auto v : wn) fprintf(stderr, " %.3e", v);
+      fprintf(stderr, "\n[davidson-debug] max offdiag overlap of new columns:");
+      for (int64_t c = 0; c < nupdate; ++c) {
+        double mo = 0; int64_t arg = -1;
+        for (int64_t r = 0; r < nupdate; ++r) if (r != c && std::fabs(Gh[r + nupdate * c]) > mo) { mo = std::fabs(Gh[r + nupdate * c]); arg = r; }
+        fprintf(stderr, " %lld:%.3f(%lld)", (long long)c, mo, (long long)arg);
+      }
+      fprintf(stderr, "\n");
+    }
+    gramschmidt(x, V.get(), ncols, ncols + nupdate, work, flag);
+    ncols += nupdate;
+    if (debug) {
+      DeviceBuffer<double> G(ncols * ncols);
+      x.gemm_tn(V.get(), n, ncols, V.get(), n, ncols, G.get(), ncols, 1.0, 0.0);
+      std::vector<double> Gh(ncols * ncols);
+      VGB_CUDA(cudaMemcpyAsync(Gh.data(), G.get(), Gh.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+      VGB_CUDA(cudaStreamSynchronize(s));
+      double off = 0.0;
+      int64_t worst = -1;
+      for (int64_t c = 0; c < ncols; ++c)
+        for (int64_t r = 0; r < ncols; ++r) {
+          const double d = std::fabs(Gh[r + ncols * c] - (r == c ? 1.0 : 0.0));
+          if (d > off) { off = d; worst = r + ncols * c; }
+        }
+      fprintf(stderr, "[davidson-debug] after GS: ncols %lld  max|V^T V - I| %.3e at (%lld,%lld)\n",
+              (long long)ncols, off, (long long)(worst % ncols), (long long)(worst / ncols));
+    }
+
+    // ---- restart ----
+    if (ncols > max_space) {
+      const int64_t rs = restart_size, nv = nupdate;
+      VGB_REQUIRE(rs <= needed, "DavidsonSolver: restart size exceeds the Ritz pairs");
+      DeviceBuffer<double> keep(n * nv), avn(n * rs);
+      x.copy_cols(V.get() + (ncols - nv) * n, n, keep.get(), n, nv);
+      if (!ham) {
+        x.copy_cols(q.get(), n, V.get(), n, rs);
+        x.gemm_nn(AV.get(), n, nav, Ud.get(), m, rs, avn.get(), n, 1.0, 0.0);
+        x.copy_cols(avn.get(), n, AV.get(), n, rs);
+      } else {
+        std::vector<double> Ur(U.begin(), U.begin() + m * rs);
+        std::vector<double> O = thin_q(m, rs, Ur);
+        DeviceBuffer<double> Od(m * rs), vn(n * rs);
+        VGB_CUDA(cudaMemcpyAsync(Od.get(), O.data(), m * rs * sizeof(double), cudaMemcpyHostToDevice, s));
+        x.gemm_nn(V.get(), n, nav, Od.get(), m, rs, vn.get(), n, 1.0, 0.0);
+        x.gemm_nn(AV.get(), n, nav, Od.get(), m, rs, avn.get(), n, 1.0, 0.0);
+        x.copy_cols(vn.get(), n, V.get(), n, rs);
+        x.copy_cols(avn.get(), n, AV.get(), n, rs);
+        x.gemm_nn(AAV.get(), n, nav, Od.get(), m, rs, avn.get(), n, 1.0, 0.0);
+        x.copy_cols(avn.get(), n, AAV.get(), n, rs);
+      }
+      x.copy_cols(keep.get(), n, V.get() + rs * n, n, nv);
+      ncols = rs + nv;
+      nav = rs;
+      // T = V[:, :rs]^T AV (and B = V^T AAV for HAM)
+      cbuf.resize(rs * rs);
+      std::vector<double> blk(rs * rs);
+      x.gemm_tn(V.get(), n, rs, AV.get(), n, rs, cbuf.get(), rs, 1.0, 0.0);
+      VGB_CUDA(cudaMemcpyAsync(blk.data(), cbuf.get(), blk.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+      VGB_CUDA(cudaStreamSynchronize(s));
+      std::fill(T.begin(), T.end(), 0.0);
+      for (int64_t c = 0; c < rs; ++c)
+        for (int64_t r = 0; r < rs; ++r) T[r + ldT * c] = blk[r + rs * c];
+      if (ham) {
+        x.gemm_tn(V.get(), n, rs, AAV.get(), n, rs, cbuf.get(), rs, 1.0, 0.0);
+        VGB_CUDA(cudaMemcpyAsync(blk.data(), cbuf.get(), blk.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+        VGB_CUDA(cudaStreamSynchronize(s));
+        std::fill(Bm.begin(), Bm.end(), 0.0);
+        for (int64_t c = 0; c < rs; ++c)
+          for (int64_t r = 0; r < rs; ++r) Bm[r + ldT * c] = blk[r + rs * c];
+      }
+    }
+  }
+  VGB_CUDA(cudaStreamSynchronize(s));
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  out.seconds_matvec = matvec_ms * 1e-3;
+  out.seconds_total =
+      std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+}
+
+}  // namespace vgb

@@ -1,0 +1,23 @@
+// Mixed-precision (tensor-core) contractions of the BSE product.
+#pragma once
+
+#include "bse_ops.cuh"
+
+namespace vgb {
+
+class MixedEngine {
+ public:
+  MixedEngine();
+  ~MixedEngine();
+  // Build the split (hi/lo) operand copies from the FP64 staged blocks.
+  void stage(BseOperator &op, cudaStream_t s);
+  // Y (+)= cx Hx X - cd Hd X - cd2 Hd2 X with tensor-core split products.
+  void apply(BseOperator &op, const Coef &c, const double *X, int64_t ldx, int64_t k, double *Y,
+             int64_t ldy, bool accumulate, cudaStream_t s);
+
+ private:
+  struct Impl;
+  Impl *impl_ = nullptr;
+};
+
+}  // namespace vgb

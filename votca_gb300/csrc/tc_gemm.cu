@@ -1,0 +1,461 @@
+// tcgen05 BF16x3 GEMM (see tc_gemm.cuh).
+#include "tc_gemm.cuh"
+
+#include <cuda_bf16.h>
+
+#include <mutex>
+
+namespace vgb {
+
+namespace {
+
+constexpr int BM = 128;
+constexpr int BK = 64;  // bf16 elements per 128-byte swizzle row
+constexpr int kThreads = 192;  // warp 0: TMA, warp 1: MMA + TMEM owner, warps 2-5: epilogue
+constexpr unsigned long long kWaitNs = 2000000000ull;  // bounded waits: 2 s
+
+template <int BN>
+struct Cfg {
+  static constexpr int A_BYTES = BM * BK * 2;            // one of hi / lo
+  static constexpr int B_BYTES = BN * BK * 2;
+  static constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
+  static constexpr int STAGES = (BN == 256) ? 2 : (BN == 128 ? 3 : 4);
+  static constexpr int TMEM_COLS = 2 * BN < 32 ? 32 : 2 * BN;  // two accumulators
+  static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+};
+
+struct KParams {
+  int64_t M, N, K;
+  int64_t nbatch, a_brows, b_brows;
+  int ksplit, kc_per;
+  int64_t mt, nt, ntiles;
+  TcEpilogue epi;
+  int *err;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ uint64_t now_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: gives up after kWaitNs or when another role aborted.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag,
+                                          int *err, int code) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = now_ns();
+  for (uint32_t it = 1;; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((it & 255) == 0) {
+      if (*abort_flag) return false;
+      if (now_ns() - t0 > kWaitNs) {
+        *abort_flag = 1;
+        atomicExch(err, code);
+        return false;
+      }
+    }
+  }
+}
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, uint64_t *bar,
+                                            int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, "
+      "%3}], [%4];" ::"r"(dst),
+      "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+// SW128 K-major shared-memory matrix descriptor (8-row core groups 1024 B apart).
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+  d |= (uint64_t)(16 >> 4) << 16;    // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;  // stride byte offset
+  d |= (uint64_t)1 << 46;            // descriptor version (tcgen05)
+  d |= (uint64_t)2 << 61;            // SWIZZLE_128B
+  return d;
+}
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+      "%12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, "
+      "%30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+struct TileCoord {
+  int64_t m, n, s, b;
+};
+__device__ __forceinline__ TileCoord decode(const KParams &p, int64_t t) {
+  TileCoord c;
+  c.m = t % p.mt;
+  t /= p.mt;
+  c.n = t % p.nt;
+  t /= p.nt;
+  c.s = t % p.ksplit;
+  c.b = t / p.ksplit;
+  return c;
+}
+
+__device__ __forceinline__ void epi_store(const TcEpilogue &e, int64_t off, float v) {
+  if (e.kind == TcEpilogue::SPLIT_BF16) {
+    const __nv_bfloat16 h = __float2bfloat16_rn(v);
+    const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
+    e.out_hi[off] = __bfloat16_as_ushort(h);
+    e.out_lo[off] = __bfloat16_as_ushort(l);
+  } else if (e.kind == TcEpilogue::STORE_F32) {
+    e.out_f32[off] = v;
+  } else {
+    double *y = e.out_f64 + off;
+    const double r = e.alpha * (double)v;
+    *y = (e.beta == 0.0) ? r : fma(e.beta, *y, r);
+  }
+}
+
+template <int BN>
+__global__ void __launch_bounds__(kThreads, 1)
+    tc_gemm_kernel(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
+                   const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo,
+                   const KParams p) {
+  using C = Cfg<BN>;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t *full = (uint64_t *)(smem + C::STAGES * C::STAGE_BYTES);
+  uint64_t *empty = full + C::STAGES;
+  uint64_t *accf = empty + C::STAGES;
+  uint64_t *acce = accf + 2;
+  uint32_t *tmem_slot = (uint32_t *)(acce + 2);
+  volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
+
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < C::STAGES; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&accf[i], 1);
+      mbar_init(&acce[i], 4);  // one arrive per epilogue warp
+    }
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"((uint32_t)C::TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+  const int kchunks = (int)(p.K / BK);
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---------------- TMA producer ----------------
+      int stage = 0;
+      uint32_t phase = 0;
+      for (int64_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
+        const TileCoord tc = decode(p, t);
+        const int kb = (int)tc.s * p.kc_per, ke = min(kchunks, kb + p.kc_per);
+        const int ya = (int)(tc.b * p.a_brows + tc.m * BM);
+        const int yb = (int)(tc.b * p.b_brows + tc.n * BN);
+        for (int kc = kb; kc < ke; ++kc) {
+          if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, p.err, 1)) goto producer_done;
+          uint8_t *st = smem + stage * C::STAGE_BYTES;
+          mbar_expect_tx(&full[stage], (uint32_t)C::STAGE_BYTES);
+          tma_load_2d(smem_u32(st), &mAhi, &full[stage], kc * BK, ya);
+          tma_load_2d(smem_u32(st + C::A_BYTES), &mAlo, &full[stage], kc * BK, ya);
+          tma_load_2d(smem_u32(st + 2 * C::A_BYTES), &mBhi, &full[stage], kc * BK, yb);
+          tma_load_2d(smem_u32(st + 2 * C::A_BYTES + C::B_BYTES), &mBlo, &full[stage], kc * BK, yb);
+          if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
+        }
+      }
+      // drain: wait until the MMA warp has consumed every stage issued (bounded)
+      for (int i = 0; i < C::STAGES; ++i) {
+        if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, p.err, 5)) break;
+        if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
+      }
+    producer_done:;
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---------------- MMA issuer ----------------
+      constexpr uint32_t idesc = (1u << 4)                   // D: FP32
+                                 | (1u << 7) | (1u << 10)     // A, B: BF16
+                                 | ((uint32_t)(BN >> 3) << 17) // N
+                                 | ((uint32_t)(BM >> 4) << 24); // M
+      int stage = 0;
+      uint32_t phase = 0;
+      int buf = 0;
+      uint32_t aphase = 0;
+      for (int64_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
+        const TileCoord tc = decode(p, t);
+        const int kb = (int)tc.s * p.kc_per, ke = min(kchunks, kb + p.kc_per);
+        if (!mbar_wait(&acce[buf], aphase ^ 1, abort_flag, p.err, 2)) break;
+        fence_after();
+        const uint32_t d_tmem = tmem_base + (uint32_t)(buf * BN);
+        bool ok = true;
+        for (int kc = kb; kc < ke; ++kc) {
+          if (!mbar_wait(&full[stage], phase, abort_flag, p.err, 3)) { ok = false; break; }
+          fence_after();
+          const uint32_t st = smem_u32(smem + stage * C::STAGE_BYTES);
+          const uint32_t ahi = st, alo = st + C::A_BYTES;
+          const uint32_t bhi = st + 2 * C::A_BYTES, blo = bhi + C::B_BYTES;
+#pragma unroll
+          for (int kk = 0; kk < BK / 16; ++kk) {
+            const uint32_t koff = kk * 32;  // 16 bf16 = 32 bytes along K inside the swizzle row
+            const uint32_t acc0 = (kc > kb || kk > 0) ? 1u : 0u;
+            mma_bf16(d_tmem, sdesc(ahi + koff), sdesc(bhi + koff), idesc, acc0);
+            mma_bf16(d_tmem, sdesc(ahi + koff), sdesc(blo + koff), idesc, 1u);
+            mma_bf16(d_tmem, sdesc(alo + koff), sdesc(bhi + koff), idesc, 1u);
+          }
+          mma_commit(&empty[stage]);  // frees the smem stage when these MMAs complete
+          if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
+        }
+        if (!ok) break;
+        mma_commit(&accf[buf]);  // accumulator ready for the epilogue
+        if (++buf == 2) { buf = 0; aphase ^= 1; }
+      }
+    }
+  } else {
+    // ---------------- epilogue warps ----------------
+    const int q = warp % 4;  // TMEM lane quarter this warp may access
+    int buf = 0;
+    uint32_t aphase = 0;
+    const TcEpilogue &e = p.epi;
+    for (int64_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
+      const TileCoord tc = decode(p, t);
+      if (!mbar_wait(&accf[buf], aphase, abort_flag, p.err, 4)) break;
+      fence_after();
+      const int64_t i = tc.m * BM + q * 32 + lane;
+      const bool row_ok = i < p.M && (i % e.rd) < e.rlim;
+      const int64_t rbase = (i / e.rd) * e.ro1 + (i % e.rd) * e.ro2 + tc.b * e.bo + tc.s * e.so;
+#pragma unroll 1
+      for (int c0 = 0; c0 < BN; c0 += 32) {
+        uint32_t r[32];
+        tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + c0), r);
+        if (row_ok) {
+          int64_t n = tc.n * BN + c0;
+          int64_t nq = n / e.cd, nr = n % e.cd;
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            if (n < p.N && nr < e.clim)
+              epi_store(e, rbase + nq * e.co1 + nr * e.co2, __uint_as_float(r[j]));
+            ++n;
+            if (++nr == e.cd) { nr = 0; ++nq; }
+          }
+        }
+      }
+      fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acce[buf]);
+      if (++buf == 2) { buf = 0; aphase ^= 1; }
+    }
+  }
+  fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base),
+                 "r"((uint32_t)C::TMEM_COLS));
+  }
+}
+
+// ---------------- helpers ----------------
+
+__global__ void split_kernel(const double *__restrict__ x, int64_t rows, int64_t cols, int64_t ldr,
+                             int64_t ldc, uint16_t *__restrict__ hi, uint16_t *__restrict__ lo,
+                             int64_t ldo) {
+  const int64_t total = rows * cols;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = t / cols, c = t % cols;
+    const double v = x[r * ldr + c * ldc];
+    const __nv_bfloat16 h = __double2bfloat16(v);
+    const __nv_bfloat16 l = __double2bfloat16(v - (double)__bfloat162float(h));
+    hi[r * ldo + c] = __bfloat16_as_ushort(h);
+    lo[r * ldo + c] = __bfloat16_as_ushort(l);
+  }
+}
+
+__global__ void reduce_partials_kernel(const float *__restrict__ part, int64_t M, int64_t N,
+                                       int ksplit, const TcEpilogue e) {
+  const int64_t total = M * N;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t / N, n = t % N;
+    if ((i % e.rd) >= e.rlim || (n % e.cd) >= e.clim) continue;
+    float acc = 0.f;
+    for (int s = 0; s < ksplit; ++s) acc += part[s * total + t];
+    const int64_t off = (i / e.rd) * e.ro1 + (i % e.rd) * e.ro2 + (n / e.cd) * e.co1 + (n % e.cd) * e.co2;
+    epi_store(e, off, acc);
+  }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    VGB_CUDA(cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q));
+    if (q != cudaDriverEntryPointSuccess || !p) fail(BSE_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+    fn = (EncodeTiledFn)p;
+  });
+  return fn;
+}
+
+void encode(CUtensorMap *m, const uint16_t *base, int64_t rows, int64_t K, int64_t ld, int box_rows) {
+  VGB_REQUIRE(((uintptr_t)base & 15) == 0, "tc operand base must be 16-byte aligned");
+  VGB_REQUIRE(K % BK == 0 && (ld * 2) % 16 == 0 && ld >= K, "tc operand K/ld not padded");
+  cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)(ld * 2)};
+  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = encode_fn()(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)base, dims, strides, box,
+                           estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) fail(BSE_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+}
+
+template <int BN>
+void launch(const TcMat &A, const TcMat &B, const KParams &p, cudaStream_t s) {
+  using C = Cfg<BN>;
+  static bool attr = false;
+  if (!attr) {
+    VGB_CUDA(cudaFuncSetAttribute(tc_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  C::SMEM));
+    attr = true;
+  }
+  const int64_t grid = std::min<int64_t>(p.ntiles, sm_count());
+  tc_gemm_kernel<BN><<<(unsigned)grid, kThreads, C::SMEM, s>>>(A.map_hi, A.map_lo, B.map_hi,
+                                                               B.map_lo, p);
+  VGB_LAUNCH_CHECK();
+}
+
+unsigned grid_1d(int64_t n) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), 16LL * 152));
+}
+
+}  // namespace
+
+TcMat make_tc_mat(const uint16_t *hi, const uint16_t *lo, int64_t rows, int64_t K, int64_t ld,
+                  int box_rows) {
+  TcMat m;
+  m.hi = hi;
+  m.lo = lo;
+  m.rows = rows;
+  m.K = K;
+  m.ld = ld;
+  m.box_rows = box_rows;
+  encode(&m.map_hi, hi, rows, K, ld, box_rows);
+  encode(&m.map_lo, lo, rows, K, ld, box_rows);
+  return m;
+}
+
+void tc_gemm(const TcMat &A, const TcMat &B, const TcShape &sh, const TcEpilogue &epi, int bn,
+             int *err, cudaStream_t s) {
+  VGB_REQUIRE(bn == 32 || bn == 64 || bn == 128 || bn == 256, "tc_gemm: unsupported tile N");
+  VGB_REQUIRE(A.box_rows == BM && B.box_rows == bn, "tc_gemm: operand boxes do not match the tile");
+  VGB_REQUIRE(sh.K % BK == 0 && A.K >= sh.K && B.K >= sh.K, "tc_gemm: K not padded to 64");
+  VGB_REQUIRE(epi.rd >= 1 && epi.cd >= 1, "tc_gemm: bad epilogue map");
+  if (sh.M <= 0 || sh.N <= 0 || sh.nbatch <= 0) return;
+  // rows addressed by the last batch must exist in the operands (TMA fills beyond with zeros,
+  // but row coordinates must stay within the int32 range of the descriptor)
+  VGB_REQUIRE((sh.nbatch - 1) * sh.a_batch_rows + sh.M <= A.rows + BM, "tc_gemm: A rows");
+  VGB_REQUIRE((sh.nbatch - 1) * sh.b_batch_rows + sh.N <= B.rows + bn, "tc_gemm: B rows");
+  VGB_REQUIRE(A.rows < (1LL << 31) && B.rows < (1LL << 31), "tc_gemm: too many rows");
+  KParams p;
+  p.M = sh.M; p.N = sh.N; p.K = sh.K;
+  p.nbatch = sh.nbatch;
+  p.a_brows = sh.a_batch_rows;
+  p.b_brows = sh.b_batch_rows;
+  const int kchunks = (int)(sh.K / BK);
+  VGB_REQUIRE(kchunks >= 1, "tc_gemm: K must be positive");
+  int ks = std::max(1, std::min(sh.ksplit, kchunks));
+  p.kc_per = (int)ceil_div(kchunks, ks);
+  p.ksplit = (int)ceil_div(kchunks, p.kc_per);
+  VGB_REQUIRE(p.ksplit == 1 || epi.kind == TcEpilogue::STORE_F32, "tc_gemm: K split needs F32 partials");
+  p.mt = ceil_div(sh.M, BM);
+  p.nt = ceil_div(sh.N, bn);
+  p.ntiles = p.mt * p.nt * p.ksplit * sh.nbatch;
+  p.epi = epi;
+  p.err = err;
+  switch (bn) {
+    case 32: launch<32>(A, B, p, s); break;
+    case 64: launch<64>(A, B, p, s); break;
+    case 128: launch<128>(A, B, p, s); break;
+    default: launch<256>(A, B, p, s); break;
+  }
+}
+
+void split_f64_to_bf16(const double *x, int64_t rows, int64_t cols, int64_t ldr, int64_t ldc,
+                       uint16_t *hi, uint16_t *lo, int64_t ldo, cudaStream_t s) {
+  if (rows <= 0 || cols <= 0) return;
+  split_kernel<<<grid_1d(rows * cols), 256, 0, s>>>(x, rows, cols, ldr, ldc, hi, lo, ldo);
+  VGB_LAUNCH_CHECK();
+}
+
+void reduce_partials(const float *partial, int64_t M, int64_t N, int ksplit, const TcEpilogue &epi,
+                     cudaStream_t s) {
+  reduce_partials_kernel<<<grid_1d(M * N), 256, 0, s>>>(partial, M, N, ksplit, epi);
+  VGB_LAUNCH_CHECK();
+}
+
+}  // namespace vgb

@@ -1,0 +1,69 @@
+// BF16x3 split-product GEMM on the 5th-generation tensor cores (tcgen05, sm_103a).
+//
+//   D[M x N] (+)= sum_K A[M x K] B[N x K]^T,  A = A_hi + A_lo, B = B_hi + B_lo
+//   computed as A_hi B_hi + A_hi B_lo + A_lo B_hi with FP32 accumulation in TMEM.
+//
+// Operands are K-major bf16 matrices (rows x K, K contiguous, K padded to a
+// multiple of 64 with zeros) loaded by TMA with the 128-byte swizzle into a
+// shared-memory ring; one elected thread issues tcgen05.mma, four epilogue
+// warps drain the (double-buffered) TMEM accumulator with tcgen05.ld and write
+// the tile through a generic index map.  The kernel is persistent: one CTA per
+// SM walks the tile list, so the epilogue of tile t overlaps the MMAs of t+1.
+#pragma once
+
+#include <cuda.h>
+
+#include "common.cuh"
+
+namespace vgb {
+
+// A K-major bf16 hi/lo operand pair: rows x K (row stride ld elements).
+struct TcMat {
+  const uint16_t *hi = nullptr, *lo = nullptr;
+  int64_t rows = 0, K = 0, ld = 0;
+  CUtensorMap map_hi, map_lo;
+  int box_rows = 0;
+};
+
+// Build the TMA descriptors of an operand; box_rows = tile rows (128 for A, BN for B).
+TcMat make_tc_mat(const uint16_t *hi, const uint16_t *lo, int64_t rows, int64_t K, int64_t ld,
+                  int box_rows);
+
+// Output index map of the epilogue.  Element (i, n) of batch b, K-split s goes to
+//   (i / rd) * ro1 + (i % rd) * ro2 + (n / cd) * co1 + (n % cd) * co2 + b * bo + s * so
+// and is written only when i < M, n < N, (i % rd) < rlim, (n % cd) < clim.
+struct TcEpilogue {
+  enum Kind { SPLIT_BF16 = 0, STORE_F32 = 1, AXPBY_F64 = 2 };
+  int kind = AXPBY_F64;
+  int64_t rd = 1, ro1 = 0, ro2 = 0, rlim = 1;
+  int64_t cd = 1, co1 = 0, co2 = 0, clim = 1;
+  int64_t bo = 0, so = 0;
+  uint16_t *out_hi = nullptr, *out_lo = nullptr;
+  float *out_f32 = nullptr;
+  double *out_f64 = nullptr;
+  double alpha = 1.0, beta = 0.0;
+};
+
+struct TcShape {
+  int64_t M = 0, N = 0, K = 0;  // K: multiple of 64
+  int64_t nbatch = 1;
+  int64_t a_batch_rows = 0, b_batch_rows = 0;  // row offset of A / B per batch
+  int ksplit = 1;                              // K split into ksplit ranges (STORE_F32 partials)
+};
+
+// Launch the persistent GEMM; bn in {32, 64, 128, 256}.  err: device int set
+// non-zero if a bounded wait inside the kernel gives up.
+void tc_gemm(const TcMat &A, const TcMat &B, const TcShape &shape, const TcEpilogue &epi, int bn,
+             int *err, cudaStream_t s);
+
+// x (FP64, rows x cols, element (r, c) at x[r * ldx_r + c * ldx_c]) -> bf16 hi/lo
+// into a rows x ldo row-major padded operand: out[r * ldo + c].
+void split_f64_to_bf16(const double *x, int64_t rows, int64_t cols, int64_t ldx_r, int64_t ldx_c,
+                       uint16_t *hi, uint16_t *lo, int64_t ldo, cudaStream_t s);
+
+// Sum ksplit FP32 partial tiles (each M x N, element (i, n) at p[s * M * N + i * N + n])
+// and apply an epilogue map (SPLIT_BF16 or AXPBY_F64) with nbatch = 1.
+void reduce_partials(const float *partial, int64_t M, int64_t N, int ksplit, const TcEpilogue &epi,
+                     cudaStream_t s);
+
+}  // namespace vgb
