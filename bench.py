@@ -236,7 +236,7 @@ def main():
     opt = bo.BSEOperator_Options(homo=V - 1, rpamin=0, qpmin=0, vmin=0, cmax=V + C - 1)
     prec_name = args.precision
     if prec_name == "auto":
-        prec_name = "fp64"
+        prec_name = "mixed"
     precision = bo.PRECISION_MIXED if prec_name == "mixed" else bo.PRECISION_FP64
     t0 = time.perf_counter()
     ctx = bo.GpuBSEContext(w, Mmn, hqp, opt, precision=precision)

@@ -505,6 +505,10 @@ void BseOperator::matmul(const Coef &c, const double *X, int64_t ldx, int64_t k,
   }
 }
 
+void BseOperator::check_errors(cudaStream_t s) {
+  if (mixed) mixed->check(s);
+}
+
 void BseOperator::diagonal(const Coef &c, double *D, cudaStream_t s) {
   VGB_REQUIRE(!(c.cd != 0 && c.cd2 != 0), "Hamiltonian cannot contain Hd and Hd2 at the same time");
   DiagArgs a;

@@ -69,6 +69,8 @@ struct DeviceOperator {
   virtual void apply(const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy,
                      cudaStream_t s) = 0;
   virtual void diagonal(double *D, cudaStream_t s) = 0;
+  // raise if an asynchronous device-side failure was recorded (synchronises)
+  virtual void check(cudaStream_t) {}
 };
 
 class MixedEngine;  // tensor-core contractions (tc_engine.cu)
@@ -101,6 +103,7 @@ class BseOperator {
   void matmul(const Coef &c, const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy,
               cudaStream_t s);
   void diagonal(const Coef &c, double *D, cudaStream_t s);
+  void check_errors(cudaStream_t s);
   // [[A, B], [-B, -A]] X, X and Y (2 dim) x k
   void ham_matmul(const Coef &a, const Coef &b, const double *X, int64_t ldx, int64_t k, double *Y,
                   int64_t ldy, cudaStream_t s);
@@ -129,6 +132,7 @@ struct BseApply : DeviceOperator {
     op->matmul(coef, X, ldx, k, Y, ldy, s);
   }
   void diagonal(double *D, cudaStream_t s) override { op->diagonal(coef, D, s); }
+  void check(cudaStream_t s) override { op->check_errors(s); }
 };
 
 struct BseHamApply : DeviceOperator {
@@ -141,6 +145,7 @@ struct BseHamApply : DeviceOperator {
     op->ham_matmul(a, b, X, ldx, k, Y, ldy, s);
   }
   void diagonal(double *D, cudaStream_t s) override;
+  void check(cudaStream_t s) override { op->check_errors(s); }
 };
 
 // Dense FP64 symmetric operator(s): A, optionally B for [[A, B], [-B, -A]].

@@ -158,6 +158,7 @@ int bse_op_matmul(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd, int32_t cd
     VGB_CUDA(cudaMemcpy2DAsync(Y, ldy * sizeof(double), h->dY.get(), n * sizeof(double),
                                n * sizeof(double), k, cudaMemcpyDeviceToHost, s));
     VGB_CUDA(cudaStreamSynchronize(s));
+    if (h->kind == 0) h->bse->check_errors(s);
   });
 }
 
@@ -209,6 +210,7 @@ int bse_ham_matmul(bse_handle *h, const int32_t a_coef[4], const int32_t b_coef[
     VGB_CUDA(cudaMemcpy2DAsync(Y, ldy * sizeof(double), h->dY.get(), n * sizeof(double),
                                n * sizeof(double), k, cudaMemcpyDeviceToHost, s));
     VGB_CUDA(cudaStreamSynchronize(s));
+    if (h->kind == 0) h->bse->check_errors(s);
   });
 }
 

@@ -326,6 +326,7 @@ void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_option
     A.apply(X, n, k, Y, n, s);
     VGB_CUDA(cudaEventRecord(ev1, s));
     VGB_CUDA(cudaEventSynchronize(ev1));
+    A.check(s);
     float ms = 0.f;
     VGB_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
     matvec_ms += ms;

@@ -1,20 +1,276 @@
-// Mixed-precision engine (placeholder until the tcgen05 kernels land).
+// Mixed-precision engine of the BSE product: every contraction over the
+// auxiliary index (Hx, Hd, Hd2) as BF16x3 split products on tcgen05 tensor
+// cores with FP32 accumulation; the operator's FP64 input X is split into
+// bf16 hi/lo once per call and the results are accumulated into the FP64
+// output.  Hqp is applied in FP64 by the caller.
+//
+// Padded layouts (Kc = ct rounded up to 64, Kg = naux*vt rounded up to 64,
+// Kn = naux rounded up to 64, pair index I' = v*Kc + c, dimP = vt*Kc):
+//   Xs   [(j, v)][Kc]          X split                        (A of Hd/Hd2 stage 1, B of Hx 1)
+//   Mcc2 [(P, c1)][Kc]         M(c1, c, P)                    (B of Hd stage 1, batched over P)
+//   G2   [v1][Kg]              G(v1, P, v) (screened vv)      (B of Hd stage 2)
+//   Bvc2 [P][dimP] == [(P, v1)][Kc]  M(v, c, P)               (A of Hx 1, B of Hd2 stage 1)
+//   BvcT [I'][Kn]              M(v, c, P)                     (A of Hx 2)
+//   McvT [c1][Kg]              screened M(c1, v, P)           (A of Hd2 stage 2)
+//   S    [(j, c1)][Kg]         sum_c M(c1,c,P) X_j(v,c)       (Hd intermediate)
+//   U    [(j, v1)][Kg]         sum_c X_j(v,c) M(v1,c,P)       (Hd2 intermediate)
+//   Zs   [j][Kn]               sum_I M(I,P) X_j(I)            (Hx intermediate)
 #include "tc_engine.cuh"
+
+#include "tc_gemm.cuh"
 
 namespace vgb {
 
-struct MixedEngine::Impl {};
+namespace {
+
+int64_t pad64(int64_t x) { return ceil_div(x, 64) * 64; }
+
+struct SplitBuf {
+  DeviceBuffer<uint16_t> hi, lo;
+  int64_t rows = 0, ld = 0;
+  // (re)allocate rows x ld zero-filled
+  void ensure(int64_t r, int64_t l, cudaStream_t s) {
+    if (r * l > (int64_t)hi.count || !hi.get()) {
+      hi.resize(r * l);
+      lo.resize(r * l);
+      VGB_CUDA(cudaMemsetAsync(hi.get(), 0, r * l * sizeof(uint16_t), s));
+      VGB_CUDA(cudaMemsetAsync(lo.get(), 0, r * l * sizeof(uint16_t), s));
+    }
+    rows = r;
+    ld = l;
+  }
+};
+
+int pick_bn(int64_t N) {
+  if (N > 128) return 256;
+  if (N > 64) return 128;
+  if (N > 32) return 64;
+  return 32;
+}
+
+// K splits so that the tile count covers the SMs about twice
+int pick_ksplit(int64_t tiles, int64_t K) {
+  const int64_t target = 2LL * sm_count();
+  if (tiles >= target) return 1;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(target, tiles), K / 64 / 4));
+}
+
+}  // namespace
+
+struct MixedEngine::Impl {
+  int64_t vt = 0, ct = 0, naux = 0, dim = 0;
+  int64_t Kc = 0, Kg = 0, Kn = 0, dimP = 0;
+  SplitBuf Mcc2, G2, Bvc2, BvcT, McvT;
+  SplitBuf Xs, S, U, Zs;
+  DeviceBuffer<float> part;
+  DeviceBuffer<int> err;
+  int64_t s_budget_bytes = 4LL << 30;
+};
 
 MixedEngine::MixedEngine() : impl_(new Impl()) {}
 MixedEngine::~MixedEngine() { delete impl_; }
 
-void MixedEngine::stage(BseOperator &, cudaStream_t) {
-  fail(BSE_ERR_UNSUPPORTED, "mixed precision is not available in this build");
+void MixedEngine::stage(BseOperator &op, cudaStream_t s) {
+  Impl &m = *impl_;
+  m.vt = op.vt;
+  m.ct = op.ct;
+  m.naux = op.naux;
+  m.dim = op.dim;
+  m.Kc = pad64(op.ct);
+  m.Kg = pad64(op.naux * op.vt);
+  m.Kn = pad64(op.naux);
+  m.dimP = op.vt * m.Kc;
+  const int64_t vt = m.vt, ct = m.ct, naux = m.naux, dim = m.dim;
+  m.err.resize(1);
+  VGB_CUDA(cudaMemsetAsync(m.err.get(), 0, sizeof(int), s));
+  {  // Mcc2[(P, c1)][c] = Mcc[P*ct*ct + c*ct + c1]
+    m.Mcc2.ensure(naux * ct, m.Kc, s);
+    SplitMap sm;
+    sm.rdiv = ct; sm.rs1 = ct * ct; sm.rs2 = 1; sm.cs = ct; sm.rlim = ct;
+    split_f64_to_bf16(op.Mcc.get(), naux * ct, ct, sm, m.Mcc2.hi.get(), m.Mcc2.lo.get(), m.Kc, s);
+  }
+  {  // G2[v1][(P, v)] = Gvv[v1*naux*vt + P*vt + v]
+    m.G2.ensure(vt, m.Kg, s);
+    SplitMap sm;
+    sm.rdiv = vt; sm.rs1 = 0; sm.rs2 = naux * vt; sm.cs = 1; sm.rlim = vt;
+    split_f64_to_bf16(op.Gvv.get(), vt, naux * vt, sm, m.G2.hi.get(), m.G2.lo.get(), m.Kg, s);
+  }
+  {  // Bvc2[(P, v)][c] = Bvc[P*dim + v*ct + c]
+    m.Bvc2.ensure(naux * vt, m.Kc, s);
+    SplitMap sm;
+    sm.rdiv = vt; sm.rs1 = dim; sm.rs2 = ct; sm.cs = 1; sm.rlim = vt;
+    split_f64_to_bf16(op.Bvc.get(), naux * vt, ct, sm, m.Bvc2.hi.get(), m.Bvc2.lo.get(), m.Kc, s);
+  }
+  {  // BvcT[(v, c')][P] = Bvc[P*dim + v*ct + c'] for c' < ct
+    m.BvcT.ensure(m.dimP, m.Kn, s);
+    SplitMap sm;
+    sm.rdiv = m.Kc; sm.rs1 = ct; sm.rs2 = 1; sm.cs = dim; sm.rlim = ct;
+    split_f64_to_bf16(op.Bvc.get(), m.dimP, naux, sm, m.BvcT.hi.get(), m.BvcT.lo.get(), m.Kn, s);
+  }
+  {  // McvT[c1][(P, v)] = Mcv[(P*vt + v)*ct + c1]
+    m.McvT.ensure(ct, m.Kg, s);
+    SplitMap sm;
+    sm.rdiv = ct; sm.rs1 = 0; sm.rs2 = 1; sm.cs = ct; sm.rlim = ct;
+    split_f64_to_bf16(op.Mcv.get(), ct, naux * vt, sm, m.McvT.hi.get(), m.McvT.lo.get(), m.Kg, s);
+  }
+  VGB_CUDA(cudaStreamSynchronize(s));
 }
 
-void MixedEngine::apply(BseOperator &, const Coef &, const double *, int64_t, int64_t, double *,
-                        int64_t, bool, cudaStream_t) {
-  fail(BSE_ERR_UNSUPPORTED, "mixed precision is not available in this build");
+void MixedEngine::check(cudaStream_t s) {
+  int h = 0;
+  VGB_CUDA(cudaMemcpyAsync(&h, impl_->err.get(), sizeof(int), cudaMemcpyDeviceToHost, s));
+  VGB_CUDA(cudaStreamSynchronize(s));
+  if (h != 0) {
+    VGB_CUDA(cudaMemsetAsync(impl_->err.get(), 0, sizeof(int), s));
+    fail(BSE_ERR_TIMEOUT, "tensor-core GEMM: a bounded pipeline wait gave up (code " +
+                              std::to_string(h) + ")");
+  }
+}
+
+void MixedEngine::apply(BseOperator &op, const Coef &c, const double *X, int64_t ldx, int64_t k,
+                        double *Y, int64_t ldy, bool accumulate, cudaStream_t s) {
+  Impl &m = *impl_;
+  const int64_t vt = m.vt, ct = m.ct, naux = m.naux;
+  int *err = m.err.get();
+  bool acc = accumulate;
+  // X -> Xs[(j, v)][c]
+  op.timer.begin(STAGE_TC_SPLIT, s);
+  m.Xs.ensure(k * vt, m.Kc, s);
+  {
+    SplitMap sm;
+    sm.rdiv = vt; sm.rs1 = ldx; sm.rs2 = ct; sm.cs = 1; sm.rlim = vt;
+    split_f64_to_bf16(X, k * vt, ct, sm, m.Xs.hi.get(), m.Xs.lo.get(), m.Kc, s);
+  }
+  op.timer.end(STAGE_TC_SPLIT, s);
+
+  if (c.cx != 0) {
+    op.timer.begin(STAGE_TC_HX, s);
+    // Z[P][j] = sum_I' Bvc2[P][I'] Xs[j][I']
+    TcMat A = make_tc_mat(m.Bvc2.hi.get(), m.Bvc2.lo.get(), naux, m.dimP, m.dimP, 128);
+    const int bn = pick_bn(k);
+    TcMat B = make_tc_mat(m.Xs.hi.get(), m.Xs.lo.get(), k, m.dimP, m.dimP, bn);
+    TcShape sh;
+    sh.M = naux; sh.N = k; sh.K = m.dimP;
+    sh.ksplit = pick_ksplit(ceil_div(naux, 128) * ceil_div(k, bn), m.dimP);
+    m.part.resize((size_t)sh.ksplit * naux * k);
+    TcEpilogue e;
+    e.kind = TcEpilogue::STORE_F32;
+    e.rd = naux; e.ro2 = k; e.rlim = naux;
+    e.cd = k; e.co2 = 1; e.clim = k;
+    e.so = naux * k;
+    e.out_f32 = m.part.get();
+    const int ks = tc_gemm(A, B, sh, e, bn, err, s);
+    m.Zs.ensure(k, m.Kn, s);
+    TcEpilogue r;
+    r.kind = TcEpilogue::SPLIT_BF16;
+    r.rd = naux; r.ro2 = 1; r.rlim = naux;
+    r.cd = k; r.co2 = m.Kn; r.clim = k;
+    r.out_hi = m.Zs.hi.get(); r.out_lo = m.Zs.lo.get();
+    reduce_partials(m.part.get(), naux, k, ks, r, s);
+    // Y(I, j) (+)= cx sum_P BvcT[I'][P] Zs[j][P]
+    TcMat A2 = make_tc_mat(m.BvcT.hi.get(), m.BvcT.lo.get(), m.dimP, m.Kn, m.Kn, 128);
+    TcMat B2 = make_tc_mat(m.Zs.hi.get(), m.Zs.lo.get(), k, m.Kn, m.Kn, bn);
+    TcShape sh2;
+    sh2.M = m.dimP; sh2.N = k; sh2.K = m.Kn;
+    TcEpilogue e2;
+    e2.kind = TcEpilogue::AXPBY_F64;
+    e2.rd = m.Kc; e2.ro1 = ct; e2.ro2 = 1; e2.rlim = ct;
+    e2.cd = k; e2.co2 = ldy; e2.clim = k;
+    e2.out_f64 = Y; e2.alpha = c.cx; e2.beta = acc ? 1.0 : 0.0;
+    tc_gemm(A2, B2, sh2, e2, bn, err, s);
+    acc = true;
+    op.timer.end(STAGE_TC_HX, s);
+  }
+
+  if (c.cd != 0 || c.cd2 != 0) {
+    const bool hd = c.cd != 0;
+    const double alpha = hd ? -(double)c.cd : -(double)c.cd2;
+    op.timer.begin(hd ? STAGE_TC_HD : STAGE_TC_HD2, s);
+    // vectors per chunk so that the intermediate stays within the budget
+    const int64_t per_vec = (hd ? ct : vt) * m.Kg * 4;
+    const int64_t jc = std::max<int64_t>(1, std::min<int64_t>(k, m.s_budget_bytes / per_vec));
+    SplitBuf &T = hd ? m.S : m.U;
+    T.ensure(jc * (hd ? ct : vt), m.Kg, s);
+    for (int64_t j0 = 0; j0 < k; j0 += jc) {
+      const int64_t kc = std::min(jc, k - j0);
+      const uint16_t *xh = m.Xs.hi.get() + j0 * vt * m.Kc, *xl = m.Xs.lo.get() + j0 * vt * m.Kc;
+      TcMat Xa = make_tc_mat(xh, xl, kc * vt, m.Kc, m.Kc, 128);
+      if (hd) {
+        // stage 1: S[(j, c1)][(P, v)] = sum_c Xs[(j, v)][c] Mcc2[(P, c1)][c]   (batched over P)
+        const int bn = pick_bn(ct);
+        TcMat Bm = make_tc_mat(m.Mcc2.hi.get(), m.Mcc2.lo.get(), naux * ct, m.Kc, m.Kc, bn);
+        TcShape sh;
+        sh.M = kc * vt; sh.N = ct; sh.K = m.Kc;
+        sh.nbatch = naux; sh.a_batch_rows = 0; sh.b_batch_rows = ct;
+        TcEpilogue e;
+        e.kind = TcEpilogue::SPLIT_BF16;
+        e.rd = vt; e.ro1 = ct * m.Kg; e.ro2 = 1; e.rlim = vt;
+        e.cd = ct; e.co1 = 0; e.co2 = m.Kg; e.clim = ct;
+        e.bo = vt;
+        e.out_hi = T.hi.get(); e.out_lo = T.lo.get();
+        tc_gemm(Xa, Bm, sh, e, bn, err, s);
+        // stage 2: Y_j(c1, v1) += alpha sum_{(P,v)} S[(j, c1)][(P,v)] G2[v1][(P,v)]
+        const int bn2 = pick_bn(vt);
+        TcMat As = make_tc_mat(T.hi.get(), T.lo.get(), kc * ct, m.Kg, m.Kg, 128);
+        TcMat Bg = make_tc_mat(m.G2.hi.get(), m.G2.lo.get(), vt, m.Kg, m.Kg, bn2);
+        TcShape s2;
+        s2.M = kc * ct; s2.N = vt; s2.K = m.Kg;
+        s2.ksplit = pick_ksplit(ceil_div(kc * ct, 128) * ceil_div(vt, bn2), m.Kg);
+        m.part.resize((size_t)s2.ksplit * s2.M * s2.N);
+        TcEpilogue p;
+        p.kind = TcEpilogue::STORE_F32;
+        p.rd = s2.M; p.ro2 = s2.N; p.rlim = s2.M;
+        p.cd = s2.N; p.co2 = 1; p.clim = s2.N;
+        p.so = s2.M * s2.N;
+        p.out_f32 = m.part.get();
+        const int ks = tc_gemm(As, Bg, s2, p, bn2, err, s);
+        TcEpilogue r;
+        r.kind = TcEpilogue::AXPBY_F64;
+        r.rd = ct; r.ro1 = ldy; r.ro2 = 1; r.rlim = ct;
+        r.cd = vt; r.co2 = ct; r.clim = vt;
+        r.out_f64 = Y + j0 * ldy; r.alpha = alpha; r.beta = acc ? 1.0 : 0.0;
+        reduce_partials(m.part.get(), s2.M, s2.N, ks, r, s);
+      } else {
+        // stage 1: U[(j, v1)][(P, v)] = sum_c Xs[(j, v)][c] Bvc2[(P, v1)][c]
+        const int bn = pick_bn(naux * vt);
+        TcMat Bm = make_tc_mat(m.Bvc2.hi.get(), m.Bvc2.lo.get(), naux * vt, m.Kc, m.Kc, bn);
+        TcShape sh;
+        sh.M = kc * vt; sh.N = naux * vt; sh.K = m.Kc;
+        TcEpilogue e;
+        e.kind = TcEpilogue::SPLIT_BF16;
+        e.rd = vt; e.ro1 = vt * m.Kg; e.ro2 = 1; e.rlim = vt;
+        e.cd = vt; e.co1 = vt; e.co2 = m.Kg; e.clim = vt;
+        e.out_hi = T.hi.get(); e.out_lo = T.lo.get();
+        tc_gemm(Xa, Bm, sh, e, bn, err, s);
+        // stage 2: Y_j(c1, v1) += alpha sum_{(P,v)} McvT[c1][(P,v)] U[(j, v1)][(P,v)]
+        const int bn2 = pick_bn(kc * vt);
+        TcMat Am = make_tc_mat(m.McvT.hi.get(), m.McvT.lo.get(), ct, m.Kg, m.Kg, 128);
+        TcMat Bu = make_tc_mat(T.hi.get(), T.lo.get(), kc * vt, m.Kg, m.Kg, bn2);
+        TcShape s2;
+        s2.M = ct; s2.N = kc * vt; s2.K = m.Kg;
+        s2.ksplit = pick_ksplit(ceil_div(ct, 128) * ceil_div(kc * vt, bn2), m.Kg);
+        m.part.resize((size_t)s2.ksplit * s2.M * s2.N);
+        TcEpilogue p;
+        p.kind = TcEpilogue::STORE_F32;
+        p.rd = s2.M; p.ro2 = s2.N; p.rlim = s2.M;
+        p.cd = s2.N; p.co2 = 1; p.clim = s2.N;
+        p.so = s2.M * s2.N;
+        p.out_f32 = m.part.get();
+        const int ks = tc_gemm(Am, Bu, s2, p, bn2, err, s);
+        TcEpilogue r;
+        r.kind = TcEpilogue::AXPBY_F64;
+        r.rd = ct; r.ro2 = 1; r.rlim = ct;
+        r.cd = vt; r.co1 = ldy; r.co2 = ct; r.clim = vt;
+        r.out_f64 = Y + j0 * ldy; r.alpha = alpha; r.beta = acc ? 1.0 : 0.0;
+        reduce_partials(m.part.get(), s2.M, s2.N, ks, r, s);
+      }
+    }
+    acc = true;
+    op.timer.end(hd ? STAGE_TC_HD : STAGE_TC_HD2, s);
+  }
+  if (!acc) {
+    VGB_CUDA(cudaMemset2DAsync(Y, ldy * sizeof(double), 0, op.dim * sizeof(double), k, s));
+  }
 }
 
 }  // namespace vgb

@@ -14,6 +14,8 @@ class MixedEngine {
   // Y (+)= cx Hx X - cd Hd X - cd2 Hd2 X with tensor-core split products.
   void apply(BseOperator &op, const Coef &c, const double *X, int64_t ldx, int64_t k, double *Y,
              int64_t ldy, bool accumulate, cudaStream_t s);
+  // Synchronise and raise if a kernel reported a bounded-wait timeout.
+  void check(cudaStream_t s);
 
  private:
   struct Impl;

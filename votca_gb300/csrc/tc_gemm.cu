@@ -314,14 +314,16 @@ __global__ void __launch_bounds__(kThreads, 1)
 
 // ---------------- helpers ----------------
 
-__global__ void split_kernel(const double *__restrict__ x, int64_t rows, int64_t cols, int64_t ldr,
-                             int64_t ldc, uint16_t *__restrict__ hi, uint16_t *__restrict__ lo,
+__global__ void split_kernel(const double *__restrict__ x, int64_t rows, int64_t cols,
+                             const SplitMap m, uint16_t *__restrict__ hi, uint16_t *__restrict__ lo,
                              int64_t ldo) {
   const int64_t total = rows * cols;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
        t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = t / cols, c = t % cols;
-    const double v = x[r * ldr + c * ldc];
+    const int64_t rq = r / m.rdiv, rr = r % m.rdiv;
+    if (rr >= m.rlim) continue;
+    const double v = x[rq * m.rs1 + rr * m.rs2 + c * m.cs];
     const __nv_bfloat16 h = __double2bfloat16(v);
     const __nv_bfloat16 l = __double2bfloat16(v - (double)__bfloat162float(h));
     hi[r * ldo + c] = __bfloat16_as_ushort(h);
@@ -409,13 +411,13 @@ TcMat make_tc_mat(const uint16_t *hi, const uint16_t *lo, int64_t rows, int64_t 
   return m;
 }
 
-void tc_gemm(const TcMat &A, const TcMat &B, const TcShape &sh, const TcEpilogue &epi, int bn,
-             int *err, cudaStream_t s) {
+int tc_gemm(const TcMat &A, const TcMat &B, const TcShape &sh, const TcEpilogue &epi, int bn,
+            int *err, cudaStream_t s) {
   VGB_REQUIRE(bn == 32 || bn == 64 || bn == 128 || bn == 256, "tc_gemm: unsupported tile N");
   VGB_REQUIRE(A.box_rows == BM && B.box_rows == bn, "tc_gemm: operand boxes do not match the tile");
   VGB_REQUIRE(sh.K % BK == 0 && A.K >= sh.K && B.K >= sh.K, "tc_gemm: K not padded to 64");
   VGB_REQUIRE(epi.rd >= 1 && epi.cd >= 1, "tc_gemm: bad epilogue map");
-  if (sh.M <= 0 || sh.N <= 0 || sh.nbatch <= 0) return;
+  if (sh.M <= 0 || sh.N <= 0 || sh.nbatch <= 0) return 0;
   // rows addressed by the last batch must exist in the operands (TMA fills beyond with zeros,
   // but row coordinates must stay within the int32 range of the descriptor)
   VGB_REQUIRE((sh.nbatch - 1) * sh.a_batch_rows + sh.M <= A.rows + BM, "tc_gemm: A rows");
@@ -443,12 +445,14 @@ void tc_gemm(const TcMat &A, const TcMat &B, const TcShape &sh, const TcEpilogue
     case 128: launch<128>(A, B, p, s); break;
     default: launch<256>(A, B, p, s); break;
   }
+  return p.ksplit;
 }
 
-void split_f64_to_bf16(const double *x, int64_t rows, int64_t cols, int64_t ldr, int64_t ldc,
-                       uint16_t *hi, uint16_t *lo, int64_t ldo, cudaStream_t s) {
+void split_f64_to_bf16(const double *x, int64_t rows, int64_t cols, const SplitMap &m, uint16_t *hi,
+                       uint16_t *lo, int64_t ldo, cudaStream_t s) {
   if (rows <= 0 || cols <= 0) return;
-  split_kernel<<<grid_1d(rows * cols), 256, 0, s>>>(x, rows, cols, ldr, ldc, hi, lo, ldo);
+  VGB_REQUIRE(m.rdiv >= 1, "split: bad row map");
+  split_kernel<<<grid_1d(rows * cols), 256, 0, s>>>(x, rows, cols, m, hi, lo, ldo);
   VGB_LAUNCH_CHECK();
 }
 

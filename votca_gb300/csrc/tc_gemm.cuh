@@ -52,14 +52,20 @@ struct TcShape {
 };
 
 // Launch the persistent GEMM; bn in {32, 64, 128, 256}.  err: device int set
-// non-zero if a bounded wait inside the kernel gives up.
-void tc_gemm(const TcMat &A, const TcMat &B, const TcShape &shape, const TcEpilogue &epi, int bn,
+// non-zero if a bounded wait inside the kernel gives up.  Returns the number of
+// K splits actually used (partials written for STORE_F32).
+int tc_gemm(const TcMat &A, const TcMat &B, const TcShape &shape, const TcEpilogue &epi, int bn,
              int *err, cudaStream_t s);
 
-// x (FP64, rows x cols, element (r, c) at x[r * ldx_r + c * ldx_c]) -> bf16 hi/lo
-// into a rows x ldo row-major padded operand: out[r * ldo + c].
-void split_f64_to_bf16(const double *x, int64_t rows, int64_t cols, int64_t ldx_r, int64_t ldx_c,
-                       uint16_t *hi, uint16_t *lo, int64_t ldo, cudaStream_t s);
+// FP64 -> bf16 hi/lo split into a row-major padded operand out[r * ldo + c] for
+// r < rows, c < cols; the source element (r, c) is
+//   x[(r / rdiv) * rs1 + (r % rdiv) * rs2 + c * cs]
+// and rows with (r % rdiv) >= rlim are skipped (left as they are: zero padding).
+struct SplitMap {
+  int64_t rdiv = 1, rs1 = 0, rs2 = 0, cs = 1, rlim = 1;
+};
+void split_f64_to_bf16(const double *x, int64_t rows, int64_t cols, const SplitMap &m, uint16_t *hi,
+                       uint16_t *lo, int64_t ldo, cudaStream_t s);
 
 // Sum ksplit FP32 partial tiles (each M x N, element (i, n) at p[s * M * N + i * N + n])
 // and apply an epilogue map (SPLIT_BF16 or AXPBY_F64) with nbatch = 1.
