@@ -115,6 +115,25 @@ int bse_op_matmul_device(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd,
                          int32_t cd2, const double *dX, int64_t ldx, int64_t k,
                          double *dY, int64_t ldy, void *stream);
 
+/* Allocation-free variant of bse_op_matmul_device.  It has no counterpart in
+ * the reference.  It is for callers that cannot call cudaMalloc when they need
+ * a product: code running while another component owns the device memory
+ * through its own pool and forbids runtime allocations, or code that must not
+ * take the device-wide synchronisation an allocation can cause inside a
+ * pipelined solve.  The product is computed in FP64 (whatever precision the
+ * handle was created with) with every temporary taken from one static 64 MiB
+ * device array that each GPU loading this library holds until process exit;
+ * no cudaMalloc, cudaFree or allocating library call is made.  Limits: a
+ * request with Naux*k above 7 Mi doubles (Hx) or one column above 7 Mi doubles
+ * of intermediate (Naux*v*c for Hd, Naux*v*v for Hd2) is rejected with
+ * BSE_ERR_ARGUMENT.  The first call on a device looks up the array's device
+ * address; make it before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU race, so serialise them on one stream. */
+int bse_op_matmul_device_noalloc(bse_handle *h, int32_t cqp, int32_t cx,
+                                 int32_t cd, int32_t cd2, const double *dX,
+                                 int64_t ldx, int64_t k, double *dY,
+                                 int64_t ldy, void *stream);
+
 /* D = diagonal of H(cqp,cx,cd,cd2), host pointer of length size.
  * Replaces BSE_OPERATOR::diagonal (bse_operator.cc:133-175). */
 int bse_op_diagonal(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd,

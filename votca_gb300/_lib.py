@@ -48,6 +48,8 @@ SIGNATURES = {
     "bse_op_size": (c_i32, [c_vp, ctypes.POINTER(c_i64)]),
     "bse_op_matmul": (c_i32, [c_vp, c_i32, c_i32, c_i32, c_i32, c_dp, c_i64, c_i64, c_dp, c_i64]),
     "bse_op_matmul_device": (c_i32, [c_vp, c_i32, c_i32, c_i32, c_i32, c_vp, c_i64, c_i64, c_vp, c_i64, c_vp]),
+    "bse_op_matmul_device_noalloc": (c_i32, [c_vp, c_i32, c_i32, c_i32, c_i32, c_vp, c_i64, c_i64, c_vp, c_i64,
+                                             c_vp]),
     "bse_op_diagonal": (c_i32, [c_vp, c_i32, c_i32, c_i32, c_i32, c_dp]),
     "bse_op_diagonal_device": (c_i32, [c_vp, c_i32, c_i32, c_i32, c_i32, c_vp, c_vp]),
     "bse_ham_matmul": (c_i32, [c_vp, ctypes.POINTER(c_i32), ctypes.POINTER(c_i32), c_dp, c_i64, c_i64, c_dp,

@@ -180,4 +180,8 @@ void ham_combine(const double *TA, const double *TB, int64_t dim, int64_t k, dou
 // D2 = [D; -D]
 void ham_diag(const double *D, int64_t dim, double *D2, cudaStream_t s);
 
+// FP64 product with every temporary in a static device array (noalloc.cu).
+void matmul_noalloc(BseOperator &op, const Coef &c, const double *X, int64_t ldx, int64_t k,
+                    double *Y, int64_t ldy, cudaStream_t s);
+
 }  // namespace vgb

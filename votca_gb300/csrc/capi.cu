@@ -138,6 +138,16 @@ int bse_op_matmul_device(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd, int
   });
 }
 
+int bse_op_matmul_device_noalloc(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd,
+                                 int32_t cd2, const double *dX, int64_t ldx, int64_t k,
+                                 double *dY, int64_t ldy, void *stream) {
+  return guarded([&] {
+    require_handle(h);
+    VGB_REQUIRE(h->kind == 0, "bse_op_matmul_device_noalloc: not a BSE operator");
+    vgb::matmul_noalloc(*h->bse, coef(cqp, cx, cd, cd2), dX, ldx, k, dY, ldy, (cudaStream_t)stream);
+  });
+}
+
 int bse_op_matmul(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd, int32_t cd2,
                   const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy) {
   return guarded([&] {

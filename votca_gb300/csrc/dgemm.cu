@@ -194,4 +194,42 @@ void dgemm(const GemmDesc &d, cudaStream_t stream, GemmWorkspace *ws, int splitk
   }
 }
 
+void dgemm_prealloc(const GemmDesc &d, cudaStream_t stream, double *ws, int64_t ws_count) {
+  VGB_REQUIRE(d.M >= 0 && d.N >= 0 && d.K >= 0, "dgemm: negative size");
+  const int64_t nbatch = d.nb1 * d.nb2;
+  if (d.M == 0 || d.N == 0 || nbatch == 0) return;
+  if (d.K == 0) {
+    const int64_t total = d.M * d.N * nbatch;
+    scale_kernel<<<(unsigned)std::min<int64_t>(ceil_div(total, 256), 65535), 256, 0, stream>>>(d, nbatch);
+    VGB_LAUNCH_CHECK();
+    return;
+  }
+  Grid g;
+  g.mt = ceil_div(d.M, TM);
+  g.nt = ceil_div(d.N, TN);
+  g.nbatch = nbatch;
+  const int64_t tiles = g.mt * g.nt * nbatch;
+  int64_t splits = 1;
+  const int64_t target = 3LL * sm_count();
+  if (ws && tiles < target && d.K > 4 * TK) {
+    splits = std::min<int64_t>(ceil_div(target, tiles), ceil_div(d.K, 8 * TK));
+    splits = std::max<int64_t>(1, std::min<int64_t>(splits, 256));
+    const int64_t fit = ws_count / std::max<int64_t>(1, nbatch * d.M * d.N);
+    splits = std::max<int64_t>(1, std::min(splits, fit));
+  }
+  g.kchunk = ceil_div(ceil_div(d.K, splits), TK) * TK;
+  g.splits = ceil_div(d.K, g.kchunk);
+  const int64_t blocks = tiles * g.splits;
+  VGB_REQUIRE(blocks < (1LL << 31), "dgemm: grid too large");
+  dgemm_kernel<<<(unsigned)blocks, THREADS, 0, stream>>>(d, g, g.splits > 1 ? ws : nullptr,
+                                                          (d.a_rs == 1) ? 1 : 0, (d.b_rs == 1) ? 1 : 0);
+  VGB_LAUNCH_CHECK();
+  if (g.splits > 1) {
+    const int64_t total = d.M * d.N * nbatch;
+    splitk_reduce_kernel<<<(unsigned)std::min<int64_t>(ceil_div(total, 256), 8 * sm_count()), 256, 0,
+                           stream>>>(d, g, ws);
+    VGB_LAUNCH_CHECK();
+  }
+}
+
 }  // namespace vgb

@@ -54,4 +54,9 @@ struct GemmWorkspace {
 // Launch.  splitk = 0 picks a split so that the grid covers the GPU.
 void dgemm(const GemmDesc &d, cudaStream_t stream, GemmWorkspace *ws, int splitk = 0);
 
+// Same kernels with caller-owned split-K scratch of ws_count doubles: the K
+// split is reduced until its partials fit (no split when ws is null).  Never
+// allocates.
+void dgemm_prealloc(const GemmDesc &d, cudaStream_t stream, double *ws, int64_t ws_count);
+
 }  // namespace vgb
