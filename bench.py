@@ -206,6 +206,7 @@ def main():
     ap.add_argument("--no-roots", action="store_true", help="skip the time-to-roots solves")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--small", action="store_true", help="C0-sized workload (for profiling captures)")
+    ap.add_argument("--shape", default=None, help="v,c,naux,nmo override (profiling captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -226,7 +227,9 @@ def main():
     global V, C, NAUX, NMO, WORKLOAD
     if args.small:
         V, C, NAUX, NMO = 8, 64, 256, 72
-        WORKLOAD = f"tda_singlet_v{V}_c{C}_naux{NAUX}_k{K}"
+    if args.shape:
+        V, C, NAUX, NMO = (int(x) for x in args.shape.split(","))
+    WORKLOAD = f"tda_singlet_v{V}_c{C}_naux{NAUX}_k{K}"
     L = _lib.load()
     seed = 1  # every replica solves the same seeded problem
     mmn = make_mmn(seed, NAUX, NMO)
@@ -277,9 +280,9 @@ def main():
     clk = clocks.stop()
     import ctypes
 
-    stage_ms = (ctypes.c_double * 10)()
-    stage_calls = (ctypes.c_int64 * 10)()
-    _lib.check(L.bse_op_profile_read(ctx.handle, stage_ms, stage_calls, 10))
+    stage_ms = (ctypes.c_double * 12)()
+    stage_calls = (ctypes.c_int64 * 12)()
+    _lib.check(L.bse_op_profile_read(ctx.handle, stage_ms, stage_calls, 12))
     _lib.check(L.bse_op_profile(ctx.handle, 0))
     if world > 1:
         t = torch.tensor([ms], device="cuda")
@@ -331,18 +334,21 @@ def main():
                     "peak_source": "measured in-run: FP64 FMA register loop (bse_probe_fp64_tflops)",
                     "traffic": None}
     else:
-        st = 6
+        st = 6  # BSE_STAGE_TC_HD: the c-contraction GEMM of Hd on the tensor cores
         per_launch_ms = stage_ms[st] / max(1, stage_calls[st])
         launches_per_step = stage_calls[st] / max(1, args.steps)
-        achieved = 2.0 * NAUX * V * C * (V + C) * K / launches_per_step / (per_launch_ms * 1e-3) / 1e12
+        achieved = hd_stage_a_flops(V, C, NAUX, K) / launches_per_step / (per_launch_ms * 1e-3) / 1e12
         pk = peaks.get("bf16_tflops")
-        roofline = {"bound": "tensor", "kernel": "tcgen05 BF16x3 Hd", "achieved": achieved,
-                    "peak": pk / 3.0 if pk else None, "unit": "TFLOP/s (FP64-equivalent, 3 BF16 products each)",
-                    "frac": achieved / (pk / 3.0) if pk else None,
-                    "peak_source": "MEASURED_PEAKS.json bf16_tflops / 3 (of measured)", "traffic": None}
+        nprod = 4 if os.environ.get("VGB_TC_PRODUCTS") == "4" else 3
+        roofline = {"bound": "tensor",
+                    "kernel": "tc_gemm_kernel<256> (Hd c-contraction, tcgen05 BF16 split products)",
+                    "achieved": achieved, "peak": pk / nprod if pk else None,
+                    "unit": f"TFLOP/s (FP64-equivalent; {nprod} BF16 products per term)",
+                    "frac": achieved / (pk / nprod) if pk else None,
+                    "peak_source": f"MEASURED_PEAKS.json bf16_tflops / {nprod} (of measured)", "traffic": None}
     stages = {name: {"ms_per_step": stage_ms[i] / args.steps, "launches_per_step": stage_calls[i] / args.steps}
               for i, name in enumerate(["hqp", "hx", "hd_a", "hd_b", "hd2_a", "hd2_b", "tc_hd", "tc_hx",
-                                        "tc_hd2", "tc_split"]) if stage_calls[i]}
+                                        "tc_hd2", "tc_split", "tc_hd_b", "tc_hd2_b"]) if stage_calls[i]}
     gpu_launches = None
     try:
         gpu_launches = int(sum(stage_calls) / args.steps * args.steps)

@@ -92,6 +92,31 @@ int bse_op_create_dense_screening(const bse_mmn_desc *mmn,
                                   const bse_options *opt, int32_t precision,
                                   bse_handle **out);
 
+/* ---- Screening that feeds Hd (FP64 on the device) ---- */
+
+/* Static RPA dielectric matrix, RPA::calculate_epsilon_r
+ * (xtp/src/libxtp/gwbse/rpa.cc:145-200): eps = 1 - 2 sum_{m occ} M_m^T diag(chi_m) M_m
+ * with M_m = Mmn_[m].bottomRows(n_unocc) and the reference's chi at complex
+ * frequency (freq_re, freq_im), eta = 1e-4.  rpa_energies: rpamax - rpamin + 1
+ * values.  epsilon: auxsize x auxsize column-major (host). */
+int bse_rpa_epsilon(const bse_mmn_desc *mmn, const double *const *mmn_slices,
+                    const double *rpa_energies, int64_t rpatotal, int64_t homo,
+                    int64_t rpamin, int64_t rpamax, double freq_re,
+                    double freq_im, double *epsilon);
+
+/* Ainv = A^-1 for a symmetric positive definite A (blocked Cholesky on the
+ * device).  With A = eps this is the dense screening for
+ * bse_op_create_dense_screening; it replaces the host eigen-decomposition in
+ * BSE::SetupDirectInteractionOperator (xtp/src/libxtp/gwbse/bse.cc:188-204),
+ * whose rotated-diagonal screening is mathematically the same operator. */
+int bse_cholesky_inverse(int64_t n, const double *A, int64_t lda, double *Ainv,
+                         int64_t ldi);
+
+/* TCMatrix_gwbse::MultiplyRightWithAuxMatrix (xtp/src/libxtp/threecenter.cc:54-65):
+ * every slice M[m] <- M[m] * U (U auxsize x auxsize), in place on the host slices. */
+int bse_mmn_multiply_right(const bse_mmn_desc *mmn, double *const *mmn_slices,
+                           const double *U, int64_t ldu);
+
 /* A dense FP64 symmetric matrix as an operator (the reference tests'
  * HermitianBlockOperator, test_davidson.cc:265-281).  b may be NULL; when
  * given, bse_ham_* use [[a, b], [-b, -a]]. */
@@ -197,7 +222,9 @@ enum {
   BSE_STAGE_TC_HX = 7,
   BSE_STAGE_TC_HD2 = 8,
   BSE_STAGE_TC_SPLIT = 9,
-  BSE_STAGE_COUNT = 10
+  BSE_STAGE_TC_HD_B = 10,
+  BSE_STAGE_TC_HD2_B = 11,
+  BSE_STAGE_COUNT = 12
 };
 
 /* enable != 0: record CUDA events around every stage of the product on its
@@ -211,6 +238,24 @@ int bse_op_profile_read(bse_handle *h, double *stage_ms, int64_t *stage_calls,
 /* Measured FP64 FMA throughput of the current device (TFLOP/s) from a short
  * register-resident FMA loop: the roofline denominator of the FP64 path. */
 int bse_probe_fp64_tflops(double *tflops);
+
+/* ---- Adjoint (no counterpart in the reference; its forward twin is the
+ * expectation-value analysis x^T H_part x of xtp/src/libxtp/gwbse/bse.cc:490-520) ----
+ *
+ * Hellmann-Feynman gradient of sum_k weights[k] * Omega_k for normalised
+ * eigenvectors X (column-major dim x nroots, ldx) of the TDA operator
+ * H(cqp, cx, cd, 0):
+ *   grad_mmn:       same layout as the Mmn slices given to bse_op_create
+ *                   (msize x nsize x auxsize, slices back to back); entries
+ *                   outside the BSE window are zero;
+ *   grad_hqp:       (vt+ct) x (vt+ct) column-major gradient of the Hqp window;
+ *   grad_screening: auxsize (diagonal epsilon_0_inv) or auxsize^2 (dense W).
+ * Any output may be NULL.  Computed in FP64 on the device. */
+int bse_op_eig_gradient(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd,
+                        int32_t cd2, const double *X, int64_t ldx,
+                        int64_t nroots, const double *weights,
+                        double *grad_mmn, double *grad_hqp,
+                        double *grad_screening);
 
 /* Thread-local text of the last error on this thread ("" if none). */
 const char *bse_last_error(void);

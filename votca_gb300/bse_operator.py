@@ -99,6 +99,8 @@ class GpuBSEContext:
             _lib.check(L.bse_op_create_dense_screening(ctypes.byref(desc), ptrs, _p(W), _p(hqp), hqp.shape[0],
                                                        hqp.shape[0], ctypes.byref(o), precision, ctypes.byref(h)))
         else:
+            if epsilon_0_inv is None:
+                raise _lib.BSEError(1, "GpuBSEContext: epsilon_0_inv or dense_screening is required")
             w = np.ascontiguousarray(epsilon_0_inv, dtype=np.float64)
             _lib.check(L.bse_op_create(ctypes.byref(desc), ptrs, _p(w), _p(hqp), hqp.shape[0], hqp.shape[0],
                                        ctypes.byref(o), precision, ctypes.byref(h)))

@@ -1,0 +1,208 @@
+// Hellmann-Feynman adjoint of the TDA BSE eigenvalues.
+//
+// For normalised eigenvectors x_k of A = cqp Hqp + cx Hx - cd Hd, every
+// parameter derivative of Omega_k = x_k^T A x_k is x_k^T (dA) x_k; the kernel
+// returns the weighted sum  sum_k g_k dOmega_k/dtheta  (what a reverse-mode
+// backward pass needs) for the Mmn blocks, the Hqp window and the screening.
+// With X_k the v x c matrix of root k (I = ct v + c):
+//   Hqp:  dH(vt+c, vt+c') = cqp sum_k g_k sum_v X_k[v][c] X_k[v][c']
+//         dH(v, v')       = -cqp sum_k g_k sum_c X_k[v'][c] X_k[v][c]
+//   Hx:   dM(v,c,P)       = 2 cx sum_k g_k z_k[P] X_k[v][c],   z_k[P] = sum_I M(I,P) X_k[I]
+//   Hd:   S_k^P[v'][c]    = sum_c' M(c,c',P) X_k[v'][c']          (the forward stage-1 product)
+//         Q^P[v][v']      = sum_k g_k sum_c X_k[v][c] S_k^P[v'][c]
+//         dM(v,v',P)      = -cd sum_Q W_QP Q^Q[v][v']             (diagonal W: -cd w_P Q^P)
+//         dW_PQ           = -cd sum_{vv'} Q^P[v][v'] M(v,v',Q)    (diagonal: dw_P = -cd <Q^P, M_vv^P>)
+//         dM(c,c',P)      = -cd sum_k g_k sum_v X_k[v][c] (G^P X_k)[v][c'],  G^P = screened vv block
+// The forward analogue in the reference is the expectation-value analysis
+// x^T H_part x (xtp/src/libxtp/gwbse/bse.cc:490-520, 565-606).
+#include <vector>
+
+#include "bse_ops.cuh"
+
+namespace vgb {
+
+namespace {
+
+unsigned gfor(int64_t n) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), 16LL * 152));
+}
+
+__global__ void scale_cols_by_kernel(double *Z, int64_t ld, int64_t rows, int64_t ncols,
+                                     const double *g) {
+  const int64_t total = rows * ncols;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x)
+    Z[(t % rows) + ld * (t / rows)] *= g[t / rows];
+}
+
+// gH: (vt+ct)^2 column-major window gradient of Hqp
+__global__ void hqp_grad_kernel(const double *X, int64_t ldx, int64_t nr, const double *g,
+                                int64_t vt, int64_t ct, double cqp, double *gH) {
+  const int64_t n = vt + ct, total = n * n;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = t % n, col = t / n;
+    double acc = 0.0;
+    if (r >= vt && col >= vt) {  // (vt+c, vt+c')
+      const int64_t c = r - vt, c2 = col - vt;
+      for (int64_t k = 0; k < nr; ++k) {
+        const double *x = X + k * ldx;
+        double s = 0.0;
+        for (int64_t v = 0; v < vt; ++v) s += x[v * ct + c] * x[v * ct + c2];
+        acc += g[k] * s;
+      }
+      acc *= cqp;
+    } else if (r < vt && col < vt) {  // (v, v')
+      for (int64_t k = 0; k < nr; ++k) {
+        const double *x = X + k * ldx;
+        double s = 0.0;
+        for (int64_t c = 0; c < ct; ++c) s += x[col * ct + c] * x[r * ct + c];
+        acc += g[k] * s;
+      }
+      acc *= -cqp;
+    }
+    gH[t] = acc;
+  }
+}
+
+// gw[P] = alpha * sum_{vv'} Q[P][v][v'] Mvv[P][v][v']
+__global__ void dot_per_batch_kernel(const double *Q, const double *M, int64_t nb, int64_t len,
+                                     double alpha, double *out) {
+  for (int64_t b = blockIdx.x; b < nb; b += gridDim.x) {
+    double s = 0.0;
+    for (int64_t i = threadIdx.x; i < len; i += blockDim.x) s += Q[b * len + i] * M[b * len + i];
+    __shared__ double red[256];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+      if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[b] = alpha * red[0];
+    __syncthreads();
+  }
+}
+
+// gMvv[P][...] = alpha * w[P] * Q[P][...]
+__global__ void scale_batches_kernel(const double *Q, const double *w, int64_t nb, int64_t len,
+                                     double alpha, double *out) {
+  const int64_t total = nb * len;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x)
+    out[t] = alpha * w[t / len] * Q[t];
+}
+
+}  // namespace
+
+void BseOperator::eig_gradient(const Coef &c, const double *X, int64_t ldx, int64_t nr,
+                               const double *g_host, double *gMvc, double *gMvv, double *gMcc,
+                               double *gH, double *gW, cudaStream_t s) {
+  VGB_REQUIRE(c.cd2 == 0, "eig_gradient: the Hd2 (coupling block) adjoint is not available");
+  VGB_REQUIRE(nr >= 1 && ldx >= dim, "eig_gradient: bad eigenvector block");
+  DeviceBuffer<double> g(nr);
+  VGB_CUDA(cudaMemcpyAsync(g.get(), g_host, nr * sizeof(double), cudaMemcpyHostToDevice, s));
+  if (gH) {
+    hqp_grad_kernel<<<gfor((vt + ct) * (vt + ct)), 256, 0, s>>>(X, ldx, nr, g.get(), vt, ct, c.cqp, gH);
+    VGB_LAUNCH_CHECK();
+  }
+  if (gMvc) {
+    VGB_CUDA(cudaMemsetAsync(gMvc, 0, naux * dim * sizeof(double), s));
+    if (c.cx != 0) {
+      DeviceBuffer<double> Zb(naux * nr);
+      GemmDesc z;  // Z (naux x nr) = Bvc^T X
+      z.M = naux; z.N = nr; z.K = dim;
+      z.A = Bvc.get(); z.a_rs = dim; z.a_cs = 1;
+      z.B = X; z.b_rs = 1; z.b_cs = ldx;
+      z.C = Zb.get(); z.c_rs = 1; z.c_cs = naux;
+      dgemm(z, s, &ws);
+      scale_cols_by_kernel<<<gfor(naux * nr), 256, 0, s>>>(Zb.get(), naux, naux, nr, g.get());
+      VGB_LAUNCH_CHECK();
+      GemmDesc o;  // gMvc[P][I] = 2 cx sum_k Zg[P][k] X[I][k]
+      o.M = naux; o.N = dim; o.K = nr;
+      o.A = Zb.get(); o.a_rs = 1; o.a_cs = naux;
+      o.B = X; o.b_rs = ldx; o.b_cs = 1;
+      o.C = gMvc; o.c_rs = dim; o.c_cs = 1;
+      o.alpha = 2.0 * c.cx;
+      dgemm(o, s, &ws);
+    }
+  }
+  const bool need_hd = c.cd != 0 && (gMvv || gMcc || gW);
+  if (!need_hd) {
+    if (gMvv) VGB_CUDA(cudaMemsetAsync(gMvv, 0, naux * vt * vt * sizeof(double), s));
+    if (gMcc) VGB_CUDA(cudaMemsetAsync(gMcc, 0, naux * ct * ct * sizeof(double), s));
+    if (gW) VGB_CUDA(cudaMemsetAsync(gW, 0, (dense_screening ? naux * naux : naux) * sizeof(double), s));
+    VGB_CUDA(cudaStreamSynchronize(s));
+    return;
+  }
+  const double cd = c.cd;
+  DeviceBuffer<double> Sk(naux * dim), Q(naux * vt * vt);
+  // ---- Q^P = sum_k g_k X_k S_k^P^T ----
+  std::vector<double> gh(g_host, g_host + nr);
+  for (int64_t k = 0; k < nr; ++k) {
+    GemmDesc a;  // S_k[P](c1, v) = sum_c Mcc_P(c1, c) X_k(c, v)
+    a.M = ct; a.N = vt; a.K = ct;
+    a.A = Mcc.get(); a.a_rs = 1; a.a_cs = ct;
+    a.B = X + k * ldx; a.b_rs = 1; a.b_cs = ct;
+    a.C = Sk.get(); a.c_rs = 1; a.c_cs = ct;
+    a.nb1 = naux; a.a_b1 = ct * ct; a.c_b1 = dim;
+    dgemm(a, s, &ws);
+    GemmDesc q;  // Q[P](v, v') += g_k sum_c X_k(v, c) S_k[P](c, v')
+    q.M = vt; q.N = vt; q.K = ct;
+    q.A = X + k * ldx; q.a_rs = ct; q.a_cs = 1;
+    q.B = Sk.get(); q.b_rs = 1; q.b_cs = ct; q.b_b1 = dim;
+    q.C = Q.get(); q.c_rs = vt; q.c_cs = 1; q.c_b1 = vt * vt;
+    q.nb1 = naux; q.alpha = gh[k]; q.beta = k > 0 ? 1.0 : 0.0;
+    dgemm(q, s, &ws);
+  }
+  if (gMvv) {
+    if (!dense_screening) {
+      scale_batches_kernel<<<gfor(naux * vt * vt), 256, 0, s>>>(Q.get(), Wscr.get(), naux, vt * vt, -cd, gMvv);
+      VGB_LAUNCH_CHECK();
+    } else {
+      GemmDesc d;  // gMvv[Q][e] = -cd sum_P W[P][Q] Q[P][e]
+      d.M = naux; d.N = vt * vt; d.K = naux;
+      d.A = Wscr.get(); d.a_rs = naux; d.a_cs = 1;
+      d.B = Q.get(); d.b_rs = vt * vt; d.b_cs = 1;
+      d.C = gMvv; d.c_rs = vt * vt; d.c_cs = 1;
+      d.alpha = -cd;
+      dgemm(d, s, &ws);
+    }
+  }
+  if (gW) {
+    if (!dense_screening) {
+      dot_per_batch_kernel<<<(unsigned)std::min<int64_t>(naux, 4096), 256, 0, s>>>(Q.get(), Mvv.get(), naux,
+                                                                                vt * vt, -cd, gW);
+      VGB_LAUNCH_CHECK();
+    } else {
+      GemmDesc d;  // gW[P][Q] = -cd sum_e Q[P][e] Mvv[Q][e]   (column-major naux x naux)
+      d.M = naux; d.N = naux; d.K = vt * vt;
+      d.A = Q.get(); d.a_rs = vt * vt; d.a_cs = 1;
+      d.B = Mvv.get(); d.b_rs = 1; d.b_cs = vt * vt;
+      d.C = gW; d.c_rs = 1; d.c_cs = naux;
+      d.alpha = -cd;
+      dgemm(d, s, &ws);
+    }
+  }
+  if (gMcc) {
+    // gMcc[P][c][c'] = -cd sum_k g_k sum_v X_k(v, c) T_k[P](v, c'),  T_k[P] = G^P X_k
+    for (int64_t k = 0; k < nr; ++k) {
+      GemmDesc t;  // T[P](v, c') = sum_v' Gvv[v][P][v'] X_k(v', c')
+      t.M = vt; t.N = ct; t.K = vt;
+      t.A = Gvv.get(); t.a_rs = naux * vt; t.a_cs = 1; t.a_b1 = vt;
+      t.B = X + k * ldx; t.b_rs = ct; t.b_cs = 1;
+      t.C = Sk.get(); t.c_rs = ct; t.c_cs = 1; t.c_b1 = dim;
+      t.nb1 = naux;
+      dgemm(t, s, &ws);
+      GemmDesc r;  // gMcc[P](c, c') (+)= -cd g_k sum_v X_k(v, c) T[P](v, c')
+      r.M = ct; r.N = ct; r.K = vt;
+      r.A = X + k * ldx; r.a_rs = 1; r.a_cs = ct;
+      r.B = Sk.get(); r.b_rs = ct; r.b_cs = 1; r.b_b1 = dim;
+      r.C = gMcc; r.c_rs = ct; r.c_cs = 1; r.c_b1 = ct * ct;
+      r.nb1 = naux; r.alpha = -cd * gh[k]; r.beta = k > 0 ? 1.0 : 0.0;
+      dgemm(r, s, &ws);
+    }
+  }
+  VGB_CUDA(cudaStreamSynchronize(s));
+}
+
+}  // namespace vgb

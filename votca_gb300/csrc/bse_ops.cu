@@ -240,6 +240,26 @@ void StageTimer::read(double *ms, int64_t *calls, int n) {
   }
 }
 
+// Mvv[(P*vt + v1)*vt + v] = M(v1, v, P): the vv block before screening (for gradients).
+void BseOperator::stage_unscreened_vv(const bse_mmn_desc &desc, const double *const *slices,
+                                      const bse_options &opt, cudaStream_t s) {
+  msize = desc.mmax - desc.mmin + 1;
+  nsize = desc.nmax - desc.nmin + 1;
+  m_v0 = opt.vmin - desc.mmin;
+  m_c0 = opt.homo + 1 - desc.mmin;
+  n_v0 = opt.vmin - desc.nmin;
+  n_c0 = opt.homo + 1 - desc.nmin;
+  std::vector<double> h(naux * vt * vt);
+  for (int64_t v1 = 0; v1 < vt; ++v1) {
+    const double *src = slices[m_v0 + v1];
+    for (int64_t P = 0; P < naux; ++P)
+      for (int64_t v = 0; v < vt; ++v) h[(P * vt + v1) * vt + v] = src[P * nsize + n_v0 + v];
+  }
+  Mvv.resize(naux * vt * vt);
+  VGB_CUDA(cudaMemcpyAsync(Mvv.get(), h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+  VGB_CUDA(cudaStreamSynchronize(s));
+}
+
 BseOperator::BseOperator() = default;
 BseOperator::~BseOperator() = default;
 
@@ -348,6 +368,12 @@ void BseOperator::stage(const bse_mmn_desc &desc, const double *const *slices, c
   }
   dvv_from_gvv_kernel<<<grid_for(naux * vt), 256, 0, s>>>(Gvv.get(), naux, vt, dvv.get());
   VGB_LAUNCH_CHECK();
+  VGB_CUDA(cudaStreamSynchronize(s));
+  stage_unscreened_vv(desc, slices, opt, s);
+  dense_screening = dense_w;
+  Wscr.resize(dense_w ? naux * naux : naux);
+  VGB_CUDA(cudaMemcpyAsync(Wscr.get(), w, (dense_w ? naux * naux : naux) * sizeof(double),
+                           cudaMemcpyHostToDevice, s));
 
   // Hqp window (BSE_OPERATOR::Hqp_row, bse_operator.cc:121-131)
   std::vector<double> hcc(ct * ct), hvv(vt * vt);

@@ -37,7 +37,9 @@ enum Stage {
   STAGE_TC_HX = 7,
   STAGE_TC_HD2 = 8,
   STAGE_TC_SPLIT = 9,
-  STAGE_COUNT = 10
+  STAGE_TC_HD_B = 10,  // tensor-core Hd stage 2 (+ partial reduction)
+  STAGE_TC_HD2_B = 11,
+  STAGE_COUNT = 12
 };
 
 class StageTimer {
@@ -83,6 +85,11 @@ class BseOperator {
 
   // FP64 staged blocks (layouts documented in bse_ops.cu)
   DeviceBuffer<double> Bvc, Mcc, Gvv, Mcv, dcc, dvv, Hcc, Hvv;
+  // unscreened vv block [P][v1][v] and the screening (naux, or naux x naux when dense)
+  DeviceBuffer<double> Mvv, Wscr;
+  bool dense_screening = false;
+  // index window of the staged blocks inside the caller's Mmn
+  int64_t m_v0 = 0, m_c0 = 0, n_v0 = 0, n_c0 = 0, msize = 0, nsize = 0;
   // scratch
   DeviceBuffer<double> S, Z, Xc, Ttmp;
   GemmWorkspace ws;
@@ -104,6 +111,14 @@ class BseOperator {
               cudaStream_t s);
   void diagonal(const Coef &c, double *D, cudaStream_t s);
   void check_errors(cudaStream_t s);
+  void stage_unscreened_vv(const bse_mmn_desc &desc, const double *const *slices,
+                           const bse_options &opt, cudaStream_t s);
+  // Hellmann-Feynman gradients of sum_k g_k Omega_k (adjoint.cu); outputs are device
+  // buffers: gM* in the block layouts below, gH = Hqp window gradient ((vt+ct)^2),
+  // gW = screening gradient (naux, or naux^2 when dense).
+  void eig_gradient(const Coef &c, const double *X, int64_t ldx, int64_t nr, const double *g_host,
+                    double *gMvc, double *gMvv, double *gMcc, double *gH, double *gW,
+                    cudaStream_t s);
   // [[A, B], [-B, -A]] X, X and Y (2 dim) x k
   void ham_matmul(const Coef &a, const Coef &b, const double *X, int64_t ldx, int64_t k, double *Y,
                   int64_t ldy, cudaStream_t s);

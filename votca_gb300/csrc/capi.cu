@@ -1,5 +1,7 @@
 // C ABI of the library (declarations and reference mapping: include/votca_gb300_bse.h).
+#include <algorithm>
 #include <cstring>
+#include <vector>
 #include <memory>
 #include <string>
 
@@ -267,6 +269,90 @@ int bse_davidson_solve(bse_handle *h, const int32_t a_coef[4], const int32_t b_c
       result->seconds_matvec = o.seconds_matvec;
       result->seconds_total = o.seconds_total;
     }
+  });
+}
+
+int bse_op_eig_gradient(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd, int32_t cd2,
+                        const double *X, int64_t ldx, int64_t nroots, const double *weights,
+                        double *grad_mmn, double *grad_hqp, double *grad_screening) {
+  return guarded([&] {
+    require_handle(h);
+    VGB_REQUIRE(h->kind == 0, "bse_op_eig_gradient: not a BSE operator");
+    VGB_REQUIRE(X && weights && nroots >= 1, "bse_op_eig_gradient: null eigenvectors or weights");
+    vgb::BseOperator &op = *h->bse;
+    VGB_REQUIRE(ldx >= op.dim, "bse_op_eig_gradient: ldx smaller than the operator size");
+    cudaStream_t s = h->stream;
+    const int64_t vt = op.vt, ct = op.ct, naux = op.naux, dim = op.dim;
+    vgb::DeviceBuffer<double> dX(dim * nroots), gMvc, gMvv, gMcc, gH, gW;
+    VGB_CUDA(cudaMemcpy2DAsync(dX.get(), dim * sizeof(double), X, ldx * sizeof(double),
+                               dim * sizeof(double), nroots, cudaMemcpyHostToDevice, s));
+    if (grad_mmn) {
+      gMvc.resize(naux * dim);
+      gMvv.resize(naux * vt * vt);
+      gMcc.resize(naux * ct * ct);
+    }
+    const int64_t nh = (vt + ct) * (vt + ct);
+    const int64_t nw = op.dense_screening ? naux * naux : naux;
+    if (grad_hqp) gH.resize(nh);
+    if (grad_screening) gW.resize(nw);
+    op.eig_gradient(coef(cqp, cx, cd, cd2), dX.get(), dim, nroots, weights, gMvc.get(), gMvv.get(),
+                    gMcc.get(), gH.get(), gW.get(), s);
+    if (grad_hqp) VGB_CUDA(cudaMemcpy(grad_hqp, gH.get(), nh * sizeof(double), cudaMemcpyDeviceToHost));
+    if (grad_screening)
+      VGB_CUDA(cudaMemcpy(grad_screening, gW.get(), nw * sizeof(double), cudaMemcpyDeviceToHost));
+    if (grad_mmn) {
+      std::vector<double> a(naux * dim), b(naux * vt * vt), c(naux * ct * ct);
+      VGB_CUDA(cudaMemcpy(a.data(), gMvc.get(), a.size() * sizeof(double), cudaMemcpyDeviceToHost));
+      VGB_CUDA(cudaMemcpy(b.data(), gMvv.get(), b.size() * sizeof(double), cudaMemcpyDeviceToHost));
+      VGB_CUDA(cudaMemcpy(c.data(), gMcc.get(), c.size() * sizeof(double), cudaMemcpyDeviceToHost));
+      const int64_t nsz = op.nsize;
+      std::fill(grad_mmn, grad_mmn + op.msize * naux * nsz, 0.0);
+      auto at = [&](int64_t m, int64_t P, int64_t n) -> double & { return grad_mmn[(m * naux + P) * nsz + n]; };
+      for (int64_t P = 0; P < naux; ++P) {
+        for (int64_t v = 0; v < vt; ++v) {
+          for (int64_t cc = 0; cc < ct; ++cc) at(op.m_v0 + v, P, op.n_c0 + cc) += a[P * dim + v * ct + cc];
+          for (int64_t v2 = 0; v2 < vt; ++v2) at(op.m_v0 + v, P, op.n_v0 + v2) += b[(P * vt + v) * vt + v2];
+        }
+        for (int64_t c1 = 0; c1 < ct; ++c1)
+          for (int64_t c2 = 0; c2 < ct; ++c2) at(op.m_c0 + c1, P, op.n_c0 + c2) += c[(P * ct + c1) * ct + c2];
+      }
+    }
+  });
+}
+
+namespace {
+struct TmpStream {
+  cudaStream_t s = nullptr;
+  TmpStream() { VGB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)); }
+  ~TmpStream() { if (s) cudaStreamDestroy(s); }
+};
+}  // namespace
+
+int bse_rpa_epsilon(const bse_mmn_desc *mmn, const double *const *mmn_slices,
+                    const double *rpa_energies, int64_t rpatotal, int64_t homo, int64_t rpamin,
+                    int64_t rpamax, double freq_re, double freq_im, double *epsilon) {
+  return guarded([&] {
+    VGB_REQUIRE(mmn && mmn_slices && rpa_energies && epsilon, "bse_rpa_epsilon: null argument");
+    TmpStream ts;
+    vgb::rpa_epsilon(*mmn, mmn_slices, rpa_energies, rpatotal, homo, rpamin, rpamax, freq_re, freq_im,
+                     1e-4, epsilon, ts.s);
+  });
+}
+
+int bse_cholesky_inverse(int64_t n, const double *A, int64_t lda, double *Ainv, int64_t ldi) {
+  return guarded([&] {
+    VGB_REQUIRE(A && Ainv, "bse_cholesky_inverse: null matrix");
+    TmpStream ts;
+    vgb::cholesky_inverse(n, A, lda, Ainv, ldi, ts.s);
+  });
+}
+
+int bse_mmn_multiply_right(const bse_mmn_desc *mmn, double *const *mmn_slices, const double *U,
+                           int64_t ldu) {
+  return guarded([&] {
+    VGB_REQUIRE(mmn && mmn_slices && U, "bse_mmn_multiply_right: null argument");
+    TmpStream ts;
+    vgb::mmn_multiply_right(*mmn, mmn_slices, U, ldu, ts.s);
   });
 }
 

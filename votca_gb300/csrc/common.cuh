@@ -73,4 +73,13 @@ int sm_count();
 // Measured FP64 FMA throughput of the current device in TFLOP/s.
 double probe_fp64_tflops();
 
+// Screening (screening.cu)
+void rpa_epsilon(const bse_mmn_desc &desc, const double *const *slices, const double *energies,
+                 int64_t rpatotal, int64_t homo, int64_t rpamin, int64_t rpamax, double wr, double wi,
+                 double eta, double *eps_host, cudaStream_t s);
+void cholesky_inverse(int64_t n, const double *a_host, int64_t lda, double *inv_host, int64_t ldi,
+                      cudaStream_t s);
+void mmn_multiply_right(const bse_mmn_desc &desc, double *const *slices, const double *U_host,
+                        int64_t ldu, cudaStream_t s);
+
 }  // namespace vgb

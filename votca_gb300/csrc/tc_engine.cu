@@ -17,6 +17,8 @@
 //   Zs   [j][Kn]               sum_I M(I,P) X_j(I)            (Hx intermediate)
 #include "tc_engine.cuh"
 
+#include <cstdlib>
+
 #include "tc_gemm.cuh"
 
 namespace vgb {
@@ -41,6 +43,9 @@ struct SplitBuf {
   }
 };
 
+int g_bk256 = 32;  // K box of the BN = 256 tiles (4-stage ring); 64 gives a 2-stage ring
+int bk_for(int bn) { return bn == 256 ? g_bk256 : 64; }
+
 int pick_bn(int64_t N) {
   if (N > 128) return 256;
   if (N > 64) return 128;
@@ -48,11 +53,25 @@ int pick_bn(int64_t N) {
   return 32;
 }
 
-// K splits so that the tile count covers the SMs about twice
+// K splits: enough to cover the SMs about twice, and enough that no FP32
+// accumulation chain in TMEM is longer than max_chain (the partial sums are
+// reduced in FP64).
+int64_t g_max_chain = 1024;
+int g_products = 3;
 int pick_ksplit(int64_t tiles, int64_t K) {
   const int64_t target = 2LL * sm_count();
-  if (tiles >= target) return 1;
-  return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(target, tiles), K / 64 / 4));
+  int64_t ks = 1;
+  if (tiles < target) ks = std::max<int64_t>(1, std::min<int64_t>(ceil_div(target, tiles), K / 64 / 4));
+  ks = std::max<int64_t>(ks, ceil_div(K, g_max_chain));
+  return (int)std::min<int64_t>(ks, std::max<int64_t>(1, K / 64));
+}
+void read_tuning() {
+  static bool done = false;
+  if (done) return;
+  done = true;
+  if (const char *e = getenv("VGB_TC_MAX_CHAIN")) g_max_chain = std::max(64LL, atoll(e));
+  if (const char *e = getenv("VGB_TC_PRODUCTS")) g_products = atoi(e) == 4 ? 4 : 3;
+  if (const char *e = getenv("VGB_TC_BK256")) g_bk256 = atoi(e) == 64 ? 64 : 32;
 }
 
 }  // namespace
@@ -130,6 +149,7 @@ void MixedEngine::check(cudaStream_t s) {
 void MixedEngine::apply(BseOperator &op, const Coef &c, const double *X, int64_t ldx, int64_t k,
                         double *Y, int64_t ldy, bool accumulate, cudaStream_t s) {
   Impl &m = *impl_;
+  read_tuning();
   const int64_t vt = m.vt, ct = m.ct, naux = m.naux;
   int *err = m.err.get();
   bool acc = accumulate;
@@ -146,11 +166,11 @@ void MixedEngine::apply(BseOperator &op, const Coef &c, const double *X, int64_t
   if (c.cx != 0) {
     op.timer.begin(STAGE_TC_HX, s);
     // Z[P][j] = sum_I' Bvc2[P][I'] Xs[j][I']
-    TcMat A = make_tc_mat(m.Bvc2.hi.get(), m.Bvc2.lo.get(), naux, m.dimP, m.dimP, 128);
     const int bn = pick_bn(k);
-    TcMat B = make_tc_mat(m.Xs.hi.get(), m.Xs.lo.get(), k, m.dimP, m.dimP, bn);
+    TcMat A = make_tc_mat(m.Bvc2.hi.get(), m.Bvc2.lo.get(), naux, m.dimP, m.dimP, 128, bk_for(bn));
+    TcMat B = make_tc_mat(m.Xs.hi.get(), m.Xs.lo.get(), k, m.dimP, m.dimP, bn, bk_for(bn));
     TcShape sh;
-    sh.M = naux; sh.N = k; sh.K = m.dimP;
+    sh.M = naux; sh.N = k; sh.K = m.dimP; sh.products = g_products;
     sh.ksplit = pick_ksplit(ceil_div(naux, 128) * ceil_div(k, bn), m.dimP);
     m.part.resize((size_t)sh.ksplit * naux * k);
     TcEpilogue e;
@@ -168,10 +188,11 @@ void MixedEngine::apply(BseOperator &op, const Coef &c, const double *X, int64_t
     r.out_hi = m.Zs.hi.get(); r.out_lo = m.Zs.lo.get();
     reduce_partials(m.part.get(), naux, k, ks, r, s);
     // Y(I, j) (+)= cx sum_P BvcT[I'][P] Zs[j][P]
-    TcMat A2 = make_tc_mat(m.BvcT.hi.get(), m.BvcT.lo.get(), m.dimP, m.Kn, m.Kn, 128);
-    TcMat B2 = make_tc_mat(m.Zs.hi.get(), m.Zs.lo.get(), k, m.Kn, m.Kn, bn);
+    TcMat A2 = make_tc_mat(m.BvcT.hi.get(), m.BvcT.lo.get(), m.dimP, m.Kn, m.Kn, 128, bk_for(bn));
+    TcMat B2 = make_tc_mat(m.Zs.hi.get(), m.Zs.lo.get(), k, m.Kn, m.Kn, bn, bk_for(bn));
     TcShape sh2;
-    sh2.M = m.dimP; sh2.N = k; sh2.K = m.Kn;
+    sh2.M = m.dimP; sh2.N = k; sh2.K = m.Kn; sh2.products = g_products;
+    sh2.ksplit = 1;
     TcEpilogue e2;
     e2.kind = TcEpilogue::AXPBY_F64;
     e2.rd = m.Kc; e2.ro1 = ct; e2.ro2 = 1; e2.rlim = ct;
@@ -194,13 +215,13 @@ void MixedEngine::apply(BseOperator &op, const Coef &c, const double *X, int64_t
     for (int64_t j0 = 0; j0 < k; j0 += jc) {
       const int64_t kc = std::min(jc, k - j0);
       const uint16_t *xh = m.Xs.hi.get() + j0 * vt * m.Kc, *xl = m.Xs.lo.get() + j0 * vt * m.Kc;
-      TcMat Xa = make_tc_mat(xh, xl, kc * vt, m.Kc, m.Kc, 128);
       if (hd) {
         // stage 1: S[(j, c1)][(P, v)] = sum_c Xs[(j, v)][c] Mcc2[(P, c1)][c]   (batched over P)
         const int bn = pick_bn(ct);
-        TcMat Bm = make_tc_mat(m.Mcc2.hi.get(), m.Mcc2.lo.get(), naux * ct, m.Kc, m.Kc, bn);
+        TcMat Xa = make_tc_mat(xh, xl, kc * vt, m.Kc, m.Kc, 128, bk_for(bn));
+        TcMat Bm = make_tc_mat(m.Mcc2.hi.get(), m.Mcc2.lo.get(), naux * ct, m.Kc, m.Kc, bn, bk_for(bn));
         TcShape sh;
-        sh.M = kc * vt; sh.N = ct; sh.K = m.Kc;
+        sh.M = kc * vt; sh.N = ct; sh.K = m.Kc; sh.products = g_products;
         sh.nbatch = naux; sh.a_batch_rows = 0; sh.b_batch_rows = ct;
         TcEpilogue e;
         e.kind = TcEpilogue::SPLIT_BF16;
@@ -209,12 +230,14 @@ void MixedEngine::apply(BseOperator &op, const Coef &c, const double *X, int64_t
         e.bo = vt;
         e.out_hi = T.hi.get(); e.out_lo = T.lo.get();
         tc_gemm(Xa, Bm, sh, e, bn, err, s);
+        op.timer.end(STAGE_TC_HD, s);
+        op.timer.begin(STAGE_TC_HD_B, s);
         // stage 2: Y_j(c1, v1) += alpha sum_{(P,v)} S[(j, c1)][(P,v)] G2[v1][(P,v)]
         const int bn2 = pick_bn(vt);
-        TcMat As = make_tc_mat(T.hi.get(), T.lo.get(), kc * ct, m.Kg, m.Kg, 128);
-        TcMat Bg = make_tc_mat(m.G2.hi.get(), m.G2.lo.get(), vt, m.Kg, m.Kg, bn2);
+        TcMat As = make_tc_mat(T.hi.get(), T.lo.get(), kc * ct, m.Kg, m.Kg, 128, bk_for(bn2));
+        TcMat Bg = make_tc_mat(m.G2.hi.get(), m.G2.lo.get(), vt, m.Kg, m.Kg, bn2, bk_for(bn2));
         TcShape s2;
-        s2.M = kc * ct; s2.N = vt; s2.K = m.Kg;
+        s2.M = kc * ct; s2.N = vt; s2.K = m.Kg; s2.products = g_products;
         s2.ksplit = pick_ksplit(ceil_div(kc * ct, 128) * ceil_div(vt, bn2), m.Kg);
         m.part.resize((size_t)s2.ksplit * s2.M * s2.N);
         TcEpilogue p;
@@ -230,24 +253,29 @@ void MixedEngine::apply(BseOperator &op, const Coef &c, const double *X, int64_t
         r.cd = vt; r.co2 = ct; r.clim = vt;
         r.out_f64 = Y + j0 * ldy; r.alpha = alpha; r.beta = acc ? 1.0 : 0.0;
         reduce_partials(m.part.get(), s2.M, s2.N, ks, r, s);
+        op.timer.end(STAGE_TC_HD_B, s);
+        if (j0 + jc < k) op.timer.begin(STAGE_TC_HD, s);
       } else {
         // stage 1: U[(j, v1)][(P, v)] = sum_c Xs[(j, v)][c] Bvc2[(P, v1)][c]
         const int bn = pick_bn(naux * vt);
-        TcMat Bm = make_tc_mat(m.Bvc2.hi.get(), m.Bvc2.lo.get(), naux * vt, m.Kc, m.Kc, bn);
+        TcMat Xa = make_tc_mat(xh, xl, kc * vt, m.Kc, m.Kc, 128, bk_for(bn));
+        TcMat Bm = make_tc_mat(m.Bvc2.hi.get(), m.Bvc2.lo.get(), naux * vt, m.Kc, m.Kc, bn, bk_for(bn));
         TcShape sh;
-        sh.M = kc * vt; sh.N = naux * vt; sh.K = m.Kc;
+        sh.M = kc * vt; sh.N = naux * vt; sh.K = m.Kc; sh.products = g_products;
         TcEpilogue e;
         e.kind = TcEpilogue::SPLIT_BF16;
         e.rd = vt; e.ro1 = vt * m.Kg; e.ro2 = 1; e.rlim = vt;
         e.cd = vt; e.co1 = vt; e.co2 = m.Kg; e.clim = vt;
         e.out_hi = T.hi.get(); e.out_lo = T.lo.get();
         tc_gemm(Xa, Bm, sh, e, bn, err, s);
+        op.timer.end(STAGE_TC_HD2, s);
+        op.timer.begin(STAGE_TC_HD2_B, s);
         // stage 2: Y_j(c1, v1) += alpha sum_{(P,v)} McvT[c1][(P,v)] U[(j, v1)][(P,v)]
         const int bn2 = pick_bn(kc * vt);
-        TcMat Am = make_tc_mat(m.McvT.hi.get(), m.McvT.lo.get(), ct, m.Kg, m.Kg, 128);
-        TcMat Bu = make_tc_mat(T.hi.get(), T.lo.get(), kc * vt, m.Kg, m.Kg, bn2);
+        TcMat Am = make_tc_mat(m.McvT.hi.get(), m.McvT.lo.get(), ct, m.Kg, m.Kg, 128, bk_for(bn2));
+        TcMat Bu = make_tc_mat(T.hi.get(), T.lo.get(), kc * vt, m.Kg, m.Kg, bn2, bk_for(bn2));
         TcShape s2;
-        s2.M = ct; s2.N = kc * vt; s2.K = m.Kg;
+        s2.M = ct; s2.N = kc * vt; s2.K = m.Kg; s2.products = g_products;
         s2.ksplit = pick_ksplit(ceil_div(ct, 128) * ceil_div(kc * vt, bn2), m.Kg);
         m.part.resize((size_t)s2.ksplit * s2.M * s2.N);
         TcEpilogue p;
@@ -263,10 +291,11 @@ void MixedEngine::apply(BseOperator &op, const Coef &c, const double *X, int64_t
         r.cd = vt; r.co1 = ldy; r.co2 = ct; r.clim = vt;
         r.out_f64 = Y + j0 * ldy; r.alpha = alpha; r.beta = acc ? 1.0 : 0.0;
         reduce_partials(m.part.get(), s2.M, s2.N, ks, r, s);
+        op.timer.end(STAGE_TC_HD2_B, s);
+        if (j0 + jc < k) op.timer.begin(STAGE_TC_HD2, s);
       }
     }
     acc = true;
-    op.timer.end(hd ? STAGE_TC_HD : STAGE_TC_HD2, s);
   }
   if (!acc) {
     VGB_CUDA(cudaMemset2DAsync(Y, ldy * sizeof(double), 0, op.dim * sizeof(double), k, s));

@@ -10,22 +10,28 @@ namespace vgb {
 namespace {
 
 constexpr int BM = 128;
-constexpr int BK = 64;  // bf16 elements per 128-byte swizzle row
-constexpr int kThreads = 192;  // warp 0: TMA, warp 1: MMA + TMEM owner, warps 2-5: epilogue
+constexpr int kEpiWarps = 8;   // two warps per TMEM lane quarter, each drains half the columns
+constexpr int kThreads = 64 + 32 * kEpiWarps;  // warp 0: TMA, warp 1: MMA + TMEM owner, rest: epilogue
 constexpr unsigned long long kWaitNs = 2000000000ull;  // bounded waits: 2 s
+constexpr int kSmemRing = 196608;                     // bytes of operand ring per CTA
 
-template <int BN>
+// BK = bf16 elements of K per stage row: 64 -> 128-byte rows (SWIZZLE_128B),
+// 32 -> 64-byte rows (SWIZZLE_64B, half the stage size, twice the stages).
+template <int BN, int BK>
 struct Cfg {
   static constexpr int A_BYTES = BM * BK * 2;            // one of hi / lo
   static constexpr int B_BYTES = BN * BK * 2;
   static constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
-  static constexpr int STAGES = (BN == 256) ? 2 : (BN == 128 ? 3 : 4);
+  static constexpr int STAGES = kSmemRing / STAGE_BYTES > 8 ? 8 : kSmemRing / STAGE_BYTES;
   static constexpr int TMEM_COLS = 2 * BN < 32 ? 32 : 2 * BN;  // two accumulators
   static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+  static constexpr uint32_t SBO = BK == 64 ? 1024 : 512;     // 8 rows of one swizzle atom
+  static constexpr uint64_t LAYOUT = BK == 64 ? 2 : 4;       // SWIZZLE_128B / SWIZZLE_64B
 };
 
 struct KParams {
   int64_t M, N, K;
+  int products;  // 3: hi.hi + hi.lo + lo.hi;  4: + lo.lo
   int64_t nbatch, a_brows, b_brows;
   int ksplit, kc_per;
   int64_t mt, nt, ntiles;
@@ -93,14 +99,14 @@ __device__ __forceinline__ void fence_before() {
 __device__ __forceinline__ void fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
-// SW128 K-major shared-memory matrix descriptor (8-row core groups 1024 B apart).
-__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+// Swizzled K-major shared-memory matrix descriptor (8-row core groups sbo bytes apart).
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t sbo, uint64_t layout) {
   uint64_t d = 0;
   d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
-  d |= (uint64_t)(16 >> 4) << 16;    // leading byte offset (unused for swizzled K-major)
-  d |= (uint64_t)(1024 >> 4) << 32;  // stride byte offset
-  d |= (uint64_t)1 << 46;            // descriptor version (tcgen05)
-  d |= (uint64_t)2 << 61;            // SWIZZLE_128B
+  d |= (uint64_t)(16 >> 4) << 16;  // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(sbo >> 4) << 32; // stride byte offset
+  d |= (uint64_t)1 << 46;          // descriptor version (tcgen05)
+  d |= layout << 61;               // swizzle mode
   return d;
 }
 __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
@@ -145,6 +151,8 @@ __device__ __forceinline__ TileCoord decode(const KParams &p, int64_t t) {
   return c;
 }
 
+// v - float(hi) is exact in FP32 (hi is v rounded to 8 significant bits), so
+// the split costs no FP64 work in the epilogue.
 __device__ __forceinline__ void epi_store(const TcEpilogue &e, int64_t off, float v) {
   if (e.kind == TcEpilogue::SPLIT_BF16) {
     const __nv_bfloat16 h = __float2bfloat16_rn(v);
@@ -160,12 +168,12 @@ __device__ __forceinline__ void epi_store(const TcEpilogue &e, int64_t off, floa
   }
 }
 
-template <int BN>
+template <int BN, int BK>
 __global__ void __launch_bounds__(kThreads, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
                    const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo,
                    const KParams p) {
-  using C = Cfg<BN>;
+  using C = Cfg<BN, BK>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t *full = (uint64_t *)(smem + C::STAGES * C::STAGE_BYTES);
@@ -183,7 +191,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     for (int i = 0; i < 2; ++i) {
       mbar_init(&accf[i], 1);
-      mbar_init(&acce[i], 4);  // one arrive per epilogue warp
+      mbar_init(&acce[i], kEpiWarps);  // one arrive per epilogue warp
     }
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -256,9 +264,14 @@ __global__ void __launch_bounds__(kThreads, 1)
           for (int kk = 0; kk < BK / 16; ++kk) {
             const uint32_t koff = kk * 32;  // 16 bf16 = 32 bytes along K inside the swizzle row
             const uint32_t acc0 = (kc > kb || kk > 0) ? 1u : 0u;
-            mma_bf16(d_tmem, sdesc(ahi + koff), sdesc(bhi + koff), idesc, acc0);
-            mma_bf16(d_tmem, sdesc(ahi + koff), sdesc(blo + koff), idesc, 1u);
-            mma_bf16(d_tmem, sdesc(alo + koff), sdesc(bhi + koff), idesc, 1u);
+            const uint64_t dah = sdesc(ahi + koff, C::SBO, C::LAYOUT);
+            const uint64_t dal = sdesc(alo + koff, C::SBO, C::LAYOUT);
+            const uint64_t dbh = sdesc(bhi + koff, C::SBO, C::LAYOUT);
+            const uint64_t dbl = sdesc(blo + koff, C::SBO, C::LAYOUT);
+            mma_bf16(d_tmem, dah, dbh, idesc, acc0);
+            mma_bf16(d_tmem, dah, dbl, idesc, 1u);
+            mma_bf16(d_tmem, dal, dbh, idesc, 1u);
+            if (p.products == 4) mma_bf16(d_tmem, dal, dbl, idesc, 1u);
           }
           mma_commit(&empty[stage]);  // frees the smem stage when these MMAs complete
           if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
@@ -270,7 +283,13 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
   } else {
     // ---------------- epilogue warps ----------------
-    const int q = warp % 4;  // TMEM lane quarter this warp may access
+    // A warp may only read the TMEM lane quarter 32 * (warp % 4); the two warps
+    // of each quarter split the tile's columns.
+    const int q = warp % 4;
+    const int half = (warp - 2) / 4;
+    constexpr int COLS = BN >= 64 ? BN / 2 : BN;
+    const int cbeg = (BN >= 64 || half == 0) ? half * COLS : BN;
+    const int cend = (BN >= 64 || half == 0) ? cbeg + COLS : BN;
     int buf = 0;
     uint32_t aphase = 0;
     const TcEpilogue &e = p.epi;
@@ -282,12 +301,41 @@ __global__ void __launch_bounds__(kThreads, 1)
       const bool row_ok = i < p.M && (i % e.rd) < e.rlim;
       const int64_t rbase = (i / e.rd) * e.ro1 + (i % e.rd) * e.ro2 + tc.b * e.bo + tc.s * e.so;
 #pragma unroll 1
-      for (int c0 = 0; c0 < BN; c0 += 32) {
+      for (int c0 = cbeg; c0 < cend; c0 += 32) {
         uint32_t r[32];
         tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + c0), r);
-        if (row_ok) {
-          int64_t n = tc.n * BN + c0;
-          int64_t nq = n / e.cd, nr = n % e.cd;
+        if (!row_ok) continue;
+        const int64_t n0 = tc.n * BN + c0;
+        const int64_t nq0 = n0 / e.cd, nr0 = n0 % e.cd;
+        if (nr0 + 32 <= e.cd && n0 + 32 <= p.N && nr0 + 32 <= e.clim) {
+          // fast path: the 32 columns are one arithmetic run of offsets
+          const int64_t base = rbase + nq0 * e.co1 + nr0 * e.co2;
+          const int64_t st = e.co2;
+          if (e.kind == TcEpilogue::SPLIT_BF16) {
+            uint16_t *oh = e.out_hi + base, *ol = e.out_lo + base;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+              const float v = __uint_as_float(r[j]);
+              const __nv_bfloat16 h = __float2bfloat16_rn(v);
+              const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
+              oh[j * st] = __bfloat16_as_ushort(h);
+              ol[j * st] = __bfloat16_as_ushort(l);
+            }
+          } else if (e.kind == TcEpilogue::STORE_F32) {
+            float *o = e.out_f32 + base;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) o[j * st] = __uint_as_float(r[j]);
+          } else {
+            double *o = e.out_f64 + base;
+            const double al = e.alpha, be = e.beta;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+              const double rv = al * (double)__uint_as_float(r[j]);
+              o[j * st] = (be == 0.0) ? rv : fma(be, o[j * st], rv);
+            }
+          }
+        } else {
+          int64_t n = n0, nq = nq0, nr = nr0;
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
             if (n < p.N && nr < e.clim)
@@ -338,10 +386,18 @@ __global__ void reduce_partials_kernel(const float *__restrict__ part, int64_t M
        t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = t / N, n = t % N;
     if ((i % e.rd) >= e.rlim || (n % e.cd) >= e.clim) continue;
-    float acc = 0.f;
-    for (int s = 0; s < ksplit; ++s) acc += part[s * total + t];
+    double acc = 0.0;
+    for (int s = 0; s < ksplit; ++s) acc += (double)part[s * total + t];
+    // the partial sums are added in FP64; the final value enters the epilogue
+    // as FP64 for AXPBY (no extra rounding) and as FP32 for the bf16 split
     const int64_t off = (i / e.rd) * e.ro1 + (i % e.rd) * e.ro2 + (n / e.cd) * e.co1 + (n % e.cd) * e.co2;
-    epi_store(e, off, acc);
+    if (e.kind == TcEpilogue::AXPBY_F64) {
+      double *y = e.out_f64 + off;
+      const double r = e.alpha * acc;
+      *y = (e.beta == 0.0) ? r : fma(e.beta, *y, r);
+    } else {
+      epi_store(e, off, (float)acc);
+    }
   }
 }
 
@@ -363,31 +419,34 @@ EncodeTiledFn encode_fn() {
   return fn;
 }
 
-void encode(CUtensorMap *m, const uint16_t *base, int64_t rows, int64_t K, int64_t ld, int box_rows) {
+void encode(CUtensorMap *m, const uint16_t *base, int64_t rows, int64_t K, int64_t ld, int box_rows,
+            int bk) {
   VGB_REQUIRE(((uintptr_t)base & 15) == 0, "tc operand base must be 16-byte aligned");
-  VGB_REQUIRE(K % BK == 0 && (ld * 2) % 16 == 0 && ld >= K, "tc operand K/ld not padded");
+  VGB_REQUIRE(bk == 32 || bk == 64, "tc operand: K box must be 32 or 64");
+  VGB_REQUIRE(K % bk == 0 && (ld * 2) % 16 == 0 && ld >= K, "tc operand K/ld not padded");
   cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)(ld * 2)};
-  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint32_t box[2] = {(cuuint32_t)bk, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = encode_fn()(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)base, dims, strides, box,
-                           estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                           bk == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) fail(BSE_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
 }
 
-template <int BN>
+template <int BN, int BK>
 void launch(const TcMat &A, const TcMat &B, const KParams &p, cudaStream_t s) {
-  using C = Cfg<BN>;
+  using C = Cfg<BN, BK>;
   static bool attr = false;
   if (!attr) {
-    VGB_CUDA(cudaFuncSetAttribute(tc_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  C::SMEM));
+    VGB_CUDA(cudaFuncSetAttribute(tc_gemm_kernel<BN, BK>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
     attr = true;
   }
   const int64_t grid = std::min<int64_t>(p.ntiles, sm_count());
-  tc_gemm_kernel<BN><<<(unsigned)grid, kThreads, C::SMEM, s>>>(A.map_hi, A.map_lo, B.map_hi,
-                                                               B.map_lo, p);
+  tc_gemm_kernel<BN, BK><<<(unsigned)grid, kThreads, C::SMEM, s>>>(A.map_hi, A.map_lo, B.map_hi,
+                                                                   B.map_lo, p);
   VGB_LAUNCH_CHECK();
 }
 
@@ -398,7 +457,7 @@ unsigned grid_1d(int64_t n) {
 }  // namespace
 
 TcMat make_tc_mat(const uint16_t *hi, const uint16_t *lo, int64_t rows, int64_t K, int64_t ld,
-                  int box_rows) {
+                  int box_rows, int bk) {
   TcMat m;
   m.hi = hi;
   m.lo = lo;
@@ -406,8 +465,9 @@ TcMat make_tc_mat(const uint16_t *hi, const uint16_t *lo, int64_t rows, int64_t 
   m.K = K;
   m.ld = ld;
   m.box_rows = box_rows;
-  encode(&m.map_hi, hi, rows, K, ld, box_rows);
-  encode(&m.map_lo, lo, rows, K, ld, box_rows);
+  m.bk = bk;
+  encode(&m.map_hi, hi, rows, K, ld, box_rows, bk);
+  encode(&m.map_lo, lo, rows, K, ld, box_rows, bk);
   return m;
 }
 
@@ -415,7 +475,9 @@ int tc_gemm(const TcMat &A, const TcMat &B, const TcShape &sh, const TcEpilogue 
             int *err, cudaStream_t s) {
   VGB_REQUIRE(bn == 32 || bn == 64 || bn == 128 || bn == 256, "tc_gemm: unsupported tile N");
   VGB_REQUIRE(A.box_rows == BM && B.box_rows == bn, "tc_gemm: operand boxes do not match the tile");
-  VGB_REQUIRE(sh.K % BK == 0 && A.K >= sh.K && B.K >= sh.K, "tc_gemm: K not padded to 64");
+  VGB_REQUIRE(A.bk == B.bk, "tc_gemm: operands staged with different K boxes");
+  const int BK = A.bk;
+  VGB_REQUIRE(sh.K % BK == 0 && A.K >= sh.K && B.K >= sh.K, "tc_gemm: K not padded");
   VGB_REQUIRE(epi.rd >= 1 && epi.cd >= 1, "tc_gemm: bad epilogue map");
   if (sh.M <= 0 || sh.N <= 0 || sh.nbatch <= 0) return 0;
   // rows addressed by the last batch must exist in the operands (TMA fills beyond with zeros,
@@ -425,6 +487,7 @@ int tc_gemm(const TcMat &A, const TcMat &B, const TcShape &sh, const TcEpilogue 
   VGB_REQUIRE(A.rows < (1LL << 31) && B.rows < (1LL << 31), "tc_gemm: too many rows");
   KParams p;
   p.M = sh.M; p.N = sh.N; p.K = sh.K;
+  p.products = sh.products == 4 ? 4 : 3;
   p.nbatch = sh.nbatch;
   p.a_brows = sh.a_batch_rows;
   p.b_brows = sh.b_batch_rows;
@@ -439,11 +502,20 @@ int tc_gemm(const TcMat &A, const TcMat &B, const TcShape &sh, const TcEpilogue 
   p.ntiles = p.mt * p.nt * p.ksplit * sh.nbatch;
   p.epi = epi;
   p.err = err;
-  switch (bn) {
-    case 32: launch<32>(A, B, p, s); break;
-    case 64: launch<64>(A, B, p, s); break;
-    case 128: launch<128>(A, B, p, s); break;
-    default: launch<256>(A, B, p, s); break;
+  if (BK == 64) {
+    switch (bn) {
+      case 32: launch<32, 64>(A, B, p, s); break;
+      case 64: launch<64, 64>(A, B, p, s); break;
+      case 128: launch<128, 64>(A, B, p, s); break;
+      default: launch<256, 64>(A, B, p, s); break;
+    }
+  } else {
+    switch (bn) {
+      case 32: launch<32, 32>(A, B, p, s); break;
+      case 64: launch<64, 32>(A, B, p, s); break;
+      case 128: launch<128, 32>(A, B, p, s); break;
+      default: launch<256, 32>(A, B, p, s); break;
+    }
   }
   return p.ksplit;
 }

@@ -23,11 +23,13 @@ struct TcMat {
   int64_t rows = 0, K = 0, ld = 0;
   CUtensorMap map_hi, map_lo;
   int box_rows = 0;
+  int bk = 64;
 };
 
-// Build the TMA descriptors of an operand; box_rows = tile rows (128 for A, BN for B).
+// Build the TMA descriptors of an operand; box_rows = tile rows (128 for A, BN for B);
+// bk = K elements per pipeline stage (64: 128-byte swizzle, 32: 64-byte swizzle).
 TcMat make_tc_mat(const uint16_t *hi, const uint16_t *lo, int64_t rows, int64_t K, int64_t ld,
-                  int box_rows);
+                  int box_rows, int bk = 64);
 
 // Output index map of the epilogue.  Element (i, n) of batch b, K-split s goes to
 //   (i / rd) * ro1 + (i % rd) * ro2 + (n / cd) * co1 + (n % cd) * co2 + b * bo + s * so
@@ -49,6 +51,7 @@ struct TcShape {
   int64_t nbatch = 1;
   int64_t a_batch_rows = 0, b_batch_rows = 0;  // row offset of A / B per batch
   int ksplit = 1;                              // K split into ksplit ranges (STORE_F32 partials)
+  int products = 3;                            // 3 (BF16x3) or 4 (adds A_lo B_lo)
 };
 
 // Launch the persistent GEMM; bn in {32, 64, 128, 256}.  err: device int set
