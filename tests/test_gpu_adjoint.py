@@ -33,16 +33,15 @@ def dense_eigs(mmn, hqp, w):
     """Lowest eigenvalues from the oracle-assembled operator (FP64 CPU).  A dense W
     is folded exactly into the vv block (M(v1, v, .) <- W M(v1, v, .)), which is
     the operator the dense-screening handle applies.  A single perturbed Mmn entry
-    makes the operator non-symmetric, so the general eigensolver is used then."""
+    makes the operator non-symmetric; its symmetric part has the same first-order
+    eigenvalue change (x^T E x = x^T E^T x), so the symmetrised matrix is used."""
     if w.ndim == 2:
         mmn = mmn.copy()
         mmn[:V, :, :V] = np.einsum("pq,mqn->mpn", w, mmn[:V, :, :V])
         w = np.ones(w.shape[0])
     prob = oracle.BSEProblem(mmn, w, hqp, V, C)
     H = prob.dense("singlet")
-    if np.array_equal(H, H.T):
-        return np.linalg.eigvalsh(H)[:NROOTS]
-    return np.sort(np.linalg.eigvals(H).real)[:NROOTS]
+    return np.linalg.eigvalsh(0.5 * (H + H.T))[:NROOTS]
 
 
 def fd_tolerance(fd, g, lam, h):

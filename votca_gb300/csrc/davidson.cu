@@ -277,6 +277,17 @@ void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_option
                     const double *host_guess, int64_t guess_cols, double *evecs_dev,
                     DavidsonOutput &out, cudaStream_t s) {
   const auto t_start = std::chrono::steady_clock::now();
+  // phase timing (verbose >= 2): synchronises at phase boundaries
+  const bool phases = opt.verbose >= 2;
+  double ph[6] = {0, 0, 0, 0, 0, 0};  // projection, small eig, ritz+residual, correction, GS, restart
+  auto tick = std::chrono::steady_clock::now();
+  auto mark = [&](int i) {
+    if (!phases) return;
+    cudaStreamSynchronize(s);
+    const auto now = std::chrono::steady_clock::now();
+    ph[i] += std::chrono::duration<double>(now - tick).count();
+    tick = now;
+  };
   const bool ham = opt.matrix_type == 1;
   const bool debug = getenv("VGB_DAVIDSON_DEBUG") != nullptr;
   const int64_t n = A.size();
@@ -369,6 +380,7 @@ void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_option
   for (int64_t it = 0; it < iter_max; ++it) {
     out.iterations = it;
     // ---- updateProjection ----
+    if (phases) { cudaStreamSynchronize(s); tick = std::chrono::steady_clock::now(); }
     {
       const int64_t old = (it == 0) ? 0 : nav, nvec = ncols - old;
       apply(V.get() + old * n, nvec, AV.get() + old * n);
@@ -425,6 +437,7 @@ void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_option
     }
     const int64_t needed = std::min(m, std::max(restart_size, size_update));
 
+    mark(0);
     // ---- getRitzEigenPairs (small problem on the host) ----
     if (!ham) {
       std::vector<double> ev, evec;
@@ -492,6 +505,7 @@ void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_option
         lam[c] = sacc;
       }
     }
+    mark(1);
     // q = V U, res = AV U - q Lambda
     Ud.resize(m * needed);
     lamd.resize(needed);
@@ -504,6 +518,7 @@ void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_option
     residual_kernel<<<blocks_for(n * needed), 256, 0, s>>>(res.get(), q.get(), n, needed, lamd.get());
     VGB_LAUNCH_CHECK();
 
+    mark(2);
     // ---- checkConvergence ----
     const int64_t nn_check = std::min(needed, size_update);
     work.resize(std::max<int64_t>(needed, 1) + 8);
@@ -598,8 +613,10 @@ void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_option
       }
       fprintf(stderr, "\n");
     }
+    mark(3);
     gramschmidt(x, V.get(), ncols, ncols + nupdate, work, flag);
     ncols += nupdate;
+    mark(4);
     if (debug) {
       DeviceBuffer<double> G(ncols * ncols);
       x.gemm_tn(V.get(), n, ncols, V.get(), n, ncols, G.get(), ncols, 1.0, 0.0);
@@ -619,6 +636,7 @@ void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_option
 
     // ---- restart ----
     if (ncols > max_space) {
+      struct M5 { decltype(mark) &m; ~M5() { m(5); } } m5_{mark};
       const int64_t rs = restart_size, nv = nupdate;
       VGB_REQUIRE(rs <= needed, "DavidsonSolver: restart size exceeds the Ritz pairs");
       DeviceBuffer<double> keep(n * nv), avn(n * rs);
@@ -664,6 +682,11 @@ void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_option
   VGB_CUDA(cudaStreamSynchronize(s));
   cudaEventDestroy(ev0);
   cudaEventDestroy(ev1);
+  if (phases)
+    fprintf(stderr,
+            "[davidson] phases (s): projection+matvec %.4f (matvec %.4f)  small-eig %.4f  ritz %.4f  "
+            "correction %.4f  gram-schmidt %.4f  restart %.4f\n",
+            ph[0], matvec_ms * 1e-3, ph[1], ph[2], ph[3], ph[4], ph[5]);
   out.seconds_matvec = matvec_ms * 1e-3;
   out.seconds_total =
       std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();

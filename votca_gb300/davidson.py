@@ -100,7 +100,7 @@ class DavidsonSolver:
         else:
             raise TypeError("DavidsonSolver.solve needs a GPU operator")
         opt = _lib.bse_davidson_options(self.iter_max_, self.tol_, self.max_search_space_, self.correction_,
-                                        self.update_, self.matrix_type_, 1 if self.verbose else 0)
+                                        self.update_, self.matrix_type_, int(self.verbose))
         evals = np.zeros(neigen)
         evecs = np.zeros((n, neigen), order="F")
         res = _lib.bse_davidson_result()
