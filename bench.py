@@ -340,12 +340,20 @@ def main():
         achieved = hd_stage_a_flops(V, C, NAUX, K) / launches_per_step / (per_launch_ms * 1e-3) / 1e12
         pk = peaks.get("bf16_tflops")
         nprod = 4 if os.environ.get("VGB_TC_PRODUCTS") == "4" else 3
+        # DRAM bytes per launch of this kernel: Mcc2 (hi+lo) read once, X read, the S intermediate
+        # written; this model matches the ncu capture of the same kernel on a small case
+        # (dram__bytes_read/write.sum, see profiles/tc_gemm_hd_stage1_*.md)
+        kc = -(-C // 64) * 64
+        kg = -(-(NAUX * V) // 64) * 64
+        per_launch_cols = K / launches_per_step
+        traffic = NAUX * C * kc * 4 + per_launch_cols * V * kc * 4 + per_launch_cols * C * kg * 4
         roofline = {"bound": "tensor",
-                    "kernel": "tc_gemm_kernel<256> (Hd c-contraction, tcgen05 BF16 split products)",
+                    "kernel": "tc_gemm_kernel<256,32> (Hd c-contraction, tcgen05 BF16 split products)",
                     "achieved": achieved, "peak": pk / nprod if pk else None,
                     "unit": f"TFLOP/s (FP64-equivalent; {nprod} BF16 products per term)",
                     "frac": achieved / (pk / nprod) if pk else None,
-                    "peak_source": f"MEASURED_PEAKS.json bf16_tflops / {nprod} (of measured)", "traffic": None}
+                    "peak_source": f"MEASURED_PEAKS.json bf16_tflops / {nprod} (of measured)",
+                    "traffic": traffic, "traffic_source": "bytes per launch, model validated by ncu dram__bytes"}
     stages = {name: {"ms_per_step": stage_ms[i] / args.steps, "launches_per_step": stage_calls[i] / args.steps}
               for i, name in enumerate(["hqp", "hx", "hd_a", "hd_b", "hd2_a", "hd2_b", "tc_hd", "tc_hx",
                                         "tc_hd2", "tc_split", "tc_hd_b", "tc_hd2_b"]) if stage_calls[i]}

@@ -142,6 +142,117 @@ __global__ void copy_block_kernel(const double *src, int64_t lds, double *dst, i
   }
 }
 
+// ---- column-wise classical Gram-Schmidt in one cooperative launch ----
+//
+// The reference's inner loop (davidsonsolver.cc:453-458 / 468-477) walks the new
+// columns one by one: h = Q_{nstart..j-1}^T q_j, q_j -= Q h, normalise, and in
+// the second pass checks ||q_j|| against 1e-12 of the column's original norm.
+// Each step is a matrix-vector product over dim rows, so as separate launches it
+// is launch- and sync-bound.  Here every block owns a contiguous slice of rows;
+// one grid barrier after the partial dots and one after the partial norms make
+// a column step, and the next column's dots read only the block's own rows, so
+// no barrier is needed after the scaling.  The barrier is a bounded spin: if a
+// block does not arrive within the limit the kernel records an error and stops.
+constexpr int kGsThreads = 256;
+constexpr int kGsMaxRange = 1024;
+
+__device__ bool gs_grid_barrier(unsigned *count, volatile unsigned *gen, unsigned nblocks,
+                                volatile int *err) {
+  __syncthreads();
+  __shared__ int failed;
+  if (threadIdx.x == 0) {
+    failed = 0;
+    const unsigned g = *gen;
+    __threadfence();
+    const unsigned arrived = atomicAdd(count, 1u);
+    if (arrived == nblocks - 1) {
+      *count = 0;
+      __threadfence();
+      atomicAdd((unsigned *)gen, 1u);
+    } else {
+      const uint64_t t0 = clock64();
+      while (*gen == g) {
+        if (*err) { failed = 1; break; }
+        if (clock64() - t0 > (1ull << 32)) {  // ~2 s at 2 GHz
+          *err = 2;
+          failed = 1;
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return failed == 0;
+}
+
+__global__ void __launch_bounds__(kGsThreads)
+    gs_columns_kernel(double *Q, int64_t n, int64_t nstart, int64_t ncols, int check,
+                      const double *__restrict__ norms0, double *partial, double *npartial,
+                      unsigned *bar_count, unsigned *bar_gen, int *flag, int *err) {
+  const unsigned nb = gridDim.x;
+  const int64_t rows_per = ceil_div(n, (int64_t)nb);
+  const int64_t r0 = min(n, (int64_t)blockIdx.x * rows_per), r1 = min(n, r0 + rows_per);
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  __shared__ double h[kGsMaxRange];
+  __shared__ double red[kGsThreads / 32];
+  const double *M = Q + nstart * n;
+  for (int64_t j = nstart + 1; j < ncols; ++j) {
+    const int64_t range = j - nstart;
+    double *qj = Q + j * n;
+    double *part = partial + (j & 1) * (int64_t)nb * kGsMaxRange;
+    double *npart = npartial + (j & 1) * (int64_t)nb;
+    // partial dots of q_j with the previous new columns over this block's rows
+    for (int64_t l = warp; l < range; l += kGsThreads / 32) {
+      const double *ml = M + l * n;
+      double sacc = 0.0;
+      for (int64_t i = r0 + lane; i < r1; i += 32) sacc = fma(ml[i], qj[i], sacc);
+      for (int o = 16; o > 0; o >>= 1) sacc += __shfl_down_sync(0xffffffffu, sacc, o);
+      if (lane == 0) __stcg(part + (int64_t)blockIdx.x * kGsMaxRange + l, sacc);
+    }
+    if (!gs_grid_barrier(bar_count, bar_gen, nb, err)) return;
+    // h = sum over blocks (fixed order: deterministic)
+    for (int64_t l = threadIdx.x; l < range; l += kGsThreads) {
+      double sacc = 0.0;
+      // other blocks wrote these: read through L2 (an L1 line from two columns ago is stale)
+      for (unsigned b = 0; b < nb; ++b) sacc += __ldcg(part + (int64_t)b * kGsMaxRange + l);
+      h[l] = sacc;
+    }
+    __syncthreads();
+    // q_j -= M h on own rows, partial squared norm
+    double nacc = 0.0;
+    for (int64_t i = r0 + threadIdx.x; i < r1; i += kGsThreads) {
+      double sacc = 0.0;
+      for (int64_t l = 0; l < range; ++l) sacc = fma(M[l * n + i], h[l], sacc);
+      const double v = qj[i] - sacc;
+      qj[i] = v;
+      nacc = fma(v, v, nacc);
+    }
+    for (int o = 16; o > 0; o >>= 1) nacc += __shfl_down_sync(0xffffffffu, nacc, o);
+    if (lane == 0) red[warp] = nacc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < kGsThreads / 32; ++w) t += red[w];
+      __stcg(npart + blockIdx.x, t);
+    }
+    if (!gs_grid_barrier(bar_count, bar_gen, nb, err)) return;
+    __shared__ double nrm;
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (unsigned b = 0; b < nb; ++b) t += __ldcg(npart + b);
+      nrm = sqrt(t);
+      if (check && blockIdx.x == 0 && !(nrm > 1e-12 * norms0[range])) *flag = 1;
+    }
+    __syncthreads();
+    const double nv = nrm;
+    if (nv > 0.0)  // Eigen's normalize leaves a zero column unchanged
+      for (int64_t i = r0 + threadIdx.x; i < r1; i += kGsThreads) qj[i] /= nv;
+    __syncthreads();  // the next column's dots read rows scaled by other threads of the block
+  }
+}
+
 }  // namespace
 
 namespace {
@@ -150,7 +261,9 @@ struct Ctx {
   cudaStream_t s;
   int64_t n;
   GemmWorkspace ws;
-  DeviceBuffer<double> red_partial, scal;
+  DeviceBuffer<double> red_partial, scal, gs_part;
+  DeviceBuffer<unsigned> gs_bar;
+  DeviceBuffer<int> gs_err;
 
   // out[c] = ||A[:, c]|| (or dot(A[:, c], B[:, c]) when B given), device
   void coldots(const double *A, int64_t lda, const double *B, int64_t ldb, int64_t ncols,
@@ -214,24 +327,35 @@ void gramschmidt(Ctx &x, double *Q, int64_t nstart, int64_t ncols, DeviceBuffer<
       x.coldots(Q + nstart * n, n, nullptr, 0, nupdate, norms, true);
       x.scale_cols(Q + nstart * n, n, nupdate, norms);
     }
-    for (int64_t j = nstart + 1; j < ncols; ++j) {
-      const int64_t range = j - nstart;
-      double *qj = Q + j * n;
-      const double *M = Q + nstart * n;
-      x.gemm_tn(M, n, range, qj, n, 1, h, range, 1.0, 0.0);
-      x.gemm_nn(M, n, range, h, range, 1, qj, n, -1.0, 1.0);
-      x.coldots(qj, n, nullptr, 0, 1, norms, true);
-      if (pass == 1) {
-        gs_check_kernel<<<1, 32, 0, x.s>>>(norms, norms0 + range, flag.get());
-        VGB_LAUNCH_CHECK();
-      }
-      x.scale_cols(qj, n, 1, norms);
+    if (ncols - nstart > 1) {
+      VGB_REQUIRE(ncols - nstart <= kGsMaxRange, "Gram-Schmidt: too many new columns in one step");
+      int dev = 0, per_sm = 0;
+      VGB_CUDA(cudaGetDevice(&dev));
+      VGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gs_columns_kernel, kGsThreads, 0));
+      const int64_t want = std::max<int64_t>(1, ceil_div(n, (int64_t)kGsThreads));
+      const unsigned nb = (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)per_sm * sm_count()));
+      x.gs_part.resize(2 * (size_t)nb * kGsMaxRange + 2 * (size_t)nb);
+      x.gs_bar.resize(2);
+      x.gs_err.resize(1);
+      VGB_CUDA(cudaMemsetAsync(x.gs_bar.get(), 0, 2 * sizeof(unsigned), x.s));
+      VGB_CUDA(cudaMemsetAsync(x.gs_err.get(), 0, sizeof(int), x.s));
+      double *Qp = Q;
+      int64_t nn = n, ns = nstart, nc = ncols;
+      int chk = pass == 1 ? 1 : 0;
+      double *pp = x.gs_part.get(), *np = x.gs_part.get() + 2 * (size_t)nb * kGsMaxRange;
+      unsigned *bc = x.gs_bar.get(), *bg = x.gs_bar.get() + 1;
+      int *fl = flag.get(), *er = x.gs_err.get();
+      void *args[] = {&Qp, &nn, &ns, &nc, &chk, &norms0, &pp, &np, &bc, &bg, &fl, &er};
+      VGB_CUDA(cudaLaunchCooperativeKernel((void *)gs_columns_kernel, dim3(nb), dim3(kGsThreads), args, 0, x.s));
     }
   }
-  int hflag = 0;
-  VGB_CUDA(cudaMemcpyAsync(&hflag, flag.get(), sizeof(int), cudaMemcpyDeviceToHost, x.s));
+  int hflag[2] = {0, 0};
+  VGB_CUDA(cudaMemcpyAsync(&hflag[0], flag.get(), sizeof(int), cudaMemcpyDeviceToHost, x.s));
+  if (ncols - nstart > 1)
+    VGB_CUDA(cudaMemcpyAsync(&hflag[1], x.gs_err.get(), sizeof(int), cudaMemcpyDeviceToHost, x.s));
   VGB_CUDA(cudaStreamSynchronize(x.s));
-  if (hflag) fail(BSE_ERR_NUMERICAL, "Linear dependencies in Gram-Schmidt.");
+  if (hflag[1]) fail(BSE_ERR_TIMEOUT, "Gram-Schmidt: grid barrier gave up");
+  if (hflag[0]) fail(BSE_ERR_NUMERICAL, "Linear dependencies in Gram-Schmidt.");
 }
 
 // Householder QR, thin Q (m x r) of the m x r column-major matrix A (DavidsonSolver::qr)
