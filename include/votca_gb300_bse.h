@@ -257,6 +257,20 @@ int bse_op_eig_gradient(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd,
                         double *grad_mmn, double *grad_hqp,
                         double *grad_screening);
 
+/* Many independent molecules (one handle each, e.g. of uneven BSE dimension):
+ * solves every handle's operator with bse_davidson_solve semantics (no guess,
+ * eigenvalues only) on nthreads host threads, each handle on its own stream with
+ * stream-ordered scratch, so the small per-molecule kernels of different
+ * molecules run concurrently on the GPU.  evals: nhandles x neigen (row per
+ * molecule); infos / iterations: per molecule, may be NULL.  No counterpart in
+ * the reference, which solves one molecule per process (xtp_parallel farms jobs,
+ * xtp/src/libxtp/parallelxjobcalc.cc:52-74). */
+int bse_davidson_solve_batch(bse_handle *const *handles, int64_t nhandles,
+                             const int32_t a_coef[4], const int32_t b_coef[4],
+                             const bse_davidson_options *opt, int64_t neigen,
+                             double *evals, int32_t *infos,
+                             int64_t *iterations, int32_t nthreads);
+
 /* Thread-local text of the last error on this thread ("" if none). */
 const char *bse_last_error(void);
 

@@ -1,0 +1,95 @@
+"""Batched solves of independent molecules (bse_davidson_solve_batch).
+
+Molecules of uneven shape are solved concurrently, each handle on its own
+stream; every molecule's roots must equal those of its own single solve and,
+in FP64, the dense eigenvalues of its TDA singlet Hamiltonian.
+"""
+import numpy as np
+import pytest
+
+from votca_gb300.synthetic import Problem
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [  # v, c, naux, seed: uneven, as in a batch of different molecules
+    (4, 32, 64, 1), (5, 40, 96, 2), (7, 33, 80, 3), (4, 64, 128, 4), (6, 48, 72, 5),
+    (8, 37, 100, 6), (3, 50, 64, 7), (9, 35, 120, 8), (4, 45, 90, 9), (6, 60, 110, 10),
+]
+
+
+def _contexts(precision):
+    from votca_gb300 import bse_operator as bo
+
+    out = []
+    for v, c, naux, seed in SHAPES:
+        p = Problem(v=v, c=c, naux=naux, nmo=v + c + 8, seed=seed)
+        opt = bo.BSEOperator_Options(homo=v - 1, rpamin=0, qpmin=0, vmin=0, cmax=v + c - 1)
+        out.append((p, bo.GpuBSEContext(p.w, bo.TCMatrix_gwbse(p.mmn), p.hqp[:v + c, :v + c], opt,
+                                        precision=precision)))
+    return out
+
+
+def _solver():
+    from votca_gb300.davidson import DavidsonSolver
+
+    ds = DavidsonSolver()
+    ds.set_tolerance(1e-7)
+    ds.set_max_search_space(50)
+    return ds
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batch_equals_single_solves(precision):
+    from votca_gb300 import bse_operator as bo
+
+    ctxs = _contexts(precision)
+    ops = [bo.SingletOperator_TDA(ctx) for _, ctx in ctxs]
+    nroots = 5
+    ev, info, iters = _solver().solve_batch(ops, nroots, nthreads=4)
+    assert ev.shape == (len(SHAPES), nroots)
+    assert all(i == "Success" for i in info)
+    for m, (op, (p, _)) in enumerate(zip(ops, ctxs)):
+        ds = _solver()
+        lam, _ = ds.solve(op, nroots)
+        # same kernels, same deterministic reductions: the batch changes only the stream
+        np.testing.assert_allclose(ev[m], lam, rtol=0, atol=1e-12)
+        assert iters[m] == ds.num_iterations()
+        if precision == 0:
+            H = op.matmul(np.eye(op.rows()))
+            exact = np.linalg.eigvalsh(0.5 * (H + H.T))[:nroots]
+            np.testing.assert_allclose(ev[m], exact, rtol=0, atol=1e-9)
+    for _, ctx in ctxs:
+        ctx.close()
+
+
+def test_batch_repeated_is_deterministic():
+    from votca_gb300 import bse_operator as bo
+
+    ctxs = _contexts(1)
+    ops = [bo.SingletOperator_TDA(ctx) for _, ctx in ctxs]
+    a, _, _ = _solver().solve_batch(ops, 5, nthreads=8)
+    b, _, _ = _solver().solve_batch(ops, 5, nthreads=3)
+    np.testing.assert_array_equal(a, b)
+    for _, ctx in ctxs:
+        ctx.close()
+
+
+def test_batch_reports_failing_molecule():
+    from votca_gb300 import _lib
+    from votca_gb300 import bse_operator as bo
+
+    ctxs = _contexts(0)[:3]
+    ops = [bo.SingletOperator_TDA(ctx) for _, ctx in ctxs]
+    small = ops[0].rows()
+    with pytest.raises(_lib.BSEError, match="molecule 0"):
+        _solver().solve_batch(ops, small + 1, nthreads=2)  # more roots than rows
+    # the handles stay usable after a failed batch
+    ev, info, _ = _solver().solve_batch(ops, 3, nthreads=2)
+    assert all(i == "Success" for i in info)
+    for _, ctx in ctxs:
+        ctx.close()
+
+
+def test_batch_empty():
+    ev, info, iters = _solver().solve_batch([], 5)
+    assert ev.shape == (0, 5) and info == [] and iters.size == 0

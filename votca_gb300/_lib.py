@@ -57,6 +57,9 @@ SIGNATURES = {
     "bse_davidson_solve": (c_i32, [c_vp, ctypes.POINTER(c_i32), ctypes.POINTER(c_i32),
                                    ctypes.POINTER(bse_davidson_options), c_i64, c_dp, c_i64, c_dp, c_dp, c_i64,
                                    ctypes.POINTER(bse_davidson_result)]),
+    "bse_davidson_solve_batch": (c_i32, [ctypes.POINTER(c_vp), c_i64, ctypes.POINTER(c_i32), ctypes.POINTER(c_i32),
+                                         ctypes.POINTER(bse_davidson_options), c_i64, c_dp,
+                                         ctypes.POINTER(c_i32), ctypes.POINTER(c_i64), c_i32]),
     "bse_op_eig_gradient": (c_i32, [c_vp, c_i32, c_i32, c_i32, c_i32, c_dp, c_i64, c_i64, c_dp, c_dp, c_dp, c_dp]),
     "bse_rpa_epsilon": (c_i32, [ctypes.POINTER(bse_mmn_desc), ctypes.POINTER(c_dp), c_dp, c_i64, c_i64, c_i64,
                                 c_i64, ctypes.c_double, ctypes.c_double, c_dp]),

@@ -1,5 +1,8 @@
 // C ABI of the library (declarations and reference mapping: include/votca_gb300_bse.h).
 #include <algorithm>
+#include <atomic>
+#include <mutex>
+#include <thread>
 #include <cstring>
 #include <vector>
 #include <memory>
@@ -68,10 +71,13 @@ static int create_impl(const bse_mmn_desc *mmn, const double *const *slices, con
     std::unique_ptr<bse_handle> h(new bse_handle());
     h->kind = 0;
     create_stream(h.get());
+    vgb::AllocStreamScope alloc_scope(h->stream);
     h->bse.reset(new vgb::BseOperator());
     try {
       h->bse->stage(*mmn, slices, w, dense_w, hqp, ldh, hqp_size, *opt, precision, h->stream);
     } catch (...) {
+      h->bse.reset();  // frees on the handle stream, before it goes away
+      cudaStreamSynchronize(h->stream);
       cudaStreamDestroy(h->stream);
       h->stream = nullptr;
       throw;
@@ -102,8 +108,17 @@ int bse_dense_op_create(const double *a, const double *b, int64_t n, int64_t lda
     std::unique_ptr<bse_handle> h(new bse_handle());
     h->kind = 1;
     create_stream(h.get());
+    vgb::AllocStreamScope alloc_scope(h->stream);
     h->dense.reset(new vgb::DenseOperator());
-    h->dense->stage(a, b, n, lda, h->stream);
+    try {
+      h->dense->stage(a, b, n, lda, h->stream);
+    } catch (...) {
+      h->dense.reset();
+      cudaStreamSynchronize(h->stream);
+      cudaStreamDestroy(h->stream);
+      h->stream = nullptr;
+      throw;
+    }
     *out = h.release();
   });
 }
@@ -113,8 +128,15 @@ int bse_op_destroy(bse_handle *h) {
     if (!h) return;
     if (h->stream) cudaStreamSynchronize(h->stream);
     cudaStream_t s = h->stream;
-    delete h;
-    if (s) cudaStreamDestroy(s);
+    {
+      vgb::AllocStreamScope alloc_scope(s);
+      delete h;
+    }
+    if (s) {
+      cudaStreamSynchronize(s);
+      cudaStreamDestroy(s);
+    }
+    vgb::trim_pool();
   });
 }
 
@@ -154,6 +176,7 @@ int bse_op_matmul(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd, int32_t cd
                   const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy) {
   return guarded([&] {
     require_handle(h);
+    vgb::AllocStreamScope alloc_scope(h->stream);
     const int64_t n = h->size();
     VGB_REQUIRE(X && Y, "bse_op_matmul: null matrix");
     VGB_REQUIRE(ldx >= n && ldy >= n && k >= 0, "bse_op_matmul: bad leading dimension or k");
@@ -187,6 +210,7 @@ int bse_op_diagonal_device(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd, i
 int bse_op_diagonal(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd, int32_t cd2, double *D) {
   return guarded([&] {
     require_handle(h);
+    vgb::AllocStreamScope alloc_scope(h->stream);
     VGB_REQUIRE(D != nullptr, "bse_op_diagonal: null output");
     const int64_t n = h->size();
     h->dD.resize(n);
@@ -202,6 +226,7 @@ int bse_ham_matmul(bse_handle *h, const int32_t a_coef[4], const int32_t b_coef[
                    const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy) {
   return guarded([&] {
     require_handle(h);
+    vgb::AllocStreamScope alloc_scope(h->stream);
     const int64_t n = 2 * h->size();
     VGB_REQUIRE(X && Y, "bse_ham_matmul: null matrix");
     VGB_REQUIRE(ldx >= n && ldy >= n && k >= 0, "bse_ham_matmul: bad leading dimension or k");
@@ -232,6 +257,7 @@ int bse_davidson_solve(bse_handle *h, const int32_t a_coef[4], const int32_t b_c
                        bse_davidson_result *result) {
   return guarded([&] {
     require_handle(h);
+    vgb::AllocStreamScope alloc_scope(h->stream);
     VGB_REQUIRE(opt != nullptr, "bse_davidson_solve: null options");
     const bool ham = opt->matrix_type == 1;
     std::unique_ptr<vgb::DeviceOperator> op;
@@ -277,6 +303,7 @@ int bse_op_eig_gradient(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd, int3
                         double *grad_mmn, double *grad_hqp, double *grad_screening) {
   return guarded([&] {
     require_handle(h);
+    vgb::AllocStreamScope alloc_scope(h->stream);
     VGB_REQUIRE(h->kind == 0, "bse_op_eig_gradient: not a BSE operator");
     VGB_REQUIRE(X && weights && nroots >= 1, "bse_op_eig_gradient: null eigenvectors or weights");
     vgb::BseOperator &op = *h->bse;
@@ -353,6 +380,49 @@ int bse_mmn_multiply_right(const bse_mmn_desc *mmn, double *const *mmn_slices, c
     VGB_REQUIRE(mmn && mmn_slices && U, "bse_mmn_multiply_right: null argument");
     TmpStream ts;
     vgb::mmn_multiply_right(*mmn, mmn_slices, U, ldu, ts.s);
+  });
+}
+
+int bse_davidson_solve_batch(bse_handle *const *handles, int64_t nhandles, const int32_t a_coef[4],
+                             const int32_t b_coef[4], const bse_davidson_options *opt,
+                             int64_t neigen, double *evals, int32_t *infos, int64_t *iterations,
+                             int32_t nthreads) {
+  return guarded([&] {
+    VGB_REQUIRE(handles && opt && evals && nhandles >= 0, "bse_davidson_solve_batch: null argument");
+    for (int64_t i = 0; i < nhandles; ++i) require_handle(handles[i]);
+    int dev = 0;
+    VGB_CUDA(cudaGetDevice(&dev));
+    const int nt = (int)std::max<int64_t>(1, std::min<int64_t>(nthreads > 0 ? nthreads : 8, nhandles));
+    std::atomic<int64_t> next(0);
+    std::mutex mu;
+    int first_code = 0;
+    int64_t first_index = nhandles;  // the lowest failing molecule is reported
+    std::string first_msg;
+    auto worker = [&] {
+      cudaSetDevice(dev);
+      for (;;) {
+        const int64_t i = next.fetch_add(1);
+        if (i >= nhandles) break;
+        bse_davidson_result r;
+        const int rc = bse_davidson_solve(handles[i], a_coef, b_coef, opt, neigen, nullptr, 0,
+                                          evals + i * neigen, nullptr, 0, &r);
+        if (rc != BSE_OK) {
+          std::lock_guard<std::mutex> lock(mu);
+          if (i < first_index) {
+            first_index = i;
+            first_code = rc;
+            first_msg = "molecule " + std::to_string(i) + ": " + bse_last_error();
+          }
+          continue;
+        }
+        if (infos) infos[i] = r.info;
+        if (iterations) iterations[i] = r.iterations;
+      }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nt; ++t) pool.emplace_back(worker);
+    for (auto &t : pool) t.join();
+    if (first_code != 0) vgb::fail(first_code, first_msg);
   });
 }
 

@@ -34,18 +34,40 @@ inline void cuda_check(cudaError_t e, const char *what, const char *file, int li
     if (!(cond)) ::vgb::fail(BSE_ERR_ARGUMENT, std::string(msg)); \
   } while (0)
 
+// Stream on which DeviceBuffer allocates and frees on the calling thread (set by
+// the C ABI entry points to the handle's stream).  With a stream set, buffers
+// use the stream-ordered allocator (cudaMallocAsync / cudaFreeAsync), which does
+// not synchronise the device, so independent handles can work concurrently.
+cudaStream_t &alloc_stream();
+struct AllocStreamScope {
+  cudaStream_t saved;
+  explicit AllocStreamScope(cudaStream_t s) : saved(alloc_stream()) { alloc_stream() = s; }
+  ~AllocStreamScope() { alloc_stream() = saved; }
+};
+void *device_alloc(size_t bytes, cudaStream_t &used);
+void device_free(void *p, cudaStream_t used);
+void trim_pool();  // return unused stream-ordered blocks to the driver
+
 // Owning device buffer.
 template <typename T>
 struct DeviceBuffer {
   T *ptr = nullptr;
   size_t count = 0;
+  cudaStream_t stream = nullptr;  // stream of the stream-ordered allocation (null: cudaMalloc)
   DeviceBuffer() = default;
   explicit DeviceBuffer(size_t n) { resize(n); }
   DeviceBuffer(const DeviceBuffer &) = delete;
   DeviceBuffer &operator=(const DeviceBuffer &) = delete;
-  DeviceBuffer(DeviceBuffer &&o) noexcept : ptr(o.ptr), count(o.count) { o.ptr = nullptr; o.count = 0; }
+  DeviceBuffer(DeviceBuffer &&o) noexcept : ptr(o.ptr), count(o.count), stream(o.stream) {
+    o.ptr = nullptr;
+    o.count = 0;
+  }
   DeviceBuffer &operator=(DeviceBuffer &&o) noexcept {
-    if (this != &o) { release(); ptr = o.ptr; count = o.count; o.ptr = nullptr; o.count = 0; }
+    if (this != &o) {
+      release();
+      ptr = o.ptr; count = o.count; stream = o.stream;
+      o.ptr = nullptr; o.count = 0;
+    }
     return *this;
   }
   ~DeviceBuffer() { release(); }
@@ -53,11 +75,11 @@ struct DeviceBuffer {
     if (n <= count && ptr) return;
     release();
     if (n == 0) return;
-    VGB_CUDA(cudaMalloc(&ptr, n * sizeof(T)));
+    ptr = (T *)device_alloc(n * sizeof(T), stream);
     count = n;
   }
   void release() {
-    if (ptr) cudaFree(ptr);
+    if (ptr) device_free(ptr, stream);
     ptr = nullptr;
     count = 0;
   }

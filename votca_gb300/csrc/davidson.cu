@@ -126,12 +126,6 @@ __global__ void scale_columns_kernel(double *A, int64_t lda, int64_t n, int64_t 
   }
 }
 
-// Gram-Schmidt linear-dependence check of one column (davidsonsolver.cc:472-475)
-__global__ void gs_check_kernel(const double *norm, const double *norm0, int *flag) {
-  if (threadIdx.x == 0 && blockIdx.x == 0)
-    if (!(norm[0] > 1e-12 * norm0[0])) flag[0] = 1;
-}
-
 __global__ void copy_block_kernel(const double *src, int64_t lds, double *dst, int64_t ldd,
                                   int64_t n, int64_t ncols) {
   const int64_t total = n * ncols;

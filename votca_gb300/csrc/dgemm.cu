@@ -1,6 +1,8 @@
 // FP64 strided batched GEMM (see dgemm.cuh for the design note).
 #include "dgemm.cuh"
 
+#include <mutex>
+
 namespace vgb {
 
 namespace {
@@ -138,13 +140,69 @@ __global__ void scale_kernel(const GemmDesc d, int64_t nbatch) {
 
 }  // namespace
 
-int sm_count() {
-  static int n = 0;
-  if (n == 0) {
+cudaStream_t &alloc_stream() {
+  static thread_local cudaStream_t s = nullptr;
+  return s;
+}
+
+namespace {
+// Freed blocks stay in the device's default pool instead of being returned to
+// the driver at every synchronisation (the Davidson loop synchronises once per
+// iteration); bse_op_destroy trims the pool.
+void keep_pool_blocks() {
+  static std::once_flag once;
+  std::call_once(once, [] {
     int dev = 0;
-    VGB_CUDA(cudaGetDevice(&dev));
-    VGB_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+    cudaMemPool_t pool;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t thr = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+  });
+}
+}  // namespace
+
+void *device_alloc(size_t bytes, cudaStream_t &used) {
+  void *p = nullptr;
+  used = alloc_stream();
+  if (used) {
+    keep_pool_blocks();
+    VGB_CUDA(cudaMallocAsync(&p, bytes, used));
+  } else {
+    VGB_CUDA(cudaMalloc(&p, bytes));
   }
+  return p;
+}
+
+// A stream-ordered block is freed on the stream of the running call, which is
+// ordered after every use in this call; uses in earlier calls on other streams
+// are complete by the handle's contract.  Outside a stream scope the free waits
+// for the device first, as cudaFree does.
+void device_free(void *p, cudaStream_t used) {
+  if (!used) {
+    cudaFree(p);
+  } else if (cudaStream_t cur = alloc_stream()) {
+    cudaFreeAsync(p, cur);
+  } else {
+    cudaDeviceSynchronize();
+    cudaFreeAsync(p, used);
+  }
+}
+
+void trim_pool() {
+  int dev = 0;
+  cudaMemPool_t pool;
+  if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess)
+    cudaMemPoolTrimTo(pool, 0);
+}
+
+int sm_count() {
+  static const int n = [] {
+    int dev = 0, v = 0;
+    VGB_CUDA(cudaGetDevice(&dev));
+    VGB_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
+    return v;
+  }();
   return n;
 }
 

@@ -18,6 +18,7 @@
 #include "tc_engine.cuh"
 
 #include <cstdlib>
+#include <mutex>
 
 #include "tc_gemm.cuh"
 
@@ -66,12 +67,12 @@ int pick_ksplit(int64_t tiles, int64_t K) {
   return (int)std::min<int64_t>(ks, std::max<int64_t>(1, K / 64));
 }
 void read_tuning() {
-  static bool done = false;
-  if (done) return;
-  done = true;
-  if (const char *e = getenv("VGB_TC_MAX_CHAIN")) g_max_chain = std::max(64LL, atoll(e));
-  if (const char *e = getenv("VGB_TC_PRODUCTS")) g_products = atoi(e) == 4 ? 4 : 3;
-  if (const char *e = getenv("VGB_TC_BK256")) g_bk256 = atoi(e) == 64 ? 64 : 32;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    if (const char *e = getenv("VGB_TC_MAX_CHAIN")) g_max_chain = std::max(64LL, atoll(e));
+    if (const char *e = getenv("VGB_TC_PRODUCTS")) g_products = atoi(e) == 4 ? 4 : 3;
+    if (const char *e = getenv("VGB_TC_BK256")) g_bk256 = atoi(e) == 64 ? 64 : 32;
+  });
 }
 
 }  // namespace

@@ -412,7 +412,7 @@ EncodeTiledFn encode_fn() {
   std::call_once(once, [] {
     void *p = nullptr;
     cudaDriverEntryPointQueryResult q;
-    VGB_CUDA(cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q));
+    VGB_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
     if (q != cudaDriverEntryPointSuccess || !p) fail(BSE_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
     fn = (EncodeTiledFn)p;
   });
@@ -438,12 +438,11 @@ void encode(CUtensorMap *m, const uint16_t *base, int64_t rows, int64_t K, int64
 template <int BN, int BK>
 void launch(const TcMat &A, const TcMat &B, const KParams &p, cudaStream_t s) {
   using C = Cfg<BN, BK>;
-  static bool attr = false;
-  if (!attr) {
+  static std::once_flag attr;
+  std::call_once(attr, [] {
     VGB_CUDA(cudaFuncSetAttribute(tc_gemm_kernel<BN, BK>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
-    attr = true;
-  }
+  });
   const int64_t grid = std::min<int64_t>(p.ntiles, sm_count());
   tc_gemm_kernel<BN, BK><<<(unsigned)grid, kThreads, C::SMEM, s>>>(A.map_hi, A.map_lo, B.map_hi,
                                                                    B.map_lo, p);

@@ -5,6 +5,10 @@ and xtp/src/libxtp/davidsonsolver.cc:101-170.  solve(op, neigen[, guess])
 mirrors both solve overloads (davidsonsolver.h:64-190); the whole iteration
 (projection, small eigenproblem, residuals, corrections, Gram-Schmidt,
 restart) is done by bse_davidson_solve in libvotca_gb300.so.
+
+solve_batch(ops, neigen) solves many independent molecules with the same
+options concurrently (bse_davidson_solve_batch); the reference solves one
+molecule per process.
 """
 from __future__ import annotations
 
@@ -78,6 +82,47 @@ class DavidsonSolver:
     def num_iterations(self):
         return self.i_iter_
 
+    def _options(self):
+        return _lib.bse_davidson_options(self.iter_max_, self.tol_, self.max_search_space_, self.correction_,
+                                         self.update_, self.matrix_type_, int(self.verbose))
+
+    def solve_batch(self, ops, neigen, nthreads=8):
+        """Lowest neigen eigenvalues of every operator in ops (BSE_OPERATORs with one
+        coefficient set, or DenseGpuOperators), solved concurrently on the GPU.
+        Returns (evals [len(ops) x neigen], info per molecule, iterations per molecule)."""
+        ops = list(ops)
+        n = len(ops)
+        if n == 0:
+            return np.zeros((0, neigen)), [], np.zeros(0, dtype=np.int64)
+        if self.matrix_type_ != MATRIX_TYPES["SYMM"]:
+            raise RuntimeError("DavidsonSolver.solve_batch: only SYMM operators are batched")
+        first = ops[0]
+        if isinstance(first, BSE_OPERATOR):
+            coef = first.coef
+            if any(not isinstance(o, BSE_OPERATOR) or o.coef != coef for o in ops):
+                raise TypeError("solve_batch: all operators must share one BSE_OPERATOR coefficient set")
+            L = first.ctx._L
+            handles = [o.ctx.handle for o in ops]
+        elif isinstance(first, DenseGpuOperator):
+            if any(not isinstance(o, DenseGpuOperator) for o in ops):
+                raise TypeError("solve_batch: mixed operator kinds")
+            coef = (0, 0, 0, 0)
+            L = first._L
+            handles = [o.handle for o in ops]
+        else:
+            raise TypeError("DavidsonSolver.solve_batch needs GPU operators")
+        harr = (ctypes.c_void_p * n)(*[h.value if isinstance(h, ctypes.c_void_p) else h for h in handles])
+        a = (ctypes.c_int32 * 4)(*coef)
+        b = (ctypes.c_int32 * 4)(0, 0, 0, 0)
+        opt = self._options()
+        evals = np.zeros((n, neigen))
+        infos = (ctypes.c_int32 * n)()
+        iters = (ctypes.c_int64 * n)()
+        _lib.check(L.bse_davidson_solve_batch(harr, n, a, b, ctypes.byref(opt), neigen, _p(evals), infos, iters,
+                                              int(nthreads)))
+        info = ["Success" if infos[i] == 0 else "NoConvergence" for i in range(n)]
+        return evals, info, np.array(iters[:], dtype=np.int64)
+
     def solve(self, A, neigen, initial_guess=None):
         if isinstance(A, HamiltonianOperator):
             if isinstance(A.A_, DenseGpuOperator):
@@ -99,8 +144,7 @@ class DavidsonSolver:
             n = A.rows()
         else:
             raise TypeError("DavidsonSolver.solve needs a GPU operator")
-        opt = _lib.bse_davidson_options(self.iter_max_, self.tol_, self.max_search_space_, self.correction_,
-                                        self.update_, self.matrix_type_, int(self.verbose))
+        opt = self._options()
         evals = np.zeros(neigen)
         evecs = np.zeros((n, neigen), order="F")
         res = _lib.bse_davidson_result()

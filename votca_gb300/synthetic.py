@@ -103,9 +103,21 @@ class Problem:
         self.coff = self.v
 
 
+def batched_shapes(n, seed=0):
+    """Shapes of n independent molecules: v ~ U{4..32}, c ~ U{32..256},
+    Naux ~ U{128..1024}, Nmo = v + c + 8, and a per-molecule seed."""
+    idx = np.arange(n, dtype=np.uint64)
+    v = 4 + np.floor(_uniform(seed, 21, idx) * 29).astype(int)
+    c = 32 + np.floor(_uniform(seed, 22, idx) * 225).astype(int)
+    naux = 128 + np.floor(_uniform(seed, 23, idx) * 897).astype(int)
+    return [dict(v=int(v[i]), c=int(c[i]), naux=int(naux[i]), nmo=int(v[i] + c[i] + 8),
+                 seed=int(seed * 100003 + i + 1)) for i in range(n)]
+
+
 CONFIGS = {
     # v, c, naux, nmo, roots
     "C0": dict(v=8, c=64, naux=256, nmo=72, roots=10),
     "C1": dict(v=64, c=512, naux=2048, nmo=576, roots=20),
     "C2": dict(v=128, c=1024, naux=4096, nmo=1152, roots=10),
+    "C3": dict(molecules=256, roots=5),  # shapes from batched_shapes
 }
