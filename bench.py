@@ -57,25 +57,10 @@ def dist_env():
 
 
 def make_mmn(seed, naux, nmo):
-    """Seeded Mmn, layout (m, P, n) == the reference's slices laid end to end.
-    Each aux slice is a symmetric N(0,1) matrix ((G + G^T)/sqrt(2) off the
-    diagonal, G_mm on it) times 0.1/sqrt(Naux) exp(-|m-n|/40); drawn on the GPU
-    when one is present."""
-    import torch
+    """Seeded Mmn, layout (m, P, n) == the reference's slices laid end to end."""
+    from votca_gb300.synthetic import mmn_tensor_torch
 
-    dev = "cuda" if torch.cuda.is_available() else "cpu"
-    g = torch.Generator(device=dev).manual_seed(seed)
-    m = torch.arange(nmo, dtype=torch.float64, device=dev)
-    decay = torch.exp(-(m[:, None] - m[None, :]).abs() / 40.0) * (0.1 / np.sqrt(naux))
-    out = torch.empty((nmo, naux, nmo), dtype=torch.float64)
-    chunk = 128
-    for p0 in range(0, naux, chunk):
-        p1 = min(naux, p0 + chunk)
-        G = torch.randn((p1 - p0, nmo, nmo), generator=g, dtype=torch.float64, device=dev)
-        M = (G + G.transpose(1, 2)) * (1.0 / np.sqrt(2.0))
-        M.diagonal(dim1=1, dim2=2).copy_(G.diagonal(dim1=1, dim2=2))
-        out[:, p0:p1, :] = (M * decay).permute(1, 0, 2).cpu()
-    return out.numpy()
+    return mmn_tensor_torch(seed, naux, nmo)
 
 
 class ClockSampler:
@@ -254,6 +239,85 @@ def batched_solve(n_molecules, nthreads, roots=5, tol=1e-7):
     }
 
 
+def full_bse_report(roots=10, tol=1e-7, k=32, check=False):
+    """Full (non-TDA) singlet BSE at v=128, c=1024 (dim 131072 per block),
+    Naux=4096, Nmo=1152: HAM Davidson on [[A, B], [-B, -A]] in mixed precision,
+    lowest `roots` roots; plus the HAM product throughput at k trial vectors.
+    With check, the mixed eigenpairs are evaluated with FP64 products:
+    omega = (X^T A X + Y^T A Y + 2 X^T B Y) / (X^T X - Y^T Y) (stationary in
+    the eigenvector error) and the FP64 residual."""
+    import ctypes
+
+    import torch
+
+    from votca_gb300 import _lib
+    from votca_gb300 import bse_operator as bo
+    from votca_gb300.bse import DavidsonOptions, solve_nonhermitian_davidson
+    from votca_gb300.synthetic import qp_energies, screening_w
+
+    v, c, naux, nmo, seed = 128, 1024, 4096, 1152, 2
+    t0 = time.perf_counter()
+    mmn = make_mmn(seed, naux, nmo)
+    t_gen = time.perf_counter() - t0
+    w = screening_w(seed, naux)
+    hqp = np.diag(qp_energies(seed, v, c))
+    opt = bo.BSEOperator_Options(homo=v - 1, rpamin=0, qpmin=0, vmin=0, cmax=v + c - 1)
+    t0 = time.perf_counter()
+    ctx = bo.GpuBSEContext(w, bo.TCMatrix_gwbse(mmn), hqp, opt, precision=bo.PRECISION_MIXED)
+    t_stage = time.perf_counter() - t0
+    A, B = bo.SingletOperator_TDA(ctx), bo.SingletOperator_BTDA_B(ctx)
+    n = ctx.size
+    # HAM product throughput through the host-pointer call (copies included)
+    L = ctx._L
+    rng = np.random.default_rng(4)
+    X = np.asfortranarray(rng.standard_normal((2 * n, k)))
+    Y = np.zeros_like(X)
+    a = (ctypes.c_int32 * 4)(*A.coef)
+    b = (ctypes.c_int32 * 4)(*B.coef)
+    _lib.check(L.bse_ham_matmul(ctx.handle, a, b, bo._p(X), 2 * n, k, bo._p(Y), 2 * n))
+    reps = 3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        _lib.check(L.bse_ham_matmul(ctx.handle, a, b, bo._p(X), 2 * n, k, bo._p(Y), 2 * n))
+    t_ham = (time.perf_counter() - t0) / reps
+    vc = v * c
+    flops_a = 2.0 * naux * vc * (v + c) + 4.0 * naux * vc + 2.0 * vc
+    flops_b = 4.0 * naux * v * v * c + 4.0 * naux * vc
+    F = 2 * k * (flops_a + flops_b)
+    dopt = DavidsonOptions(davidson_tolerance=tol, nmax=roots)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lam, Xr, Yr, ds = solve_nonhermitian_davidson(A, B, dopt)
+    t_solve = time.perf_counter() - t0
+    out = {
+        "workload": f"full_bse_singlet_v{v}_c{c}_naux{naux}_roots{roots}", "precision": "mixed",
+        "tolerance": tol, "mmn_generate_seconds": t_gen, "staging_seconds": t_stage,
+        "ham_matvec": {"k": k, "seconds": t_ham, "tflops": F / t_ham / 1e12,
+                       "flops": F, "note": "host-pointer call, H2D/D2H of 2 x 2n x k doubles included"},
+        "time_to_roots_seconds": t_solve, "iterations": int(ds.num_iterations()), "info": ds.info(),
+        "matvec_seconds": ds.result.seconds_matvec, "matvec_columns": int(ds.result.matvec_columns),
+        "roots_eV": [round(float(x), 9) for x in lam],
+    }
+    ctx.close()
+    if check:
+        c64 = bo.GpuBSEContext(w, bo.TCMatrix_gwbse(mmn), hqp, opt, precision=bo.PRECISION_FP64)
+        A64, B64 = bo.SingletOperator_TDA(c64), bo.SingletOperator_BTDA_B(c64)
+        XY = np.asfortranarray(np.hstack([Xr, Yr]))
+        AXY, BXY = A64.matmul(XY), B64.matmul(XY)
+        AX, AY, BX, BY = AXY[:, :roots], AXY[:, roots:], BXY[:, :roots], BXY[:, roots:]
+        num = np.sum(Xr * AX, 0) + np.sum(Yr * AY, 0) + 2 * np.sum(Xr * BY, 0)
+        den = np.sum(Xr * Xr, 0) - np.sum(Yr * Yr, 0)
+        om = num / den
+        r1 = AX + BY - Xr * om
+        r2 = -BX - AY - Yr * om
+        res = np.sqrt(np.sum(r1 * r1, 0) + np.sum(r2 * r2, 0)) / np.sqrt(np.sum(Xr * Xr, 0) + np.sum(Yr * Yr, 0))
+        out["fp64_check"] = {"omega_fp64_eV": [round(float(x), 9) for x in om],
+                             "max_abs_diff_meV": float(np.max(np.abs(om - lam)) * 1e3),
+                             "max_fp64_residual": float(res.max())}
+        c64.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -268,6 +332,9 @@ def main():
     ap.add_argument("--molecules", type=int, default=256,
                     help="batched independent molecules (0 skips the batched solve report)")
     ap.add_argument("--batch-threads", type=int, default=16, help="host threads of the batched solve")
+    ap.add_argument("--full-bse", action="store_true",
+                    help="also run the full-BSE report (v=128, c=1024, Naux=4096; minutes, ~110 GB of HBM)")
+    ap.add_argument("--full-bse-check", action="store_true", help="FP64 evaluation of the full-BSE roots")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -442,6 +509,7 @@ def main():
     }
     if rank == 0 and not args.no_roots:
         roots = {}
+        evecs = {}
         for pname, pr in (("fp64", bo.PRECISION_FP64), ("mixed", bo.PRECISION_MIXED)):
             try:
                 c2 = ctx if pr == precision else bo.GpuBSEContext(w, Mmn, hqp, opt, precision=pr)
@@ -453,23 +521,29 @@ def main():
             ds.set_max_search_space(10 * ROOTS)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            lam, _ = ds.solve(bo.SingletOperator_TDA(c2), ROOTS)
+            lam, vecs = ds.solve(bo.SingletOperator_TDA(c2), ROOTS)
             dt = time.perf_counter() - t0
+            evecs[pname] = vecs
             roots[pname] = {"seconds": dt, "iterations": int(ds.num_iterations()), "info": ds.info(),
                             "matvec_seconds": ds.result.seconds_matvec,
                             "matvec_columns": int(ds.result.matvec_columns),
                             "roots_eV": [round(float(x), 9) for x in lam]}
             if c2 is not ctx:
                 c2.close()
-        if "lam" in roots.get("fp64", {}) and "roots_eV" in roots.get("mixed", {}):
-            pass
         if "roots_eV" in roots.get("fp64", {}) and "roots_eV" in roots.get("mixed", {}):
             d = np.abs(np.array(roots["fp64"]["roots_eV"]) - np.array(roots["mixed"]["roots_eV"])) * 1e3
             roots["max_abs_diff_meV"] = float(d.max())
+            # |<x_fp64, x_mixed>| per root (unit vectors; 1 = identical up to sign)
+            ov = np.abs(np.sum(evecs["fp64"] * evecs["mixed"], axis=0))
+            roots["min_eigvec_overlap"] = float(ov.min())
+            roots["max_one_minus_overlap"] = float((1.0 - ov).max())
         line["time_to_20_roots"] = roots
-    if rank == 0 and args.molecules > 0:
+    if rank == 0 and (args.molecules > 0 or args.full_bse):
         ctx.close()
+    if rank == 0 and args.molecules > 0:
         line["batched"] = batched_solve(args.molecules, args.batch_threads)
+    if rank == 0 and args.full_bse:
+        line["full_bse"] = full_bse_report(check=args.full_bse_check)
     if rank == 0 and world == 1 and not args.no_cpu:
         cb = cpu_baseline(mmn, w, hqp)
         cb.pop("seconds_per_matvec", None)

@@ -60,6 +60,28 @@ def mmn_tensor(seed, naux, nmo, dtype=np.float64):
     return out
 
 
+def mmn_tensor_torch(seed, naux, nmo):
+    """Same distribution as mmn_tensor, drawn with torch's seeded generator on
+    the GPU when one is present (large sizes).  Each aux slice is a symmetric
+    N(0,1) matrix ((G + G^T)/sqrt(2) off the diagonal, G_mm on it) times
+    0.1/sqrt(Naux) exp(-|m-n|/40).  Layout (m, P, n), float64 host array."""
+    import torch
+
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    g = torch.Generator(device=dev).manual_seed(int(seed))
+    m = torch.arange(nmo, dtype=torch.float64, device=dev)
+    decay = torch.exp(-(m[:, None] - m[None, :]).abs() / 40.0) * (0.1 / np.sqrt(naux))
+    out = torch.empty((nmo, naux, nmo), dtype=torch.float64)
+    chunk = 128
+    for p0 in range(0, naux, chunk):
+        p1 = min(naux, p0 + chunk)
+        G = torch.randn((p1 - p0, nmo, nmo), generator=g, dtype=torch.float64, device=dev)
+        M = (G + G.transpose(1, 2)) * (1.0 / np.sqrt(2.0))
+        M.diagonal(dim1=1, dim2=2).copy_(G.diagonal(dim1=1, dim2=2))
+        out[:, p0:p1, :] = (M * decay).permute(1, 0, 2).cpu()
+    return out.numpy()
+
+
 def qp_energies(seed, v, c):
     occ = np.sort(-20.0 + 15.0 * _uniform(seed, 11, np.arange(v, dtype=np.uint64)))
     virt = np.sort(0.5 + 29.5 * _uniform(seed, 12, np.arange(c, dtype=np.uint64)))
