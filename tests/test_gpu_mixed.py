@@ -66,6 +66,26 @@ def test_mixed_many_vectors_chunked():
     assert np.linalg.norm(ym - yf) / np.linalg.norm(inter) < REL_TOL
 
 
+@pytest.mark.parametrize("v,c,naux,seed", [
+    (5, 200, 700, 21),   # ragged K of the Hd2 stage-2 chain (naux * v = 3500)
+    (20, 64, 3000, 22),  # long aux chains (K = 60000 split into chains of <= 1024)
+])
+def test_mixed_long_aux_products(v, c, naux, seed):
+    """Products with many aux functions per (v, c) pair, 30 vectors."""
+    from votca_gb300 import bse_operator as bo
+
+    p = Problem(v=v, c=c, naux=naux, nmo=v + c, seed=seed)
+    f, m = contexts(p, v, c)
+    X = np.random.default_rng(seed).standard_normal((v * c, 30))
+    hq = bo.HqpOperator(f).matmul(X)
+    for op in ("hd", "hd2", "singlet", "singlet_b"):
+        yf = bo.BSE_OPERATOR(f, *oracle.OPERATORS[op]).matmul(X)
+        ym = bo.BSE_OPERATOR(m, *oracle.OPERATORS[op]).matmul(X)
+        inter = yf - (hq if oracle.OPERATORS[op][0] else 0)
+        err = np.linalg.norm(ym - yf) / np.linalg.norm(inter)
+        assert err < REL_TOL, (op, err)
+
+
 def test_mixed_davidson_roots_within_tolerance():
     """C0 singlets and triplets, 10 roots at residual 1e-7: every root within 0.01 meV of FP64."""
     from votca_gb300 import bse_operator as bo

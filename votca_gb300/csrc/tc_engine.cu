@@ -174,20 +174,22 @@ void MixedEngine::apply(BseOperator &op, const Coef &c, const double *X, int64_t
     sh.M = naux; sh.N = k; sh.K = m.dimP; sh.products = g_products;
     sh.ksplit = pick_ksplit(ceil_div(naux, 128) * ceil_div(k, bn), m.dimP);
     m.part.resize((size_t)sh.ksplit * naux * k);
+    // partials column-major [split][j][P]: the epilogue lanes (rows P) store contiguously
     TcEpilogue e;
     e.kind = TcEpilogue::STORE_F32;
-    e.rd = naux; e.ro2 = k; e.rlim = naux;
-    e.cd = k; e.co2 = 1; e.clim = k;
+    e.rd = naux; e.ro2 = 1; e.rlim = naux;
+    e.cd = k; e.co2 = naux; e.clim = k;
     e.so = naux * k;
     e.out_f32 = m.part.get();
     const int ks = tc_gemm(A, B, sh, e, bn, err, s);
     m.Zs.ensure(k, m.Kn, s);
+    // reduced as the transposed (j x P) problem, so that reads and writes run along P
     TcEpilogue r;
     r.kind = TcEpilogue::SPLIT_BF16;
-    r.rd = naux; r.ro2 = 1; r.rlim = naux;
-    r.cd = k; r.co2 = m.Kn; r.clim = k;
+    r.rd = k; r.ro2 = m.Kn; r.rlim = k;
+    r.cd = naux; r.co2 = 1; r.clim = naux;
     r.out_hi = m.Zs.hi.get(); r.out_lo = m.Zs.lo.get();
-    reduce_partials(m.part.get(), naux, k, ks, r, s);
+    reduce_partials(m.part.get(), k, naux, ks, r, s);
     // Y(I, j) (+)= cx sum_P BvcT[I'][P] Zs[j][P]
     TcMat A2 = make_tc_mat(m.BvcT.hi.get(), m.BvcT.lo.get(), m.dimP, m.Kn, m.Kn, 128, bk_for(bn));
     TcMat B2 = make_tc_mat(m.Zs.hi.get(), m.Zs.lo.get(), k, m.Kn, m.Kn, bn, bk_for(bn));
@@ -241,19 +243,21 @@ void MixedEngine::apply(BseOperator &op, const Coef &c, const double *X, int64_t
         s2.M = kc * ct; s2.N = vt; s2.K = m.Kg; s2.products = g_products;
         s2.ksplit = pick_ksplit(ceil_div(kc * ct, 128) * ceil_div(vt, bn2), m.Kg);
         m.part.resize((size_t)s2.ksplit * s2.M * s2.N);
+        // partials column-major [split][v1][(j, c1)] (coalesced epilogue stores)
         TcEpilogue p;
         p.kind = TcEpilogue::STORE_F32;
-        p.rd = s2.M; p.ro2 = s2.N; p.rlim = s2.M;
-        p.cd = s2.N; p.co2 = 1; p.clim = s2.N;
+        p.rd = s2.M; p.ro2 = 1; p.rlim = s2.M;
+        p.cd = s2.N; p.co2 = s2.M; p.clim = s2.N;
         p.so = s2.M * s2.N;
         p.out_f32 = m.part.get();
         const int ks = tc_gemm(As, Bg, s2, p, bn2, err, s);
+        // reduced as the transposed problem: rows v1, columns (j, c1)
         TcEpilogue r;
         r.kind = TcEpilogue::AXPBY_F64;
-        r.rd = ct; r.ro1 = ldy; r.ro2 = 1; r.rlim = ct;
-        r.cd = vt; r.co2 = ct; r.clim = vt;
+        r.rd = vt; r.ro2 = ct; r.rlim = vt;
+        r.cd = ct; r.co1 = ldy; r.co2 = 1; r.clim = ct;
         r.out_f64 = Y + j0 * ldy; r.alpha = alpha; r.beta = acc ? 1.0 : 0.0;
-        reduce_partials(m.part.get(), s2.M, s2.N, ks, r, s);
+        reduce_partials(m.part.get(), s2.N, s2.M, ks, r, s);
         op.timer.end(STAGE_TC_HD_B, s);
         if (j0 + jc < k) op.timer.begin(STAGE_TC_HD, s);
       } else {
@@ -279,19 +283,21 @@ void MixedEngine::apply(BseOperator &op, const Coef &c, const double *X, int64_t
         s2.M = ct; s2.N = kc * vt; s2.K = m.Kg; s2.products = g_products;
         s2.ksplit = pick_ksplit(ceil_div(ct, 128) * ceil_div(kc * vt, bn2), m.Kg);
         m.part.resize((size_t)s2.ksplit * s2.M * s2.N);
+        // partials column-major [split][(j, v1)][c1] (coalesced epilogue stores)
         TcEpilogue p;
         p.kind = TcEpilogue::STORE_F32;
-        p.rd = s2.M; p.ro2 = s2.N; p.rlim = s2.M;
-        p.cd = s2.N; p.co2 = 1; p.clim = s2.N;
+        p.rd = s2.M; p.ro2 = 1; p.rlim = s2.M;
+        p.cd = s2.N; p.co2 = s2.M; p.clim = s2.N;
         p.so = s2.M * s2.N;
         p.out_f32 = m.part.get();
         const int ks = tc_gemm(Am, Bu, s2, p, bn2, err, s);
+        // reduced as the transposed problem: rows (j, v1), columns c1
         TcEpilogue r;
         r.kind = TcEpilogue::AXPBY_F64;
-        r.rd = ct; r.ro2 = 1; r.rlim = ct;
-        r.cd = vt; r.co1 = ldy; r.co2 = ct; r.clim = vt;
+        r.rd = vt; r.ro1 = ldy; r.ro2 = ct; r.rlim = vt;
+        r.cd = ct; r.co2 = 1; r.clim = ct;
         r.out_f64 = Y + j0 * ldy; r.alpha = alpha; r.beta = acc ? 1.0 : 0.0;
-        reduce_partials(m.part.get(), s2.M, s2.N, ks, r, s);
+        reduce_partials(m.part.get(), s2.N, s2.M, ks, r, s);
         op.timer.end(STAGE_TC_HD2_B, s);
         if (j0 + jc < k) op.timer.begin(STAGE_TC_HD2, s);
       }
