@@ -257,14 +257,17 @@ int bse_op_eig_gradient(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd,
                         double *grad_mmn, double *grad_hqp,
                         double *grad_screening);
 
-/* Many independent molecules (one handle each, e.g. of uneven BSE dimension):
- * solves every handle's operator with bse_davidson_solve semantics (no guess,
- * eigenvalues only) on nthreads host threads, each handle on its own stream with
- * stream-ordered scratch, so the small per-molecule kernels of different
- * molecules run concurrently on the GPU.  evals: nhandles x neigen (row per
- * molecule); infos / iterations: per molecule, may be NULL.  No counterpart in
- * the reference, which solves one molecule per process (xtp_parallel farms jobs,
- * xtp/src/libxtp/parallelxjobcalc.cc:52-74). */
+/* Many independent molecules (one handle each, e.g. of uneven BSE dimension),
+ * bse_davidson_solve semantics (no guess, eigenvalues only).
+ * nthreads <= 0: lockstep -- all molecules iterate together and every step of an
+ *   iteration (tensor-core product stages, projections, Ritz vectors, DPR
+ *   corrections, Gram-Schmidt) is one grouped launch over the molecules still
+ *   iterating; needs BSE operator handles, matrix_type SYMM and DPR.
+ * nthreads > 0: one independent solve per handle on that many host threads, each
+ *   on its handle's stream with stream-ordered scratch (any handle and options).
+ * evals: nhandles x neigen (row per molecule); infos / iterations: per molecule,
+ * may be NULL.  No counterpart in the reference, which solves one molecule per
+ * process (xtp_parallel farms jobs, xtp/src/libxtp/parallelxjobcalc.cc:52-74). */
 int bse_davidson_solve_batch(bse_handle *const *handles, int64_t nhandles,
                              const int32_t a_coef[4], const int32_t b_coef[4],
                              const bse_davidson_options *opt, int64_t neigen,

@@ -1,8 +1,9 @@
 """Batched solves of independent molecules (bse_davidson_solve_batch).
 
-Molecules of uneven shape are solved concurrently, each handle on its own
-stream; every molecule's roots must equal those of its own single solve and,
-in FP64, the dense eigenvalues of its TDA singlet Hamiltonian.
+Molecules of uneven shape are solved (a) concurrently, each handle on its own
+stream, and (b) in lockstep with one grouped launch per step.  Every
+molecule's roots must equal those of its own single solve and, in FP64, the
+dense eigenvalues of its TDA singlet Hamiltonian.
 """
 import numpy as np
 import pytest
@@ -29,12 +30,12 @@ def _contexts(precision):
     return out
 
 
-def _solver():
+def _solver(max_space=50):
     from votca_gb300.davidson import DavidsonSolver
 
     ds = DavidsonSolver()
     ds.set_tolerance(1e-7)
-    ds.set_max_search_space(50)
+    ds.set_max_search_space(max_space)
     return ds
 
 
@@ -62,6 +63,73 @@ def test_batch_equals_single_solves(precision):
         ctx.close()
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("max_space", [50, 14])  # 14: restarts (restart 10 + update 7 > 14)
+def test_lockstep_equals_single_solves(precision, max_space):
+    from votca_gb300 import bse_operator as bo
+
+    ctxs = _contexts(precision)
+    ops = [bo.SingletOperator_TDA(ctx) for _, ctx in ctxs]
+    nroots = 5
+    ev, info, iters = _solver(max_space).solve_batch(ops, nroots, nthreads=0)
+    assert all(i == "Success" for i in info)
+    for m, op in enumerate(ops):
+        ds = _solver(max_space)
+        lam, _ = ds.solve(op, nroots)
+        # the same iteration; the FP64 reduction orders of the grouped kernels differ (and
+        # for split precision the K splits of the grouped products, which only need to
+        # bound the FP32 chains), which can move a residual at the tolerance across it
+        np.testing.assert_allclose(ev[m], lam, rtol=0, atol=1e-10 if precision == 0 else 1e-7)
+        if precision == 0:
+            assert abs(iters[m] - ds.num_iterations()) <= 1
+        if precision == 0:
+            H = op.matmul(np.eye(op.rows()))
+            exact = np.linalg.eigvalsh(0.5 * (H + H.T))[:nroots]
+            np.testing.assert_allclose(ev[m], exact, rtol=0, atol=1e-9)
+    for _, ctx in ctxs:
+        ctx.close()
+
+
+def test_lockstep_triplets_and_tight_tolerance():
+    """FP64 operators (a 1e-9 residual is below the split-precision floor)."""
+    from votca_gb300 import bse_operator as bo
+    from votca_gb300.davidson import DavidsonSolver
+
+    ctxs = _contexts(0)
+    ops = [bo.TripletOperator_TDA(ctx) for _, ctx in ctxs]
+    ds = DavidsonSolver()
+    ds.set_tolerance("lapack")
+    ds.set_max_search_space(40)
+    ev, info, _ = ds.solve_batch(ops, 3, nthreads=0)
+    assert all(i == "Success" for i in info)
+    for m, op in enumerate(ops):
+        d1 = DavidsonSolver()
+        d1.set_tolerance("lapack")
+        d1.set_max_search_space(40)
+        lam, _ = d1.solve(op, 3)
+        np.testing.assert_allclose(ev[m], lam, rtol=0, atol=1e-10)
+    for _, ctx in ctxs:
+        ctx.close()
+
+
+def test_lockstep_reports_failing_molecule():
+    from votca_gb300 import _lib
+    from votca_gb300 import bse_operator as bo
+
+    ctxs = _contexts(1)[:3]
+    ops = [bo.SingletOperator_TDA(ctx) for _, ctx in ctxs]
+    with pytest.raises(_lib.BSEError, match="molecule 0"):
+        _solver().solve_batch(ops, ops[0].rows() + 1, nthreads=0)
+    with pytest.raises(_lib.BSEError):
+        ds = _solver()
+        ds.set_correction("OLSEN")  # lockstep supports DPR only
+        ds.solve_batch(ops, 3, nthreads=0)
+    ev, info, _ = _solver().solve_batch(ops, 3, nthreads=0)
+    assert all(i == "Success" for i in info)
+    for _, ctx in ctxs:
+        ctx.close()
+
+
 def test_batch_repeated_is_deterministic():
     from votca_gb300 import bse_operator as bo
 
@@ -70,6 +138,9 @@ def test_batch_repeated_is_deterministic():
     a, _, _ = _solver().solve_batch(ops, 5, nthreads=8)
     b, _, _ = _solver().solve_batch(ops, 5, nthreads=3)
     np.testing.assert_array_equal(a, b)
+    c, _, _ = _solver().solve_batch(ops, 5, nthreads=0)
+    d, _, _ = _solver().solve_batch(ops, 5, nthreads=0)
+    np.testing.assert_array_equal(c, d)
     for _, ctx in ctxs:
         ctx.close()
 

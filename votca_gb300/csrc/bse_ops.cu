@@ -90,6 +90,37 @@ __global__ void hqp_diag_kernel(double cqp, const double *__restrict__ Hcc,
   }
 }
 
+struct HqpJob {
+  double cqp;
+  const double *Hcc, *Hvv;
+  int64_t vt, ct;
+  const double *X;
+  int64_t ldx, k;
+  double *Y;
+  int64_t ldy;
+  int accumulate;
+};
+constexpr int kHqpJobsMax = 128;
+struct HqpGroup {
+  HqpJob j[kHqpJobsMax];
+  int n;
+};
+static_assert(sizeof(HqpGroup) <= 32000, "Hqp job list too large");
+
+__global__ void hqp_diag_group_kernel(const __grid_constant__ HqpGroup g) {
+  const HqpJob q = g.j[blockIdx.y];
+  const int64_t dim = q.vt * q.ct, total = dim * q.k;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t I = t % dim, j = t / dim;
+    const int64_t v = I / q.ct, c = I % q.ct;
+    const double e = q.Hcc[c + q.ct * c] - q.Hvv[v + q.vt * v];
+    const double val = q.cqp * e * q.X[I + q.ldx * j];
+    double *y = q.Y + I + q.ldy * j;
+    *y = q.accumulate ? *y + val : val;
+  }
+}
+
 __global__ void zero_cols_kernel(double *Y, int64_t ldy, int64_t rows, int64_t k) {
   const int64_t total = rows * k;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
@@ -105,9 +136,8 @@ struct DiagArgs {
 };
 
 // BSE_OPERATOR::diagonal (bse_operator.cc:133-175), one thread per pair.
-__global__ void diagonal_kernel(const DiagArgs a) {
-  for (int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; I < a.dim;
-       I += (int64_t)gridDim.x * blockDim.x) {
+__device__ __forceinline__ void diagonal_range(const DiagArgs &a, int64_t I0, int64_t step) {
+  for (int64_t I = I0; I < a.dim; I += step) {
     const int64_t v = I / a.ct, c = I % a.ct;
     double entry = 0.0;
     if (a.cx != 0.0) {
@@ -131,6 +161,22 @@ __global__ void diagonal_kernel(const DiagArgs a) {
     }
     a.D[I] = entry;
   }
+}
+
+__global__ void diagonal_kernel(const DiagArgs a) {
+  diagonal_range(a, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, (int64_t)gridDim.x * blockDim.x);
+}
+
+constexpr int kDiagJobsMax = 192;
+struct DiagGroup {
+  DiagArgs j[kDiagJobsMax];
+  int n;
+};
+static_assert(sizeof(DiagGroup) <= 32000, "diagonal job list too large");
+
+__global__ void diagonal_group_kernel(const __grid_constant__ DiagGroup g) {
+  const DiagArgs a = g.j[blockIdx.y];
+  diagonal_range(a, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, (int64_t)gridDim.x * blockDim.x);
 }
 
 __global__ void ham_combine_kernel(const double *__restrict__ TA, const double *__restrict__ TB,
@@ -531,6 +577,45 @@ void BseOperator::matmul(const Coef &c, const double *X, int64_t ldx, int64_t k,
   }
 }
 
+void matmul_grouped(const Coef &c, const std::vector<GroupedItem> &items, cudaStream_t s) {
+  VGB_REQUIRE(c.cd2 == 0, "grouped products: Hd2 is not grouped");
+  std::vector<GroupedItem> mixed_items;
+  std::vector<HqpJob> hq;
+  for (const GroupedItem &it : items) {
+    BseOperator &op = *it.op;
+    VGB_REQUIRE(it.ldx >= op.dim && it.ldy >= op.dim, "matmul: leading dimension smaller than the operator size");
+    if (it.k <= 0) continue;
+    if (op.precision != BSE_PRECISION_MIXED || !op.mixed) {  // FP64 operators: one product each
+      op.matmul(c, it.X, it.ldx, it.k, it.Y, it.ldy, s);
+      continue;
+    }
+    if (c.cqp != 0) {
+      if (op.hqp_diagonal) {
+        HqpJob j;
+        j.cqp = c.cqp; j.Hcc = op.Hcc.get(); j.Hvv = op.Hvv.get(); j.vt = op.vt; j.ct = op.ct;
+        j.X = it.X; j.ldx = it.ldx; j.k = it.k; j.Y = it.Y; j.ldy = it.ldy; j.accumulate = 0;
+        hq.push_back(j);
+      } else {
+        op.apply_hqp(c.cqp, it.X, it.ldx, it.k, it.Y, it.ldy, false, s);
+      }
+    }
+    mixed_items.push_back(it);
+  }
+  std::unique_ptr<HqpGroup> g(new HqpGroup());
+  for (size_t i = 0; i < hq.size();) {
+    g->n = 0;
+    int64_t mx = 0;
+    for (; i < hq.size() && g->n < kHqpJobsMax; ++i) {
+      g->j[g->n++] = hq[i];
+      mx = std::max(mx, hq[i].vt * hq[i].ct * hq[i].k);
+    }
+    const unsigned bx = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(mx, 256), 64));
+    hqp_diag_group_kernel<<<dim3(bx, (unsigned)g->n), 256, 0, s>>>(*g);
+    VGB_LAUNCH_CHECK();
+  }
+  MixedEngine::apply_grouped(c, mixed_items, c.cqp != 0, s);
+}
+
 void BseOperator::check_errors(cudaStream_t s) {
   if (mixed) mixed->check(s);
 }
@@ -544,6 +629,28 @@ void BseOperator::diagonal(const Coef &c, double *D, cudaStream_t s) {
   a.Hcc = Hcc.get(); a.Hvv = Hvv.get(); a.D = D;
   diagonal_kernel<<<grid_for(dim, 128), 128, 0, s>>>(a);
   VGB_LAUNCH_CHECK();
+}
+
+void diagonal_grouped(const Coef &c, const std::vector<BseOperator *> &ops,
+                      const std::vector<double *> &D, cudaStream_t s) {
+  VGB_REQUIRE(!(c.cd != 0 && c.cd2 != 0), "Hamiltonian cannot contain Hd and Hd2 at the same time");
+  VGB_REQUIRE(ops.size() == D.size(), "diagonal_grouped: one output per operator");
+  std::unique_ptr<DiagGroup> g(new DiagGroup());
+  for (size_t i = 0; i < ops.size();) {
+    g->n = 0;
+    int64_t mx = 1;
+    for (; i < ops.size() && g->n < kDiagJobsMax; ++i) {
+      const BseOperator &op = *ops[i];
+      DiagArgs &a = g->j[g->n++];
+      a.cqp = c.cqp; a.cx = c.cx; a.cd = c.cd; a.cd2 = c.cd2;
+      a.vt = op.vt; a.ct = op.ct; a.naux = op.naux; a.dim = op.dim;
+      a.Bvc = op.Bvc.get(); a.Mcv = op.Mcv.get(); a.dcc = op.dcc.get(); a.dvv = op.dvv.get();
+      a.Hcc = op.Hcc.get(); a.Hvv = op.Hvv.get(); a.D = D[i];
+      mx = std::max(mx, op.dim);
+    }
+    diagonal_group_kernel<<<dim3((unsigned)ceil_div(mx, 128), (unsigned)g->n), 128, 0, s>>>(*g);
+    VGB_LAUNCH_CHECK();
+  }
 }
 
 void BseOperator::ham_matmul(const Coef &a, const Coef &b, const double *X, int64_t ldx, int64_t k,

@@ -137,6 +137,22 @@ class BseOperator {
   DeviceBuffer<double> hamA_, hamB_, hamX_;
 };
 
+// One molecule's share of a grouped product: Y = H(c) X on its own operator.
+struct GroupedItem {
+  BseOperator *op = nullptr;
+  const double *X = nullptr;
+  int64_t ldx = 0, k = 0;
+  double *Y = nullptr;
+  int64_t ldy = 0;
+};
+// Products of many operators with one coefficient set, stage by stage: every
+// tensor-core stage of all mixed-precision operators runs as grouped launches
+// (FP64 operators fall back to one product each).  Hd2 is not supported here.
+void matmul_grouped(const Coef &c, const std::vector<GroupedItem> &items, cudaStream_t s);
+// Diagonals of many operators (same arithmetic as BseOperator::diagonal) in one launch per 192.
+void diagonal_grouped(const Coef &c, const std::vector<BseOperator *> &ops,
+                      const std::vector<double *> &D, cudaStream_t s);
+
 struct BseApply : DeviceOperator {
   BseOperator *op;
   Coef coef;

@@ -9,6 +9,7 @@
 #include <string>
 
 #include "bse_ops.cuh"
+#include "batch_davidson.cuh"
 #include "davidson.cuh"
 
 struct bse_handle {
@@ -49,6 +50,12 @@ vgb::Coef coef(int32_t a, int32_t b, int32_t c, int32_t d) {
 }
 
 void require_handle(const bse_handle *h) { VGB_REQUIRE(h != nullptr, "null handle"); }
+
+struct TmpStream {
+  cudaStream_t s = nullptr;
+  TmpStream() { VGB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)); }
+  ~TmpStream() { if (s) cudaStreamDestroy(s); }
+};
 
 void create_stream(bse_handle *h) {
   VGB_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
@@ -348,11 +355,6 @@ int bse_op_eig_gradient(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd, int3
 }
 
 namespace {
-struct TmpStream {
-  cudaStream_t s = nullptr;
-  TmpStream() { VGB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)); }
-  ~TmpStream() { if (s) cudaStreamDestroy(s); }
-};
 }  // namespace
 
 int bse_rpa_epsilon(const bse_mmn_desc *mmn, const double *const *mmn_slices,
@@ -390,6 +392,21 @@ int bse_davidson_solve_batch(bse_handle *const *handles, int64_t nhandles, const
   return guarded([&] {
     VGB_REQUIRE(handles && opt && evals && nhandles >= 0, "bse_davidson_solve_batch: null argument");
     for (int64_t i = 0; i < nhandles; ++i) require_handle(handles[i]);
+    if (nhandles == 0) return;
+    if (nthreads <= 0) {
+      // lockstep: every step one grouped launch over all molecules
+      VGB_REQUIRE(a_coef != nullptr, "bse_davidson_solve_batch: null operator coefficients");
+      std::vector<vgb::BseOperator *> ops;
+      for (int64_t i = 0; i < nhandles; ++i) {
+        VGB_REQUIRE(handles[i]->kind == 0, "bse_davidson_solve_batch: lockstep mode needs BSE operators");
+        if (handles[i]->stream) VGB_CUDA(cudaStreamSynchronize(handles[i]->stream));
+        ops.push_back(handles[i]->bse.get());
+      }
+      TmpStream ts;
+      vgb::davidson_solve_batch(ops, coef(a_coef[0], a_coef[1], a_coef[2], a_coef[3]), neigen, *opt,
+                                evals, infos, iterations, ts.s);
+      return;
+    }
     int dev = 0;
     VGB_CUDA(cudaGetDevice(&dev));
     const int nt = (int)std::max<int64_t>(1, std::min<int64_t>(nthreads > 0 ? nthreads : 8, nhandles));

@@ -184,8 +184,8 @@ void device_free(void *p, cudaStream_t used) {
   } else if (cudaStream_t cur = alloc_stream()) {
     cudaFreeAsync(p, cur);
   } else {
-    cudaDeviceSynchronize();
-    cudaFreeAsync(p, used);
+    cudaDeviceSynchronize();  // nothing is in flight: any stream may take the free
+    cudaFreeAsync(p, 0);
   }
 }
 

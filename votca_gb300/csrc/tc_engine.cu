@@ -18,6 +18,8 @@
 #include "tc_engine.cuh"
 
 #include <cstdlib>
+#include <map>
+#include <tuple>
 #include <mutex>
 
 #include "tc_gemm.cuh"
@@ -85,6 +87,16 @@ struct MixedEngine::Impl {
   DeviceBuffer<float> part;
   DeviceBuffer<int> err;
   int64_t s_budget_bytes = 4LL << 30;
+  // operand descriptors of the grouped products, encoded once per (buffer, shape)
+  // (the key holds every value the descriptors encode, so a hit is exact even when an
+  // address is reused by a later allocation)
+  std::map<std::tuple<const void *, const void *, int64_t, int64_t, int, int>, TcMat> maps;
+  const TcMat &mat(const uint16_t *hi, const uint16_t *lo, int64_t rows, int64_t K, int box_rows, int bk) {
+    const auto key = std::make_tuple((const void *)hi, (const void *)lo, rows, K, box_rows, bk);
+    auto it = maps.find(key);
+    if (it == maps.end()) it = maps.emplace(key, make_tc_mat(hi, lo, rows, K, K, box_rows, bk)).first;
+    return it->second;
+  }
 };
 
 MixedEngine::MixedEngine() : impl_(new Impl()) {}
@@ -219,18 +231,17 @@ void MixedEngine::apply(BseOperator &op, const Coef &c, const double *X, int64_t
       const int64_t kc = std::min(jc, k - j0);
       const uint16_t *xh = m.Xs.hi.get() + j0 * vt * m.Kc, *xl = m.Xs.lo.get() + j0 * vt * m.Kc;
       if (hd) {
-        // stage 1: S[(j, c1)][(P, v)] = sum_c Xs[(j, v)][c] Mcc2[(P, c1)][c]   (batched over P)
-        const int bn = pick_bn(ct);
+        // stage 1: S[(j, c1)][(P, v)] = sum_c Xs[(j, v)][c] Mcc2[(P, c1)][c]: one GEMM whose N
+        // runs over (P, c1), so N tiles pack across aux indices when ct is not a tile multiple
+        const int bn = pick_bn(naux * ct);
         TcMat Xa = make_tc_mat(xh, xl, kc * vt, m.Kc, m.Kc, 128, bk_for(bn));
         TcMat Bm = make_tc_mat(m.Mcc2.hi.get(), m.Mcc2.lo.get(), naux * ct, m.Kc, m.Kc, bn, bk_for(bn));
         TcShape sh;
-        sh.M = kc * vt; sh.N = ct; sh.K = m.Kc; sh.products = g_products;
-        sh.nbatch = naux; sh.a_batch_rows = 0; sh.b_batch_rows = ct;
+        sh.M = kc * vt; sh.N = naux * ct; sh.K = m.Kc; sh.products = g_products;
         TcEpilogue e;
         e.kind = TcEpilogue::SPLIT_BF16;
         e.rd = vt; e.ro1 = ct * m.Kg; e.ro2 = 1; e.rlim = vt;
-        e.cd = ct; e.co1 = 0; e.co2 = m.Kg; e.clim = ct;
-        e.bo = vt;
+        e.cd = ct; e.co1 = vt; e.co2 = m.Kg; e.clim = ct;
         e.out_hi = T.hi.get(); e.out_lo = T.lo.get();
         tc_gemm(Xa, Bm, sh, e, bn, err, s);
         op.timer.end(STAGE_TC_HD, s);
@@ -306,6 +317,194 @@ void MixedEngine::apply(BseOperator &op, const Coef &c, const double *X, int64_t
   }
   if (!acc) {
     VGB_CUDA(cudaMemset2DAsync(Y, ldy * sizeof(double), 0, op.dim * sizeof(double), k, s));
+  }
+}
+
+namespace {
+
+// Grouped launches of one stage: problems bucketed by tile shape (bn, K box).
+struct GemmBuckets {
+  std::map<int, std::vector<const TcProblem *>> by_shape;
+  std::map<int, std::vector<size_t>> owner;
+  void add(const TcProblem *p, int bn, size_t item) {
+    const int key = bn * 1000 + p->A.bk;
+    by_shape[key].push_back(p);
+    owner[key].push_back(item);
+  }
+  // launches every bucket; ks[item] = K splits of that item's problem
+  void run(int *err, cudaStream_t s, std::vector<int> &ks) {
+    for (auto &kv : by_shape) {
+      std::vector<int> k(kv.second.size(), 0);
+      tc_gemm_grouped(kv.second, kv.first / 1000, err, s, k.data());
+      const auto &own = owner[kv.first];
+      for (size_t i = 0; i < own.size(); ++i) ks[own[i]] = k[i];
+    }
+  }
+};
+
+}  // namespace
+
+void MixedEngine::apply_grouped(const Coef &c, const std::vector<GroupedItem> &items,
+                                bool accumulate, cudaStream_t s) {
+  read_tuning();
+  const size_t n = items.size();
+  if (n == 0) return;
+  VGB_REQUIRE(c.cd2 == 0, "grouped products: Hd2 is not grouped");
+  std::vector<Impl *> eng(n);
+  for (size_t i = 0; i < n; ++i) {
+    VGB_REQUIRE(items[i].op && items[i].op->mixed, "grouped products need mixed-precision operators");
+    eng[i] = items[i].op->mixed->impl_;
+  }
+  int *err = eng[0]->err.get();  // one error flag for the whole group
+  // X -> Xs[(j, v)][c]
+  {
+    std::vector<SplitJob> jobs(n);
+    for (size_t i = 0; i < n; ++i) {
+      Impl &m = *eng[i];
+      const GroupedItem &it = items[i];
+      m.Xs.ensure(it.k * m.vt, m.Kc, s);
+      SplitJob &j = jobs[i];
+      j.x = it.X; j.rows = it.k * m.vt; j.cols = m.ct;
+      j.map.rdiv = m.vt; j.map.rs1 = it.ldx; j.map.rs2 = m.ct; j.map.cs = 1; j.map.rlim = m.vt;
+      j.hi = m.Xs.hi.get(); j.lo = m.Xs.lo.get(); j.ldo = m.Kc;
+    }
+    split_grouped(jobs, s);
+  }
+  bool acc = accumulate;
+  if (c.cx != 0) {
+    // Z[P][j] = sum_I' Bvc2[P][I'] Xs[j][I']  (partials column-major), reduced into Zs[j][P]
+    std::vector<TcProblem> pr(n);
+    std::vector<int> ks(n, 0);
+    GemmBuckets b;
+    for (size_t i = 0; i < n; ++i) {
+      Impl &m = *eng[i];
+      const int64_t k = items[i].k;
+      const int bn = pick_bn(k);
+      TcProblem &q = pr[i];
+      // descriptors over the whole (grown-only) buffers: rows past k are never stored
+      q.A = m.mat(m.Bvc2.hi.get(), m.Bvc2.lo.get(), m.naux, m.dimP, 128, bk_for(bn));
+      q.B = m.mat(m.Xs.hi.get(), m.Xs.lo.get(), (int64_t)m.Xs.hi.count / m.dimP, m.dimP, bn, bk_for(bn));
+      q.shape.M = m.naux; q.shape.N = k; q.shape.K = m.dimP; q.shape.products = g_products;
+      // the same K splits as the single product: identical FP32 chains, identical numbers
+      q.shape.ksplit = pick_ksplit(ceil_div(m.naux, 128) * ceil_div(k, bn), m.dimP);
+      m.part.resize((size_t)q.shape.ksplit * m.naux * k);
+      q.epi.kind = TcEpilogue::STORE_F32;
+      q.epi.rd = m.naux; q.epi.ro2 = 1; q.epi.rlim = m.naux;
+      q.epi.cd = k; q.epi.co2 = m.naux; q.epi.clim = k;
+      q.epi.so = m.naux * k;
+      q.epi.out_f32 = m.part.get();
+      m.Zs.ensure(k, m.Kn, s);
+      b.add(&q, bn, i);
+    }
+    b.run(err, s, ks);
+    std::vector<ReduceJob> rj(n);
+    for (size_t i = 0; i < n; ++i) {
+      Impl &m = *eng[i];
+      const int64_t k = items[i].k;
+      ReduceJob &r = rj[i];
+      r.part = m.part.get(); r.M = k; r.N = m.naux; r.ksplit = ks[i];
+      r.epi.kind = TcEpilogue::SPLIT_BF16;
+      r.epi.rd = k; r.epi.ro2 = m.Kn; r.epi.rlim = k;
+      r.epi.cd = m.naux; r.epi.co2 = 1; r.epi.clim = m.naux;
+      r.epi.out_hi = m.Zs.hi.get(); r.epi.out_lo = m.Zs.lo.get();
+    }
+    reduce_grouped(rj, s);
+    // Y(I, j) (+)= cx sum_P BvcT[I'][P] Zs[j][P]
+    std::vector<TcProblem> p2(n);
+    GemmBuckets b2;
+    for (size_t i = 0; i < n; ++i) {
+      Impl &m = *eng[i];
+      const GroupedItem &it = items[i];
+      const int bn = pick_bn(it.k);
+      TcProblem &q = p2[i];
+      q.A = m.mat(m.BvcT.hi.get(), m.BvcT.lo.get(), m.dimP, m.Kn, 128, bk_for(bn));
+      q.B = m.mat(m.Zs.hi.get(), m.Zs.lo.get(), (int64_t)m.Zs.hi.count / m.Kn, m.Kn, bn, bk_for(bn));
+      q.shape.M = m.dimP; q.shape.N = it.k; q.shape.K = m.Kn; q.shape.products = g_products;
+      q.epi.kind = TcEpilogue::AXPBY_F64;
+      q.epi.rd = m.Kc; q.epi.ro1 = m.ct; q.epi.ro2 = 1; q.epi.rlim = m.ct;
+      q.epi.cd = it.k; q.epi.co2 = it.ldy; q.epi.clim = it.k;
+      q.epi.out_f64 = it.Y; q.epi.alpha = c.cx; q.epi.beta = acc ? 1.0 : 0.0;
+      b2.add(&q, bn, i);
+    }
+    b2.run(err, s, ks);
+    acc = true;
+  }
+  if (c.cd != 0) {
+    const double alpha = -(double)c.cd;
+    // vector chunks per operator so that its intermediate stays within its budget
+    std::vector<int64_t> jc(n);
+    int64_t rounds = 0;
+    for (size_t i = 0; i < n; ++i) {
+      Impl &m = *eng[i];
+      const int64_t per_vec = m.ct * m.Kg * 4;
+      jc[i] = std::max<int64_t>(1, std::min<int64_t>(items[i].k, m.s_budget_bytes / per_vec));
+      m.S.ensure(jc[i] * m.ct, m.Kg, s);
+      rounds = std::max(rounds, ceil_div(items[i].k, jc[i]));
+    }
+    for (int64_t rd = 0; rd < rounds; ++rd) {
+      // stage 1: S[(j, c1)][(P, v)] = sum_c Xs[(j, v)][c] Mcc2[(P, c1)][c], N over (P, c1)
+      std::vector<TcProblem> p1(n), p2(n);
+      std::vector<int> ks(n, 0);
+      GemmBuckets b1, b2;
+      std::vector<size_t> live;
+      for (size_t i = 0; i < n; ++i) {
+        const int64_t j0 = rd * jc[i];
+        if (j0 >= items[i].k) continue;
+        live.push_back(i);
+        Impl &m = *eng[i];
+        const int64_t kc = std::min(jc[i], items[i].k - j0);
+        const uint16_t *xh = m.Xs.hi.get() + j0 * m.vt * m.Kc, *xl = m.Xs.lo.get() + j0 * m.vt * m.Kc;
+        const int bn = pick_bn(m.naux * m.ct);
+        TcProblem &q = p1[i];
+        q.A = m.mat(xh, xl, ((int64_t)m.Xs.hi.count - j0 * m.vt * m.Kc) / m.Kc, m.Kc, 128, bk_for(bn));
+        q.B = m.mat(m.Mcc2.hi.get(), m.Mcc2.lo.get(), m.naux * m.ct, m.Kc, bn, bk_for(bn));
+        q.shape.M = kc * m.vt; q.shape.N = m.naux * m.ct; q.shape.K = m.Kc; q.shape.products = g_products;
+        q.epi.kind = TcEpilogue::SPLIT_BF16;
+        q.epi.rd = m.vt; q.epi.ro1 = m.ct * m.Kg; q.epi.ro2 = 1; q.epi.rlim = m.vt;
+        q.epi.cd = m.ct; q.epi.co1 = m.vt; q.epi.co2 = m.Kg; q.epi.clim = m.ct;
+        q.epi.out_hi = m.S.hi.get(); q.epi.out_lo = m.S.lo.get();
+        b1.add(&q, bn, i);
+      }
+      b1.run(err, s, ks);
+      // stage 2: partials [split][v1][(j, c1)] of sum_{(P,v)} S[(j, c1)][(P,v)] G2[v1][(P,v)]
+      for (size_t i : live) {
+        Impl &m = *eng[i];
+        const int64_t kc = std::min(jc[i], items[i].k - rd * jc[i]);
+        const int bn2 = pick_bn(m.vt);
+        TcProblem &q = p2[i];
+        q.A = m.mat(m.S.hi.get(), m.S.lo.get(), (int64_t)m.S.hi.count / m.Kg, m.Kg, 128, bk_for(bn2));
+        q.B = m.mat(m.G2.hi.get(), m.G2.lo.get(), m.vt, m.Kg, bn2, bk_for(bn2));
+        q.shape.M = kc * m.ct; q.shape.N = m.vt; q.shape.K = m.Kg; q.shape.products = g_products;
+        q.shape.ksplit = pick_ksplit(ceil_div(kc * m.ct, 128) * ceil_div(m.vt, bn2), m.Kg);
+        m.part.resize((size_t)q.shape.ksplit * q.shape.M * q.shape.N);
+        q.epi.kind = TcEpilogue::STORE_F32;
+        q.epi.rd = q.shape.M; q.epi.ro2 = 1; q.epi.rlim = q.shape.M;
+        q.epi.cd = q.shape.N; q.epi.co2 = q.shape.M; q.epi.clim = q.shape.N;
+        q.epi.so = q.shape.M * q.shape.N;
+        q.epi.out_f32 = m.part.get();
+        b2.add(&q, bn2, i);
+      }
+      b2.run(err, s, ks);
+      std::vector<ReduceJob> rj;
+      for (size_t i : live) {
+        Impl &m = *eng[i];
+        const int64_t j0 = rd * jc[i];
+        const int64_t kc = std::min(jc[i], items[i].k - j0);
+        ReduceJob r;
+        r.part = m.part.get(); r.M = m.vt; r.N = kc * m.ct; r.ksplit = ks[i];
+        r.epi.kind = TcEpilogue::AXPBY_F64;
+        r.epi.rd = m.vt; r.epi.ro2 = m.ct; r.epi.rlim = m.vt;
+        r.epi.cd = m.ct; r.epi.co1 = items[i].ldy; r.epi.co2 = 1; r.epi.clim = m.ct;
+        r.epi.out_f64 = items[i].Y + j0 * items[i].ldy; r.epi.alpha = alpha; r.epi.beta = acc ? 1.0 : 0.0;
+        rj.push_back(r);
+      }
+      reduce_grouped(rj, s);
+    }
+    acc = true;
+  }
+  if (!acc) {
+    for (const GroupedItem &it : items)
+      VGB_CUDA(cudaMemset2DAsync(it.Y, it.ldy * sizeof(double), 0, it.op->dim * sizeof(double), it.k, s));
   }
 }
 

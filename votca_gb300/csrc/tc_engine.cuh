@@ -14,6 +14,10 @@ class MixedEngine {
   // Y (+)= cx Hx X - cd Hd X - cd2 Hd2 X with tensor-core split products.
   void apply(BseOperator &op, const Coef &c, const double *X, int64_t ldx, int64_t k, double *Y,
              int64_t ldy, bool accumulate, cudaStream_t s);
+  // The same for many operators at once (GroupedItem.op->mixed engines), one grouped
+  // launch per stage and tile shape; accumulate: Y already holds the Hqp term.
+  static void apply_grouped(const Coef &c, const std::vector<GroupedItem> &items, bool accumulate,
+                            cudaStream_t s);
   // Synchronise and raise if a kernel reported a bounded-wait timeout.
   void check(cudaStream_t s);
 

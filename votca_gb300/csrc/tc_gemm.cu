@@ -3,6 +3,7 @@
 
 #include <cuda_bf16.h>
 
+#include <memory>
 #include <mutex>
 
 namespace vgb {
@@ -168,11 +169,44 @@ __device__ __forceinline__ void epi_store(const TcEpilogue &e, int64_t off, floa
   }
 }
 
-template <int BN, int BK>
-__global__ void __launch_bounds__(kThreads, 1)
-    tc_gemm_kernel(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
-                   const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo,
-                   const KParams p) {
+// Problem sources of the persistent kernel: one problem, or a group of up to
+// kGroupMax problems (same tile shape) whose tile lists are concatenated.  Both
+// live in the kernel parameter space, so every tensor map is a __grid_constant__.
+struct SingleSrc {
+  CUtensorMap maps[4];  // A hi, A lo, B hi, B lo
+  KParams p;
+  __device__ __forceinline__ int64_t total() const { return p.ntiles; }
+  __device__ __forceinline__ int locate(int64_t t, int64_t &local, int &) const {
+    local = t;
+    return 0;
+  }
+  __device__ __forceinline__ const KParams &params(int) const { return p; }
+  __device__ __forceinline__ const CUtensorMap *map(int, int w) const { return &maps[w]; }
+  __device__ __forceinline__ int *err() const { return p.err; }
+};
+
+constexpr int kGroupMax = 32;
+struct GroupSrc {
+  CUtensorMap maps[4 * kGroupMax];
+  KParams p[kGroupMax];
+  int64_t begin[kGroupMax + 1];  // first global tile of each problem; begin[n] = total
+  int n;
+  int *err_ptr;
+  __device__ __forceinline__ int64_t total() const { return begin[n]; }
+  // t grows along a CTA's walk, so the problem index only moves forward from the hint
+  __device__ __forceinline__ int locate(int64_t t, int64_t &local, int &hint) const {
+    while (hint + 1 < n && begin[hint + 1] <= t) ++hint;
+    local = t - begin[hint];
+    return hint;
+  }
+  __device__ __forceinline__ const KParams &params(int i) const { return p[i]; }
+  __device__ __forceinline__ const CUtensorMap *map(int i, int w) const { return &maps[4 * i + w]; }
+  __device__ __forceinline__ int *err() const { return err_ptr; }
+};
+static_assert(sizeof(GroupSrc) <= 32000, "grouped GEMM parameters exceed the kernel parameter space");
+
+template <int BN, int BK, class Src>
+__global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_constant__ Src src) {
   using C = Cfg<BN, BK>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -206,32 +240,40 @@ __global__ void __launch_bounds__(kThreads, 1)
   __syncthreads();
   fence_after();
   const uint32_t tmem_base = *tmem_slot;
-  const int kchunks = (int)(p.K / BK);
+  int *const err = src.err();
+  const int64_t ntiles = src.total();
 
   if (warp == 0) {
     if (lane == 0) {
       // ---------------- TMA producer ----------------
       int stage = 0;
       uint32_t phase = 0;
-      for (int64_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
-        const TileCoord tc = decode(p, t);
+      int hint = 0;
+      for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        int64_t lt;
+        const int pi = src.locate(t, lt, hint);
+        const KParams p = src.params(pi);  // registers: no reloads behind the stores
+        const TileCoord tc = decode(p, lt);
+        const int kchunks = (int)(p.K / BK);
         const int kb = (int)tc.s * p.kc_per, ke = min(kchunks, kb + p.kc_per);
         const int ya = (int)(tc.b * p.a_brows + tc.m * BM);
         const int yb = (int)(tc.b * p.b_brows + tc.n * BN);
+        const CUtensorMap *mAhi = src.map(pi, 0), *mAlo = src.map(pi, 1);
+        const CUtensorMap *mBhi = src.map(pi, 2), *mBlo = src.map(pi, 3);
         for (int kc = kb; kc < ke; ++kc) {
-          if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, p.err, 1)) goto producer_done;
+          if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, err, 1)) goto producer_done;
           uint8_t *st = smem + stage * C::STAGE_BYTES;
           mbar_expect_tx(&full[stage], (uint32_t)C::STAGE_BYTES);
-          tma_load_2d(smem_u32(st), &mAhi, &full[stage], kc * BK, ya);
-          tma_load_2d(smem_u32(st + C::A_BYTES), &mAlo, &full[stage], kc * BK, ya);
-          tma_load_2d(smem_u32(st + 2 * C::A_BYTES), &mBhi, &full[stage], kc * BK, yb);
-          tma_load_2d(smem_u32(st + 2 * C::A_BYTES + C::B_BYTES), &mBlo, &full[stage], kc * BK, yb);
+          tma_load_2d(smem_u32(st), mAhi, &full[stage], kc * BK, ya);
+          tma_load_2d(smem_u32(st + C::A_BYTES), mAlo, &full[stage], kc * BK, ya);
+          tma_load_2d(smem_u32(st + 2 * C::A_BYTES), mBhi, &full[stage], kc * BK, yb);
+          tma_load_2d(smem_u32(st + 2 * C::A_BYTES + C::B_BYTES), mBlo, &full[stage], kc * BK, yb);
           if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
         }
       }
       // drain: wait until the MMA warp has consumed every stage issued (bounded)
       for (int i = 0; i < C::STAGES; ++i) {
-        if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, p.err, 5)) break;
+        if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, err, 5)) break;
         if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
       }
     producer_done:;
@@ -247,15 +289,19 @@ __global__ void __launch_bounds__(kThreads, 1)
       uint32_t phase = 0;
       int buf = 0;
       uint32_t aphase = 0;
-      for (int64_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
-        const TileCoord tc = decode(p, t);
+      int hint = 0;
+      for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        int64_t lt;
+        const KParams p = src.params(src.locate(t, lt, hint));
+        const TileCoord tc = decode(p, lt);
+        const int kchunks = (int)(p.K / BK);
         const int kb = (int)tc.s * p.kc_per, ke = min(kchunks, kb + p.kc_per);
-        if (!mbar_wait(&acce[buf], aphase ^ 1, abort_flag, p.err, 2)) break;
+        if (!mbar_wait(&acce[buf], aphase ^ 1, abort_flag, err, 2)) break;
         fence_after();
         const uint32_t d_tmem = tmem_base + (uint32_t)(buf * BN);
         bool ok = true;
         for (int kc = kb; kc < ke; ++kc) {
-          if (!mbar_wait(&full[stage], phase, abort_flag, p.err, 3)) { ok = false; break; }
+          if (!mbar_wait(&full[stage], phase, abort_flag, err, 3)) { ok = false; break; }
           fence_after();
           const uint32_t st = smem_u32(smem + stage * C::STAGE_BYTES);
           const uint32_t ahi = st, alo = st + C::A_BYTES;
@@ -292,10 +338,14 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int cend = (BN >= 64 || half == 0) ? cbeg + COLS : BN;
     int buf = 0;
     uint32_t aphase = 0;
-    const TcEpilogue &e = p.epi;
-    for (int64_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
-      const TileCoord tc = decode(p, t);
-      if (!mbar_wait(&accf[buf], aphase, abort_flag, p.err, 4)) break;
+    int hint = 0;
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+      int64_t lt;
+      // a register copy: the stores below cannot alias it, so nothing is reloaded per element
+      const KParams p = src.params(src.locate(t, lt, hint));
+      const TcEpilogue &e = p.epi;
+      const TileCoord tc = decode(p, lt);
+      if (!mbar_wait(&accf[buf], aphase, abort_flag, err, 4)) break;
       fence_after();
       const int64_t i = tc.m * BM + q * 32 + lane;
       const bool row_ok = i < p.M && (i % e.rd) < e.rlim;
@@ -362,12 +412,12 @@ __global__ void __launch_bounds__(kThreads, 1)
 
 // ---------------- helpers ----------------
 
-__global__ void split_kernel(const double *__restrict__ x, int64_t rows, int64_t cols,
-                             const SplitMap m, uint16_t *__restrict__ hi, uint16_t *__restrict__ lo,
-                             int64_t ldo) {
+__device__ __forceinline__ void split_range(const double *__restrict__ x, int64_t rows, int64_t cols,
+                                            const SplitMap &m, uint16_t *__restrict__ hi,
+                                            uint16_t *__restrict__ lo, int64_t ldo, int64_t t0,
+                                            int64_t step) {
   const int64_t total = rows * cols;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
-       t += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t t = t0; t < total; t += step) {
     const int64_t r = t / cols, c = t % cols;
     const int64_t rq = r / m.rdiv, rr = r % m.rdiv;
     if (rr >= m.rlim) continue;
@@ -379,11 +429,34 @@ __global__ void split_kernel(const double *__restrict__ x, int64_t rows, int64_t
   }
 }
 
-__global__ void reduce_partials_kernel(const float *__restrict__ part, int64_t M, int64_t N,
-                                       int ksplit, const TcEpilogue e) {
+__global__ void split_kernel(const double *__restrict__ x, int64_t rows, int64_t cols,
+                             const SplitMap m, uint16_t *__restrict__ hi, uint16_t *__restrict__ lo,
+                             int64_t ldo) {
+  split_range(x, rows, cols, m, hi, lo, ldo, blockIdx.x * (int64_t)blockDim.x + threadIdx.x,
+              (int64_t)gridDim.x * blockDim.x);
+}
+
+constexpr int kJobsMax = 96;  // jobs per grouped elementwise launch (parameter space)
+struct SplitGroup {
+  SplitJob j[kJobsMax];
+  int n;
+};
+struct ReduceGroup {
+  ReduceJob j[kJobsMax];
+  int n;
+};
+static_assert(sizeof(SplitGroup) <= 32000 && sizeof(ReduceGroup) <= 32000, "grouped job lists too large");
+
+__global__ void split_group_kernel(const __grid_constant__ SplitGroup g) {
+  const SplitJob q = g.j[blockIdx.y];
+  split_range(q.x, q.rows, q.cols, q.map, q.hi, q.lo, q.ldo,
+              blockIdx.x * (int64_t)blockDim.x + threadIdx.x, (int64_t)gridDim.x * blockDim.x);
+}
+
+__device__ __forceinline__ void reduce_range(const float *__restrict__ part, int64_t M, int64_t N,
+                                             int ksplit, const TcEpilogue &e, int64_t t0, int64_t step) {
   const int64_t total = M * N;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
-       t += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t t = t0; t < total; t += step) {
     const int64_t i = t / N, n = t % N;
     if ((i % e.rd) >= e.rlim || (n % e.cd) >= e.clim) continue;
     double acc = 0.0;
@@ -399,6 +472,18 @@ __global__ void reduce_partials_kernel(const float *__restrict__ part, int64_t M
       epi_store(e, off, (float)acc);
     }
   }
+}
+
+__global__ void reduce_partials_kernel(const float *__restrict__ part, int64_t M, int64_t N,
+                                       int ksplit, const TcEpilogue e) {
+  reduce_range(part, M, N, ksplit, e, blockIdx.x * (int64_t)blockDim.x + threadIdx.x,
+               (int64_t)gridDim.x * blockDim.x);
+}
+
+__global__ void reduce_group_kernel(const __grid_constant__ ReduceGroup g) {
+  const ReduceJob q = g.j[blockIdx.y];
+  reduce_range(q.part, q.M, q.N, q.ksplit, q.epi, blockIdx.x * (int64_t)blockDim.x + threadIdx.x,
+               (int64_t)gridDim.x * blockDim.x);
 }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
@@ -435,18 +520,36 @@ void encode(CUtensorMap *m, const uint16_t *base, int64_t rows, int64_t K, int64
   if (r != CUDA_SUCCESS) fail(BSE_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
 }
 
-template <int BN, int BK>
-void launch(const TcMat &A, const TcMat &B, const KParams &p, cudaStream_t s) {
+template <int BN, int BK, class Src>
+void launch_src(const Src &src, int64_t ntiles, cudaStream_t s) {
   using C = Cfg<BN, BK>;
   static std::once_flag attr;
   std::call_once(attr, [] {
-    VGB_CUDA(cudaFuncSetAttribute(tc_gemm_kernel<BN, BK>,
+    VGB_CUDA(cudaFuncSetAttribute(tc_gemm_kernel<BN, BK, Src>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
   });
-  const int64_t grid = std::min<int64_t>(p.ntiles, sm_count());
-  tc_gemm_kernel<BN, BK><<<(unsigned)grid, kThreads, C::SMEM, s>>>(A.map_hi, A.map_lo, B.map_hi,
-                                                                   B.map_lo, p);
+  const int64_t grid = std::min<int64_t>(ntiles, sm_count());
+  tc_gemm_kernel<BN, BK, Src><<<(unsigned)grid, kThreads, C::SMEM, s>>>(src);
   VGB_LAUNCH_CHECK();
+}
+
+template <class Src>
+void launch_any(int bn, int bk, const Src &src, int64_t ntiles, cudaStream_t s) {
+  if (bk == 64) {
+    switch (bn) {
+      case 32: launch_src<32, 64>(src, ntiles, s); break;
+      case 64: launch_src<64, 64>(src, ntiles, s); break;
+      case 128: launch_src<128, 64>(src, ntiles, s); break;
+      default: launch_src<256, 64>(src, ntiles, s); break;
+    }
+  } else {
+    switch (bn) {
+      case 32: launch_src<32, 32>(src, ntiles, s); break;
+      case 64: launch_src<64, 32>(src, ntiles, s); break;
+      case 128: launch_src<128, 32>(src, ntiles, s); break;
+      default: launch_src<256, 32>(src, ntiles, s); break;
+    }
+  }
 }
 
 unsigned grid_1d(int64_t n) {
@@ -470,21 +573,26 @@ TcMat make_tc_mat(const uint16_t *hi, const uint16_t *lo, int64_t rows, int64_t 
   return m;
 }
 
-int tc_gemm(const TcMat &A, const TcMat &B, const TcShape &sh, const TcEpilogue &epi, int bn,
-            int *err, cudaStream_t s) {
+namespace {
+
+// Validated kernel parameters of one problem (tiles == 0 when there is nothing to do).
+KParams make_params(const TcMat &A, const TcMat &B, const TcShape &sh, const TcEpilogue &epi, int bn,
+                    int *err) {
   VGB_REQUIRE(bn == 32 || bn == 64 || bn == 128 || bn == 256, "tc_gemm: unsupported tile N");
   VGB_REQUIRE(A.box_rows == BM && B.box_rows == bn, "tc_gemm: operand boxes do not match the tile");
   VGB_REQUIRE(A.bk == B.bk, "tc_gemm: operands staged with different K boxes");
   const int BK = A.bk;
   VGB_REQUIRE(sh.K % BK == 0 && A.K >= sh.K && B.K >= sh.K, "tc_gemm: K not padded");
   VGB_REQUIRE(epi.rd >= 1 && epi.cd >= 1, "tc_gemm: bad epilogue map");
-  if (sh.M <= 0 || sh.N <= 0 || sh.nbatch <= 0) return 0;
+  KParams p;
+  p.ntiles = 0;
+  p.ksplit = 0;
+  if (sh.M <= 0 || sh.N <= 0 || sh.nbatch <= 0) return p;
   // rows addressed by the last batch must exist in the operands (TMA fills beyond with zeros,
   // but row coordinates must stay within the int32 range of the descriptor)
   VGB_REQUIRE((sh.nbatch - 1) * sh.a_batch_rows + sh.M <= A.rows + BM, "tc_gemm: A rows");
   VGB_REQUIRE((sh.nbatch - 1) * sh.b_batch_rows + sh.N <= B.rows + bn, "tc_gemm: B rows");
   VGB_REQUIRE(A.rows < (1LL << 31) && B.rows < (1LL << 31), "tc_gemm: too many rows");
-  KParams p;
   p.M = sh.M; p.N = sh.N; p.K = sh.K;
   p.products = sh.products == 4 ? 4 : 3;
   p.nbatch = sh.nbatch;
@@ -501,22 +609,54 @@ int tc_gemm(const TcMat &A, const TcMat &B, const TcShape &sh, const TcEpilogue 
   p.ntiles = p.mt * p.nt * p.ksplit * sh.nbatch;
   p.epi = epi;
   p.err = err;
-  if (BK == 64) {
-    switch (bn) {
-      case 32: launch<32, 64>(A, B, p, s); break;
-      case 64: launch<64, 64>(A, B, p, s); break;
-      case 128: launch<128, 64>(A, B, p, s); break;
-      default: launch<256, 64>(A, B, p, s); break;
-    }
-  } else {
-    switch (bn) {
-      case 32: launch<32, 32>(A, B, p, s); break;
-      case 64: launch<64, 32>(A, B, p, s); break;
-      case 128: launch<128, 32>(A, B, p, s); break;
-      default: launch<256, 32>(A, B, p, s); break;
-    }
-  }
+  return p;
+}
+
+}  // namespace
+
+int tc_gemm(const TcMat &A, const TcMat &B, const TcShape &sh, const TcEpilogue &epi, int bn,
+            int *err, cudaStream_t s) {
+  const KParams p = make_params(A, B, sh, epi, bn, err);
+  if (p.ntiles == 0) return 0;
+  SingleSrc src;
+  src.maps[0] = A.map_hi;
+  src.maps[1] = A.map_lo;
+  src.maps[2] = B.map_hi;
+  src.maps[3] = B.map_lo;
+  src.p = p;
+  launch_any(bn, A.bk, src, p.ntiles, s);
   return p.ksplit;
+}
+
+void tc_gemm_grouped(const std::vector<const TcProblem *> &probs, int bn, int *err, cudaStream_t s,
+                     int *ksplit_out) {
+  std::unique_ptr<GroupSrc> src(new GroupSrc());
+  int bk = 0;
+  size_t i = 0;
+  while (i < probs.size()) {
+    src->n = 0;
+    src->err_ptr = err;
+    int64_t total = 0;
+    for (; i < probs.size() && src->n < kGroupMax; ++i) {
+      const TcProblem &q = *probs[i];
+      const KParams p = make_params(q.A, q.B, q.shape, q.epi, bn, err);
+      if (ksplit_out) ksplit_out[i] = p.ksplit;
+      if (p.ntiles == 0) continue;
+      VGB_REQUIRE(bk == 0 || bk == q.A.bk, "tc_gemm_grouped: problems with different K boxes");
+      bk = q.A.bk;
+      const int g = src->n++;
+      src->maps[4 * g + 0] = q.A.map_hi;
+      src->maps[4 * g + 1] = q.A.map_lo;
+      src->maps[4 * g + 2] = q.B.map_hi;
+      src->maps[4 * g + 3] = q.B.map_lo;
+      src->p[g] = p;
+      src->begin[g] = total;
+      total += p.ntiles;
+    }
+    if (src->n == 0) continue;
+    src->begin[src->n] = total;
+    launch_any(bn, bk, *src, total, s);
+  }
 }
 
 void split_f64_to_bf16(const double *x, int64_t rows, int64_t cols, const SplitMap &m, uint16_t *hi,
@@ -525,6 +665,50 @@ void split_f64_to_bf16(const double *x, int64_t rows, int64_t cols, const SplitM
   VGB_REQUIRE(m.rdiv >= 1, "split: bad row map");
   split_kernel<<<grid_1d(rows * cols), 256, 0, s>>>(x, rows, cols, m, hi, lo, ldo);
   VGB_LAUNCH_CHECK();
+}
+
+namespace {
+// blocks per job of a grouped elementwise launch: about 4 waves of 256-thread blocks in total
+unsigned group_blocks(int64_t max_elems, int njobs) {
+  const int64_t want = ceil_div(max_elems, 256);
+  const int64_t cap = std::max<int64_t>(1, (4LL * 8 * sm_count()) / std::max(1, njobs));
+  return (unsigned)std::max<int64_t>(1, std::min(want, std::max<int64_t>(cap, 4)));
+}
+}  // namespace
+
+void split_grouped(const std::vector<SplitJob> &jobs, cudaStream_t s) {
+  std::unique_ptr<SplitGroup> g(new SplitGroup());
+  size_t i = 0;
+  while (i < jobs.size()) {
+    g->n = 0;
+    int64_t mx = 0;
+    for (; i < jobs.size() && g->n < kJobsMax; ++i) {
+      if (jobs[i].rows <= 0 || jobs[i].cols <= 0) continue;
+      VGB_REQUIRE(jobs[i].map.rdiv >= 1, "split: bad row map");
+      g->j[g->n++] = jobs[i];
+      mx = std::max(mx, jobs[i].rows * jobs[i].cols);
+    }
+    if (g->n == 0) continue;
+    split_group_kernel<<<dim3(group_blocks(mx, g->n), (unsigned)g->n), 256, 0, s>>>(*g);
+    VGB_LAUNCH_CHECK();
+  }
+}
+
+void reduce_grouped(const std::vector<ReduceJob> &jobs, cudaStream_t s) {
+  std::unique_ptr<ReduceGroup> g(new ReduceGroup());
+  size_t i = 0;
+  while (i < jobs.size()) {
+    g->n = 0;
+    int64_t mx = 0;
+    for (; i < jobs.size() && g->n < kJobsMax; ++i) {
+      if (jobs[i].M <= 0 || jobs[i].N <= 0 || jobs[i].ksplit <= 0) continue;
+      g->j[g->n++] = jobs[i];
+      mx = std::max(mx, jobs[i].M * jobs[i].N);
+    }
+    if (g->n == 0) continue;
+    reduce_group_kernel<<<dim3(group_blocks(mx, g->n), (unsigned)g->n), 256, 0, s>>>(*g);
+    VGB_LAUNCH_CHECK();
+  }
 }
 
 void reduce_partials(const float *partial, int64_t M, int64_t N, int ksplit, const TcEpilogue &epi,

@@ -13,6 +13,8 @@
 
 #include <cuda.h>
 
+#include <vector>
+
 #include "common.cuh"
 
 namespace vgb {
@@ -60,6 +62,20 @@ struct TcShape {
 int tc_gemm(const TcMat &A, const TcMat &B, const TcShape &shape, const TcEpilogue &epi, int bn,
              int *err, cudaStream_t s);
 
+// One GEMM of a group: operands, shape and epilogue as for tc_gemm.
+struct TcProblem {
+  TcMat A, B;
+  TcShape shape;
+  TcEpilogue epi;
+};
+
+// Several independent GEMMs with the same tile (bn, K box) in as few launches as
+// possible: each launch walks the concatenated tile lists of up to 32 problems,
+// whose tensor maps and parameters travel in the kernel parameter space.
+// ksplit_out[i] (optional) receives problem i's K splits, as tc_gemm returns.
+void tc_gemm_grouped(const std::vector<const TcProblem *> &probs, int bn, int *err, cudaStream_t s,
+                     int *ksplit_out = nullptr);
+
 // FP64 -> bf16 hi/lo split into a row-major padded operand out[r * ldo + c] for
 // r < rows, c < cols; the source element (r, c) is
 //   x[(r / rdiv) * rs1 + (r % rdiv) * rs2 + c * cs]
@@ -70,9 +86,26 @@ struct SplitMap {
 void split_f64_to_bf16(const double *x, int64_t rows, int64_t cols, const SplitMap &m, uint16_t *hi,
                        uint16_t *lo, int64_t ldo, cudaStream_t s);
 
+// Many independent splits / reductions in one launch per 96 jobs (one grid row per job).
+struct SplitJob {
+  const double *x = nullptr;
+  int64_t rows = 0, cols = 0;
+  SplitMap map;
+  uint16_t *hi = nullptr, *lo = nullptr;
+  int64_t ldo = 0;
+};
+void split_grouped(const std::vector<SplitJob> &jobs, cudaStream_t s);
+
 // Sum ksplit FP32 partial tiles (each M x N, element (i, n) at p[s * M * N + i * N + n])
 // and apply an epilogue map (SPLIT_BF16 or AXPBY_F64) with nbatch = 1.
 void reduce_partials(const float *partial, int64_t M, int64_t N, int ksplit, const TcEpilogue &epi,
                      cudaStream_t s);
+struct ReduceJob {
+  const float *part = nullptr;
+  int64_t M = 0, N = 0;
+  int ksplit = 0;
+  TcEpilogue epi;
+};
+void reduce_grouped(const std::vector<ReduceJob> &jobs, cudaStream_t s);
 
 }  // namespace vgb

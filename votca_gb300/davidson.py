@@ -86,9 +86,11 @@ class DavidsonSolver:
         return _lib.bse_davidson_options(self.iter_max_, self.tol_, self.max_search_space_, self.correction_,
                                          self.update_, self.matrix_type_, int(self.verbose))
 
-    def solve_batch(self, ops, neigen, nthreads=8):
+    def solve_batch(self, ops, neigen, nthreads=0):
         """Lowest neigen eigenvalues of every operator in ops (BSE_OPERATORs with one
-        coefficient set, or DenseGpuOperators), solved concurrently on the GPU.
+        coefficient set, or DenseGpuOperators).  nthreads=0: all molecules iterate in
+        lockstep, every step one grouped launch (BSE operators, DPR); nthreads>0: one
+        independent solve per molecule on that many host threads (any operator/option).
         Returns (evals [len(ops) x neigen], info per molecule, iterations per molecule)."""
         ops = list(ops)
         n = len(ops)
