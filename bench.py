@@ -107,47 +107,109 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.rows)}
 
 
+def sample_matvec(prob, v, c, k, op, seconds_target, nthreads, last_v1=False):
+    """Time the reference loop nest (oracle port of bse_operator.cc:39-119 with the CPU
+    branches of openmp_cuda.cc) on a bounded sample of one k-column product of `op`: a
+    sub-range of c1 for the Hd/Hqp row stage and of v1 for the Hx block stage, scaled to
+    the full product by the share of work sampled (the work per c1 is uniform; per v1 it
+    is proportional to the number of v2 >= v1 pairs).  last_v1 samples the v1 blocks with
+    the fewest pairs (large v).  Returns (seconds per product, description)."""
+    X = np.asfortranarray(np.random.default_rng(1).standard_normal((v * c, k)))
+    wave = min(c, nthreads)
+    t0 = time.perf_counter()
+    prob.matmul_ref(X, op, c1_range=(0, wave), v1_range=(0, 0))
+    t_wave = time.perf_counter() - t0
+    waves = int(max(1, min(c // wave, (seconds_target * 0.6) // max(t_wave, 1e-3))))
+    n_c1 = wave * waves
+    if waves > 1:
+        t0 = time.perf_counter()
+        prob.matmul_ref(X, op, c1_range=(0, n_c1), v1_range=(0, 0))
+        t_rows = time.perf_counter() - t0
+    else:
+        t_rows = t_wave
+    n_v1 = min(v, nthreads)
+    v1r = (v - n_v1, v) if last_v1 else (0, n_v1)
+    t0 = time.perf_counter()
+    prob.matmul_ref(X, op, c1_range=(0, 0), v1_range=v1r)
+    t_hx = time.perf_counter() - t0
+    pairs_total = v * (v + 1) // 2
+    pairs_s = sum(v - v1 for v1 in range(*v1r))
+    t_full = t_rows * (c / n_c1) + t_hx * (pairs_total / pairs_s)
+    desc = (f"reference loop nest (row-built Hd + v-pair Hx) on {n_c1}/{c} c1 rows and v1 blocks "
+            f"{v1r[0]}..{v1r[1] - 1} ({pairs_s:.0f}/{pairs_total} pairs) of one k={k} {op} product, "
+            f"extrapolated: {t_full:.1f} s per product")
+    return t_full, desc
+
+
 def cpu_baseline(mmn, w, hqp, seconds_target=20.0, full=False):
-    """The reference's CPU loop nest (oracle port of bse_operator.cc:39-119 with
-    the CPU branches of openmp_cuda.cc) on a bounded sample of one matvec:
-    a sub-range of c1 for the Hd/Hqp row stage and of v1 for the Hx block stage,
-    scaled to the full product by the share of work sampled (the work per c1 is
-    uniform; per v1 it is proportional to the number of v2 >= v1 pairs)."""
+    """The reference's CPU loop nest on a bounded sample of one singlet matvec at the
+    benchmark workload, with all host threads."""
     import oracle
 
     nthreads = os.cpu_count() or 1
     oracle.set_threads(nthreads)
     prob = oracle.BSEProblem(mmn, w, hqp, V, C)
-    X = np.asfortranarray(np.random.default_rng(1).standard_normal((V * C, K)))
-    # Row stage: OpenMP over c1 as in the reference; one wave = one c1 per thread.
-    wave = min(C, nthreads)
-    t0 = time.perf_counter()
-    prob.matmul_ref(X, "singlet", c1_range=(0, wave), v1_range=(0, 0))
-    t_wave = time.perf_counter() - t0
-    waves = int(max(1, min(C // wave, (seconds_target * 0.6) // max(t_wave, 1e-3))))
-    n_c1 = wave * waves
-    if waves > 1:
-        t0 = time.perf_counter()
-        prob.matmul_ref(X, "singlet", c1_range=(0, n_c1), v1_range=(0, 0))
-        t_rows = time.perf_counter() - t0
-    else:
-        t_rows = t_wave
-    # Hx block stage: OpenMP over v1; v1 carries V - v1 pairs (v2 >= v1).
-    n_v1 = min(V, nthreads)
-    t0 = time.perf_counter()
-    prob.matmul_ref(X, "singlet", c1_range=(0, 0), v1_range=(0, n_v1))
-    t_hx = time.perf_counter() - t0
-    pairs_total = V * (V + 1) // 2
-    pairs_s = sum(V - v1 for v1 in range(n_v1))
-    t_full = t_rows * (C / n_c1) + t_hx * (pairs_total / pairs_s)
+    t_full, desc = sample_matvec(prob, V, C, K, "singlet", seconds_target, nthreads)
     F = algorithmic_flops(V, C, NAUX, K)
     return {
         "value": F / t_full / 1e12, "unit": "TFLOP/s", "cores": nthreads, "kind": "port",
-        "sample": (f"reference loop nest (row-built Hd + v-pair Hx) on {n_c1}/{C} c1 rows and "
-                   f"{n_v1} of {V} v1 blocks ({pairs_s:.0f}/{pairs_total} pairs) of one k={K} singlet "
-                   f"matvec, extrapolated: {t_full:.1f} s per matvec"),
-        "seconds_per_matvec": t_full,
+        "sample": desc, "seconds_per_matvec": t_full,
     }
+
+
+def ref_matvec_flops(v, c, naux, k):
+    """Flops of the reference algorithm per TDA singlet product (rows rebuilt per call)."""
+    vc = v * c
+    return 2.0 * vc * vc * naux + v * (v + 1) * c * c * naux + 2.0 * vc * vc * k
+
+
+def cpu_baseline_batched(shapes, roots, tol, n_sample=6):
+    """The reference CPU path (the DavidsonSolver restatement driving the reference
+    loop nest on all host threads) on a seeded subset of the molecules, scaled to the
+    whole set by the reference algorithm's flops per product."""
+    import oracle
+    from oracle.davidson_oracle import DavidsonOracle
+    from votca_gb300.synthetic import qp_energies, screening_w
+
+    nthreads = os.cpu_count() or 1
+    oracle.set_threads(nthreads)
+    pick = np.linspace(0, len(shapes) - 1, n_sample).round().astype(int)
+    t_sample, cost_sample, iters = 0.0, 0.0, []
+    for i in pick:
+        sh = shapes[i]
+        v, c, naux, seed = sh["v"], sh["c"], sh["naux"], sh["seed"]
+        prob = oracle.BSEProblem(make_mmn(seed, naux, sh["nmo"]), screening_w(seed, naux),
+                                 np.diag(qp_energies(seed, v, c)), v, c)
+        d = DavidsonOracle()
+        d.set_tolerance(tol)
+        d.max_search_space = 10 * roots
+        t0 = time.perf_counter()
+        d.solve(lambda X: prob.matmul_ref(X, "singlet"), prob.diagonal("singlet"), roots)
+        t_sample += time.perf_counter() - t0
+        cost_sample += ref_matvec_flops(v, c, naux, 1)
+        iters.append(d.i_iter)
+    cost_all = sum(ref_matvec_flops(s["v"], s["c"], s["naux"], 1) for s in shapes)
+    t_all = t_sample * cost_all / cost_sample
+    nroots = len(shapes) * roots
+    return {
+        "value": nroots / t_all, "unit": "roots/s", "cores": nthreads, "kind": "port",
+        "sample": (f"{n_sample} of {len(shapes)} molecules (evenly spaced) solved one after the other "
+                   f"({t_sample:.1f} s, iterations {iters}), scaled by the reference algorithm's "
+                   f"flops per product to all molecules: {t_all:.0f} s"),
+    }
+
+
+def cpu_baseline_full_bse(mmn, w, hqp, v, c, k, seconds_target=20.0):
+    """One Hamiltonian application of the reference path at k trial vectors: A and B
+    each applied to 2k columns (bseoperator_btda.h:116-149), sampled and extrapolated."""
+    import oracle
+
+    nthreads = os.cpu_count() or 1
+    oracle.set_threads(nthreads)
+    prob = oracle.BSEProblem(mmn, w, hqp, v, c)
+    ta, da = sample_matvec(prob, v, c, 2 * k, "singlet", seconds_target / 2, nthreads, last_v1=True)
+    tb, db = sample_matvec(prob, v, c, 2 * k, "singlet_b", seconds_target / 2, nthreads, last_v1=True)
+    return ta + tb, f"A: {da}; B: {db} (extrapolated)"
 
 
 def reference_arm(args):
@@ -181,7 +243,7 @@ def reference_arm(args):
     print(json.dumps(line))
 
 
-def batched_solve(n_molecules, nthreads, roots=5, tol=1e-7):
+def batched_solve(n_molecules, nthreads, roots=5, tol=1e-7, cpu=False):
     """Independent molecules of uneven shape (v ~ U{4..32}, c ~ U{32..256},
     Naux ~ U{128..1024}, Nmo = v+c+8), lowest `roots` TDA singlets each, mixed
     precision.  Timed twice: the batched solve alone (operators staged in HBM)
@@ -229,7 +291,7 @@ def batched_solve(n_molecules, nthreads, roots=5, tol=1e-7):
         cx.close()
     t_destroy = time.perf_counter() - t0
     nroots = len(ops) * roots
-    return {
+    out = {
         "workload": f"batched_tda_singlet_{n_molecules}mol_roots{roots}",
         "molecules": n_molecules, "roots_per_molecule": roots, "tolerance": tol, "precision": "mixed",
         "mode": "lockstep: one grouped launch per Davidson step over all molecules",
@@ -250,9 +312,12 @@ def batched_solve(n_molecules, nthreads, roots=5, tol=1e-7):
         "threads_match_one_thread": bool(np.array_equal(evt[:ns], ev1)),
         "dims": [int(s["v"] * s["c"]) for s in shapes[:4]] + ["..."],
     }
+    if cpu:
+        out["cpu_baseline"] = cpu_baseline_batched(shapes, roots, tol)
+    return out
 
 
-def full_bse_report(roots=10, tol=1e-7, k=32, check=False):
+def full_bse_report(roots=10, tol=1e-7, k=32, check=False, cpu=False):
     """Full (non-TDA) singlet BSE at v=128, c=1024 (dim 131072 per block),
     Naux=4096, Nmo=1152: HAM Davidson on [[A, B], [-B, -A]] in mixed precision,
     lowest `roots` roots; plus the HAM product throughput at k trial vectors.
@@ -312,6 +377,11 @@ def full_bse_report(roots=10, tol=1e-7, k=32, check=False):
         "roots_eV": [round(float(x), 9) for x in lam],
     }
     ctx.close()
+    if cpu:
+        t_cpu, desc = cpu_baseline_full_bse(mmn, w, hqp, v, c, k)
+        out["cpu_baseline"] = {"value": F / t_cpu / 1e12, "unit": "TFLOP/s (HAM product, algorithmic)",
+                               "cores": os.cpu_count() or 1, "kind": "port", "sample": desc,
+                               "seconds_per_ham_product": t_cpu}
     if check:
         c64 = bo.GpuBSEContext(w, bo.TCMatrix_gwbse(mmn), hqp, opt, precision=bo.PRECISION_FP64)
         A64, B64 = bo.SingletOperator_TDA(c64), bo.SingletOperator_BTDA_B(c64)
@@ -554,9 +624,9 @@ def main():
     if rank == 0 and (args.molecules > 0 or args.full_bse):
         ctx.close()
     if rank == 0 and args.molecules > 0:
-        line["batched"] = batched_solve(args.molecules, args.batch_threads)
+        line["batched"] = batched_solve(args.molecules, args.batch_threads, cpu=world == 1 and not args.no_cpu)
     if rank == 0 and args.full_bse:
-        line["full_bse"] = full_bse_report(check=args.full_bse_check)
+        line["full_bse"] = full_bse_report(check=args.full_bse_check, cpu=world == 1 and not args.no_cpu)
     if rank == 0 and world == 1 and not args.no_cpu:
         cb = cpu_baseline(mmn, w, hqp)
         cb.pop("seconds_per_matvec", None)
