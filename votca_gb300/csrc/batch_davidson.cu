@@ -485,6 +485,7 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
       p += 64;
     }
   }
+  GroupScratch arena;  // Hd intermediates of the grouped products, shared by all molecules
   DeviceBuffer<int> flags(nm);
   VGB_CUDA(cudaMemsetAsync(flags.get(), 0, nm * sizeof(int), s));
   for (size_t b = 0; b < nm; ++b) mols[b].flag = flags.get() + b;
@@ -549,7 +550,7 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
         items.push_back(gi);
         tn.push_back({M, M->V, M->AV + old * M->n, M->ncols, nvec, M->cbuf, M->ncols});
       }
-      matmul_grouped(coef, items, s);
+      matmul_grouped(coef, items, s, &arena);
       mark(0);
       run_tn(tn, s);
       for (Mol *M : act) {

@@ -577,7 +577,8 @@ void BseOperator::matmul(const Coef &c, const double *X, int64_t ldx, int64_t k,
   }
 }
 
-void matmul_grouped(const Coef &c, const std::vector<GroupedItem> &items, cudaStream_t s) {
+void matmul_grouped(const Coef &c, const std::vector<GroupedItem> &items, cudaStream_t s,
+                    GroupScratch *scratch) {
   VGB_REQUIRE(c.cd2 == 0, "grouped products: Hd2 is not grouped");
   std::vector<GroupedItem> mixed_items;
   std::vector<HqpJob> hq;
@@ -613,7 +614,7 @@ void matmul_grouped(const Coef &c, const std::vector<GroupedItem> &items, cudaSt
     hqp_diag_group_kernel<<<dim3(bx, (unsigned)g->n), 256, 0, s>>>(*g);
     VGB_LAUNCH_CHECK();
   }
-  MixedEngine::apply_grouped(c, mixed_items, c.cqp != 0, s);
+  MixedEngine::apply_grouped(c, mixed_items, c.cqp != 0, s, scratch);
 }
 
 void BseOperator::check_errors(cudaStream_t s) {

@@ -145,10 +145,17 @@ struct GroupedItem {
   double *Y = nullptr;
   int64_t ldy = 0;
 };
+// Scratch shared by the operators of a grouped product (the Hd intermediates); kept by
+// the caller across products so that it is allocated once.
+struct GroupScratch {
+  DeviceBuffer<uint16_t> hi, lo;
+  int64_t elems = 0;
+};
 // Products of many operators with one coefficient set, stage by stage: every
 // tensor-core stage of all mixed-precision operators runs as grouped launches
 // (FP64 operators fall back to one product each).  Hd2 is not supported here.
-void matmul_grouped(const Coef &c, const std::vector<GroupedItem> &items, cudaStream_t s);
+void matmul_grouped(const Coef &c, const std::vector<GroupedItem> &items, cudaStream_t s,
+                    GroupScratch *scratch = nullptr);
 // Diagonals of many operators (same arithmetic as BseOperator::diagonal) in one launch per 192.
 void diagonal_grouped(const Coef &c, const std::vector<BseOperator *> &ops,
                       const std::vector<double *> &D, cudaStream_t s);

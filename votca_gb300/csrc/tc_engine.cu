@@ -60,6 +60,7 @@ int pick_bn(int64_t N) {
 // accumulation chain in TMEM is longer than max_chain (the partial sums are
 // reduced in FP64).
 int64_t g_max_chain = 1024;
+constexpr int64_t kGroupArenaElems = 1LL << 30;  // shared Hd intermediates of a group: 4 GB (hi + lo)
 int g_products = 3;
 int pick_ksplit(int64_t tiles, int64_t K) {
   const int64_t target = 2LL * sm_count();
@@ -345,7 +346,7 @@ struct GemmBuckets {
 }  // namespace
 
 void MixedEngine::apply_grouped(const Coef &c, const std::vector<GroupedItem> &items,
-                                bool accumulate, cudaStream_t s) {
+                                bool accumulate, cudaStream_t s, GroupScratch *scratch) {
   read_tuning();
   const size_t n = items.size();
   if (n == 0) return;
@@ -431,74 +432,105 @@ void MixedEngine::apply_grouped(const Coef &c, const std::vector<GroupedItem> &i
   }
   if (c.cd != 0) {
     const double alpha = -(double)c.cd;
-    // vector chunks per operator so that its intermediate stays within its budget
-    std::vector<int64_t> jc(n);
-    int64_t rounds = 0;
+    // The Hd intermediates S live in one arena shared by the group: per round of vector
+    // chunks the operators are taken in slices whose intermediates fit the arena, and
+    // each slice runs stage 1, stage 2 and the reduction before the next reuses it.
+    GroupScratch local;
+    GroupScratch &arena = scratch ? *scratch : local;
+    std::vector<int64_t> jc(n), need(n);
+    int64_t rounds = 0, total = 0, largest = 0;
     for (size_t i = 0; i < n; ++i) {
       Impl &m = *eng[i];
       const int64_t per_vec = m.ct * m.Kg * 4;
       jc[i] = std::max<int64_t>(1, std::min<int64_t>(items[i].k, m.s_budget_bytes / per_vec));
-      m.S.ensure(jc[i] * m.ct, m.Kg, s);
+      need[i] = jc[i] * m.ct * m.Kg;  // elements (a multiple of 64: regions stay 128-byte aligned)
+      total += need[i];
+      largest = std::max(largest, need[i]);
       rounds = std::max(rounds, ceil_div(items[i].k, jc[i]));
     }
+    const int64_t want = std::max(largest, std::min(total, kGroupArenaElems));
+    if (arena.elems < want) {
+      arena.hi.resize(want);
+      arena.lo.resize(want);
+      // zero once: pad columns of S are read (times zero pads of G2) and must be finite
+      VGB_CUDA(cudaMemsetAsync(arena.hi.get(), 0, want * sizeof(uint16_t), s));
+      VGB_CUDA(cudaMemsetAsync(arena.lo.get(), 0, want * sizeof(uint16_t), s));
+      arena.elems = want;
+    }
     for (int64_t rd = 0; rd < rounds; ++rd) {
-      // stage 1: S[(j, c1)][(P, v)] = sum_c Xs[(j, v)][c] Mcc2[(P, c1)][c], N over (P, c1)
-      std::vector<TcProblem> p1(n), p2(n);
-      std::vector<int> ks(n, 0);
-      GemmBuckets b1, b2;
       std::vector<size_t> live;
-      for (size_t i = 0; i < n; ++i) {
-        const int64_t j0 = rd * jc[i];
-        if (j0 >= items[i].k) continue;
-        live.push_back(i);
-        Impl &m = *eng[i];
-        const int64_t kc = std::min(jc[i], items[i].k - j0);
-        const uint16_t *xh = m.Xs.hi.get() + j0 * m.vt * m.Kc, *xl = m.Xs.lo.get() + j0 * m.vt * m.Kc;
-        const int bn = pick_bn(m.naux * m.ct);
-        TcProblem &q = p1[i];
-        q.A = m.mat(xh, xl, ((int64_t)m.Xs.hi.count - j0 * m.vt * m.Kc) / m.Kc, m.Kc, 128, bk_for(bn));
-        q.B = m.mat(m.Mcc2.hi.get(), m.Mcc2.lo.get(), m.naux * m.ct, m.Kc, bn, bk_for(bn));
-        q.shape.M = kc * m.vt; q.shape.N = m.naux * m.ct; q.shape.K = m.Kc; q.shape.products = g_products;
-        q.epi.kind = TcEpilogue::SPLIT_BF16;
-        q.epi.rd = m.vt; q.epi.ro1 = m.ct * m.Kg; q.epi.ro2 = 1; q.epi.rlim = m.vt;
-        q.epi.cd = m.ct; q.epi.co1 = m.vt; q.epi.co2 = m.Kg; q.epi.clim = m.ct;
-        q.epi.out_hi = m.S.hi.get(); q.epi.out_lo = m.S.lo.get();
-        b1.add(&q, bn, i);
+      for (size_t i = 0; i < n; ++i)
+        if (rd * jc[i] < items[i].k) live.push_back(i);
+      size_t a = 0;
+      while (a < live.size()) {
+        // slice [a, b) of the live operators, regions packed in the arena
+        std::vector<int64_t> off(n, 0);
+        int64_t used = 0;
+        size_t b = a;
+        while (b < live.size() && (b == a || used + need[live[b]] <= arena.elems)) {
+          off[live[b]] = used;
+          used += need[live[b]];
+          ++b;
+        }
+        std::vector<TcProblem> p1(n), p2(n);
+        std::vector<int> ks(n, 0);
+        GemmBuckets b1, b2;
+        // stage 1: S[(j, c1)][(P, v)] = sum_c Xs[(j, v)][c] Mcc2[(P, c1)][c], N over (P, c1)
+        for (size_t t = a; t < b; ++t) {
+          const size_t i = live[t];
+          Impl &m = *eng[i];
+          const int64_t j0 = rd * jc[i];
+          const int64_t kc = std::min(jc[i], items[i].k - j0);
+          const uint16_t *xh = m.Xs.hi.get() + j0 * m.vt * m.Kc, *xl = m.Xs.lo.get() + j0 * m.vt * m.Kc;
+          const int bn = pick_bn(m.naux * m.ct);
+          TcProblem &q = p1[i];
+          q.A = m.mat(xh, xl, ((int64_t)m.Xs.hi.count - j0 * m.vt * m.Kc) / m.Kc, m.Kc, 128, bk_for(bn));
+          q.B = m.mat(m.Mcc2.hi.get(), m.Mcc2.lo.get(), m.naux * m.ct, m.Kc, bn, bk_for(bn));
+          q.shape.M = kc * m.vt; q.shape.N = m.naux * m.ct; q.shape.K = m.Kc; q.shape.products = g_products;
+          q.epi.kind = TcEpilogue::SPLIT_BF16;
+          q.epi.rd = m.vt; q.epi.ro1 = m.ct * m.Kg; q.epi.ro2 = 1; q.epi.rlim = m.vt;
+          q.epi.cd = m.ct; q.epi.co1 = m.vt; q.epi.co2 = m.Kg; q.epi.clim = m.ct;
+          q.epi.out_hi = arena.hi.get() + off[i]; q.epi.out_lo = arena.lo.get() + off[i];
+          b1.add(&q, bn, i);
+        }
+        b1.run(err, s, ks);
+        // stage 2: partials [split][v1][(j, c1)] of sum_{(P,v)} S[(j, c1)][(P,v)] G2[v1][(P,v)]
+        for (size_t t = a; t < b; ++t) {
+          const size_t i = live[t];
+          Impl &m = *eng[i];
+          const int64_t kc = std::min(jc[i], items[i].k - rd * jc[i]);
+          const int bn2 = pick_bn(m.vt);
+          TcProblem &q = p2[i];
+          q.A = m.mat(arena.hi.get() + off[i], arena.lo.get() + off[i], jc[i] * m.ct, m.Kg, 128, bk_for(bn2));
+          q.B = m.mat(m.G2.hi.get(), m.G2.lo.get(), m.vt, m.Kg, bn2, bk_for(bn2));
+          q.shape.M = kc * m.ct; q.shape.N = m.vt; q.shape.K = m.Kg; q.shape.products = g_products;
+          q.shape.ksplit = pick_ksplit(ceil_div(kc * m.ct, 128) * ceil_div(m.vt, bn2), m.Kg);
+          m.part.resize((size_t)q.shape.ksplit * q.shape.M * q.shape.N);
+          q.epi.kind = TcEpilogue::STORE_F32;
+          q.epi.rd = q.shape.M; q.epi.ro2 = 1; q.epi.rlim = q.shape.M;
+          q.epi.cd = q.shape.N; q.epi.co2 = q.shape.M; q.epi.clim = q.shape.N;
+          q.epi.so = q.shape.M * q.shape.N;
+          q.epi.out_f32 = m.part.get();
+          b2.add(&q, bn2, i);
+        }
+        b2.run(err, s, ks);
+        std::vector<ReduceJob> rj;
+        for (size_t t = a; t < b; ++t) {
+          const size_t i = live[t];
+          Impl &m = *eng[i];
+          const int64_t j0 = rd * jc[i];
+          const int64_t kc = std::min(jc[i], items[i].k - j0);
+          ReduceJob r;
+          r.part = m.part.get(); r.M = m.vt; r.N = kc * m.ct; r.ksplit = ks[i];
+          r.epi.kind = TcEpilogue::AXPBY_F64;
+          r.epi.rd = m.vt; r.epi.ro2 = m.ct; r.epi.rlim = m.vt;
+          r.epi.cd = m.ct; r.epi.co1 = items[i].ldy; r.epi.co2 = 1; r.epi.clim = m.ct;
+          r.epi.out_f64 = items[i].Y + j0 * items[i].ldy; r.epi.alpha = alpha; r.epi.beta = acc ? 1.0 : 0.0;
+          rj.push_back(r);
+        }
+        reduce_grouped(rj, s);
+        a = b;
       }
-      b1.run(err, s, ks);
-      // stage 2: partials [split][v1][(j, c1)] of sum_{(P,v)} S[(j, c1)][(P,v)] G2[v1][(P,v)]
-      for (size_t i : live) {
-        Impl &m = *eng[i];
-        const int64_t kc = std::min(jc[i], items[i].k - rd * jc[i]);
-        const int bn2 = pick_bn(m.vt);
-        TcProblem &q = p2[i];
-        q.A = m.mat(m.S.hi.get(), m.S.lo.get(), (int64_t)m.S.hi.count / m.Kg, m.Kg, 128, bk_for(bn2));
-        q.B = m.mat(m.G2.hi.get(), m.G2.lo.get(), m.vt, m.Kg, bn2, bk_for(bn2));
-        q.shape.M = kc * m.ct; q.shape.N = m.vt; q.shape.K = m.Kg; q.shape.products = g_products;
-        q.shape.ksplit = pick_ksplit(ceil_div(kc * m.ct, 128) * ceil_div(m.vt, bn2), m.Kg);
-        m.part.resize((size_t)q.shape.ksplit * q.shape.M * q.shape.N);
-        q.epi.kind = TcEpilogue::STORE_F32;
-        q.epi.rd = q.shape.M; q.epi.ro2 = 1; q.epi.rlim = q.shape.M;
-        q.epi.cd = q.shape.N; q.epi.co2 = q.shape.M; q.epi.clim = q.shape.N;
-        q.epi.so = q.shape.M * q.shape.N;
-        q.epi.out_f32 = m.part.get();
-        b2.add(&q, bn2, i);
-      }
-      b2.run(err, s, ks);
-      std::vector<ReduceJob> rj;
-      for (size_t i : live) {
-        Impl &m = *eng[i];
-        const int64_t j0 = rd * jc[i];
-        const int64_t kc = std::min(jc[i], items[i].k - j0);
-        ReduceJob r;
-        r.part = m.part.get(); r.M = m.vt; r.N = kc * m.ct; r.ksplit = ks[i];
-        r.epi.kind = TcEpilogue::AXPBY_F64;
-        r.epi.rd = m.vt; r.epi.ro2 = m.ct; r.epi.rlim = m.vt;
-        r.epi.cd = m.ct; r.epi.co1 = items[i].ldy; r.epi.co2 = 1; r.epi.clim = m.ct;
-        r.epi.out_f64 = items[i].Y + j0 * items[i].ldy; r.epi.alpha = alpha; r.epi.beta = acc ? 1.0 : 0.0;
-        rj.push_back(r);
-      }
-      reduce_grouped(rj, s);
     }
     acc = true;
   }

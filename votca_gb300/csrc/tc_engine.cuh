@@ -17,7 +17,7 @@ class MixedEngine {
   // The same for many operators at once (GroupedItem.op->mixed engines), one grouped
   // launch per stage and tile shape; accumulate: Y already holds the Hqp term.
   static void apply_grouped(const Coef &c, const std::vector<GroupedItem> &items, bool accumulate,
-                            cudaStream_t s);
+                            cudaStream_t s, GroupScratch *scratch);
   // Synchronise and raise if a kernel reported a bounded-wait timeout.
   void check(cudaStream_t s);
 
