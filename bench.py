@@ -401,6 +401,121 @@ def full_bse_report(roots=10, tol=1e-7, k=32, check=False, cpu=False):
     return out
 
 
+def roots_report(ctx, precision, w, Mmn, hqp, opt):
+    """Time-to-20-roots (tolerance 1e-7) of singlets and triplets for each precision
+    built, the per-root difference and eigenvector overlaps of mixed vs FP64, and the
+    adjoint gradient of the 5 lowest singlets (FP64 eigenvectors, one call)."""
+    import ctypes
+
+    import torch
+
+    from votca_gb300 import _lib
+    from votca_gb300 import bse_operator as bo
+    from votca_gb300.davidson import DavidsonSolver
+
+    out = {}
+    ctxs = {}
+    for pname, pr in (("fp64", bo.PRECISION_FP64), ("mixed", bo.PRECISION_MIXED)):
+        try:
+            ctxs[pname] = ctx if pr == precision else bo.GpuBSEContext(w, Mmn, hqp, opt, precision=pr)
+        except _lib.BSEError as e:
+            out[pname] = {"unavailable": str(e)}
+    for kind, cls in (("singlets", bo.SingletOperator_TDA), ("triplets", bo.TripletOperator_TDA)):
+        res, vecs = {}, {}
+        for pname, c2 in ctxs.items():
+            ds = DavidsonSolver()
+            ds.set_tolerance(1e-7)
+            ds.set_max_search_space(10 * ROOTS)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            lam, v = ds.solve(cls(c2), ROOTS)
+            dt = time.perf_counter() - t0
+            vecs[pname] = v
+            res[pname] = {"seconds": dt, "iterations": int(ds.num_iterations()), "info": ds.info(),
+                          "matvec_seconds": ds.result.seconds_matvec,
+                          "matvec_columns": int(ds.result.matvec_columns),
+                          "roots_eV": [round(float(x), 9) for x in lam]}
+        if "fp64" in vecs and "mixed" in vecs:
+            d = np.abs(np.array(res["fp64"]["roots_eV"]) - np.array(res["mixed"]["roots_eV"])) * 1e3
+            res["max_abs_diff_meV"] = float(d.max())
+            # |<x_fp64, x_mixed>| per root (unit vectors; 1 = identical up to sign)
+            ov = np.abs(np.sum(vecs["fp64"] * vecs["mixed"], axis=0))
+            res["min_eigvec_overlap"] = float(ov.min())
+            res["max_one_minus_overlap"] = float((1.0 - ov).max())
+            res["speedup_mixed_vs_fp64"] = res["fp64"]["seconds"] / res["mixed"]["seconds"]
+        out[kind] = res
+        if kind == "singlets" and "fp64" in ctxs:
+            # adjoint: d(sum_k g_k Omega_k)/d(Mmn, Hqp, w) for the 5 lowest singlets
+            c64 = ctxs["fp64"]
+            X = np.asfortranarray(vecs["fp64"][:, :5])
+            g = np.ones(5)
+            gm = np.zeros(Mmn.data.shape)
+            nh = opt.cmax - opt.vmin + 1
+            gh = np.zeros((nh, nh), order="F")
+            gw = np.zeros(w.shape)
+            t0 = time.perf_counter()
+            _lib.check(c64._L.bse_op_eig_gradient(c64.handle, 1, 2, 1, 0, bo._p(X), X.shape[0], 5, bo._p(g),
+                                                  bo._p(gm), bo._p(gh), bo._p(gw)))
+            out["adjoint_5_singlets"] = {
+                "seconds": time.perf_counter() - t0,
+                "note": "one bse_op_eig_gradient call: gradients w.r.t. all Mmn entries (5.4 GB, copied "
+                        "to the host), the Hqp window and the screening; FP64"}
+    for pname, c2 in ctxs.items():
+        if c2 is not ctx:
+            c2.close()
+    return out
+
+
+def c0_report(cpu=True):
+    """The reference's CPU-runnable case (v=8, c=64, Naux=256, 10 roots, tolerance 1e-7):
+    full solves on the GPU (FP64, mixed) and of the reference CPU path (the
+    DavidsonSolver restatement driving the reference loop nest on all host threads)."""
+    import torch
+
+    from votca_gb300 import bse_operator as bo
+    from votca_gb300.davidson import DavidsonSolver
+    from votca_gb300.synthetic import qp_energies, screening_w
+
+    v, c, naux, nmo, roots, seed = 8, 64, 256, 72, 10, 0
+    mmn = make_mmn(seed, naux, nmo)
+    w = screening_w(seed, naux)
+    hqp = np.diag(qp_energies(seed, v, c))
+    opt = bo.BSEOperator_Options(homo=v - 1, rpamin=0, qpmin=0, vmin=0, cmax=v + c - 1)
+    out = {"workload": "tda_singlet_v8_c64_naux256_roots10"}
+    ref = None
+    for pname, pr in (("fp64", bo.PRECISION_FP64), ("mixed", bo.PRECISION_MIXED)):
+        cx = bo.GpuBSEContext(w, bo.TCMatrix_gwbse(mmn), hqp, opt, precision=pr)
+        ds = DavidsonSolver()
+        ds.set_tolerance(1e-7)
+        ds.set_max_search_space(10 * roots)
+        ds.solve(bo.SingletOperator_TDA(cx), roots)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        lam, _ = ds.solve(bo.SingletOperator_TDA(cx), roots)
+        out[pname] = {"seconds": time.perf_counter() - t0, "iterations": int(ds.num_iterations()),
+                      "info": ds.info()}
+        if ref is None:
+            ref = lam
+        else:
+            out[pname]["max_abs_diff_meV_vs_fp64"] = float(np.max(np.abs(lam - ref)) * 1e3)
+        cx.close()
+    if cpu:
+        import oracle
+        from oracle.davidson_oracle import DavidsonOracle
+
+        oracle.set_threads(os.cpu_count() or 1)
+        prob = oracle.BSEProblem(mmn, w, hqp, v, c)
+        d = DavidsonOracle()
+        d.set_tolerance(1e-7)
+        d.max_search_space = 10 * roots
+        t0 = time.perf_counter()
+        lam_cpu = d.solve(lambda X: prob.matmul_ref(X, "singlet"), prob.diagonal("singlet"), roots)[0]
+        out["cpu_reference"] = {"seconds": time.perf_counter() - t0, "cores": os.cpu_count() or 1,
+                                "kind": "port", "iterations": int(d.i_iter),
+                                "max_abs_diff_meV_vs_gpu_fp64": float(np.max(np.abs(np.asarray(lam_cpu) - ref)) * 1e3)}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -591,36 +706,8 @@ def main():
         "gpu_launches": gpu_launches,
     }
     if rank == 0 and not args.no_roots:
-        roots = {}
-        evecs = {}
-        for pname, pr in (("fp64", bo.PRECISION_FP64), ("mixed", bo.PRECISION_MIXED)):
-            try:
-                c2 = ctx if pr == precision else bo.GpuBSEContext(w, Mmn, hqp, opt, precision=pr)
-            except _lib.BSEError as e:
-                roots[pname] = {"unavailable": str(e)}
-                continue
-            ds = DavidsonSolver()
-            ds.set_tolerance(1e-7)
-            ds.set_max_search_space(10 * ROOTS)
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            lam, vecs = ds.solve(bo.SingletOperator_TDA(c2), ROOTS)
-            dt = time.perf_counter() - t0
-            evecs[pname] = vecs
-            roots[pname] = {"seconds": dt, "iterations": int(ds.num_iterations()), "info": ds.info(),
-                            "matvec_seconds": ds.result.seconds_matvec,
-                            "matvec_columns": int(ds.result.matvec_columns),
-                            "roots_eV": [round(float(x), 9) for x in lam]}
-            if c2 is not ctx:
-                c2.close()
-        if "roots_eV" in roots.get("fp64", {}) and "roots_eV" in roots.get("mixed", {}):
-            d = np.abs(np.array(roots["fp64"]["roots_eV"]) - np.array(roots["mixed"]["roots_eV"])) * 1e3
-            roots["max_abs_diff_meV"] = float(d.max())
-            # |<x_fp64, x_mixed>| per root (unit vectors; 1 = identical up to sign)
-            ov = np.abs(np.sum(evecs["fp64"] * evecs["mixed"], axis=0))
-            roots["min_eigvec_overlap"] = float(ov.min())
-            roots["max_one_minus_overlap"] = float((1.0 - ov).max())
-        line["time_to_20_roots"] = roots
+        line["time_to_20_roots"] = roots_report(ctx, precision, w, Mmn, hqp, opt)
+        line["c0_time_to_10_roots"] = c0_report(cpu=world == 1 and not args.no_cpu)
     if rank == 0 and (args.molecules > 0 or args.full_bse):
         ctx.close()
     if rank == 0 and args.molecules > 0:
