@@ -56,6 +56,24 @@ def dist_env():
     return world, rank, local
 
 
+def max_over_ranks(x, world, device):
+    """The slowest rank's time (the job's time) when N replicas run; x itself at N = 1."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(work_per_rank, seconds, world):
+    """Whole-job throughput of N independent replicas (weak scaling): every rank does the
+    same work, the job takes the slowest rank's time."""
+    return world * work_per_rank / seconds
+
+
 def make_mmn(seed, naux, nmo):
     """Seeded Mmn, layout (m, P, n) == the reference's slices laid end to end."""
     from votca_gb300.synthetic import mmn_tensor_torch
@@ -610,10 +628,7 @@ def main():
     stage_calls = (ctypes.c_int64 * 12)()
     _lib.check(L.bse_op_profile_read(ctx.handle, stage_ms, stage_calls, 12))
     _lib.check(L.bse_op_profile(ctx.handle, 0))
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world, "cuda")
 
     # e2e through the host-pointer C ABI call with pinned buffers
     Xp = torch.empty((K, dim), dtype=torch.float64).pin_memory()
@@ -629,17 +644,14 @@ def main():
     for _ in range(args.steps):
         _lib.check(L.bse_op_matmul(ctx.handle, *op.coef, Xptr, dim, K, Yptr, dim))
     e2e_s = (time.perf_counter() - t0) / args.steps
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s, world, "cuda")
     # consistency of the two paths
     yd = dY.cpu().numpy()
     rel = float(np.linalg.norm(Yp.numpy() - yd) / np.linalg.norm(yd))
 
     F = algorithmic_flops(V, C, NAUX, K)
-    value = world * F / (ms * 1e-3) / 1e12
-    e2e_val = world * F / e2e_s / 1e12
+    value = replica_throughput(F, ms * 1e-3, world) / 1e12
+    e2e_val = replica_throughput(F, e2e_s, world) / 1e12
 
     # roofline of the dominant kernel
     peaks = {}
