@@ -15,6 +15,7 @@
 //         dM(c,c',P)      = -cd sum_k g_k sum_v X_k[v][c] (G^P X_k)[v][c'],  G^P = screened vv block
 // The forward analogue in the reference is the expectation-value analysis
 // x^T H_part x (xtp/src/libxtp/gwbse/bse.cc:490-520, 565-606).
+#include <algorithm>
 #include <vector>
 
 #include "bse_ops.cuh"
@@ -92,7 +93,53 @@ __global__ void scale_batches_kernel(const double *Q, const double *w, int64_t n
     out[t] = alpha * w[t / len] * Q[t];
 }
 
+// One chunk [m0, m0 + cnt) of the Mmn-shaped gradient, slice layout out[(mi * naux + P) * nsize + n]:
+// the vc, vv and cc block gradients at their window positions, zero elsewhere.
+struct ScatterGradArgs {
+  const double *gMvc, *gMvv, *gMcc;
+  int64_t m0, cnt, naux, nsize, vt, ct, dim, m_v0, m_c0, n_v0, n_c0;
+  double *out;
+};
+__global__ void scatter_grad_kernel(const ScatterGradArgs a) {
+  const int64_t total = a.cnt * a.naux * a.nsize;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t n = t % a.nsize, P = (t / a.nsize) % a.naux, m = a.m0 + t / (a.nsize * a.naux);
+    const int64_t v = m - a.m_v0, c1 = m - a.m_c0, nv = n - a.n_v0, nc = n - a.n_c0;
+    double g = 0.0;
+    if (v >= 0 && v < a.vt) {
+      if (nc >= 0 && nc < a.ct) g = a.gMvc[P * a.dim + v * a.ct + nc];
+      else if (nv >= 0 && nv < a.vt) g = a.gMvv[(P * a.vt + v) * a.vt + nv];
+    } else if (c1 >= 0 && c1 < a.ct && nc >= 0 && nc < a.ct) {
+      g = a.gMcc[(P * a.ct + c1) * a.ct + nc];
+    }
+    a.out[t] = g;
+  }
+}
+
 }  // namespace
+
+void scatter_mmn_gradient(const BseOperator &op, const double *gMvc, const double *gMvv,
+                          const double *gMcc, double *host_out, cudaStream_t s) {
+  const int64_t slice = op.naux * op.nsize;
+  const int64_t per = std::max<int64_t>(1, std::min<int64_t>(op.msize, (512LL << 20) / (slice * 8)));
+  DeviceBuffer<double> buf(per * slice);
+  for (int64_t m0 = 0; m0 < op.msize; m0 += per) {
+    ScatterGradArgs a;
+    a.gMvc = gMvc; a.gMvv = gMvv; a.gMcc = gMcc;
+    a.m0 = m0; a.cnt = std::min(per, op.msize - m0);
+    a.naux = op.naux; a.nsize = op.nsize; a.vt = op.vt; a.ct = op.ct; a.dim = op.dim;
+    a.m_v0 = op.m_v0; a.m_c0 = op.m_c0; a.n_v0 = op.n_v0; a.n_c0 = op.n_c0;
+    a.out = buf.get();
+    const int64_t total = a.cnt * slice;
+    scatter_grad_kernel<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(total, 256), 16LL * 152)),
+                          256, 0, s>>>(a);
+    VGB_LAUNCH_CHECK();
+    VGB_CUDA(cudaMemcpyAsync(host_out + m0 * slice, buf.get(), total * sizeof(double),
+                             cudaMemcpyDeviceToHost, s));
+    VGB_CUDA(cudaStreamSynchronize(s));  // buf is reused by the next chunk
+  }
+}
 
 void BseOperator::eig_gradient(const Coef &c, const double *X, int64_t ldx, int64_t nr,
                                const double *g_host, double *gMvc, double *gMvv, double *gMcc,

@@ -24,6 +24,7 @@
 #include <thread>
 
 #include "host_eig.hpp"
+#include "tc_engine.cuh"
 
 namespace vgb {
 
@@ -484,6 +485,11 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
       M.part = take(M.chunks * M.capc * M.capc);
       p += 64;
     }
+  }
+  {
+    int64_t kmax = 1;
+    for (const Mol &M : mols) kmax = std::max(kmax, std::max(M.ncols, M.size_update));
+    MixedEngine::prepare_grouped(ops, kmax, s);
   }
   GroupScratch arena;  // Hd intermediates of the grouped products, shared by all molecules
   DeviceBuffer<int> flags(nm);

@@ -137,6 +137,11 @@ class BseOperator {
   DeviceBuffer<double> hamA_, hamB_, hamX_;
 };
 
+// The Mmn-shaped gradient (the caller's slice layout, msize x naux x nsize, host memory) from the
+// block gradients of BseOperator::eig_gradient: scattered on the device, copied in chunks.
+void scatter_mmn_gradient(const BseOperator &op, const double *gMvc, const double *gMvv,
+                          const double *gMcc, double *host_out, cudaStream_t s);
+
 // One molecule's share of a grouped product: Y = H(c) X on its own operator.
 struct GroupedItem {
   BseOperator *op = nullptr;

@@ -334,28 +334,9 @@ int bse_op_eig_gradient(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd, int3
     if (grad_hqp) VGB_CUDA(cudaMemcpy(grad_hqp, gH.get(), nh * sizeof(double), cudaMemcpyDeviceToHost));
     if (grad_screening)
       VGB_CUDA(cudaMemcpy(grad_screening, gW.get(), nw * sizeof(double), cudaMemcpyDeviceToHost));
-    if (grad_mmn) {
-      std::vector<double> a(naux * dim), b(naux * vt * vt), c(naux * ct * ct);
-      VGB_CUDA(cudaMemcpy(a.data(), gMvc.get(), a.size() * sizeof(double), cudaMemcpyDeviceToHost));
-      VGB_CUDA(cudaMemcpy(b.data(), gMvv.get(), b.size() * sizeof(double), cudaMemcpyDeviceToHost));
-      VGB_CUDA(cudaMemcpy(c.data(), gMcc.get(), c.size() * sizeof(double), cudaMemcpyDeviceToHost));
-      const int64_t nsz = op.nsize;
-      std::fill(grad_mmn, grad_mmn + op.msize * naux * nsz, 0.0);
-      auto at = [&](int64_t m, int64_t P, int64_t n) -> double & { return grad_mmn[(m * naux + P) * nsz + n]; };
-      for (int64_t P = 0; P < naux; ++P) {
-        for (int64_t v = 0; v < vt; ++v) {
-          for (int64_t cc = 0; cc < ct; ++cc) at(op.m_v0 + v, P, op.n_c0 + cc) += a[P * dim + v * ct + cc];
-          for (int64_t v2 = 0; v2 < vt; ++v2) at(op.m_v0 + v, P, op.n_v0 + v2) += b[(P * vt + v) * vt + v2];
-        }
-        for (int64_t c1 = 0; c1 < ct; ++c1)
-          for (int64_t c2 = 0; c2 < ct; ++c2) at(op.m_c0 + c1, P, op.n_c0 + c2) += c[(P * ct + c1) * ct + c2];
-      }
-    }
+    if (grad_mmn) vgb::scatter_mmn_gradient(op, gMvc.get(), gMvv.get(), gMcc.get(), grad_mmn, s);
   });
 }
-
-namespace {
-}  // namespace
 
 int bse_rpa_epsilon(const bse_mmn_desc *mmn, const double *const *mmn_slices,
                     const double *rpa_energies, int64_t rpatotal, int64_t homo, int64_t rpamin,

@@ -345,6 +345,43 @@ struct GemmBuckets {
 
 }  // namespace
 
+void MixedEngine::prepare_grouped(const std::vector<BseOperator *> &ops, int64_t kmax, cudaStream_t s) {
+  read_tuning();
+  // sizes of every per-operator buffer a grouped product of <= kmax columns touches
+  struct Need { Impl *m; int64_t xs, zs, part; };
+  std::vector<Need> need;
+  int64_t bytes = 0;
+  for (BseOperator *op : ops) {
+    if (!op->mixed) continue;
+    Impl &m = *op->mixed->impl_;
+    Need q;
+    q.m = &m;
+    q.xs = kmax * m.vt * m.Kc;
+    q.zs = kmax * m.Kn;
+    const int64_t ks1 = pick_ksplit(ceil_div(m.naux, 128) * ceil_div(kmax, pick_bn(kmax)), m.dimP);
+    int64_t part = ks1 * m.naux * kmax;
+    for (int64_t kc = 1; kc <= kmax; ++kc) {  // Hd stage 2 partials for any vector count
+      const int64_t ks2 = pick_ksplit(ceil_div(kc * m.ct, 128) * ceil_div(m.vt, pick_bn(m.vt)), m.Kg);
+      part = std::max(part, ks2 * kc * m.ct * m.vt);
+    }
+    q.part = part;
+    need.push_back(q);
+    bytes += 4 * (q.xs + q.zs) + 4 * q.part + 4096;
+  }
+  if (need.empty()) return;
+  // grow the stream-ordered pool once instead of once per buffer
+  if (alloc_stream()) {
+    void *p = nullptr;
+    if (cudaMallocAsync(&p, (size_t)bytes, s) == cudaSuccess) VGB_CUDA(cudaFreeAsync(p, s));
+    else cudaGetLastError();  // no headroom for one block: the buffers are allocated one by one
+  }
+  for (Need &q : need) {
+    if ((int64_t)q.m->Xs.hi.count < q.xs) q.m->Xs.ensure(q.xs / q.m->Kc, q.m->Kc, s);
+    if ((int64_t)q.m->Zs.hi.count < q.zs) q.m->Zs.ensure(q.zs / q.m->Kn, q.m->Kn, s);
+    q.m->part.resize((size_t)q.part);
+  }
+}
+
 void MixedEngine::apply_grouped(const Coef &c, const std::vector<GroupedItem> &items,
                                 bool accumulate, cudaStream_t s, GroupScratch *scratch) {
   read_tuning();

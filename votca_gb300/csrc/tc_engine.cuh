@@ -18,6 +18,9 @@ class MixedEngine {
   // launch per stage and tile shape; accumulate: Y already holds the Hqp term.
   static void apply_grouped(const Coef &c, const std::vector<GroupedItem> &items, bool accumulate,
                             cudaStream_t s, GroupScratch *scratch);
+  // Allocate, ahead of a series of grouped products of at most kmax columns, every
+  // per-operator buffer they use (one pool growth instead of one per buffer).
+  static void prepare_grouped(const std::vector<BseOperator *> &ops, int64_t kmax, cudaStream_t s);
   // Synchronise and raise if a kernel reported a bounded-wait timeout.
   void check(cudaStream_t s);
 

@@ -64,14 +64,16 @@ def mmn_tensor_torch(seed, naux, nmo):
     """Same distribution as mmn_tensor, drawn with torch's seeded generator on
     the GPU when one is present (large sizes).  Each aux slice is a symmetric
     N(0,1) matrix ((G + G^T)/sqrt(2) off the diagonal, G_mm on it) times
-    0.1/sqrt(Naux) exp(-|m-n|/40).  Layout (m, P, n), float64 host array."""
+    0.1/sqrt(Naux) exp(-|m-n|/40).  Layout (m, P, n), float64 host array (a view of a
+    page-locked torch tensor when a GPU is present)."""
     import torch
 
     dev = "cuda" if torch.cuda.is_available() else "cpu"
     g = torch.Generator(device=dev).manual_seed(int(seed))
     m = torch.arange(nmo, dtype=torch.float64, device=dev)
     decay = torch.exp(-(m[:, None] - m[None, :]).abs() / 40.0) * (0.1 / np.sqrt(naux))
-    out = torch.empty((nmo, naux, nmo), dtype=torch.float64)
+    # page-locked when a GPU is present: the operator staging then copies at full link speed
+    out = torch.empty((nmo, naux, nmo), dtype=torch.float64, pin_memory=torch.cuda.is_available())
     chunk = 128
     for p0 in range(0, naux, chunk):
         p1 = min(naux, p0 + chunk)
