@@ -76,16 +76,41 @@ def test_lockstep_equals_single_solves(precision, max_space):
     for m, op in enumerate(ops):
         ds = _solver(max_space)
         lam, _ = ds.solve(op, nroots)
-        # the same iteration; the FP64 reduction orders of the grouped kernels differ (and
-        # for split precision the K splits of the grouped products, which only need to
-        # bound the FP32 chains), which can move a residual at the tolerance across it
-        np.testing.assert_allclose(ev[m], lam, rtol=0, atol=1e-10 if precision == 0 else 1e-7)
+        # the same iteration; the FP64 reduction orders of the grouped kernels differ, and
+        # for split precision the lockstep solve of these small operators uses their dense
+        # form (a differently rounded operator): 0.001 meV
+        np.testing.assert_allclose(ev[m], lam, rtol=0, atol=1e-10 if precision == 0 else 1e-6)
         if precision == 0:
             assert abs(iters[m] - ds.num_iterations()) <= 1
         if precision == 0:
             H = op.matmul(np.eye(op.rows()))
             exact = np.linalg.eigvalsh(0.5 * (H + H.T))[:nroots]
             np.testing.assert_allclose(ev[m], exact, rtol=0, atol=1e-9)
+    for _, ctx in ctxs:
+        ctx.close()
+
+
+def test_lockstep_dense_form_matches_factorised_products(monkeypatch):
+    """Small split-precision operators run the lockstep solve through their dense form
+    (H built once on the tensor cores); with the dense form disabled the factorised products
+    are used.  Both agree with each other and with the FP64 dense eigenvalues."""
+    from votca_gb300 import bse_operator as bo
+
+    ctxs = _contexts(1)
+    fp64 = _contexts(0)
+    ops = [bo.SingletOperator_TDA(ctx) for _, ctx in ctxs]
+    monkeypatch.setenv("VGB_BATCH_DENSE", "0")
+    ev_f, info_f, _ = _solver().solve_batch(ops, 5, nthreads=0)
+    monkeypatch.delenv("VGB_BATCH_DENSE")
+    ev_d, info_d, _ = _solver().solve_batch(ops, 5, nthreads=0)
+    assert all(i == "Success" for i in info_f + info_d)
+    np.testing.assert_allclose(ev_d, ev_f, rtol=0, atol=1e-6)  # two split-precision operators
+    for m, (_, c64) in enumerate(fp64):
+        op = bo.SingletOperator_TDA(c64)
+        H = op.matmul(np.eye(op.rows()))
+        exact = np.linalg.eigvalsh(0.5 * (H + H.T))[:5]
+        np.testing.assert_allclose(ev_d[m], exact, rtol=0, atol=1e-6)  # 0.001 meV
+        c64.close()
     for _, ctx in ctxs:
         ctx.close()
 

@@ -16,6 +16,7 @@
 #include <atomic>
 #include <chrono>
 #include <cstdio>
+#include <cstdlib>
 #include <cmath>
 #include <exception>
 #include <memory>
@@ -38,6 +39,12 @@ constexpr int kTileLd = kTile + 1;
 constexpr int kTnCols = 160;     // m + p columns per transposed-product job
 constexpr int kTnOut = 8;        // outputs per thread: m * p <= 8 * 256
 constexpr int kNnSmem = 48 * 1024;
+// Dense form up to dim 4096 (64 MB of bf16 hi/lo per molecule).  Its bf16 representation adds
+// full-rank noise of ~1e-5 relative per element to an interaction of rank <= 2 Naux; from dim
+// ~5000 (with Naux ~150-300) that noise held some residuals above 1e-7 (up to 49 iterations
+// instead of 3), while at dim <= 4096 every molecule of the 256-molecule set converged as with
+// the factorised products.
+constexpr int64_t kDenseMaxDim = 4096;
 
 template <class Job>
 struct Group {
@@ -294,6 +301,7 @@ unsigned rows_blocks(int64_t n) { return (unsigned)std::max<int64_t>(1, std::min
 
 struct Mol {
   BseOperator *op = nullptr;
+  bool dense = false;  // products through the operator's dense form
   int64_t n = 0, size_update = 0, restart_size = 0, max_space = 0, capc = 0, needmax = 0;
   int64_t ncols = 0, nav = 0, m = 0, needed = 0, nupdate = 0, chunks = 0;
   bool done = false;
@@ -487,6 +495,20 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
     }
   }
   {
+    // small split-precision TDA operators: the dense form (one GEMM per product)
+    const char *env = getenv("VGB_BATCH_DENSE");
+    const bool allow_dense = !(env && atoi(env) == 0);
+    const char *envmax = getenv("VGB_BATCH_DENSE_MAX");
+    const int64_t dense_max = envmax ? atoll(envmax) : kDenseMaxDim;
+    std::vector<BseOperator *> dense;
+    for (BseOperator *op : ops)
+      if (allow_dense && coef.cd2 == 0 && op->precision == BSE_PRECISION_MIXED && op->mixed &&
+          op->hqp_diagonal && op->dim <= dense_max && ceil_div(op->naux, 64) * 64 <= 1024)
+        dense.push_back(op);
+    MixedEngine::build_dense_grouped(dense, coef, s);
+    for (BseOperator *op : dense)
+      for (Mol &M : mols)
+        if (M.op == op) M.dense = true;
     int64_t kmax = 1;
     for (const Mol &M : mols) kmax = std::max(kmax, std::max(M.ncols, M.size_update));
     MixedEngine::prepare_grouped(ops, kmax, s);
@@ -552,7 +574,7 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
         const int64_t old = (it == 0) ? 0 : M->nav, nvec = M->ncols - old;
         GroupedItem gi;
         gi.op = M->op; gi.X = M->V + old * M->n; gi.ldx = M->n; gi.k = nvec;
-        gi.Y = M->AV + old * M->n; gi.ldy = M->n;
+        gi.Y = M->AV + old * M->n; gi.ldy = M->n; gi.dense = M->dense;
         items.push_back(gi);
         tn.push_back({M, M->V, M->AV + old * M->n, M->ncols, nvec, M->cbuf, M->ncols});
       }

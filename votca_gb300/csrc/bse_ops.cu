@@ -580,12 +580,13 @@ void BseOperator::matmul(const Coef &c, const double *X, int64_t ldx, int64_t k,
 void matmul_grouped(const Coef &c, const std::vector<GroupedItem> &items, cudaStream_t s,
                     GroupScratch *scratch) {
   VGB_REQUIRE(c.cd2 == 0, "grouped products: Hd2 is not grouped");
-  std::vector<GroupedItem> mixed_items;
+  std::vector<GroupedItem> mixed_items, dense_items;
   std::vector<HqpJob> hq;
   for (const GroupedItem &it : items) {
     BseOperator &op = *it.op;
     VGB_REQUIRE(it.ldx >= op.dim && it.ldy >= op.dim, "matmul: leading dimension smaller than the operator size");
     if (it.k <= 0) continue;
+    if (it.dense) VGB_REQUIRE(op.mixed && op.mixed->dense_ready(c), "grouped products: dense form not built");
     if (op.precision != BSE_PRECISION_MIXED || !op.mixed) {  // FP64 operators: one product each
       op.matmul(c, it.X, it.ldx, it.k, it.Y, it.ldy, s);
       continue;
@@ -600,7 +601,7 @@ void matmul_grouped(const Coef &c, const std::vector<GroupedItem> &items, cudaSt
         op.apply_hqp(c.cqp, it.X, it.ldx, it.k, it.Y, it.ldy, false, s);
       }
     }
-    mixed_items.push_back(it);
+    (it.dense ? dense_items : mixed_items).push_back(it);
   }
   std::unique_ptr<HqpGroup> g(new HqpGroup());
   for (size_t i = 0; i < hq.size();) {
@@ -615,6 +616,7 @@ void matmul_grouped(const Coef &c, const std::vector<GroupedItem> &items, cudaSt
     VGB_LAUNCH_CHECK();
   }
   MixedEngine::apply_grouped(c, mixed_items, c.cqp != 0, s, scratch);
+  MixedEngine::apply_dense_grouped(c, dense_items, c.cqp != 0, s);
 }
 
 void BseOperator::check_errors(cudaStream_t s) {

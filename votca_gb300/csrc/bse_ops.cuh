@@ -149,6 +149,7 @@ struct GroupedItem {
   int64_t ldx = 0, k = 0;
   double *Y = nullptr;
   int64_t ldy = 0;
+  bool dense = false;  // use the operator's dense form (MixedEngine::build_dense_grouped)
 };
 // Scratch shared by the operators of a grouped product (the Hd intermediates); kept by
 // the caller across products so that it is allocated once.

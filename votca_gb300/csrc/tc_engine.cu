@@ -88,6 +88,11 @@ struct MixedEngine::Impl {
   DeviceBuffer<float> part;
   DeviceBuffer<int> err;
   int64_t s_budget_bytes = 4LL << 30;
+  // dense form (small operators in batches): H(coef) as bf16 hi/lo rows [I][Kd], Kd = pad64(dim)
+  SplitBuf Hdense, Xd;  // Xd [j][Kd]: its own buffer, the K padding of Xs must stay zero
+  int64_t Kd = 0;
+  bool dense_ready = false;
+  Coef dense_coef;
   // operand descriptors of the grouped products, encoded once per (buffer, shape)
   // (the key holds every value the descriptors encode, so a hit is exact even when an
   // address is reused by a later allocation)
@@ -345,6 +350,224 @@ struct GemmBuckets {
 
 }  // namespace
 
+namespace {
+
+// H = (H + H^T) / 2: the two halves of the split products round differently (A_hi B_lo
+// against A_lo B_hi), and a nonsymmetric operator leaves a floor on the Davidson residual.
+__global__ void symmetrize_kernel(double *H, int64_t n) {
+  const int64_t total = n * n;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t / n, j = t % n;
+    if (j <= i) continue;
+    const double a = 0.5 * (H[i * n + j] + H[j * n + i]);
+    H[i * n + j] = a;
+    H[j * n + i] = a;
+  }
+}
+
+// the dense form holds cx Hx - cd Hd; Hqp is applied in FP64 beside it
+bool same_coef(const Coef &a, const Coef &b) {
+  return a.cx == b.cx && a.cd == b.cd && a.cd2 == b.cd2;
+}
+
+}  // namespace
+
+bool MixedEngine::dense_ready(const Coef &c) const {
+  return impl_->dense_ready && same_coef(impl_->dense_coef, c);
+}
+
+void MixedEngine::build_dense_grouped(const std::vector<BseOperator *> &ops, const Coef &c, cudaStream_t s) {
+  read_tuning();
+  VGB_REQUIRE(c.cd2 == 0, "dense form: TDA operators only");
+  std::vector<BseOperator *> todo;
+  for (BseOperator *op : ops) {
+    VGB_REQUIRE(op->mixed && op->hqp_diagonal, "dense form: mixed-precision operators with a diagonal Hqp");
+    if (!op->mixed->dense_ready(c)) todo.push_back(op);
+  }
+  int *err = todo.empty() ? nullptr : todo[0]->mixed->impl_->err.get();
+  // slices of operators whose FP64 temporaries (H and the two K = Naux splits) fit 8 GB
+  const int64_t budget = 8LL << 30;
+  size_t a = 0;
+  while (a < todo.size()) {
+    size_t b = a;
+    int64_t used = 0;
+    std::vector<int64_t> hoff, aoff, boff;
+    while (b < todo.size()) {
+      const BseOperator &op = *todo[b];
+      const Impl &m = *op.mixed->impl_;
+      const int64_t h = op.dim * op.dim * 8, av = op.vt * op.vt * m.Kn * 4, bc = op.ct * op.ct * m.Kn * 4;
+      if (b > a && used + h + av + bc > budget) break;
+      used += h + av + bc;
+      ++b;
+    }
+    // temporaries of the slice
+    int64_t nh = 0, na = 0, nb = 0;
+    for (size_t t = a; t < b; ++t) {
+      const BseOperator &op = *todo[t];
+      const Impl &m = *op.mixed->impl_;
+      hoff.push_back(nh); aoff.push_back(na); boff.push_back(nb);
+      nh += op.dim * op.dim;
+      na += pad64(op.vt * op.vt) * m.Kn;
+      nb += pad64(op.ct * op.ct) * m.Kn;
+    }
+    DeviceBuffer<double> H(nh);
+    SplitBuf Av, Bc;
+    Av.ensure(1, na, s);  // zero-filled: K padding columns multiply as zeros
+    Bc.ensure(1, nb, s);
+    std::vector<SplitJob> sj;
+    for (size_t t = a; t < b; ++t) {
+      const BseOperator &op = *todo[t];
+      const Impl &m = *op.mixed->impl_;
+      const size_t q = t - a;
+      // Av[(v1, v)][P] = w_P M(v1, v, P) = Gvv[v1][P][v]
+      SplitJob j1;
+      j1.x = op.Gvv.get(); j1.rows = op.vt * op.vt; j1.cols = op.naux;
+      j1.map.rdiv = op.vt; j1.map.rs1 = op.naux * op.vt; j1.map.rs2 = 1; j1.map.cs = op.vt; j1.map.rlim = op.vt;
+      j1.hi = Av.hi.get() + aoff[q]; j1.lo = Av.lo.get() + aoff[q]; j1.ldo = m.Kn;
+      sj.push_back(j1);
+      // Bc[(c1, c)][P] = M(c1, c, P) = Mcc[P][c][c1]
+      SplitJob j2;
+      j2.x = op.Mcc.get(); j2.rows = op.ct * op.ct; j2.cols = op.naux;
+      j2.map.rdiv = op.ct; j2.map.rs1 = 1; j2.map.rs2 = op.ct; j2.map.cs = op.ct * op.ct; j2.map.rlim = op.ct;
+      j2.hi = Bc.hi.get() + boff[q]; j2.lo = Bc.lo.get() + boff[q]; j2.ldo = m.Kn;
+      sj.push_back(j2);
+    }
+    split_grouped(sj, s);
+    std::vector<int> ks(b - a, 0);
+    // Hx: H[(v, c)][(v', c')] = cx sum_P B(vc, P) B(v'c', P)  (rows/cols in the padded v*Kc + c index)
+    if (c.cx != 0) {
+      std::vector<TcProblem> px(b - a);
+      GemmBuckets bx;
+      for (size_t t = a; t < b; ++t) {
+        const BseOperator &op = *todo[t];
+        Impl &m = *op.mixed->impl_;
+        const size_t q = t - a;
+        const int bn = pick_bn(m.dimP);
+        TcProblem &pr = px[q];
+        pr.A = m.mat(m.BvcT.hi.get(), m.BvcT.lo.get(), m.dimP, m.Kn, 128, bk_for(bn));
+        pr.B = m.mat(m.BvcT.hi.get(), m.BvcT.lo.get(), m.dimP, m.Kn, bn, bk_for(bn));
+        pr.shape.M = m.dimP; pr.shape.N = m.dimP; pr.shape.K = m.Kn; pr.shape.products = g_products;
+        pr.epi.kind = TcEpilogue::AXPBY_F64;
+        pr.epi.rd = m.Kc; pr.epi.ro1 = op.ct * op.dim; pr.epi.ro2 = op.dim; pr.epi.rlim = op.ct;
+        pr.epi.cd = m.Kc; pr.epi.co1 = op.ct; pr.epi.co2 = 1; pr.epi.clim = op.ct;
+        pr.epi.out_f64 = H.get() + hoff[q]; pr.epi.alpha = c.cx; pr.epi.beta = 0.0;
+        VGB_REQUIRE(m.Kn <= g_max_chain, "dense form: Naux above the FP32 chain bound");
+        bx.add(&pr, bn, q);
+      }
+      bx.run(err, s, ks);
+    }
+    // Hd: H[(v1, c1)][(v, c)] -= cd sum_P w_P M(v1, v, P) M(c1, c, P): rows (v1, v), columns (c1, c)
+    if (c.cd != 0) {
+      std::vector<TcProblem> pd(b - a);
+      GemmBuckets bd;
+      for (size_t t = a; t < b; ++t) {
+        const BseOperator &op = *todo[t];
+        Impl &m = *op.mixed->impl_;
+        const size_t q = t - a;
+        const int bn = pick_bn(op.ct * op.ct);
+        TcProblem &pr = pd[q];
+        pr.A = make_tc_mat(Av.hi.get() + aoff[q], Av.lo.get() + aoff[q], op.vt * op.vt, m.Kn, m.Kn, 128, bk_for(bn));
+        pr.B = make_tc_mat(Bc.hi.get() + boff[q], Bc.lo.get() + boff[q], op.ct * op.ct, m.Kn, m.Kn, bn, bk_for(bn));
+        pr.shape.M = op.vt * op.vt; pr.shape.N = op.ct * op.ct; pr.shape.K = m.Kn; pr.shape.products = g_products;
+        pr.epi.kind = TcEpilogue::AXPBY_F64;
+        pr.epi.rd = op.vt; pr.epi.ro1 = op.ct * op.dim; pr.epi.ro2 = op.ct; pr.epi.rlim = op.vt;
+        pr.epi.cd = op.ct; pr.epi.co1 = op.dim; pr.epi.co2 = 1; pr.epi.clim = op.ct;
+        pr.epi.out_f64 = H.get() + hoff[q]; pr.epi.alpha = -(double)c.cd; pr.epi.beta = c.cx != 0 ? 1.0 : 0.0;
+        bd.add(&pr, bn, q);
+      }
+      bd.run(err, s, ks);
+    }
+    for (size_t t = a; t < b; ++t) {
+      BseOperator &op = *todo[t];
+      Impl &m = *op.mixed->impl_;
+      const size_t q = t - a;
+      if (c.cx == 0 && c.cd == 0)
+        VGB_CUDA(cudaMemsetAsync(H.get() + hoff[q], 0, op.dim * op.dim * sizeof(double), s));
+      symmetrize_kernel<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(op.dim * op.dim, 256), 4096)),
+                          256, 0, s>>>(H.get() + hoff[q], op.dim);
+      VGB_LAUNCH_CHECK();
+      m.Kd = pad64(op.dim);
+      m.Hdense.ensure(op.dim, m.Kd, s);
+    }
+    std::vector<SplitJob> hj;
+    for (size_t t = a; t < b; ++t) {
+      const BseOperator &op = *todo[t];
+      Impl &m = *op.mixed->impl_;
+      SplitJob j;
+      j.x = H.get() + hoff[t - a]; j.rows = op.dim; j.cols = op.dim;
+      j.map.rdiv = 1; j.map.rs1 = op.dim; j.map.rs2 = 0; j.map.cs = 1; j.map.rlim = 1;
+      j.hi = m.Hdense.hi.get(); j.lo = m.Hdense.lo.get(); j.ldo = m.Kd;
+      hj.push_back(j);
+    }
+    split_grouped(hj, s);
+    VGB_CUDA(cudaStreamSynchronize(s));  // the slice temporaries are freed next
+    for (size_t t = a; t < b; ++t) {
+      Impl &m = *todo[t]->mixed->impl_;
+      m.dense_ready = true;
+      m.dense_coef = c;
+    }
+    a = b;
+  }
+}
+
+void MixedEngine::apply_dense_grouped(const Coef &c, const std::vector<GroupedItem> &items, bool accumulate,
+                                      cudaStream_t s) {
+  const size_t n = items.size();
+  if (n == 0) return;
+  std::vector<Impl *> eng(n);
+  for (size_t i = 0; i < n; ++i) {
+    VGB_REQUIRE(items[i].op->mixed && items[i].op->mixed->dense_ready(c), "dense product: form not built");
+    eng[i] = items[i].op->mixed->impl_;
+  }
+  int *err = eng[0]->err.get();
+  // X -> Xd[j][I] (bf16 hi/lo, K = Kd)
+  std::vector<SplitJob> jobs(n);
+  for (size_t i = 0; i < n; ++i) {
+    Impl &m = *eng[i];
+    const GroupedItem &it = items[i];
+    m.Xd.ensure(it.k, m.Kd, s);
+    SplitJob &j = jobs[i];
+    j.x = it.X; j.rows = it.k; j.cols = m.dim;
+    j.map.rdiv = 1; j.map.rs1 = it.ldx; j.map.rs2 = 0; j.map.cs = 1; j.map.rlim = 1;
+    j.hi = m.Xd.hi.get(); j.lo = m.Xd.lo.get(); j.ldo = m.Kd;
+  }
+  split_grouped(jobs, s);
+  // partials [split][j][I] of H X, then Y[I + j ldy] (+)= sum (the dense H holds Hx and Hd)
+  std::vector<TcProblem> pr(n);
+  std::vector<int> ks(n, 0);
+  GemmBuckets b;
+  for (size_t i = 0; i < n; ++i) {
+    Impl &m = *eng[i];
+    const GroupedItem &it = items[i];
+    const int bn = pick_bn(it.k);
+    TcProblem &q = pr[i];
+    q.A = m.mat(m.Hdense.hi.get(), m.Hdense.lo.get(), m.dim, m.Kd, 128, bk_for(bn));
+    q.B = m.mat(m.Xd.hi.get(), m.Xd.lo.get(), (int64_t)m.Xd.hi.count / m.Kd, m.Kd, bn, bk_for(bn));
+    q.shape.M = m.dim; q.shape.N = it.k; q.shape.K = m.Kd; q.shape.products = g_products;
+    q.shape.ksplit = pick_ksplit(ceil_div(m.dim, 128) * ceil_div(it.k, bn), m.Kd);
+    m.part.resize((size_t)q.shape.ksplit * m.dim * it.k);
+    q.epi.kind = TcEpilogue::STORE_F32;
+    q.epi.rd = m.dim; q.epi.ro2 = 1; q.epi.rlim = m.dim;
+    q.epi.cd = it.k; q.epi.co2 = m.dim; q.epi.clim = it.k;
+    q.epi.so = m.dim * it.k;
+    q.epi.out_f32 = m.part.get();
+    b.add(&q, bn, i);
+  }
+  b.run(err, s, ks);
+  std::vector<ReduceJob> rj(n);
+  for (size_t i = 0; i < n; ++i) {
+    Impl &m = *eng[i];
+    const GroupedItem &it = items[i];
+    ReduceJob &r = rj[i];
+    r.part = m.part.get(); r.M = it.k; r.N = m.dim; r.ksplit = ks[i];
+    r.epi.kind = TcEpilogue::AXPBY_F64;
+    r.epi.rd = it.k; r.epi.ro2 = it.ldy; r.epi.rlim = it.k;
+    r.epi.cd = m.dim; r.epi.co2 = 1; r.epi.clim = m.dim;
+    r.epi.out_f64 = it.Y; r.epi.alpha = 1.0; r.epi.beta = accumulate ? 1.0 : 0.0;
+  }
+  reduce_grouped(rj, s);
+}
+
 void MixedEngine::prepare_grouped(const std::vector<BseOperator *> &ops, int64_t kmax, cudaStream_t s) {
   read_tuning();
   // sizes of every per-operator buffer a grouped product of <= kmax columns touches
@@ -364,9 +587,11 @@ void MixedEngine::prepare_grouped(const std::vector<BseOperator *> &ops, int64_t
       const int64_t ks2 = pick_ksplit(ceil_div(kc * m.ct, 128) * ceil_div(m.vt, pick_bn(m.vt)), m.Kg);
       part = std::max(part, ks2 * kc * m.ct * m.vt);
     }
+    if (m.dense_ready)
+      part = std::max(part, pick_ksplit(ceil_div(m.dim, 128) * ceil_div(kmax, pick_bn(kmax)), m.Kd) * m.dim * kmax);
     q.part = part;
     need.push_back(q);
-    bytes += 4 * (q.xs + q.zs) + 4 * q.part + 4096;
+    bytes += 4 * (q.xs + q.zs + (m.dense_ready ? kmax * m.Kd : 0)) + 4 * q.part + 4096;
   }
   if (need.empty()) return;
   // grow the stream-ordered pool once instead of once per buffer
@@ -377,6 +602,7 @@ void MixedEngine::prepare_grouped(const std::vector<BseOperator *> &ops, int64_t
   }
   for (Need &q : need) {
     if ((int64_t)q.m->Xs.hi.count < q.xs) q.m->Xs.ensure(q.xs / q.m->Kc, q.m->Kc, s);
+    if (q.m->dense_ready) q.m->Xd.ensure(kmax, q.m->Kd, s);
     if ((int64_t)q.m->Zs.hi.count < q.zs) q.m->Zs.ensure(q.zs / q.m->Kn, q.m->Kn, s);
     q.m->part.resize((size_t)q.part);
   }

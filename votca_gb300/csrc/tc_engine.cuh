@@ -18,6 +18,15 @@ class MixedEngine {
   // launch per stage and tile shape; accumulate: Y already holds the Hqp term.
   static void apply_grouped(const Coef &c, const std::vector<GroupedItem> &items, bool accumulate,
                             cudaStream_t s, GroupScratch *scratch);
+  // Dense form for small TDA operators: cx Hx - cd Hd built once with two tensor-core GEMMs
+  // over the aux index into FP64, symmetrised, kept as bf16 hi/lo rows; a product is then one
+  // GEMM.  Hqp stays FP64 beside it (its ~10 eV diagonal would lose digits in a bf16 split).
+  // Needs a diagonal Hqp and Naux <= 1024 (one FP32 chain per element).
+  static void build_dense_grouped(const std::vector<BseOperator *> &ops, const Coef &c, cudaStream_t s);
+  bool dense_ready(const Coef &c) const;
+  // Y (+)= (cx Hx - cd Hd) X with the dense form for every item; accumulate: Y holds Hqp X.
+  static void apply_dense_grouped(const Coef &c, const std::vector<GroupedItem> &items, bool accumulate,
+                                  cudaStream_t s);
   // Allocate, ahead of a series of grouped products of at most kmax columns, every
   // per-operator buffer they use (one pool growth instead of one per buffer).
   static void prepare_grouped(const std::vector<BseOperator *> &ops, int64_t kmax, cudaStream_t s);
