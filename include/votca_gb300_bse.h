@@ -36,7 +36,7 @@ typedef enum bse_status {
   BSE_ERR_CUDA = 3,          /* CUDA runtime error */
   BSE_ERR_TIMEOUT = 4,       /* a bounded device wait gave up */
   BSE_ERR_NUMERICAL = 5,     /* small eigenproblem failed, Gram-Schmidt linear dependence, ... */
-  BSE_ERR_UNSUPPORTED = 6    /* option not available in this build */
+  BSE_ERR_UNSUPPORTED = 6    /* option not supported by this library */
 } bse_status;
 
 typedef enum bse_precision {

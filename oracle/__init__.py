@@ -1,7 +1,8 @@
 """CPU oracle for the BSE hot path (TEST INFRASTRUCTURE ONLY).
 
 Only tests/, __graft_entry__.smoke() and the CPU-baseline leg of bench.py may
-import this package, and only as the checker or the timed CPU reference.  The
+import this package, and only to compare results against or as the timed CPU
+reference.  The
 product package (votca_gb300) never imports it.
 
   bse_oracle.c        restated BSE_OPERATOR loop nest + diagonal + factorised form

@@ -3,8 +3,8 @@
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the shipped library links, loads or
  * calls this file; only the test-suite, the smoke check and the CPU-baseline
- * leg of the benchmark use it, and only as the checker / the timed CPU
- * reference.
+ * leg of the benchmark use it, and only to compare results against or as the
+ * timed CPU reference.
  *
  * This is a plain-C restatement of VOTCA-XTP's CPU code path for
  *   BSE_OPERATOR<cqp,cx,cd,cd2>::matmul      xtp/src/libxtp/gwbse/bse_operator.cc:39-119

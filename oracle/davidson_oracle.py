@@ -1,7 +1,7 @@
 """NumPy restatement of VOTCA-XTP's DavidsonSolver (TEST INFRASTRUCTURE ONLY).
 
 The shipped library never imports this module.  Tests, the smoke check and the
-CPU-baseline leg of the benchmark use it as the checker.
+CPU-baseline leg of the benchmark use it as the reference for comparisons.
 
 Follows, step by step:
   DavidsonSolver::solve (both overloads)     xtp/include/votca/xtp/davidsonsolver.h:64-190

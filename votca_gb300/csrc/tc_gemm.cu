@@ -460,6 +460,9 @@ __device__ __forceinline__ void reduce_range(const float *__restrict__ part, int
     const int64_t i = t / N, n = t % N;
     if ((i % e.rd) >= e.rlim || (n % e.cd) >= e.clim) continue;
     double acc = 0.0;
+    // the same summation order as a plain loop; the unroll lets the independent loads of
+    // eight partials be in flight together (the loop is latency-bound otherwise)
+#pragma unroll 8
     for (int s = 0; s < ksplit; ++s) acc += (double)part[s * total + t];
     // the partial sums are added in FP64; the final value enters the epilogue
     // as FP64 for AXPBY (no extra rounding) and as FP32 for the bf16 split
