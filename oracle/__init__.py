@@ -2,8 +2,7 @@
 
 Only tests/, __graft_entry__.smoke() and the CPU-baseline leg of bench.py may
 import this package, and only to compare results against or as the timed CPU
-reference.  The
-product package (votca_gb300) never imports it.
+reference.  The product package (votca_gb300) never imports it.
 
   bse_oracle.c        restated BSE_OPERATOR loop nest + diagonal + factorised form
                       + HamiltonianOperator product (ctypes-loaded below)
