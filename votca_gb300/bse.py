@@ -4,6 +4,9 @@
   solve_nonhermitian_davidson BSE::Solve_nonhermitian_Davidson, bse.cc:315-360
   full_bse_ranked_guess       BuildFullBSEXRankedInitialGuess,
                               xtp/include/votca/xtp/bse_initialization.h:47-92
+  expectation_value_operator  BSE::ExpectationValue_Operator, bse.cc:500-520
+  analyze_eh_interaction      BSE::Analyze_eh_interaction, bse.cc:551-606 (with
+                              ExchangePrefactor, bse.cc:136-145)
 
 The Davidson iteration itself runs on the GPU (bse_davidson_solve).
 """
@@ -13,7 +16,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from .bse_operator import HamiltonianOperator
+from .bse_operator import HamiltonianOperator, HdOperator, Hd2Operator, HqpOperator, HxOperator
 from .davidson import DavidsonSolver
 
 
@@ -70,3 +73,47 @@ def solve_nonhermitian_davidson(A, B, opt: DavidsonOptions):
     with np.errstate(invalid="ignore", divide="ignore"):
         s = np.sqrt(1.0 / (np.sum(X * X, axis=0) - np.sum(Y * Y, axis=0)))
     return evals, X * s, Y * s, ds
+
+
+def _expval(a, b):
+    return np.sum(a * b, axis=0)
+
+
+def expectation_value_operator(H, X, Y=None):
+    """(direct, cross) of operator H for eigenvectors X (and Y for full BSE): direct = X.HX
+    (+ Y.HY), cross = 2 Y.HX (empty in TDA).  One product per block on the GPU."""
+    X = np.asfortranarray(X, dtype=np.float64)
+    HX = H.matmul(X)
+    direct = _expval(X, HX)
+    if Y is None:
+        return direct, np.zeros(0)
+    Y = np.asfortranarray(Y, dtype=np.float64)
+    direct = direct + _expval(Y, H.matmul(Y))
+    return direct, 2.0 * _expval(Y, HX)
+
+
+def exchange_prefactor(spin):
+    if spin == "singlet":
+        return 2.0
+    if spin == "triplet":
+        return 0.0
+    raise RuntimeError("Unsupported QMStateType in BSE::ExchangePrefactor")
+
+
+def analyze_eh_interaction(ctx, X, Y=None, spin="singlet"):
+    """Composition of the excitation energies (per root): qp_contrib = <Hqp>, direct_contrib =
+    <-Hd> (+ the 2 Y.(-Hd2)X cross term in full BSE), exchange_contrib = eta <Hx> (+ its
+    cross term), eta = 2 for singlets, 0 for triplets.  For normalised eigenpairs the three
+    add up to the excitation energy."""
+    out = {"qp_contrib": expectation_value_operator(HqpOperator(ctx), X, Y)[0]}
+    direct, _ = expectation_value_operator(HdOperator(ctx), X, Y)
+    if Y is not None:
+        direct = direct + expectation_value_operator(Hd2Operator(ctx), X, Y)[1]
+    out["direct_contrib"] = direct
+    xpref = exchange_prefactor(spin)
+    if xpref != 0.0:
+        d, cr = expectation_value_operator(HxOperator(ctx), X, Y)
+        out["exchange_contrib"] = xpref * (d + cr if Y is not None else d)
+    else:
+        out["exchange_contrib"] = np.zeros(direct.size)
+    return out
