@@ -62,6 +62,8 @@ int pick_bn(int64_t N) {
 int64_t g_max_chain = 1024;
 constexpr int64_t kGroupArenaElems = 1LL << 30;  // shared Hd intermediates of a group: 4 GB (hi + lo)
 int g_products = 3;
+int g_kacc = 1;                   // in-CTA K accumulation for N <= 64 stages with enough tiles
+int64_t g_s_budget = 10LL << 30;  // bytes of Hd/Hd2 intermediate per vector chunk
 int pick_ksplit(int64_t tiles, int64_t K) {
   const int64_t target = 2LL * sm_count();
   int64_t ks = 1;
@@ -75,6 +77,8 @@ void read_tuning() {
     if (const char *e = getenv("VGB_TC_MAX_CHAIN")) g_max_chain = std::max(64LL, atoll(e));
     if (const char *e = getenv("VGB_TC_PRODUCTS")) g_products = atoi(e) == 4 ? 4 : 3;
     if (const char *e = getenv("VGB_TC_BK256")) g_bk256 = atoi(e) == 64 ? 64 : 32;
+    if (const char *e = getenv("VGB_TC_KACC")) g_kacc = atoi(e) != 0;
+    if (const char *e = getenv("VGB_TC_S_BUDGET_GB")) g_s_budget = std::max(1LL, atoll(e)) << 30;
   });
 }
 
@@ -87,7 +91,6 @@ struct MixedEngine::Impl {
   SplitBuf Xs, S, U, Zs;
   DeviceBuffer<float> part;
   DeviceBuffer<int> err;
-  int64_t s_budget_bytes = 4LL << 30;
   // dense form (small operators in batches): H(coef) as bf16 hi/lo rows [I][Kd], Kd = pad64(dim)
   SplitBuf Hdense, Xd;  // Xd [j][Kd]: its own buffer, the K padding of Xs must stay zero
   int64_t Kd = 0;
@@ -230,7 +233,7 @@ void MixedEngine::apply(BseOperator &op, const Coef &c, const double *X, int64_t
     op.timer.begin(hd ? STAGE_TC_HD : STAGE_TC_HD2, s);
     // vectors per chunk so that the intermediate stays within the budget
     const int64_t per_vec = (hd ? ct : vt) * m.Kg * 4;
-    const int64_t jc = std::max<int64_t>(1, std::min<int64_t>(k, m.s_budget_bytes / per_vec));
+    const int64_t jc = std::max<int64_t>(1, std::min<int64_t>(k, g_s_budget / per_vec));
     SplitBuf &T = hd ? m.S : m.U;
     T.ensure(jc * (hd ? ct : vt), m.Kg, s);
     for (int64_t j0 = 0; j0 < k; j0 += jc) {
@@ -259,6 +262,21 @@ void MixedEngine::apply(BseOperator &op, const Coef &c, const double *X, int64_t
         TcShape s2;
         s2.M = kc * ct; s2.N = vt; s2.K = m.Kg; s2.products = g_products;
         s2.ksplit = pick_ksplit(ceil_div(kc * ct, 128) * ceil_div(vt, bn2), m.Kg);
+        const int64_t tiles2 = ceil_div(s2.M, 128) * ceil_div(s2.N, bn2);
+        if (g_kacc && bn2 <= 64 && s2.ksplit > 1 && tiles2 * 4 >= 3 * sm_count()) {
+          // enough tiles to keep the SMs busy: each CTA sums the K splits of its tile in FP64
+          // and writes Y directly (no partials, no reduction launch; same numbers)
+          s2.kacc = true;
+          TcEpilogue r;
+          r.kind = TcEpilogue::AXPBY_F64;
+          r.rd = ct; r.ro1 = ldy; r.ro2 = 1; r.rlim = ct;
+          r.cd = vt; r.co2 = ct; r.clim = vt;
+          r.out_f64 = Y + j0 * ldy; r.alpha = alpha; r.beta = acc ? 1.0 : 0.0;
+          tc_gemm(As, Bg, s2, r, bn2, err, s);
+          op.timer.end(STAGE_TC_HD_B, s);
+          if (j0 + jc < k) op.timer.begin(STAGE_TC_HD, s);
+          continue;
+        }
         m.part.resize((size_t)s2.ksplit * s2.M * s2.N);
         // partials column-major [split][v1][(j, c1)] (coalesced epilogue stores)
         TcEpilogue p;
@@ -705,7 +723,7 @@ void MixedEngine::apply_grouped(const Coef &c, const std::vector<GroupedItem> &i
     for (size_t i = 0; i < n; ++i) {
       Impl &m = *eng[i];
       const int64_t per_vec = m.ct * m.Kg * 4;
-      jc[i] = std::max<int64_t>(1, std::min<int64_t>(items[i].k, m.s_budget_bytes / per_vec));
+      jc[i] = std::max<int64_t>(1, std::min<int64_t>(items[i].k, (4LL << 30) / per_vec));
       need[i] = jc[i] * m.ct * m.Kg;  // elements (a multiple of 64: regions stay 128-byte aligned)
       total += need[i];
       largest = std::max(largest, need[i]);

@@ -35,6 +35,7 @@ struct KParams {
   int products;  // 3: hi.hi + hi.lo + lo.hi;  4: + lo.lo
   int64_t nbatch, a_brows, b_brows;
   int ksplit, kc_per;
+  int kacc;  // 1: one CTA runs all K splits of a tile and sums them in FP64 registers
   int64_t mt, nt, ntiles;
   TcEpilogue epi;
   int *err;
@@ -138,11 +139,28 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// Next job of a CTA: the rest of the current run of `run` jobs, then the run gridDim.x
+// items further on.
+__device__ __forceinline__ int64_t next_job(int64_t t, int64_t &u, int64_t run) {
+  if (++u < run) return t + 1;
+  u = 0;
+  return t + 1 + (int64_t)(gridDim.x - 1) * run;
+}
+
 struct TileCoord {
   int64_t m, n, s, b;
 };
 __device__ __forceinline__ TileCoord decode(const KParams &p, int64_t t) {
   TileCoord c;
+  if (p.kacc) {  // the K splits of a tile are consecutive jobs of one CTA
+    c.s = t % p.ksplit;
+    t /= p.ksplit;
+    c.m = t % p.mt;
+    t /= p.mt;
+    c.n = t % p.nt;
+    c.b = t / p.nt;
+    return c;
+  }
   c.m = t % p.mt;
   t /= p.mt;
   c.n = t % p.nt;
@@ -183,6 +201,8 @@ struct SingleSrc {
   __device__ __forceinline__ const KParams &params(int) const { return p; }
   __device__ __forceinline__ const CUtensorMap *map(int, int w) const { return &maps[w]; }
   __device__ __forceinline__ int *err() const { return p.err; }
+  // jobs run by a CTA in runs of run() consecutive indices (all K splits of a tile when kacc)
+  __device__ __forceinline__ int64_t run() const { return p.kacc ? p.ksplit : 1; }
 };
 
 constexpr int kGroupMax = 32;
@@ -202,6 +222,7 @@ struct GroupSrc {
   __device__ __forceinline__ const KParams &params(int i) const { return p[i]; }
   __device__ __forceinline__ const CUtensorMap *map(int i, int w) const { return &maps[4 * i + w]; }
   __device__ __forceinline__ int *err() const { return err_ptr; }
+  __device__ __forceinline__ int64_t run() const { return 1; }
 };
 static_assert(sizeof(GroupSrc) <= 32000, "grouped GEMM parameters exceed the kernel parameter space");
 
@@ -242,6 +263,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
   const uint32_t tmem_base = *tmem_slot;
   int *const err = src.err();
   const int64_t ntiles = src.total();
+  const int64_t run = src.run();  // job t = item * run + u, u < run, items strided over CTAs
 
   if (warp == 0) {
     if (lane == 0) {
@@ -249,7 +271,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
       int stage = 0;
       uint32_t phase = 0;
       int hint = 0;
-      for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+      for (int64_t t = blockIdx.x * run, u = 0; t < ntiles; t = next_job(t, u, run)) {
         int64_t lt;
         const int pi = src.locate(t, lt, hint);
         const KParams p = src.params(pi);  // registers: no reloads behind the stores
@@ -290,7 +312,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
       int buf = 0;
       uint32_t aphase = 0;
       int hint = 0;
-      for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+      for (int64_t t = blockIdx.x * run, u = 0; t < ntiles; t = next_job(t, u, run)) {
         int64_t lt;
         const KParams p = src.params(src.locate(t, lt, hint));
         const TileCoord tc = decode(p, lt);
@@ -336,10 +358,13 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
     constexpr int COLS = BN >= 64 ? BN / 2 : BN;
     const int cbeg = (BN >= 64 || half == 0) ? half * COLS : BN;
     const int cend = (BN >= 64 || half == 0) ? cbeg + COLS : BN;
+    // FP64 sums over the K splits of a tile (kacc; BN <= 64: at most 32 columns per thread)
+    constexpr int KACC = BN <= 64 ? 32 : 1;
+    double kv[KACC];
     int buf = 0;
     uint32_t aphase = 0;
     int hint = 0;
-    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    for (int64_t t = blockIdx.x * run, u = 0; t < ntiles; t = next_job(t, u, run)) {
       int64_t lt;
       // a register copy: the stores below cannot alias it, so nothing is reloaded per element
       const KParams p = src.params(src.locate(t, lt, hint));
@@ -349,7 +374,44 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
       fence_after();
       const int64_t i = tc.m * BM + q * 32 + lane;
       const bool row_ok = i < p.M && (i % e.rd) < e.rlim;
-      const int64_t rbase = (i / e.rd) * e.ro1 + (i % e.rd) * e.ro2 + tc.b * e.bo + tc.s * e.so;
+      const int64_t rbase = (i / e.rd) * e.ro1 + (i % e.rd) * e.ro2 + tc.b * e.bo +
+                            (p.kacc ? 0 : tc.s * e.so);
+      if constexpr (BN <= 64) {
+        if (p.kacc) {
+          // this thread's 32 columns (cbeg == cend for the idle half of a BN = 32 tile)
+          if (cbeg < cend) {
+            uint32_t r[32];
+            tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + cbeg), r);
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+              kv[j] = (tc.s == 0 ? 0.0 : kv[j]) + (double)__uint_as_float(r[j]);
+            if (row_ok && tc.s == p.ksplit - 1) {
+              // the K splits summed in FP64 in split order, as the reduction kernel does
+              int64_t n = tc.n * BN + cbeg, nq = n / e.cd, nr = n % e.cd;
+#pragma unroll
+              for (int j = 0; j < 32; ++j) {
+                if (n < p.N && nr < e.clim) {
+                  const int64_t off = rbase + nq * e.co1 + nr * e.co2;
+                  if (e.kind == TcEpilogue::AXPBY_F64) {
+                    double *y = e.out_f64 + off;
+                    const double rv = e.alpha * kv[j];
+                    *y = (e.beta == 0.0) ? rv : fma(e.beta, *y, rv);
+                  } else {
+                    epi_store(e, off, (float)kv[j]);
+                  }
+                }
+                ++n;
+                if (++nr == e.cd) { nr = 0; ++nq; }
+              }
+            }
+          }
+          fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&acce[buf]);
+          if (++buf == 2) { buf = 0; aphase ^= 1; }
+          continue;
+        }
+      }
 #pragma unroll 1
       for (int c0 = cbeg; c0 < cend; c0 += 32) {
         uint32_t r[32];
@@ -606,7 +668,11 @@ KParams make_params(const TcMat &A, const TcMat &B, const TcShape &sh, const TcE
   int ks = std::max(1, std::min(sh.ksplit, kchunks));
   p.kc_per = (int)ceil_div(kchunks, ks);
   p.ksplit = (int)ceil_div(kchunks, p.kc_per);
-  VGB_REQUIRE(p.ksplit == 1 || epi.kind == TcEpilogue::STORE_F32, "tc_gemm: K split needs F32 partials");
+  p.kacc = (sh.kacc && p.ksplit > 1) ? 1 : 0;
+  VGB_REQUIRE(!p.kacc || (bn <= 64 && epi.kind != TcEpilogue::STORE_F32),
+              "tc_gemm: in-CTA K accumulation needs BN <= 64 and a final (split or FP64) epilogue");
+  VGB_REQUIRE(p.ksplit == 1 || p.kacc || epi.kind == TcEpilogue::STORE_F32,
+              "tc_gemm: K split needs F32 partials or in-CTA accumulation");
   p.mt = ceil_div(sh.M, BM);
   p.nt = ceil_div(sh.N, bn);
   p.ntiles = p.mt * p.nt * p.ksplit * sh.nbatch;
@@ -642,6 +708,7 @@ void tc_gemm_grouped(const std::vector<const TcProblem *> &probs, int bn, int *e
     int64_t total = 0;
     for (; i < probs.size() && src->n < kGroupMax; ++i) {
       const TcProblem &q = *probs[i];
+      VGB_REQUIRE(!q.shape.kacc, "tc_gemm_grouped: in-CTA K accumulation is not grouped");
       const KParams p = make_params(q.A, q.B, q.shape, q.epi, bn, err);
       if (ksplit_out) ksplit_out[i] = p.ksplit;
       if (p.ntiles == 0) continue;

@@ -54,6 +54,9 @@ struct TcShape {
   int64_t a_batch_rows = 0, b_batch_rows = 0;  // row offset of A / B per batch
   int ksplit = 1;                              // K split into ksplit ranges (STORE_F32 partials)
   int products = 3;                            // 3 (BF16x3) or 4 (adds A_lo B_lo)
+  // with ksplit > 1 and BN <= 64: one CTA runs all splits of a tile and sums them in FP64
+  // registers (in split order) before the epilogue map; no partials, no reduction launch
+  bool kacc = false;
 };
 
 // Launch the persistent GEMM; bn in {32, 64, 128, 256}.  err: device int set
