@@ -112,6 +112,14 @@ int bse_rpa_epsilon(const bse_mmn_desc *mmn, const double *const *mmn_slices,
 int bse_cholesky_inverse(int64_t n, const double *A, int64_t lda, double *Ainv,
                          int64_t ldi);
 
+/* The screening of BSE::SetupDirectInteractionOperator (xtp/src/libxtp/gwbse/bse.cc:188-204)
+ * as one dense matrix for any symmetric A (e.g. eps at a frequency beyond the first RPA
+ * pole, where the Cholesky factorisation fails): A = U diag(lambda) U^T, W = U diag(w) U^T with
+ * w = 1/lambda for lambda > cutoff (the reference uses 1e-8) and 0 otherwise.  The eigenproblem
+ * is solved on the host, as in the reference; W is formed on the device. */
+int bse_positive_inverse(int64_t n, const double *A, int64_t lda, double cutoff, double *W,
+                         int64_t ldw);
+
 /* TCMatrix_gwbse::MultiplyRightWithAuxMatrix (xtp/src/libxtp/threecenter.cc:54-65):
  * every slice M[m] <- M[m] * U (U auxsize x auxsize), in place on the host slices. */
 int bse_mmn_multiply_right(const bse_mmn_desc *mmn, double *const *mmn_slices,

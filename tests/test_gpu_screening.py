@@ -68,6 +68,24 @@ def test_cholesky_rejects_indefinite():
     assert rc == 5 and b"positive definite" in L.bse_last_error()
 
 
+def test_positive_inverse_drops_small_and_negative_modes():
+    """The reference's screening for any symmetric eps: modes with lambda <= 1e-8 dropped."""
+    from votca_gb300.screening import positive_inverse
+
+    rng = np.random.default_rng(7)
+    Q, _ = np.linalg.qr(rng.standard_normal((50, 50)))
+    # kept modes well above the cutoff and dropped modes well below it (an eigenvalue next to
+    # the cutoff would make 1/lambda depend on rounding)
+    lam = np.concatenate([np.linspace(0.5, 4.0, 45), [-0.3, -1e-3, 0.0, 1e-10, -1e-10]])
+    A = (Q * lam) @ Q.T
+    A = 0.5 * (A + A.T)
+    W = positive_inverse(A, 1e-8)
+    lam_n, U = np.linalg.eigh(A)
+    w = np.where(lam_n > 1e-8, 1.0 / np.where(lam_n > 1e-8, lam_n, 1.0), 0.0)
+    assert np.allclose(W, (U * w) @ U.T, rtol=1e-10, atol=1e-12)
+    assert np.linalg.matrix_rank(W, tol=1e-8) == 45
+
+
 def test_multiply_right_with_aux_matrix():
     from votca_gb300 import _lib
 

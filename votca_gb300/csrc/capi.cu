@@ -357,6 +357,14 @@ int bse_cholesky_inverse(int64_t n, const double *A, int64_t lda, double *Ainv, 
   });
 }
 
+int bse_positive_inverse(int64_t n, const double *A, int64_t lda, double cutoff, double *W, int64_t ldw) {
+  return guarded([&] {
+    VGB_REQUIRE(A && W, "bse_positive_inverse: null matrix");
+    TmpStream ts;
+    vgb::positive_inverse(n, A, lda, cutoff, W, ldw, ts.s);
+  });
+}
+
 int bse_mmn_multiply_right(const bse_mmn_desc *mmn, double *const *mmn_slices, const double *U,
                            int64_t ldu) {
   return guarded([&] {

@@ -101,6 +101,8 @@ void rpa_epsilon(const bse_mmn_desc &desc, const double *const *slices, const do
                  double eta, double *eps_host, cudaStream_t s);
 void cholesky_inverse(int64_t n, const double *a_host, int64_t lda, double *inv_host, int64_t ldi,
                       cudaStream_t s);
+void positive_inverse(int64_t n, const double *a_host, int64_t lda, double cutoff, double *inv_host,
+                      int64_t ldi, cudaStream_t s);
 void mmn_multiply_right(const bse_mmn_desc &desc, double *const *slices, const double *U_host,
                         int64_t ldu, cudaStream_t s);
 

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "dgemm.cuh"
+#include "host_eig.hpp"
 
 namespace vgb {
 
@@ -259,6 +260,38 @@ void mmn_multiply_right(const bse_mmn_desc &desc, double *const *slices, const d
                                cudaMemcpyDeviceToHost, s));
     VGB_CUDA(cudaStreamSynchronize(s));
   }
+}
+
+// W = U diag(w) U^T with A = U diag(lambda) U^T and w = 1/lambda for lambda > cutoff, else 0:
+// the screening of BSE::SetupDirectInteractionOperator (bse.cc:188-204: eigen-decomposition of
+// eps, modes with lambda <= 1e-8 dropped) as one dense matrix.  The symmetric eigenproblem is
+// solved on the host (as the reference does), the product U diag(w) U^T on the device.
+void positive_inverse(int64_t n, const double *a_host, int64_t lda, double cutoff, double *inv_host,
+                      int64_t ldi, cudaStream_t s) {
+  VGB_REQUIRE(n >= 1 && lda >= n && ldi >= n, "positive_inverse: bad size");
+  std::vector<double> A(n * n);
+  for (int64_t j = 0; j < n; ++j)
+    for (int64_t i = 0; i < n; ++i) A[i + n * j] = a_host[i + lda * j];
+  std::vector<double> lam, U;
+  if (!sym_eig(n, A.data(), lam, U)) fail(BSE_ERR_NUMERICAL, "positive_inverse: eigenvalue problem failed");
+  std::vector<double> UW(n * n);
+  for (int64_t j = 0; j < n; ++j) {
+    const double w = lam[j] > cutoff ? 1.0 / lam[j] : 0.0;
+    for (int64_t i = 0; i < n; ++i) UW[i + n * j] = U[i + n * j] * w;
+  }
+  DeviceBuffer<double> dU(n * n), dUW(n * n), dW(n * n);
+  VGB_CUDA(cudaMemcpyAsync(dU.get(), U.data(), n * n * sizeof(double), cudaMemcpyHostToDevice, s));
+  VGB_CUDA(cudaMemcpyAsync(dUW.get(), UW.data(), n * n * sizeof(double), cudaMemcpyHostToDevice, s));
+  GemmDesc g;  // W = (U diag(w)) U^T
+  g.M = n; g.N = n; g.K = n;
+  g.A = dUW.get(); g.a_rs = 1; g.a_cs = n;
+  g.B = dU.get(); g.b_rs = n; g.b_cs = 1;
+  g.C = dW.get(); g.c_rs = 1; g.c_cs = n;
+  GemmWorkspace ws;
+  dgemm(g, s, &ws);
+  VGB_CUDA(cudaMemcpy2DAsync(inv_host, ldi * sizeof(double), dW.get(), n * sizeof(double), n * sizeof(double), n,
+                             cudaMemcpyDeviceToHost, s));
+  VGB_CUDA(cudaStreamSynchronize(s));
 }
 
 }  // namespace vgb

@@ -1,0 +1,118 @@
+"""Screening that feeds the direct term, and the perturbative dynamical screening of
+the excitation energies, on the GPU.
+
+  rpa_epsilon                  RPA::calculate_epsilon_r (xtp/src/libxtp/gwbse/rpa.cc),
+                               bse_rpa_epsilon
+  cholesky_inverse             the inverse of a symmetric positive definite matrix,
+                               bse_cholesky_inverse (blocked Cholesky on the device)
+  positive_inverse             U diag(1/lambda, lambda > cutoff) U^T, bse_positive_inverse
+  screened_context             BSE::SetupDirectInteractionOperator (bse.cc:188-204) in the
+                               dense form: W = eps(omega)^-1 folded into the operator
+  perturbative_dynamical_screening
+                               BSE::Perturbative_DynamicalScreening (bse.cc:610-681)
+
+The reference diagonalises eps, rotates Mmn by its eigenvectors and weights the rotated
+aux functions by 1/lambda (lambda > 1e-8).  With all eigenvalues above that cutoff this is
+the same operator as sum_PQ M^P (eps^-1)_PQ M^Q, which is what the dense form computes (by
+a Cholesky inverse on the device).  When eps(omega) is not positive definite (omega beyond
+the first RPA pole) the modes with lambda <= 1e-8 are dropped as in the reference
+(positive_inverse).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .bse_operator import GpuBSEContext, HdOperator, Hd2Operator, TCMatrix_gwbse, _p
+from .bse import expectation_value_operator
+
+
+def _desc_ptrs(Mmn: TCMatrix_gwbse):
+    d = Mmn.data
+    desc = _lib.bse_mmn_desc(Mmn.auxsize(), Mmn.get_mmin(), Mmn.get_mmax(), Mmn.get_nmin(), Mmn.get_nmax())
+    ptrs = (_lib.c_dp * Mmn.msize())(*[ctypes.cast(d.ctypes.data + m * d.strides[0], _lib.c_dp)
+                                       for m in range(Mmn.msize())])
+    return desc, ptrs
+
+
+def rpa_epsilon(Mmn: TCMatrix_gwbse, rpa_energies, homo, rpamin, rpamax, frequency=0.0):
+    """eps(omega) (auxsize x auxsize) of the RPA on the levels rpamin..rpamax."""
+    L = _lib.load()
+    e = np.ascontiguousarray(rpa_energies, dtype=np.float64)
+    naux = Mmn.auxsize()
+    eps = np.zeros((naux, naux), order="F")
+    desc, ptrs = _desc_ptrs(Mmn)
+    w = complex(frequency)
+    _lib.check(L.bse_rpa_epsilon(ctypes.byref(desc), ptrs, _p(e), e.size, homo, rpamin, rpamax, w.real, w.imag,
+                                 _p(eps)))
+    return eps
+
+
+def cholesky_inverse(A):
+    L = _lib.load()
+    A = np.asfortranarray(A, dtype=np.float64)
+    n = A.shape[0]
+    Ai = np.zeros((n, n), order="F")
+    _lib.check(L.bse_cholesky_inverse(n, _p(A), n, _p(Ai), n))
+    return Ai
+
+
+def positive_inverse(A, cutoff=1e-8):
+    """U diag(w) U^T with w = 1/lambda for eigenvalues lambda > cutoff, else 0."""
+    L = _lib.load()
+    A = np.asfortranarray(A, dtype=np.float64)
+    n = A.shape[0]
+    W = np.zeros((n, n), order="F")
+    _lib.check(L.bse_positive_inverse(n, _p(A), n, cutoff, _p(W), n))
+    return W
+
+
+def screened_context(Mmn, Hqp, opt, rpa_energies, rpa_window, frequency=0.0, precision=0):
+    """Operator context with the direct term screened as SetupDirectInteractionOperator
+    screens it at `frequency`: eps^-1 by Cholesky when eps is positive definite, else the
+    eigenmodes with lambda > 1e-8 only (the reference's cutoff)."""
+    homo, rpamin, rpamax = rpa_window
+    eps = rpa_epsilon(Mmn, rpa_energies, homo, rpamin, rpamax, frequency)
+    try:
+        W = cholesky_inverse(eps)
+    except _lib.BSEError as e:
+        if e.code != 5:  # BSE_ERR_NUMERICAL: not positive definite
+            raise
+        W = positive_inverse(eps, 1e-8)
+    return GpuBSEContext(None, Mmn, Hqp, opt, precision=precision, dense_screening=W)
+
+
+def _direct(ctx, X, Y):
+    direct, _ = expectation_value_operator(HdOperator(ctx), X, Y)
+    if Y is not None:
+        direct = direct + expectation_value_operator(Hd2Operator(ctx), X, Y)[1]
+    return direct
+
+
+def perturbative_dynamical_screening(Mmn, Hqp, opt, rpa_energies, rpa_window, energies, X, Y=None,
+                                     max_iter=10, tolerance=1e-5, precision=0):
+    """Excitation energies with the direct term screened at the excitation's own energy,
+    to first order around the static solution (energies, X[, Y]) of the same operator:
+    Omega_i <- Omega_i + <-Hd(0)>_i - <-Hd(Omega_i')>_i, iterated on Omega_i' until two
+    successive values differ by less than `tolerance` or `max_iter` rounds are done."""
+    energies = np.asarray(energies, dtype=np.float64)
+    X = np.asfortranarray(X, dtype=np.float64)
+    Y = None if Y is None else np.asfortranarray(Y, dtype=np.float64)
+    static = screened_context(Mmn, Hqp, opt, rpa_energies, rpa_window, 0.0, precision)
+    hd_static = _direct(static, X, Y)
+    static.close()
+    dynamic = energies.copy()
+    for i in range(energies.size):
+        xi = X[:, i:i + 1]
+        yi = None if Y is None else Y[:, i:i + 1]
+        for _ in range(max_iter):
+            old = dynamic[i]
+            ctx = screened_context(Mmn, Hqp, opt, rpa_energies, rpa_window, old, precision)
+            hd_dyn = _direct(ctx, xi, yi)[0]
+            ctx.close()
+            dynamic[i] = energies[i] + hd_static[i] - hd_dyn
+            if abs(dynamic[i] - old) < tolerance:
+                break
+    return dynamic
