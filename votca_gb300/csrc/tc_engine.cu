@@ -233,7 +233,10 @@ void MixedEngine::apply(BseOperator &op, const Coef &c, const double *X, int64_t
     op.timer.begin(hd ? STAGE_TC_HD : STAGE_TC_HD2, s);
     // vectors per chunk so that the intermediate stays within the budget
     const int64_t per_vec = (hd ? ct : vt) * m.Kg * 4;
-    const int64_t jc = std::max<int64_t>(1, std::min<int64_t>(k, g_s_budget / per_vec));
+    int64_t jmax = std::max<int64_t>(1, std::min<int64_t>(k, g_s_budget / per_vec));
+    // Hd stage 2 runs one tile per CTA (in-CTA K accumulation): at most one wave of tiles
+    if (hd && g_kacc) jmax = std::max<int64_t>(1, std::min<int64_t>(jmax, sm_count() * 128 / ct));
+    const int64_t jc = ceil_div(k, ceil_div(k, jmax));  // equal chunks: no small remainder pass
     SplitBuf &T = hd ? m.S : m.U;
     T.ensure(jc * (hd ? ct : vt), m.Kg, s);
     for (int64_t j0 = 0; j0 < k; j0 += jc) {
@@ -263,7 +266,7 @@ void MixedEngine::apply(BseOperator &op, const Coef &c, const double *X, int64_t
         s2.M = kc * ct; s2.N = vt; s2.K = m.Kg; s2.products = g_products;
         s2.ksplit = pick_ksplit(ceil_div(kc * ct, 128) * ceil_div(vt, bn2), m.Kg);
         const int64_t tiles2 = ceil_div(s2.M, 128) * ceil_div(s2.N, bn2);
-        if (g_kacc && bn2 <= 64 && s2.ksplit > 1 && tiles2 * 4 >= 3 * sm_count()) {
+        if (g_kacc && bn2 <= 64 && s2.ksplit > 1 && tiles2 * 2 >= sm_count()) {
           // enough tiles to keep the SMs busy: each CTA sums the K splits of its tile in FP64
           // and writes Y directly (no partials, no reduction launch; same numbers)
           s2.kacc = true;
