@@ -424,6 +424,25 @@ void host_parallel(size_t count, F f) {
   if (first) std::rethrow_exception(first);
 }
 
+// Page-locked staging of the packed transfers, kept per host thread across solves
+// (allocating page-locked memory costs milliseconds).
+double *pinned_scratch(size_t doubles) {
+  struct Buf {
+    double *p = nullptr;
+    size_t cap = 0;
+    ~Buf() { if (p) cudaFreeHost(p); }
+  };
+  static thread_local Buf buf;
+  if (buf.cap < doubles) {
+    if (buf.p) cudaFreeHost(buf.p);
+    buf.p = nullptr;
+    buf.cap = 0;
+    VGB_CUDA(cudaMallocHost(&buf.p, doubles * sizeof(double)));
+    buf.cap = doubles;
+  }
+  return buf.p;
+}
+
 }  // namespace
 
 void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coef, int64_t neigen,
@@ -470,9 +489,7 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
   AllocStreamScope scope(s);
   DeviceBuffer<double> pool(pool_doubles);
   DeviceBuffer<double> din(in_doubles), dout(out_doubles);
-  double *hbuf = nullptr;
-  VGB_CUDA(cudaMallocHost(&hbuf, (in_doubles + out_doubles) * sizeof(double)));
-  struct HostFree { double *p; ~HostFree() { cudaFreeHost(p); } } hfree{hbuf};
+  double *hbuf = pinned_scratch((size_t)(in_doubles + out_doubles));
   double *hin = hbuf, *hout = hbuf + in_doubles;
   VGB_CUDA(cudaMemsetAsync(pool.get(), 0, pool_doubles * sizeof(double), s));
   {
@@ -530,15 +547,19 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
   VGB_CUDA(cudaStreamSynchronize(s));
   {
     std::vector<UnitJob> uj;
-    for (Mol &M : mols) {
+    host_parallel(mols.size(), [&](size_t b) {
+      Mol &M = mols[b];
       std::vector<int64_t> idx(M.n);
       std::iota(idx.begin(), idx.end(), 0);
       const double *Dh = hout + M.off_out;
-      std::stable_sort(idx.begin(), idx.end(), [&](int64_t a, int64_t c) { return Dh[a] < Dh[c]; });
+      // the first ncols of a stable argsort of the diagonal (ties by index)
+      std::partial_sort(idx.begin(), idx.begin() + M.ncols, idx.end(), [&](int64_t a, int64_t c) {
+        return Dh[a] < Dh[c] || (Dh[a] == Dh[c] && a < c);
+      });
       // stage the row list in the H2D buffer (as doubles holding exact small integers)
       double *dst = hin + M.off_in;
       for (int64_t j = 0; j < M.ncols; ++j) dst[j] = (double)idx[j];
-    }
+    });
     VGB_CUDA(cudaMemcpyAsync(din.get(), hin, in_doubles * sizeof(double), cudaMemcpyHostToDevice, s));
     for (Mol &M : mols) {
       UnitJob u;

@@ -24,6 +24,8 @@
 
 #include "tc_gemm.cuh"
 
+#include <cuda_bf16.h>
+
 namespace vgb {
 
 namespace {
@@ -373,6 +375,32 @@ struct GemmBuckets {
 
 namespace {
 
+// Bc[(c1, c)][P] = split(M(c1, c, P)) from Mcc[P][c][c1] (= the [P][q] matrix, q = c ct + c1):
+// a 32 x 32 tiled transpose through shared memory, so that reads run along q and writes
+// along P.
+__global__ void transpose_split_cc_kernel(const double *__restrict__ Mcc, int64_t naux, int64_t ct,
+                                          uint16_t *__restrict__ hi, uint16_t *__restrict__ lo, int64_t ldo) {
+  __shared__ double tile[32][33];
+  const int64_t q0 = (int64_t)blockIdx.x * 32, p0 = (int64_t)blockIdx.y * 32;
+  const int64_t nq = ct * ct;
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int64_t P = p0 + r, q = q0 + threadIdx.x;
+    tile[r][threadIdx.x] = (P < naux && q < nq) ? Mcc[P * nq + q] : 0.0;
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int64_t q = q0 + r, P = p0 + threadIdx.x;
+    if (q >= nq || P >= naux) continue;
+    const int64_t c = q / ct, c1 = q % ct;
+    const double v = tile[threadIdx.x][r];
+    const __nv_bfloat16 h = __double2bfloat16(v);
+    const __nv_bfloat16 l = __double2bfloat16(v - (double)__bfloat162float(h));
+    const int64_t off = (c1 * ct + c) * ldo + P;
+    hi[off] = __bfloat16_as_ushort(h);
+    lo[off] = __bfloat16_as_ushort(l);
+  }
+}
+
 // H = (H + H^T) / 2: the two halves of the split products round differently (A_hi B_lo
 // against A_lo B_hi), and a nonsymmetric operator leaves a floor on the Davidson residual.
 __global__ void symmetrize_kernel(double *H, int64_t n) {
@@ -408,6 +436,14 @@ void MixedEngine::build_dense_grouped(const std::vector<BseOperator *> &ops, con
   int *err = todo.empty() ? nullptr : todo[0]->mixed->impl_->err.get();
   // slices of operators whose FP64 temporaries (H and the two K = Naux splits) fit 8 GB
   const int64_t budget = 8LL << 30;
+  if (!todo.empty() && alloc_stream()) {
+    // grow the stream-ordered pool once: the kept dense forms plus one slice of temporaries
+    int64_t bytes = budget + (1LL << 20);
+    for (BseOperator *op : todo) bytes += op->dim * pad64(op->dim) * 4 + 4096;
+    void *p = nullptr;
+    if (cudaMallocAsync(&p, (size_t)bytes, s) == cudaSuccess) VGB_CUDA(cudaFreeAsync(p, s));
+    else cudaGetLastError();  // no headroom for one block: allocated piece by piece
+  }
   size_t a = 0;
   while (a < todo.size()) {
     size_t b = a;
@@ -446,12 +482,11 @@ void MixedEngine::build_dense_grouped(const std::vector<BseOperator *> &ops, con
       j1.map.rdiv = op.vt; j1.map.rs1 = op.naux * op.vt; j1.map.rs2 = 1; j1.map.cs = op.vt; j1.map.rlim = op.vt;
       j1.hi = Av.hi.get() + aoff[q]; j1.lo = Av.lo.get() + aoff[q]; j1.ldo = m.Kn;
       sj.push_back(j1);
-      // Bc[(c1, c)][P] = M(c1, c, P) = Mcc[P][c][c1]
-      SplitJob j2;
-      j2.x = op.Mcc.get(); j2.rows = op.ct * op.ct; j2.cols = op.naux;
-      j2.map.rdiv = op.ct; j2.map.rs1 = 1; j2.map.rs2 = op.ct; j2.map.cs = op.ct * op.ct; j2.map.rlim = op.ct;
-      j2.hi = Bc.hi.get() + boff[q]; j2.lo = Bc.lo.get() + boff[q]; j2.ldo = m.Kn;
-      sj.push_back(j2);
+      // Bc[(c1, c)][P] = M(c1, c, P) = Mcc[P][c][c1]: a transpose, done through shared memory
+      const dim3 grid((unsigned)ceil_div(op.ct * op.ct, 32), (unsigned)ceil_div(op.naux, 32));
+      transpose_split_cc_kernel<<<grid, dim3(32, 8), 0, s>>>(op.Mcc.get(), op.naux, op.ct, Bc.hi.get() + boff[q],
+                                                            Bc.lo.get() + boff[q], m.Kn);
+      VGB_LAUNCH_CHECK();
     }
     split_grouped(sj, s);
     std::vector<int> ks(b - a, 0);
