@@ -208,7 +208,7 @@ struct GsJob {
   int check;
   int *flag;
 };
-__global__ void __launch_bounds__(kThreads) gs_kernel(const __grid_constant__ Group<GsJob> g) {
+__global__ void __launch_bounds__(kThreads, 2) gs_kernel(const __grid_constant__ Group<GsJob> g) {
   const GsJob q = g.j[blockIdx.x];
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   constexpr int kMaxRange = 256;
