@@ -595,7 +595,7 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
         const int64_t old = (it == 0) ? 0 : M->nav, nvec = M->ncols - old;
         GroupedItem gi;
         gi.op = M->op; gi.X = M->V + old * M->n; gi.ldx = M->n; gi.k = nvec;
-        gi.Y = M->AV + old * M->n; gi.ldy = M->n; gi.dense = M->dense;
+        gi.Y = M->AV + old * M->n; gi.ldy = M->n; gi.dense = M->dense; gi.diag = M->D;
         items.push_back(gi);
         tn.push_back({M, M->V, M->AV + old * M->n, M->ncols, nvec, M->cbuf, M->ncols});
       }

@@ -93,6 +93,7 @@ __global__ void hqp_diag_kernel(double cqp, const double *__restrict__ Hcc,
 struct HqpJob {
   double cqp;
   const double *Hcc, *Hvv;
+  const double *diag;  // if set: Y = diag o X (the full diagonal), Hcc/Hvv unused
   int64_t vt, ct;
   const double *X;
   int64_t ldx, k;
@@ -114,8 +115,8 @@ __global__ void hqp_diag_group_kernel(const __grid_constant__ HqpGroup g) {
        t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t I = t % dim, j = t / dim;
     const int64_t v = I / q.ct, c = I % q.ct;
-    const double e = q.Hcc[c + q.ct * c] - q.Hvv[v + q.vt * v];
-    const double val = q.cqp * e * q.X[I + q.ldx * j];
+    const double e = q.diag ? q.diag[I] : q.cqp * (q.Hcc[c + q.ct * c] - q.Hvv[v + q.vt * v]);
+    const double val = e * q.X[I + q.ldx * j];
     double *y = q.Y + I + q.ldy * j;
     *y = q.accumulate ? *y + val : val;
   }
@@ -586,7 +587,15 @@ void matmul_grouped(const Coef &c, const std::vector<GroupedItem> &items, cudaSt
     BseOperator &op = *it.op;
     VGB_REQUIRE(it.ldx >= op.dim && it.ldy >= op.dim, "matmul: leading dimension smaller than the operator size");
     if (it.k <= 0) continue;
-    if (it.dense) VGB_REQUIRE(op.mixed && op.mixed->dense_ready(c), "grouped products: dense form not built");
+    if (it.dense) {
+      VGB_REQUIRE(op.mixed && op.mixed->dense_ready(c) && it.diag, "grouped products: dense form not built");
+      HqpJob j;  // the exact diagonal, then the off-diagonal dense part accumulates
+      j.cqp = 1; j.Hcc = nullptr; j.Hvv = nullptr; j.diag = it.diag; j.vt = op.vt; j.ct = op.ct;
+      j.X = it.X; j.ldx = it.ldx; j.k = it.k; j.Y = it.Y; j.ldy = it.ldy; j.accumulate = 0;
+      hq.push_back(j);
+      dense_items.push_back(it);
+      continue;
+    }
     if (op.precision != BSE_PRECISION_MIXED || !op.mixed) {  // FP64 operators: one product each
       op.matmul(c, it.X, it.ldx, it.k, it.Y, it.ldy, s);
       continue;
@@ -594,14 +603,14 @@ void matmul_grouped(const Coef &c, const std::vector<GroupedItem> &items, cudaSt
     if (c.cqp != 0) {
       if (op.hqp_diagonal) {
         HqpJob j;
-        j.cqp = c.cqp; j.Hcc = op.Hcc.get(); j.Hvv = op.Hvv.get(); j.vt = op.vt; j.ct = op.ct;
+        j.cqp = c.cqp; j.Hcc = op.Hcc.get(); j.Hvv = op.Hvv.get(); j.diag = nullptr; j.vt = op.vt; j.ct = op.ct;
         j.X = it.X; j.ldx = it.ldx; j.k = it.k; j.Y = it.Y; j.ldy = it.ldy; j.accumulate = 0;
         hq.push_back(j);
       } else {
         op.apply_hqp(c.cqp, it.X, it.ldx, it.k, it.Y, it.ldy, false, s);
       }
     }
-    (it.dense ? dense_items : mixed_items).push_back(it);
+    mixed_items.push_back(it);
   }
   std::unique_ptr<HqpGroup> g(new HqpGroup());
   for (size_t i = 0; i < hq.size();) {
@@ -616,7 +625,7 @@ void matmul_grouped(const Coef &c, const std::vector<GroupedItem> &items, cudaSt
     VGB_LAUNCH_CHECK();
   }
   MixedEngine::apply_grouped(c, mixed_items, c.cqp != 0, s, scratch);
-  MixedEngine::apply_dense_grouped(c, dense_items, c.cqp != 0, s);
+  MixedEngine::apply_dense_grouped(c, dense_items, true, s);
 }
 
 void BseOperator::check_errors(cudaStream_t s) {

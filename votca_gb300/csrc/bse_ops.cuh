@@ -150,6 +150,7 @@ struct GroupedItem {
   double *Y = nullptr;
   int64_t ldy = 0;
   bool dense = false;  // use the operator's dense form (MixedEngine::build_dense_grouped)
+  const double *diag = nullptr;  // with dense: the operator's full diagonal (device, FP64)
 };
 // Scratch shared by the operators of a grouped product (the Hd intermediates); kept by
 // the caller across products so that it is allocated once.

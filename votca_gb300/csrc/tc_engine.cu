@@ -401,13 +401,20 @@ __global__ void transpose_split_cc_kernel(const double *__restrict__ Mcc, int64_
   }
 }
 
-// H = (H + H^T) / 2: the two halves of the split products round differently (A_hi B_lo
-// against A_lo B_hi), and a nonsymmetric operator leaves a floor on the Davidson residual.
+// H = (H + H^T) / 2 off the diagonal: the two halves of the split products round differently
+// (A_hi B_lo against A_lo B_hi), and a nonsymmetric operator leaves a floor on the Davidson
+// residual.
+// The diagonal is zeroed: the products add the exact FP64 diagonal of the whole operator
+// beside the dense part, so the largest entries are not rounded to bf16 hi/lo.
 __global__ void symmetrize_kernel(double *H, int64_t n) {
   const int64_t total = n * n;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = t / n, j = t % n;
-    if (j <= i) continue;
+    if (j < i) continue;
+    if (j == i) {
+      H[i * n + i] = 0.0;
+      continue;
+    }
     const double a = 0.5 * (H[i * n + j] + H[j * n + i]);
     H[i * n + j] = a;
     H[j * n + i] = a;

@@ -18,13 +18,14 @@ class MixedEngine {
   // launch per stage and tile shape; accumulate: Y already holds the Hqp term.
   static void apply_grouped(const Coef &c, const std::vector<GroupedItem> &items, bool accumulate,
                             cudaStream_t s, GroupScratch *scratch);
-  // Dense form for small TDA operators: cx Hx - cd Hd built once with two tensor-core GEMMs
-  // over the aux index into FP64, symmetrised, kept as bf16 hi/lo rows; a product is then one
-  // GEMM.  Hqp stays FP64 beside it (its ~10 eV diagonal would lose digits in a bf16 split).
-  // Needs a diagonal Hqp and Naux <= 1024 (one FP32 chain per element).
+  // Dense form for small TDA operators: the off-diagonal part of cx Hx - cd Hd, built once with
+  // two tensor-core GEMMs over the aux index into FP64, symmetrised, kept as bf16 hi/lo rows; a
+  // product is one GEMM plus the operator's exact FP64 diagonal (Hqp included) applied beside
+  // it (GroupedItem::diag), so the large diagonal is never rounded to bf16.  Needs a diagonal
+  // Hqp and Naux <= 1024 (one FP32 chain per element).
   static void build_dense_grouped(const std::vector<BseOperator *> &ops, const Coef &c, cudaStream_t s);
   bool dense_ready(const Coef &c) const;
-  // Y (+)= (cx Hx - cd Hd) X with the dense form for every item; accumulate: Y holds Hqp X.
+  // Y (+)= (off-diagonal part of cx Hx - cd Hd) X for every item; accumulate: Y holds diag X.
   static void apply_dense_grouped(const Coef &c, const std::vector<GroupedItem> &items, bool accumulate,
                                   cudaStream_t s);
   // Allocate, ahead of a series of grouped products of at most kmax columns, every
