@@ -39,12 +39,13 @@ constexpr int kTileLd = kTile + 1;
 constexpr int kTnCols = 160;     // m + p columns per transposed-product job
 constexpr int kTnOut = 8;        // outputs per thread: m * p <= 8 * 256
 constexpr int kNnSmem = 48 * 1024;
-// Dense form up to dim 4096 (64 MB of bf16 hi/lo per molecule).  Its bf16 representation adds
-// full-rank noise of ~1e-5 relative per element to an interaction of rank <= 2 Naux; from dim
-// ~5000 (with Naux ~150-300) that noise held some residuals above 1e-7 (up to 49 iterations
-// instead of 3), while at dim <= 4096 every molecule of the 256-molecule set converged as with
-// the factorised products.
-constexpr int64_t kDenseMaxDim = 4096;
+// Dense form up to dim 16384 (1 GB of bf16 hi/lo per molecule), smallest molecules first, while
+// the dense forms of the batch stay within 32 GB.  A dense product costs 6 d^2 flops per column
+// against 6 Naux v c^2 for the factorised Hd alone (v < Naux in practice) and reads 4 d^2 bytes.
+// Its FP32 chains over K = dim are kept at 256 terms (the dense chain bound of the engine): with
+// 1024-term chains some residuals of the 256-molecule set stalled above 1e-7 from dim ~5000.
+constexpr int64_t kDenseMaxDim = 16384;
+constexpr int64_t kDenseBudgetBytes = 32LL << 30;
 
 template <class Job>
 struct Group {
@@ -520,8 +521,18 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
     std::vector<BseOperator *> dense;
     for (BseOperator *op : ops)
       if (allow_dense && coef.cd2 == 0 && op->precision == BSE_PRECISION_MIXED && op->mixed &&
-          op->hqp_diagonal && op->dim <= dense_max && ceil_div(op->naux, 64) * 64 <= 1024)
+          op->hqp_diagonal && op->dim <= dense_max && ceil_div(op->naux, 64) * 64 <= 1024 &&
+          std::find(dense.begin(), dense.end(), op) == dense.end())
         dense.push_back(op);
+    std::stable_sort(dense.begin(), dense.end(),
+                     [](const BseOperator *a, const BseOperator *b) { return a->dim < b->dim; });
+    int64_t dense_bytes = 0;
+    size_t nd = 0;
+    for (; nd < dense.size(); ++nd) {
+      dense_bytes += 4 * dense[nd]->dim * ceil_div(dense[nd]->dim, 64) * 64;
+      if (dense_bytes > kDenseBudgetBytes) break;
+    }
+    dense.resize(nd);
     MixedEngine::build_dense_grouped(dense, coef, s);
     for (BseOperator *op : dense)
       for (Mol &M : mols)

@@ -66,11 +66,12 @@ constexpr int64_t kGroupArenaElems = 1LL << 30;  // shared Hd intermediates of a
 int g_products = 3;
 int g_kacc = 1;                   // in-CTA K accumulation for N <= 64 stages with enough tiles
 int64_t g_s_budget = 10LL << 30;  // bytes of Hd/Hd2 intermediate per vector chunk
-int pick_ksplit(int64_t tiles, int64_t K) {
+int64_t g_dense_chain = 256;      // chain bound of the dense-form products (K = dim)
+int pick_ksplit(int64_t tiles, int64_t K, int64_t chain = 0) {
   const int64_t target = 2LL * sm_count();
   int64_t ks = 1;
   if (tiles < target) ks = std::max<int64_t>(1, std::min<int64_t>(ceil_div(target, tiles), K / 64 / 4));
-  ks = std::max<int64_t>(ks, ceil_div(K, g_max_chain));
+  ks = std::max<int64_t>(ks, ceil_div(K, chain > 0 ? chain : g_max_chain));
   return (int)std::min<int64_t>(ks, std::max<int64_t>(1, K / 64));
 }
 void read_tuning() {
@@ -81,6 +82,7 @@ void read_tuning() {
     if (const char *e = getenv("VGB_TC_BK256")) g_bk256 = atoi(e) == 64 ? 64 : 32;
     if (const char *e = getenv("VGB_TC_KACC")) g_kacc = atoi(e) != 0;
     if (const char *e = getenv("VGB_TC_S_BUDGET_GB")) g_s_budget = std::max(1LL, atoll(e)) << 30;
+    if (const char *e = getenv("VGB_TC_DENSE_CHAIN")) g_dense_chain = std::max(64LL, atoll(e));
   });
 }
 
@@ -607,7 +609,7 @@ void MixedEngine::apply_dense_grouped(const Coef &c, const std::vector<GroupedIt
     q.A = m.mat(m.Hdense.hi.get(), m.Hdense.lo.get(), m.dim, m.Kd, 128, bk_for(bn));
     q.B = m.mat(m.Xd.hi.get(), m.Xd.lo.get(), (int64_t)m.Xd.hi.count / m.Kd, m.Kd, bn, bk_for(bn));
     q.shape.M = m.dim; q.shape.N = it.k; q.shape.K = m.Kd; q.shape.products = g_products;
-    q.shape.ksplit = pick_ksplit(ceil_div(m.dim, 128) * ceil_div(it.k, bn), m.Kd);
+    q.shape.ksplit = pick_ksplit(ceil_div(m.dim, 128) * ceil_div(it.k, bn), m.Kd, g_dense_chain);
     m.part.resize((size_t)q.shape.ksplit * m.dim * it.k);
     q.epi.kind = TcEpilogue::STORE_F32;
     q.epi.rd = m.dim; q.epi.ro2 = 1; q.epi.rlim = m.dim;
