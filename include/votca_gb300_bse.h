@@ -92,6 +92,43 @@ int bse_op_create_dense_screening(const bse_mmn_desc *mmn,
                                   const bse_options *opt, int32_t precision,
                                   bse_handle **out);
 
+/* ---- Unrestricted (UKS) BSE operator ---- */
+
+/* BSEOperatorUKS_Options (xtp/include/votca/xtp/bse_operator_uks.h:31-38). */
+typedef struct bse_uks_options {
+  int64_t homo_alpha;
+  int64_t homo_beta;
+  int64_t rpamin;
+  int64_t qpmin;
+  int64_t vmin;
+  int64_t cmax;
+} bse_uks_options;
+
+/* Create a device-resident unrestricted BSE operator: replaces the construction of
+ * BSE_OPERATOR_UKS(epsilon_0_inv, TCMatrix_gwbse_spin{alpha, beta}, Hqp_alpha, Hqp_beta)
+ * + configure(opt) (bse_operator_uks.h:41-55, bse_operator_uks.cc:37-43).  Each spin
+ * channel is given as bse_op_create takes one Mmn (slices, window) and its own Hqp
+ * (window-local, occupied first); both share epsilon_0_inv (same auxsize).  The operator
+ * acts on [x_alpha; x_beta] (alpha pairs first, pair index v * ctotal + c per channel,
+ * vtotal = homo - vmin + 1, ctotal = cmax - homo); its size is the sum of the two channels.
+ * The returned handle serves bse_op_size / bse_op_matmul(_device) / bse_op_diagonal(_device)
+ * / bse_ham_matmul / bse_davidson_solve with BSE_OPERATOR_UKS<cqp, cx, cd, cd2>
+ * coefficients (ExcitonUKSOperator_TDA = 1,1,1,0; ExcitonUKSOperator_BTDA_B = 0,1,0,1;
+ * HdUKSOperator = 0,0,1,0; Hd2UKSOperator = 0,0,0,1; QpUKSOperator = 1,0,0,0;
+ * HxUKSOperator = 0,1,0,0, bse_operator_uks.h:111-124).  Products follow
+ * BSE_OPERATOR_UKS::matmul (bse_operator_uks.cc:220-270): same-spin Hqp, Hx, Hd, Hd2 per
+ * channel, the cross-spin TDA term -cd sum_P w_P M_s(c1, v1, P) M_s'(v2, c2, P) and the
+ * cross-spin -cd2 Hd2 term; the diagonal has the same-spin terms only (:283-352).
+ * precision: BSE_PRECISION_MIXED applies to the same-spin blocks; the cross-spin products
+ * run in FP64.  Not supported for UKS handles: bse_op_matmul_device_noalloc,
+ * bse_op_eig_gradient, bse_op_profile, lockstep batches (BSE_ERR_ARGUMENT). */
+int bse_uks_op_create(const bse_mmn_desc *mmn_alpha, const double *const *mmn_alpha_slices,
+                      const bse_mmn_desc *mmn_beta, const double *const *mmn_beta_slices,
+                      const double *epsilon_0_inv, const double *hqp_alpha, int64_t ldh_alpha,
+                      int64_t hqp_alpha_size, const double *hqp_beta, int64_t ldh_beta,
+                      int64_t hqp_beta_size, const bse_uks_options *opt, int32_t precision,
+                      bse_handle **out);
+
 /* ---- Screening that feeds Hd (FP64 on the device) ---- */
 
 /* Static RPA dielectric matrix, RPA::calculate_epsilon_r

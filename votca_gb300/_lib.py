@@ -22,6 +22,11 @@ class bse_options(ctypes.Structure):
     _fields_ = [("homo", c_i64), ("rpamin", c_i64), ("qpmin", c_i64), ("vmin", c_i64), ("cmax", c_i64)]
 
 
+class bse_uks_options(ctypes.Structure):
+    _fields_ = [("homo_alpha", c_i64), ("homo_beta", c_i64), ("rpamin", c_i64), ("qpmin", c_i64),
+                ("vmin", c_i64), ("cmax", c_i64)]
+
+
 class bse_mmn_desc(ctypes.Structure):
     _fields_ = [("auxsize", c_i64), ("mmin", c_i64), ("mmax", c_i64), ("nmin", c_i64), ("nmax", c_i64)]
 
@@ -43,6 +48,9 @@ SIGNATURES = {
     "bse_op_create_dense_screening": (c_i32, [ctypes.POINTER(bse_mmn_desc), ctypes.POINTER(c_dp), c_dp, c_dp,
                                               c_i64, c_i64, ctypes.POINTER(bse_options), c_i32,
                                               ctypes.POINTER(c_vp)]),
+    "bse_uks_op_create": (c_i32, [ctypes.POINTER(bse_mmn_desc), ctypes.POINTER(c_dp), ctypes.POINTER(bse_mmn_desc),
+                                  ctypes.POINTER(c_dp), c_dp, c_dp, c_i64, c_i64, c_dp, c_i64, c_i64,
+                                  ctypes.POINTER(bse_uks_options), c_i32, ctypes.POINTER(c_vp)]),
     "bse_dense_op_create": (c_i32, [c_dp, c_dp, c_i64, c_i64, ctypes.POINTER(c_vp)]),
     "bse_op_destroy": (c_i32, [c_vp]),
     "bse_op_size": (c_i32, [c_vp, ctypes.POINTER(c_i64)]),

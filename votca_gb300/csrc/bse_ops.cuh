@@ -137,6 +137,14 @@ class BseOperator {
   DeviceBuffer<double> hamA_, hamB_, hamX_;
 };
 
+// [[A, B], [-B, -A]] assembly helpers: Y[:dim] = TA_top + TB_bot, Y[dim:] = -TA_bot - TB_top
+// for products TA = A [M1_0, M2_0, M1_1, ...], TB = B [...]; D2 = [D; -D]; column copy.
+void ham_combine(const double *TA, const double *TB, int64_t dim, int64_t k, double *Y, int64_t ldy,
+                 cudaStream_t s);
+void ham_diag(const double *D, int64_t dim, double *D2, cudaStream_t s);
+void copy_cols(const double *X, int64_t ldx, int64_t rows, int64_t k, double *Y, int64_t ldy,
+               cudaStream_t s);
+
 // The Mmn-shaped gradient (the caller's slice layout, msize x naux x nsize, host memory) from the
 // block gradients of BseOperator::eig_gradient: scattered on the device, copied in chunks.
 void scatter_mmn_gradient(const BseOperator &op, const double *gMvc, const double *gMvv,

@@ -11,14 +11,31 @@
 #include "bse_ops.cuh"
 #include "batch_davidson.cuh"
 #include "davidson.cuh"
+#include "uks_ops.cuh"
 
 struct bse_handle {
-  int kind = 0;  // 0: BSE operator, 1: dense operator
+  int kind = 0;  // 0: BSE operator, 1: dense operator, 2: unrestricted (UKS) BSE operator
   std::unique_ptr<vgb::BseOperator> bse;
   std::unique_ptr<vgb::DenseOperator> dense;
+  std::unique_ptr<vgb::UksOperator> uks;
   cudaStream_t stream = nullptr;
   vgb::DeviceBuffer<double> dX, dY, dD;
-  int64_t size() const { return kind == 0 ? bse->dim : dense->n; }
+  int64_t size() const { return kind == 0 ? bse->dim : kind == 2 ? uks->dim : dense->n; }
+  void matmul(const vgb::Coef &c, const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy,
+              cudaStream_t s) {
+    if (kind == 0) bse->matmul(c, X, ldx, k, Y, ldy, s);
+    else if (kind == 2) uks->matmul(c, X, ldx, k, Y, ldy, s);
+    else dense->matmul(X, ldx, k, Y, ldy, s);
+  }
+  void diagonal(const vgb::Coef &c, double *D, cudaStream_t s) {
+    if (kind == 0) bse->diagonal(c, D, s);
+    else if (kind == 2) uks->diagonal(c, D, s);
+    else dense->diagonal(D, s);
+  }
+  void check_errors(cudaStream_t s) {
+    if (kind == 0) bse->check_errors(s);
+    else if (kind == 2) uks->check_errors(s);
+  }
 };
 
 namespace {
@@ -107,6 +124,36 @@ int bse_op_create_dense_screening(const bse_mmn_desc *mmn, const double *const *
   return create_impl(mmn, mmn_slices, W, true, hqp, ldh, hqp_size, opt, precision, out);
 }
 
+int bse_uks_op_create(const bse_mmn_desc *mmn_alpha, const double *const *mmn_alpha_slices,
+                      const bse_mmn_desc *mmn_beta, const double *const *mmn_beta_slices,
+                      const double *epsilon_0_inv, const double *hqp_alpha, int64_t ldh_alpha,
+                      int64_t hqp_alpha_size, const double *hqp_beta, int64_t ldh_beta,
+                      int64_t hqp_beta_size, const bse_uks_options *opt, int32_t precision,
+                      bse_handle **out) {
+  return guarded([&] {
+    VGB_REQUIRE(mmn_alpha && mmn_alpha_slices && mmn_beta && mmn_beta_slices && epsilon_0_inv && hqp_alpha &&
+                    hqp_beta && opt && out,
+                "bse_uks_op_create: null argument");
+    *out = nullptr;
+    std::unique_ptr<bse_handle> h(new bse_handle());
+    h->kind = 2;
+    create_stream(h.get());
+    vgb::AllocStreamScope alloc_scope(h->stream);
+    h->uks.reset(new vgb::UksOperator());
+    try {
+      h->uks->stage(*mmn_alpha, mmn_alpha_slices, *mmn_beta, mmn_beta_slices, epsilon_0_inv, hqp_alpha,
+                    ldh_alpha, hqp_alpha_size, hqp_beta, ldh_beta, hqp_beta_size, *opt, precision, h->stream);
+    } catch (...) {
+      h->uks.reset();
+      cudaStreamSynchronize(h->stream);
+      cudaStreamDestroy(h->stream);
+      h->stream = nullptr;
+      throw;
+    }
+    *out = h.release();
+  });
+}
+
 int bse_dense_op_create(const double *a, const double *b, int64_t n, int64_t lda,
                         bse_handle **out) {
   return guarded([&] {
@@ -160,12 +207,7 @@ int bse_op_matmul_device(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd, int
                          void *stream) {
   return guarded([&] {
     require_handle(h);
-    cudaStream_t s = (cudaStream_t)stream;
-    if (h->kind == 0) {
-      h->bse->matmul(coef(cqp, cx, cd, cd2), dX, ldx, k, dY, ldy, s);
-    } else {
-      h->dense->matmul(dX, ldx, k, dY, ldy, s);
-    }
+    h->matmul(coef(cqp, cx, cd, cd2), dX, ldx, k, dY, ldy, (cudaStream_t)stream);
   });
 }
 
@@ -193,14 +235,11 @@ int bse_op_matmul(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd, int32_t cd
     cudaStream_t s = h->stream;
     VGB_CUDA(cudaMemcpy2DAsync(h->dX.get(), n * sizeof(double), X, ldx * sizeof(double),
                                n * sizeof(double), k, cudaMemcpyHostToDevice, s));
-    if (h->kind == 0)
-      h->bse->matmul(coef(cqp, cx, cd, cd2), h->dX.get(), n, k, h->dY.get(), n, s);
-    else
-      h->dense->matmul(h->dX.get(), n, k, h->dY.get(), n, s);
+    h->matmul(coef(cqp, cx, cd, cd2), h->dX.get(), n, k, h->dY.get(), n, s);
     VGB_CUDA(cudaMemcpy2DAsync(Y, ldy * sizeof(double), h->dY.get(), n * sizeof(double),
                                n * sizeof(double), k, cudaMemcpyDeviceToHost, s));
     VGB_CUDA(cudaStreamSynchronize(s));
-    if (h->kind == 0) h->bse->check_errors(s);
+    h->check_errors(s);
   });
 }
 
@@ -208,9 +247,7 @@ int bse_op_diagonal_device(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd, i
                            double *dD, void *stream) {
   return guarded([&] {
     require_handle(h);
-    cudaStream_t s = (cudaStream_t)stream;
-    if (h->kind == 0) h->bse->diagonal(coef(cqp, cx, cd, cd2), dD, s);
-    else h->dense->diagonal(dD, s);
+    h->diagonal(coef(cqp, cx, cd, cd2), dD, (cudaStream_t)stream);
   });
 }
 
@@ -222,8 +259,7 @@ int bse_op_diagonal(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd, int32_t 
     const int64_t n = h->size();
     h->dD.resize(n);
     cudaStream_t s = h->stream;
-    if (h->kind == 0) h->bse->diagonal(coef(cqp, cx, cd, cd2), h->dD.get(), s);
-    else h->dense->diagonal(h->dD.get(), s);
+    h->diagonal(coef(cqp, cx, cd, cd2), h->dD.get(), s);
     VGB_CUDA(cudaMemcpyAsync(D, h->dD.get(), n * sizeof(double), cudaMemcpyDeviceToHost, s));
     VGB_CUDA(cudaStreamSynchronize(s));
   });
@@ -243,18 +279,19 @@ int bse_ham_matmul(bse_handle *h, const int32_t a_coef[4], const int32_t b_coef[
     cudaStream_t s = h->stream;
     VGB_CUDA(cudaMemcpy2DAsync(h->dX.get(), n * sizeof(double), X, ldx * sizeof(double),
                                n * sizeof(double), k, cudaMemcpyHostToDevice, s));
-    if (h->kind == 0) {
+    if (h->kind == 0 || h->kind == 2) {
       VGB_REQUIRE(a_coef && b_coef, "bse_ham_matmul: null coefficients");
-      h->bse->ham_matmul(coef(a_coef[0], a_coef[1], a_coef[2], a_coef[3]),
-                         coef(b_coef[0], b_coef[1], b_coef[2], b_coef[3]), h->dX.get(), n, k,
-                         h->dY.get(), n, s);
+      const vgb::Coef a = coef(a_coef[0], a_coef[1], a_coef[2], a_coef[3]);
+      const vgb::Coef b = coef(b_coef[0], b_coef[1], b_coef[2], b_coef[3]);
+      if (h->kind == 0) h->bse->ham_matmul(a, b, h->dX.get(), n, k, h->dY.get(), n, s);
+      else h->uks->ham_matmul(a, b, h->dX.get(), n, k, h->dY.get(), n, s);
     } else {
       h->dense->ham_matmul(h->dX.get(), n, k, h->dY.get(), n, s);
     }
     VGB_CUDA(cudaMemcpy2DAsync(Y, ldy * sizeof(double), h->dY.get(), n * sizeof(double),
                                n * sizeof(double), k, cudaMemcpyDeviceToHost, s));
     VGB_CUDA(cudaStreamSynchronize(s));
-    if (h->kind == 0) h->bse->check_errors(s);
+    h->check_errors(s);
   });
 }
 
@@ -268,14 +305,20 @@ int bse_davidson_solve(bse_handle *h, const int32_t a_coef[4], const int32_t b_c
     VGB_REQUIRE(opt != nullptr, "bse_davidson_solve: null options");
     const bool ham = opt->matrix_type == 1;
     std::unique_ptr<vgb::DeviceOperator> op;
-    if (h->kind == 0) {
+    if (h->kind == 0 || h->kind == 2) {
       VGB_REQUIRE(a_coef != nullptr, "bse_davidson_solve: null operator coefficients");
       vgb::Coef a = coef(a_coef[0], a_coef[1], a_coef[2], a_coef[3]);
+      vgb::Coef b;
       if (ham) {
         VGB_REQUIRE(b_coef != nullptr, "bse_davidson_solve: HAM needs B coefficients");
-        op.reset(new vgb::BseHamApply(h->bse.get(), a, coef(b_coef[0], b_coef[1], b_coef[2], b_coef[3])));
+        b = coef(b_coef[0], b_coef[1], b_coef[2], b_coef[3]);
+      }
+      if (h->kind == 0) {
+        if (ham) op.reset(new vgb::BseHamApply(h->bse.get(), a, b));
+        else op.reset(new vgb::BseApply(h->bse.get(), a));
       } else {
-        op.reset(new vgb::BseApply(h->bse.get(), a));
+        if (ham) op.reset(new vgb::UksHamApply(h->uks.get(), a, b));
+        else op.reset(new vgb::UksApply(h->uks.get(), a));
       }
     } else {
       VGB_REQUIRE(!ham || h->dense->has_b, "bse_davidson_solve: HAM needs a B block");

@@ -127,6 +127,39 @@ class Problem:
         self.coff = self.v
 
 
+class UKSProblem:
+    """One synthetic unrestricted problem: alpha and beta channels with their own HOMO over
+    MOs [vmin, cmax] of a window starting at rpamin = 0 (nmo MOs, extra MOs above cmax).
+    The beta Mmn is drawn from seed + 7919 so that the two channels differ; with
+    symmetric=False the (m, n) symmetry is broken by a second draw of the lower triangle
+    (exercises which of M(m, n) and M(n, m) each product reads)."""
+
+    def __init__(self, homo_alpha, homo_beta, vmin, cmax, naux, nmo=None, seed=0, symmetric=True):
+        self.homo_alpha, self.homo_beta = int(homo_alpha), int(homo_beta)
+        self.vmin, self.cmax, self.naux = int(vmin), int(cmax), int(naux)
+        self.nmo = int(nmo if nmo is not None else cmax + 1)
+        self.seed = int(seed)
+
+        def mmn(sd):
+            m = mmn_tensor(sd, self.naux, self.nmo)
+            if not symmetric:
+                low = np.tril(np.ones((self.nmo, self.nmo), dtype=bool), -1)
+                other = mmn_tensor(sd + 104729, self.naux, self.nmo)
+                m[:, :, :] = np.where(low[:, None, :], other, m)
+            return m
+
+        self.mmn_alpha = mmn(seed)
+        self.mmn_beta = mmn(seed + 7919)
+        self.w = screening_w(seed, self.naux)
+
+        def hqp(homo, sd):
+            v, c = homo - self.vmin + 1, self.cmax - homo
+            return np.diag(qp_energies(sd, v, c))
+
+        self.hqp_alpha = hqp(self.homo_alpha, seed)
+        self.hqp_beta = hqp(self.homo_beta, seed + 7919)
+
+
 def batched_shapes(n, seed=0):
     """Shapes of n independent molecules: v ~ U{4..32}, c ~ U{32..256},
     Naux ~ U{128..1024}, Nmo = v + c + 8, and a per-molecule seed."""
