@@ -162,6 +162,32 @@ int bse_positive_inverse(int64_t n, const double *A, int64_t lda, double cutoff,
 int bse_mmn_multiply_right(const bse_mmn_desc *mmn, double *const *mmn_slices,
                            const double *U, int64_t ldu);
 
+/* ---- Mmn producer (TCMatrix_gwbse::Fill, xtp/src/libxtp/threecenter.cc:79-95) ---- */
+
+/* TCMatrix_gwbse::Fill3cMO (xtp/src/libxtp/libint2_calls.cc:595-651) with the AO
+ * three-centre Coulomb integrals supplied by the caller in place of libint2:
+ *   M(m, n, P) = sum_{mu,nu} C(mu, n) (P|mu nu) C(nu, m)
+ * for m in [mmin, mmax], n in [nmin, nmax] of `mmn`; FP64 GEMMs on the device, batched over P.
+ *   ao3c: auxsize column-major nbf x nbf symmetric matrices back to back,
+ *         (P|mu nu) = ao3c[P * nbf * nbf + mu + nbf * nu].
+ *   mo_coefficients: column-major nbf x nmo (dft_orbitals), leading dimension ldc.
+ *   mmn_slices: msize output slices, each column-major nsize x auxsize (overwritten). */
+int bse_mmn_fill_3c_mo(const bse_mmn_desc *mmn, double *const *mmn_slices, const double *ao3c, int64_t nbf,
+                       const double *mo_coefficients, int64_t ldc, int64_t nmo);
+
+/* AOCoulomb::Pseudo_InvSqrt (xtp/src/libxtp/aomatrices/aomatrix.cc:88-102): V^-1/2 over the
+ * eigenvalues of V that are >= etol; `removed` (may be NULL) gets the number dropped. */
+int bse_aux_pseudo_inv_sqrt(int64_t n, const double *V, int64_t ldv, double etol, double *out, int64_t ldo,
+                            int64_t *removed);
+
+/* AOCoulomb::Pseudo_InvSqrt_GWBSE (aomatrix.cc:53-86), the matrix TCMatrix_gwbse::Fill
+ * multiplies Mmn with (threecenter.cc:86-93, etol 5e-7 there): S^-1/2 and
+ * (S^-1/2 V S^-1/2)^-1/2 over the eigenvalues >= etol, result (V'^-1/2 S^-1/2)^T; `removed`
+ * counts the functions dropped in both steps.  Eigenproblems on the host as in the reference,
+ * products on the device. */
+int bse_aux_pseudo_inv_sqrt_gwbse(int64_t n, const double *S, int64_t lds, const double *V, int64_t ldv,
+                                  double etol, double *out, int64_t ldo, int64_t *removed);
+
 /* A dense FP64 symmetric matrix as an operator (the reference tests'
  * HermitianBlockOperator, test_davidson.cc:265-281).  b may be NULL; when
  * given, bse_ham_* use [[a, b], [-b, -a]]. */

@@ -12,6 +12,11 @@ Writes bse_operator_hqp.npz:
 Writes davidson_kat.npz: the lowest 10 eigenvalues of init_matrix(N, 0.01)
 (test_davidson.cc:42-56) for N = 100, 400, from a dense symmetric eigensolver,
 the reference value its Davidson tests check against at 1e-6.
+Writes aomatrix.npz (xtp/src/tests/DataFiles/aomatrix, methane 3-21G; checked by
+xtp/src/tests/test_aomatrix.cc:43-123 at isApprox 1e-5):
+  overlap, coulomb                 AOOverlap / AOCoulomb matrices (overlap_ref.mm, coulomb_ref.mm)
+  invsqrt                          coulomb.Pseudo_InvSqrt(1e-7)          (coulombinvsqrt_ref.mm)
+  invsqrt_gwbse                    coulomb.Pseudo_InvSqrt_GWBSE(overlap, 1e-7) (coulombinvsqrtgw_ref.mm)
 """
 import os
 import sys
@@ -47,6 +52,12 @@ def main():
     for n in (100, 400):
         out[f"evals_{n}"] = np.linalg.eigvalsh(init_matrix(n, 0.01))[:10]
     np.savez(os.path.join(here, "davidson_kat.npz"), **out)
+    a = os.path.join(ref, "xtp/src/tests/DataFiles/aomatrix")
+    np.savez(os.path.join(here, "aomatrix.npz"),
+             overlap=read_mm_array(os.path.join(a, "overlap_ref.mm")),
+             coulomb=read_mm_array(os.path.join(a, "coulomb_ref.mm")),
+             invsqrt=read_mm_array(os.path.join(a, "coulombinvsqrt_ref.mm")),
+             invsqrt_gwbse=read_mm_array(os.path.join(a, "coulombinvsqrtgw_ref.mm")))
     print("wrote fixtures to", here)
 
 

@@ -74,6 +74,11 @@ SIGNATURES = {
     "bse_cholesky_inverse": (c_i32, [c_i64, c_dp, c_i64, c_dp, c_i64]),
     "bse_positive_inverse": (c_i32, [c_i64, c_dp, c_i64, ctypes.c_double, c_dp, c_i64]),
     "bse_mmn_multiply_right": (c_i32, [ctypes.POINTER(bse_mmn_desc), ctypes.POINTER(c_dp), c_dp, c_i64]),
+    "bse_mmn_fill_3c_mo": (c_i32, [ctypes.POINTER(bse_mmn_desc), ctypes.POINTER(c_dp), c_dp, c_i64, c_dp, c_i64,
+                                   c_i64]),
+    "bse_aux_pseudo_inv_sqrt": (c_i32, [c_i64, c_dp, c_i64, ctypes.c_double, c_dp, c_i64, ctypes.POINTER(c_i64)]),
+    "bse_aux_pseudo_inv_sqrt_gwbse": (c_i32, [c_i64, c_dp, c_i64, c_dp, c_i64, ctypes.c_double, c_dp, c_i64,
+                                              ctypes.POINTER(c_i64)]),
     "bse_op_profile": (c_i32, [c_vp, c_i32]),
     "bse_op_profile_read": (c_i32, [c_vp, c_dp, ctypes.POINTER(c_i64), c_i32]),
     "bse_probe_fp64_tflops": (c_i32, [c_dp]),

@@ -417,6 +417,31 @@ int bse_mmn_multiply_right(const bse_mmn_desc *mmn, double *const *mmn_slices, c
   });
 }
 
+int bse_mmn_fill_3c_mo(const bse_mmn_desc *mmn, double *const *mmn_slices, const double *ao3c, int64_t nbf,
+                       const double *mo_coefficients, int64_t ldc, int64_t nmo) {
+  return guarded([&] {
+    VGB_REQUIRE(mmn && mmn_slices && ao3c && mo_coefficients, "bse_mmn_fill_3c_mo: null argument");
+    TmpStream ts;
+    vgb::fill_3c_mo(*mmn, mmn_slices, ao3c, nbf, mo_coefficients, ldc, nmo, ts.s);
+  });
+}
+
+int bse_aux_pseudo_inv_sqrt(int64_t n, const double *V, int64_t ldv, double etol, double *out, int64_t ldo,
+                            int64_t *removed) {
+  return guarded([&] {
+    TmpStream ts;
+    vgb::aux_pseudo_inv_sqrt(n, V, ldv, etol, out, ldo, removed, ts.s);
+  });
+}
+
+int bse_aux_pseudo_inv_sqrt_gwbse(int64_t n, const double *S, int64_t lds, const double *V, int64_t ldv,
+                                  double etol, double *out, int64_t ldo, int64_t *removed) {
+  return guarded([&] {
+    TmpStream ts;
+    vgb::aux_pseudo_inv_sqrt_gwbse(n, S, lds, V, ldv, etol, out, ldo, removed, ts.s);
+  });
+}
+
 int bse_davidson_solve_batch(bse_handle *const *handles, int64_t nhandles, const int32_t a_coef[4],
                              const int32_t b_coef[4], const bse_davidson_options *opt,
                              int64_t neigen, double *evals, int32_t *infos, int64_t *iterations,

@@ -106,4 +106,12 @@ void positive_inverse(int64_t n, const double *a_host, int64_t lda, double cutof
 void mmn_multiply_right(const bse_mmn_desc &desc, double *const *slices, const double *U_host,
                         int64_t ldu, cudaStream_t s);
 
+// Mmn producer (threecenter.cu)
+void fill_3c_mo(const bse_mmn_desc &desc, double *const *slices, const double *ao3c, int64_t nbf,
+                const double *C, int64_t ldc, int64_t nmo, cudaStream_t s);
+void aux_pseudo_inv_sqrt(int64_t n, const double *V, int64_t ldv, double etol, double *out, int64_t ldo,
+                         int64_t *removed, cudaStream_t s);
+void aux_pseudo_inv_sqrt_gwbse(int64_t n, const double *S, int64_t lds, const double *V, int64_t ldv,
+                               double etol, double *out, int64_t ldo, int64_t *removed, cudaStream_t s);
+
 }  // namespace vgb
