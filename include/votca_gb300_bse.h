@@ -129,6 +129,17 @@ int bse_uks_op_create(const bse_mmn_desc *mmn_alpha, const double *const *mmn_al
                       int64_t hqp_beta_size, const bse_uks_options *opt, int32_t precision,
                       bse_handle **out);
 
+/* Same, with a dense symmetric screening matrix W (auxsize x auxsize) in place of the diagonal
+ * epsilon_0_inv: every direct term uses sum_PQ M^P W_PQ M^Q.  With W = U diag(w) U^T this is the
+ * operator BSE_UKS::SetupDirectInteractionOperator builds by rotating both Mmn with the
+ * eigenvectors U of eps and screening with w (bse_uks.cc:135-157). */
+int bse_uks_op_create_dense_screening(const bse_mmn_desc *mmn_alpha, const double *const *mmn_alpha_slices,
+                                      const bse_mmn_desc *mmn_beta, const double *const *mmn_beta_slices,
+                                      const double *W, const double *hqp_alpha, int64_t ldh_alpha,
+                                      int64_t hqp_alpha_size, const double *hqp_beta, int64_t ldh_beta,
+                                      int64_t hqp_beta_size, const bse_uks_options *opt, int32_t precision,
+                                      bse_handle **out);
+
 /* ---- Screening that feeds Hd (FP64 on the device) ---- */
 
 /* Static RPA dielectric matrix, RPA::calculate_epsilon_r

@@ -51,6 +51,10 @@ SIGNATURES = {
     "bse_uks_op_create": (c_i32, [ctypes.POINTER(bse_mmn_desc), ctypes.POINTER(c_dp), ctypes.POINTER(bse_mmn_desc),
                                   ctypes.POINTER(c_dp), c_dp, c_dp, c_i64, c_i64, c_dp, c_i64, c_i64,
                                   ctypes.POINTER(bse_uks_options), c_i32, ctypes.POINTER(c_vp)]),
+    "bse_uks_op_create_dense_screening": (c_i32, [ctypes.POINTER(bse_mmn_desc), ctypes.POINTER(c_dp),
+                                                  ctypes.POINTER(bse_mmn_desc), ctypes.POINTER(c_dp), c_dp, c_dp,
+                                                  c_i64, c_i64, c_dp, c_i64, c_i64, ctypes.POINTER(bse_uks_options),
+                                                  c_i32, ctypes.POINTER(c_vp)]),
     "bse_dense_op_create": (c_i32, [c_dp, c_dp, c_i64, c_i64, ctypes.POINTER(c_vp)]),
     "bse_op_destroy": (c_i32, [c_vp]),
     "bse_op_size": (c_i32, [c_vp, ctypes.POINTER(c_i64)]),

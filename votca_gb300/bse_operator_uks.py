@@ -57,19 +57,25 @@ class GpuBSEContextUKS:
     unrestricted BSE window given by BSEOperatorUKS_Options."""
 
     def __init__(self, epsilon_0_inv, Mmn: TCMatrix_gwbse_spin, Hqp_alpha, Hqp_beta, opt: BSEOperatorUKS_Options,
-                 precision=PRECISION_FP64):
+                 precision=PRECISION_FP64, dense_screening=None):
         L = _lib.load()
         self._L = L
         da, pa = _mmn_args(Mmn.alpha)
         db, pb = _mmn_args(Mmn.beta)
         ha = np.asfortranarray(Hqp_alpha, dtype=np.float64)
         hb = np.asfortranarray(Hqp_beta, dtype=np.float64)
-        w = np.ascontiguousarray(epsilon_0_inv, dtype=np.float64)
         o = _lib.bse_uks_options(opt.homo_alpha, opt.homo_beta, opt.rpamin, opt.qpmin, opt.vmin, opt.cmax)
         h = ctypes.c_void_p()
-        _lib.check(L.bse_uks_op_create(ctypes.byref(da), pa, ctypes.byref(db), pb, _p(w), _p(ha), ha.shape[0],
-                                       ha.shape[0], _p(hb), hb.shape[0], hb.shape[0], ctypes.byref(o), precision,
-                                       ctypes.byref(h)))
+        if dense_screening is not None:
+            w = np.asfortranarray(dense_screening, dtype=np.float64)
+            create = L.bse_uks_op_create_dense_screening
+        else:
+            if epsilon_0_inv is None:
+                raise _lib.BSEError(1, "GpuBSEContextUKS: epsilon_0_inv or dense_screening is required")
+            w = np.ascontiguousarray(epsilon_0_inv, dtype=np.float64)
+            create = L.bse_uks_op_create
+        _lib.check(create(ctypes.byref(da), pa, ctypes.byref(db), pb, _p(w), _p(ha), ha.shape[0], ha.shape[0],
+                          _p(hb), hb.shape[0], hb.shape[0], ctypes.byref(o), precision, ctypes.byref(h)))
         self.handle = h
         n = ctypes.c_int64()
         _lib.check(L.bse_op_size(h, ctypes.byref(n)))

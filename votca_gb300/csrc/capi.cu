@@ -124,12 +124,12 @@ int bse_op_create_dense_screening(const bse_mmn_desc *mmn, const double *const *
   return create_impl(mmn, mmn_slices, W, true, hqp, ldh, hqp_size, opt, precision, out);
 }
 
-int bse_uks_op_create(const bse_mmn_desc *mmn_alpha, const double *const *mmn_alpha_slices,
-                      const bse_mmn_desc *mmn_beta, const double *const *mmn_beta_slices,
-                      const double *epsilon_0_inv, const double *hqp_alpha, int64_t ldh_alpha,
-                      int64_t hqp_alpha_size, const double *hqp_beta, int64_t ldh_beta,
-                      int64_t hqp_beta_size, const bse_uks_options *opt, int32_t precision,
-                      bse_handle **out) {
+static int uks_create_impl(const bse_mmn_desc *mmn_alpha, const double *const *mmn_alpha_slices,
+                           const bse_mmn_desc *mmn_beta, const double *const *mmn_beta_slices,
+                           const double *epsilon_0_inv, bool dense_w, const double *hqp_alpha,
+                           int64_t ldh_alpha, int64_t hqp_alpha_size, const double *hqp_beta,
+                           int64_t ldh_beta, int64_t hqp_beta_size, const bse_uks_options *opt,
+                           int32_t precision, bse_handle **out) {
   return guarded([&] {
     VGB_REQUIRE(mmn_alpha && mmn_alpha_slices && mmn_beta && mmn_beta_slices && epsilon_0_inv && hqp_alpha &&
                     hqp_beta && opt && out,
@@ -141,8 +141,9 @@ int bse_uks_op_create(const bse_mmn_desc *mmn_alpha, const double *const *mmn_al
     vgb::AllocStreamScope alloc_scope(h->stream);
     h->uks.reset(new vgb::UksOperator());
     try {
-      h->uks->stage(*mmn_alpha, mmn_alpha_slices, *mmn_beta, mmn_beta_slices, epsilon_0_inv, hqp_alpha,
-                    ldh_alpha, hqp_alpha_size, hqp_beta, ldh_beta, hqp_beta_size, *opt, precision, h->stream);
+      h->uks->stage(*mmn_alpha, mmn_alpha_slices, *mmn_beta, mmn_beta_slices, epsilon_0_inv, dense_w,
+                    hqp_alpha, ldh_alpha, hqp_alpha_size, hqp_beta, ldh_beta, hqp_beta_size, *opt, precision,
+                    h->stream);
     } catch (...) {
       h->uks.reset();
       cudaStreamSynchronize(h->stream);
@@ -152,6 +153,26 @@ int bse_uks_op_create(const bse_mmn_desc *mmn_alpha, const double *const *mmn_al
     }
     *out = h.release();
   });
+}
+
+int bse_uks_op_create(const bse_mmn_desc *mmn_alpha, const double *const *mmn_alpha_slices,
+                      const bse_mmn_desc *mmn_beta, const double *const *mmn_beta_slices,
+                      const double *epsilon_0_inv, const double *hqp_alpha, int64_t ldh_alpha,
+                      int64_t hqp_alpha_size, const double *hqp_beta, int64_t ldh_beta,
+                      int64_t hqp_beta_size, const bse_uks_options *opt, int32_t precision,
+                      bse_handle **out) {
+  return uks_create_impl(mmn_alpha, mmn_alpha_slices, mmn_beta, mmn_beta_slices, epsilon_0_inv, false, hqp_alpha,
+                         ldh_alpha, hqp_alpha_size, hqp_beta, ldh_beta, hqp_beta_size, opt, precision, out);
+}
+
+int bse_uks_op_create_dense_screening(const bse_mmn_desc *mmn_alpha, const double *const *mmn_alpha_slices,
+                                      const bse_mmn_desc *mmn_beta, const double *const *mmn_beta_slices,
+                                      const double *W, const double *hqp_alpha, int64_t ldh_alpha,
+                                      int64_t hqp_alpha_size, const double *hqp_beta, int64_t ldh_beta,
+                                      int64_t hqp_beta_size, const bse_uks_options *opt, int32_t precision,
+                                      bse_handle **out) {
+  return uks_create_impl(mmn_alpha, mmn_alpha_slices, mmn_beta, mmn_beta_slices, W, true, hqp_alpha, ldh_alpha,
+                         hqp_alpha_size, hqp_beta, ldh_beta, hqp_beta_size, opt, precision, out);
 }
 
 int bse_dense_op_create(const double *a, const double *b, int64_t n, int64_t lda,

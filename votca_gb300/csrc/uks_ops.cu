@@ -51,15 +51,15 @@ void stage_factor(const HostMmn &M, const double *w, int64_t naux, int64_t rows,
 
 void UksOperator::stage(const bse_mmn_desc &desc_a, const double *const *slices_a,
                         const bse_mmn_desc &desc_b, const double *const *slices_b, const double *w,
-                        const double *hqp_a, int64_t ldh_a, int64_t size_a, const double *hqp_b,
-                        int64_t ldh_b, int64_t size_b, const bse_uks_options &opt, int prec,
-                        cudaStream_t s) {
+                        bool dense_w, const double *hqp_a, int64_t ldh_a, int64_t size_a,
+                        const double *hqp_b, int64_t ldh_b, int64_t size_b, const bse_uks_options &opt,
+                        int prec, cudaStream_t s) {
   // BSE_OPERATOR_UKS::configure / setup_block, bse_operator_uks.cc:25-43
   VGB_REQUIRE(desc_a.auxsize == desc_b.auxsize, "bse_uks_op_create: alpha and beta Naux differ");
   VGB_REQUIRE(slices_a && slices_b && w && hqp_a && hqp_b, "bse_uks_op_create: null input");
   precision = prec;
-  alpha.stage(desc_a, slices_a, w, false, hqp_a, ldh_a, size_a, channel_options(opt, opt.homo_alpha), prec, s);
-  beta.stage(desc_b, slices_b, w, false, hqp_b, ldh_b, size_b, channel_options(opt, opt.homo_beta), prec, s);
+  alpha.stage(desc_a, slices_a, w, dense_w, hqp_a, ldh_a, size_a, channel_options(opt, opt.homo_alpha), prec, s);
+  beta.stage(desc_b, slices_b, w, dense_w, hqp_b, ldh_b, size_b, channel_options(opt, opt.homo_beta), prec, s);
   dim = alpha.dim + beta.dim;
   // the cross-spin Hd2 blocks read each channel's Mmn over the other channel's ranges
   for (const bse_mmn_desc *d : {&desc_a, &desc_b}) {
@@ -70,10 +70,28 @@ void UksOperator::stage(const bse_mmn_desc &desc_a, const double *const *slices_
   const HostMmn Ma{desc_a, slices_a}, Mb{desc_b, slices_b};
   const int64_t ca0 = opt.homo_alpha + 1, cb0 = opt.homo_beta + 1;
   // Xab[P][v1][c2] = M_b(vmin + v1, cb0 + c2), Yab[P][v2][c1] = w M_a(ca0 + c1, vmin + v2)
+  const double *wd = dense_w ? nullptr : w;
   stage_factor(Mb, nullptr, naux, alpha.vt, beta.ct, opt.vmin, cb0, true, Xab, s);
-  stage_factor(Ma, w, naux, beta.vt, alpha.ct, ca0, opt.vmin, false, Yab, s);
+  stage_factor(Ma, wd, naux, beta.vt, alpha.ct, ca0, opt.vmin, false, Yab, s);
   stage_factor(Ma, nullptr, naux, beta.vt, alpha.ct, opt.vmin, ca0, true, Xba, s);
-  stage_factor(Mb, w, naux, alpha.vt, beta.ct, cb0, opt.vmin, false, Yba, s);
+  stage_factor(Mb, wd, naux, alpha.vt, beta.ct, cb0, opt.vmin, false, Yba, s);
+  if (dense_w) {
+    // Y(rc, Q) = sum_P Y(rc, P) W(P, Q): the screened factors carry the dense W
+    DeviceBuffer<double> dW(naux * naux);
+    VGB_CUDA(cudaMemcpyAsync(dW.get(), w, naux * naux * sizeof(double), cudaMemcpyHostToDevice, s));
+    for (DeviceBuffer<double> *Y : {&Yab, &Yba}) {
+      const int64_t rc = (int64_t)Y->count / naux;
+      DeviceBuffer<double> tmp(rc * naux);
+      GemmDesc g;
+      g.M = rc; g.N = naux; g.K = naux;
+      g.A = Y->get(); g.a_rs = 1; g.a_cs = rc;
+      g.B = dW.get(); g.b_rs = 1; g.b_cs = naux;
+      g.C = tmp.get(); g.c_rs = 1; g.c_cs = rc;
+      dgemm(g, s, &ws_);
+      VGB_CUDA(cudaMemcpyAsync(Y->get(), tmp.get(), rc * naux * sizeof(double), cudaMemcpyDeviceToDevice, s));
+      VGB_CUDA(cudaStreamSynchronize(s));
+    }
+  }
 }
 
 // Yout += alpha sum_P Mcv_out[P][I1] (sum_I2 Bvc_in[P][I2] Xin[I2]):

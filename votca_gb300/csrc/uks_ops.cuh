@@ -28,10 +28,12 @@ class UksOperator {
   //   Xba, Yba: the same with the spins exchanged
   DeviceBuffer<double> Xab, Yab, Xba, Yba;
 
-  // Stage both spin channels from host data (see bse_uks_op_create).
+  // Stage both spin channels from host data (see bse_uks_op_create).  w: the diagonal screening
+  // (naux), or with dense_w a symmetric naux x naux W (column-major) folded into the screened
+  // factors: sum_PQ M^P W_PQ M^Q in every direct term.
   void stage(const bse_mmn_desc &desc_a, const double *const *slices_a, const bse_mmn_desc &desc_b,
-             const double *const *slices_b, const double *w, const double *hqp_a, int64_t ldh_a,
-             int64_t size_a, const double *hqp_b, int64_t ldh_b, int64_t size_b,
+             const double *const *slices_b, const double *w, bool dense_w, const double *hqp_a,
+             int64_t ldh_a, int64_t size_a, const double *hqp_b, int64_t ldh_b, int64_t size_b,
              const bse_uks_options &opt, int prec, cudaStream_t s);
 
   // Y = H(coef) X on device, X and Y dim x k (ldx, ldy >= dim).

@@ -10,6 +10,13 @@ the excitation energies, on the GPU.
                                dense form: W = eps(omega)^-1 folded into the operator
   perturbative_dynamical_screening
                                BSE::Perturbative_DynamicalScreening (bse.cc:610-681)
+  rpa_epsilon_uks              RPA_UKS::calculate_epsilon_r (rpa_uks.cc:306-358):
+                               eps = 1 - R_alpha - R_beta, each channel's sum as in the
+                               restricted kernel (which forms 1 - 2 R)
+  screened_context_uks         BSE_UKS::SetupDirectInteractionOperator (bse_uks.cc:135-157)
+                               in the dense form, on the unrotated (raw) Mmn of both channels
+  perturbative_dynamical_screening_uks
+                               BSE_UKS::Perturbative_DynamicalScreening (bse_uks.cc:640-715)
 
 The reference diagonalises eps, rotates Mmn by its eigenvectors and weights the rotated
 aux functions by 1/lambda (lambda > 1e-8).  With all eigenvalues above that cutoff this is
@@ -111,6 +118,72 @@ def perturbative_dynamical_screening(Mmn, Hqp, opt, rpa_energies, rpa_window, en
             old = dynamic[i]
             ctx = screened_context(Mmn, Hqp, opt, rpa_energies, rpa_window, old, precision)
             hd_dyn = _direct(ctx, xi, yi)[0]
+            ctx.close()
+            dynamic[i] = energies[i] + hd_static[i] - hd_dyn
+            if abs(dynamic[i] - old) < tolerance:
+                break
+    return dynamic
+
+
+def rpa_epsilon_uks(Mmn, rpa_energies_alpha, rpa_energies_beta, homo_alpha, homo_beta, rpamin, rpamax,
+                    frequency=0.0):
+    """eps(omega) of the unrestricted RPA: 1 - R_alpha - R_beta.  The restricted kernel gives
+    1 - 2 R_s per channel, so eps = (eps_alpha + eps_beta) / 2."""
+    ea = rpa_epsilon(Mmn.alpha, rpa_energies_alpha, homo_alpha, rpamin, rpamax, frequency)
+    eb = rpa_epsilon(Mmn.beta, rpa_energies_beta, homo_beta, rpamin, rpamax, frequency)
+    return 0.5 * (ea + eb)
+
+
+def _screening_from(eps):
+    try:
+        return cholesky_inverse(eps)
+    except _lib.BSEError as e:
+        if e.code != 5:  # BSE_ERR_NUMERICAL: not positive definite
+            raise
+        return positive_inverse(eps, 1e-8)
+
+
+def screened_context_uks(Mmn, Hqp_alpha, Hqp_beta, opt, rpa_energies_alpha, rpa_energies_beta, rpamax,
+                         frequency=0.0, precision=0):
+    """UKS operator context with the direct terms screened at `frequency` (eps of both
+    channels from the raw Mmn, as the reference resets Mmn before each rotation)."""
+    from .bse_operator_uks import GpuBSEContextUKS
+
+    eps = rpa_epsilon_uks(Mmn, rpa_energies_alpha, rpa_energies_beta, opt.homo_alpha, opt.homo_beta, opt.rpamin,
+                          rpamax, frequency)
+    return GpuBSEContextUKS(None, Mmn, Hqp_alpha, Hqp_beta, opt, precision=precision,
+                            dense_screening=_screening_from(eps))
+
+
+def perturbative_dynamical_screening_uks(Mmn, Hqp_alpha, Hqp_beta, opt, rpa_energies_alpha, rpa_energies_beta,
+                                         rpamax, energies, X, Y=None, max_iter=10, tolerance=1e-5,
+                                         precision=0):
+    """UKS excitation energies with the direct terms screened at each excitation's own energy,
+    to first order around the static solution (energies, X[, Y]) of the combined operator."""
+    from .bse_operator_uks import Hd2UKSOperator, HdUKSOperator
+
+    energies = np.asarray(energies, dtype=np.float64)
+    X = np.asfortranarray(X, dtype=np.float64)
+    Y = None if Y is None else np.asfortranarray(Y, dtype=np.float64)
+
+    def direct(ctx, x, y):
+        d, _ = expectation_value_operator(HdUKSOperator(ctx), x, y)
+        if y is not None:
+            d = d + expectation_value_operator(Hd2UKSOperator(ctx), x, y)[1]
+        return d
+
+    args = (Mmn, Hqp_alpha, Hqp_beta, opt, rpa_energies_alpha, rpa_energies_beta, rpamax)
+    static = screened_context_uks(*args, 0.0, precision)
+    hd_static = direct(static, X, Y)
+    static.close()
+    dynamic = energies.copy()
+    for i in range(energies.size):
+        xi = X[:, i:i + 1]
+        yi = None if Y is None else Y[:, i:i + 1]
+        for _ in range(max_iter):
+            old = dynamic[i]
+            ctx = screened_context_uks(*args, old, precision)
+            hd_dyn = direct(ctx, xi, yi)[0]
             ctx.close()
             dynamic[i] = energies[i] + hd_static[i] - hd_dyn
             if abs(dynamic[i] - old) < tolerance:
