@@ -13,8 +13,10 @@
 #include "batch_davidson.cuh"
 
 #include <algorithm>
+#include <functional>
 #include <atomic>
 #include <chrono>
+#include <condition_variable>
 #include <cstdio>
 #include <cstdlib>
 #include <cmath>
@@ -23,6 +25,7 @@
 #include <mutex>
 #include <numeric>
 #include <thread>
+#include <unistd.h>
 
 #include "host_eig.hpp"
 #include "tc_engine.cuh"
@@ -314,8 +317,12 @@ struct Mol {
   // device (views into the pool)
   double *V, *AV, *D, *q, *res, *Ud, *lamd, *cbuf, *norms0, *norms, *h, *part;
   int *flag;
-  // packed host transfer offsets (doubles)
-  int64_t off_in = 0, off_out = 0;
+  // packed host transfer offsets (doubles): off_in = [U (capc x needmax) | lambdas (needmax) |
+  // correction columns (capc) | their lambdas (capc)] in din/hin; off_out in hout (diagonal);
+  // off_pack = this step's block in dpack/hpack (every molecule's result of a step is packed
+  // back to back and copied to the host in one transfer)
+  int64_t off_in = 0, off_out = 0, off_pack = 0;
+  int64_t dpr_in() const { return off_in + capc * needmax + needmax; }
 };
 
 // Grouped A^T B for every (mol, A, B, m, p, C) request; splits wide requests over m.
@@ -396,33 +403,88 @@ void run_cols(const std::vector<ColJob> &jobs, cudaStream_t s) {
   launch_jobs(jobs, col_kernel, rows_blocks(mx), false, s);
 }
 
-// Parallel loop over molecules on host threads.
+// Parallel loop over molecules on host threads: a pool of workers kept for the process (starting
+// 16 threads per Davidson step cost about as much as the small eigenproblems they solve).  One
+// loop runs at a time; the calling thread takes part.
+class HostPool {
+ public:
+  static HostPool &get() {
+    // never destroyed: the workers stay parked until the process exits (no join at exit, and
+    // none attempted in a forked child, where the threads do not exist)
+    static HostPool *pool = new HostPool();
+    return *pool;
+  }
+  void run(size_t count, const std::function<void(size_t)> &f) {
+    std::lock_guard<std::mutex> one(run_mu_);
+    // a forked child has no workers (threads do not survive fork): run serially there
+    if (workers_.empty() || count <= 1 || getpid() != pid_) {
+      for (size_t i = 0; i < count; ++i) f(i);
+      return;
+    }
+    {
+      std::lock_guard<std::mutex> lock(mu_);
+      f_ = &f;
+      count_ = count;
+      next_.store(0);
+      first_ = nullptr;
+      busy_ = workers_.size();
+      ++generation_;
+    }
+    cv_.notify_all();
+    work();
+    std::unique_lock<std::mutex> lock(mu_);
+    done_cv_.wait(lock, [&] { return busy_ == 0; });
+    f_ = nullptr;
+    if (first_) std::rethrow_exception(first_);
+  }
+
+ private:
+  HostPool() : pid_(getpid()) {
+    const unsigned n = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    for (unsigned t = 1; t < n; ++t) workers_.emplace_back([this] { loop(); });
+  }
+  void work() {
+    for (;;) {
+      const size_t i = next_.fetch_add(1);
+      if (i >= count_) break;
+      try {
+        (*f_)(i);
+      } catch (...) {
+        std::lock_guard<std::mutex> lock(err_mu_);
+        if (!first_) first_ = std::current_exception();
+      }
+    }
+  }
+  void loop() {
+    uint64_t seen = 0;
+    for (;;) {
+      {
+        std::unique_lock<std::mutex> lock(mu_);
+        cv_.wait(lock, [&] { return generation_ != seen; });
+        seen = generation_;
+      }
+      work();
+      {
+        std::lock_guard<std::mutex> lock(mu_);
+        if (--busy_ == 0) done_cv_.notify_one();
+      }
+    }
+  }
+  std::vector<std::thread> workers_;
+  std::mutex run_mu_, mu_, err_mu_;
+  std::condition_variable cv_, done_cv_;
+  const std::function<void(size_t)> *f_ = nullptr;
+  size_t count_ = 0, busy_ = 0;
+  std::atomic<size_t> next_{0};
+  uint64_t generation_ = 0;
+  std::exception_ptr first_;
+  pid_t pid_;
+};
+
 template <class F>
 void host_parallel(size_t count, F f) {
-  const size_t nt = std::min<size_t>(count, std::max(1u, std::min(16u, std::thread::hardware_concurrency())));
-  if (nt <= 1) {
-    for (size_t i = 0; i < count; ++i) f(i);
-    return;
-  }
-  std::vector<std::thread> pool;
-  std::atomic<size_t> next(0);
-  std::exception_ptr first;
-  std::mutex mu;
-  for (size_t t = 0; t < nt; ++t)
-    pool.emplace_back([&] {
-      for (;;) {
-        const size_t i = next.fetch_add(1);
-        if (i >= count) break;
-        try {
-          f(i);
-        } catch (...) {
-          std::lock_guard<std::mutex> lock(mu);
-          if (!first) first = std::current_exception();
-        }
-      }
-    });
-  for (auto &t : pool) t.join();
-  if (first) std::rethrow_exception(first);
+  const std::function<void(size_t)> fn = f;
+  HostPool::get().run(count, fn);
 }
 
 // Page-locked staging of the packed transfers, kept per host thread across solves
@@ -457,7 +519,7 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
   const int64_t iter_max = opt.iter_max > 0 ? opt.iter_max : 50;
   const double tol = opt.tolerance;
   std::vector<Mol> mols(nm);
-  int64_t pool_doubles = 0, in_doubles = 0, out_doubles = 0;
+  int64_t pool_doubles = 0, in_doubles = 0, out_doubles = 0, pack_doubles = 0;
   for (size_t b = 0; b < nm; ++b) {
     Mol &M = mols[b];
     M.op = ops[b];
@@ -480,18 +542,19 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
     M.chunks = ceil_div(M.n, (int64_t)kTnRows);
     M.T.assign(M.capc * M.capc, 0.0);
     M.evals.assign(neigen, 0.0);
-    pool_doubles += 2 * M.n * M.capc + M.n + 2 * M.n * M.needmax + M.capc * M.needmax + M.needmax +
-                    M.capc * M.capc + 3 * M.capc + M.capc * M.capc + M.chunks * M.capc * M.capc + 64;
+    pool_doubles += 2 * M.n * M.capc + M.n + 2 * M.n * M.needmax + 3 * M.capc + M.capc * M.capc +
+                    M.chunks * M.capc * M.capc + 64;
     M.off_in = in_doubles;
-    in_doubles += M.capc * M.capc + M.needmax + 2 * M.capc;  // U, lambdas, update lists
+    in_doubles += M.capc * M.needmax + M.needmax + 2 * M.capc + 8;  // U, lambdas, update lists
     M.off_out = out_doubles;
-    out_doubles += std::max(M.n, M.capc * M.capc) + 8;      // diagonal, T blocks, norms, flags
+    out_doubles += M.n + 8;                                           // diagonal
+    pack_doubles += M.capc * M.capc + 8;                              // T blocks or norms
   }
   AllocStreamScope scope(s);
   DeviceBuffer<double> pool(pool_doubles);
-  DeviceBuffer<double> din(in_doubles), dout(out_doubles);
-  double *hbuf = pinned_scratch((size_t)(in_doubles + out_doubles));
-  double *hin = hbuf, *hout = hbuf + in_doubles;
+  DeviceBuffer<double> din(in_doubles), dpack(pack_doubles);
+  double *hbuf = pinned_scratch((size_t)(in_doubles + out_doubles + pack_doubles));
+  double *hin = hbuf, *hout = hbuf + in_doubles, *hpack = hout + out_doubles;
   VGB_CUDA(cudaMemsetAsync(pool.get(), 0, pool_doubles * sizeof(double), s));
   {
     double *p = pool.get();
@@ -502,9 +565,6 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
       M.D = take(M.n);
       M.q = take(M.n * M.needmax);
       M.res = take(M.n * M.needmax);
-      M.Ud = take(M.capc * M.needmax);
-      M.lamd = take(M.needmax);
-      M.cbuf = take(M.capc * M.capc);
       M.norms0 = take(M.capc);
       M.norms = take(M.capc);
       M.h = take(M.capc + M.capc * M.capc);
@@ -545,6 +605,20 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
   DeviceBuffer<int> flags(nm);
   VGB_CUDA(cudaMemsetAsync(flags.get(), 0, nm * sizeof(int), s));
   for (size_t b = 0; b < nm; ++b) mols[b].flag = flags.get() + b;
+  for (Mol &M : mols) {  // the Ritz coefficients are read where the host staged them
+    M.Ud = din.get() + M.off_in;
+    M.lamd = M.Ud + M.capc * M.needmax;
+  }
+  // packs the given blocks back to back: off_pack and the device block of each molecule
+  auto pack = [&](const std::vector<Mol *> &ms, const std::function<int64_t(const Mol &)> &size) {
+    int64_t off = 0;
+    for (Mol *M : ms) {
+      M->off_pack = off;
+      M->cbuf = dpack.get() + off;
+      off += size(*M);
+    }
+    return off;
+  };
 
   // ---- diagonal and unit-vector guesses (setupInitialEigenvectors) ----
   {
@@ -601,6 +675,7 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
     {
       std::vector<GroupedItem> items;
       std::vector<TnReq> tn;
+      const int64_t packed = pack(act, [&](const Mol &M) { return M.ncols * (M.ncols - (it == 0 ? 0 : M.nav)); });
       for (Mol *M : act) {
         M->iterations = it;
         const int64_t old = (it == 0) ? 0 : M->nav, nvec = M->ncols - old;
@@ -613,11 +688,7 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
       matmul_grouped(coef, items, s, &arena);
       mark(0);
       run_tn(tn, s);
-      for (Mol *M : act) {
-        const int64_t old = (it == 0) ? 0 : M->nav, nvec = M->ncols - old;
-        VGB_CUDA(cudaMemcpyAsync(hout + M->off_out, M->cbuf, M->ncols * nvec * sizeof(double),
-                                 cudaMemcpyDeviceToHost, s));
-      }
+      VGB_CUDA(cudaMemcpyAsync(hpack, dpack.get(), packed * sizeof(double), cudaMemcpyDeviceToHost, s));
       std::vector<int> hflags(nm);
       VGB_CUDA(cudaMemcpyAsync(hflags.data(), flags.get(), nm * sizeof(int), cudaMemcpyDeviceToHost, s));
       VGB_CUDA(cudaStreamSynchronize(s));
@@ -626,7 +697,7 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
         if (hflags[b]) fail(BSE_ERR_NUMERICAL, "molecule " + std::to_string(b) + ": Linear dependencies in Gram-Schmidt.");
       for (Mol *M : act) {
         const int64_t old = (it == 0) ? 0 : M->nav, nvec = M->ncols - old;
-        const double *blk = hout + M->off_out;
+        const double *blk = hpack + M->off_pack;
         const int64_t ldT = M->capc;
         for (int64_t c = 0; c < nvec; ++c)
           for (int64_t r = 0; r < M->ncols; ++r) M->T[r + ldT * (old + c)] = blk[r + M->ncols * c];
@@ -659,10 +730,8 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
       std::vector<NnJob> nn;
       std::vector<ColJob> cj;
       std::vector<NormJob> nj;
+      const int64_t packed = pack(act, [](const Mol &M) { return std::min(M.needed, M.size_update); });
       for (Mol *M : act) {
-        const double *U = din.get() + M->off_in, *lam = U + M->capc * M->needmax;
-        VGB_CUDA(cudaMemcpyAsync(M->Ud, U, M->m * M->needed * sizeof(double), cudaMemcpyDeviceToDevice, s));
-        VGB_CUDA(cudaMemcpyAsync(M->lamd, lam, M->needed * sizeof(double), cudaMemcpyDeviceToDevice, s));
         nn.push_back({M->V, M->Ud, M->n, M->m, M->n, M->m, M->needed, M->q, M->n, 1.0, 0.0});
         nn.push_back({M->AV, M->Ud, M->n, M->m, M->n, M->m, M->needed, M->res, M->n, 1.0, 0.0});
         ColJob c;
@@ -671,15 +740,13 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
         cj.push_back(c);
         NormJob w;
         w.A = M->res; w.B = nullptr; w.lda = M->n; w.ldb = M->n; w.n = M->n;
-        w.p = std::min(M->needed, M->size_update); w.out = M->norms;
+        w.p = std::min(M->needed, M->size_update); w.out = M->cbuf;
         nj.push_back(w);
       }
       run_nn(nn, s);
       run_cols(cj, s);
       run_norms(nj, s);
-      for (Mol *M : act)
-        VGB_CUDA(cudaMemcpyAsync(hout + M->off_out, M->norms, std::min(M->needed, M->size_update) * sizeof(double),
-                                 cudaMemcpyDeviceToHost, s));
+      VGB_CUDA(cudaMemcpyAsync(hpack, dpack.get(), packed * sizeof(double), cudaMemcpyDeviceToHost, s));
       VGB_CUDA(cudaStreamSynchronize(s));
     }
     mark(3);
@@ -688,7 +755,7 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
     std::vector<Mol *> ext;
     for (Mol *M : act) {
       const int64_t nn_check = std::min(M->needed, M->size_update);
-      const double *resn = hout + M->off_out;
+      const double *resn = hpack + M->off_pack;
       std::vector<char> conv(M->size_update, 0);
       for (int64_t j = 0; j < M->size_update; ++j) conv[j] = (j < nn_check) ? (resn[j] < tol) : 0;
       bool converged = true;
@@ -709,7 +776,7 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
         if (!conv[j] && j < M->needed) { M->upd.push_back(j); M->upd_lam.push_back(M->lam[j]); }
       M->nupdate = (int64_t)M->upd.size();
       VGB_REQUIRE(M->ncols + M->nupdate <= M->capc, "DavidsonSolver: search space capacity exceeded");
-      double *dst = hin + M->off_in;  // [cols as doubles | lambdas]
+      double *dst = hin + M->dpr_in();  // [cols as doubles | lambdas]
       for (int64_t k = 0; k < M->nupdate; ++k) {
         dst[k] = (double)M->upd[k];
         dst[M->capc + k] = M->upd_lam[k];
@@ -727,7 +794,7 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
       for (Mol *M : ext) {
         ColJob c;
         c.kind = 3; c.A = M->V + M->ncols * M->n; c.B = M->res; c.D = M->D;
-        c.v = din.get() + M->off_in + M->capc; c.cols = din.get() + M->off_in;
+        c.v = din.get() + M->dpr_in() + M->capc; c.cols = din.get() + M->dpr_in();
         c.lda = M->n; c.ldb = M->n; c.n = M->n; c.p = M->nupdate;
         cj.push_back(c);
         NormJob w;
@@ -825,18 +892,16 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
       run_cols(cav, s);
       run_cols(back, s);
       std::vector<TnReq> tn;
+      const int64_t packed = pack(rst, [](const Mol &M) { return M.restart_size * M.restart_size; });
       for (Mol *M : rst) tn.push_back({M, M->V, M->AV, M->restart_size, M->restart_size, M->cbuf, M->restart_size});
       run_tn(tn, s);
-      for (Mol *M : rst) {
-        const int64_t rs = M->restart_size;
-        VGB_CUDA(cudaMemcpyAsync(hout + M->off_out, M->cbuf, rs * rs * sizeof(double), cudaMemcpyDeviceToHost, s));
-      }
+      VGB_CUDA(cudaMemcpyAsync(hpack, dpack.get(), packed * sizeof(double), cudaMemcpyDeviceToHost, s));
       VGB_CUDA(cudaStreamSynchronize(s));
       for (Mol *M : rst) {
         const int64_t rs = M->restart_size;
         std::fill(M->T.begin(), M->T.end(), 0.0);
         for (int64_t c = 0; c < rs; ++c)
-          for (int64_t r = 0; r < rs; ++r) M->T[r + M->capc * c] = hout[M->off_out + r + rs * c];
+          for (int64_t r = 0; r < rs; ++r) M->T[r + M->capc * c] = hpack[M->off_pack + r + rs * c];
         M->ncols = rs + M->nupdate;
         M->nav = rs;
       }
