@@ -35,7 +35,8 @@ namespace vgb {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kJobs = 96;        // jobs per grouped launch (kernel parameter space)
+constexpr int kJobs = 320;       // jobs per grouped launch: a 256-molecule step in one launch
+                                 // (the job list travels in the 32 KB kernel-parameter space)
 constexpr int kTnRows = 512;     // rows per block of a transposed product
 constexpr int kTile = 32;        // rows per shared-memory tile
 constexpr int kTileLd = kTile + 1;
@@ -212,13 +213,16 @@ struct GsJob {
   int check;
   int *flag;
 };
-__global__ void __launch_bounds__(kThreads, 2) gs_kernel(const __grid_constant__ Group<GsJob> g) {
+// kGsThreads threads per molecule and rows unrolled by 4: a pass over the rows of a column is a
+// few dependent loads per thread (the kernel is bound by load latency, not by bandwidth)
+constexpr int kGsThreads = 512;
+__global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(const __grid_constant__ Group<GsJob> g) {
   const GsJob q = g.j[blockIdx.x];
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   constexpr int kMaxRange = 256;
   constexpr int kReg = 8;  // dots accumulated per pass over the rows
   __shared__ double h[kMaxRange];
-  __shared__ double red[kThreads / 32][kReg];
+  __shared__ double red[kGsThreads / 32][kReg];
   __shared__ double nrm;
   const double *M = q.Q + q.nstart * q.n;
   for (int64_t j = q.nstart + 1; j < q.ncols; ++j) {
@@ -231,7 +235,8 @@ __global__ void __launch_bounds__(kThreads, 2) gs_kernel(const __grid_constant__
       double acc[kReg];
 #pragma unroll
       for (int l = 0; l < kReg; ++l) acc[l] = 0.0;
-      for (int64_t i = threadIdx.x; i < q.n; i += kThreads) {
+#pragma unroll 4
+      for (int64_t i = threadIdx.x; i < q.n; i += kGsThreads) {
         const double x = qj[i];
 #pragma unroll
         for (int l = 0; l < kReg; ++l)
@@ -246,13 +251,14 @@ __global__ void __launch_bounds__(kThreads, 2) gs_kernel(const __grid_constant__
       __syncthreads();
       if (threadIdx.x < lc) {
         double t = 0.0;
-        for (int w = 0; w < kThreads / 32; ++w) t += red[w][threadIdx.x];
+        for (int w = 0; w < kGsThreads / 32; ++w) t += red[w][threadIdx.x];
         h[l0 + threadIdx.x] = t;
       }
       __syncthreads();
     }
     double nacc = 0.0;
-    for (int64_t i = threadIdx.x; i < q.n; i += kThreads) {
+#pragma unroll 4
+    for (int64_t i = threadIdx.x; i < q.n; i += kGsThreads) {
       double s = 0.0;
       for (int64_t l = 0; l < range; ++l) s = fma(M[l * q.n + i], h[l], s);
       const double v = qj[i] - s;
@@ -264,14 +270,16 @@ __global__ void __launch_bounds__(kThreads, 2) gs_kernel(const __grid_constant__
     __syncthreads();
     if (threadIdx.x == 0) {
       double t = 0.0;
-      for (int w = 0; w < kThreads / 32; ++w) t += red[w][0];
+      for (int w = 0; w < kGsThreads / 32; ++w) t += red[w][0];
       nrm = sqrt(t);
       if (q.check && !(nrm > 1e-12 * q.norms0[range])) *q.flag = 1;
     }
     __syncthreads();
     const double nv = nrm;
-    if (nv > 0.0)  // Eigen's normalize leaves a zero column unchanged
-      for (int64_t i = threadIdx.x; i < q.n; i += kThreads) qj[i] /= nv;
+    if (nv > 0.0) {  // Eigen's normalize leaves a zero column unchanged
+#pragma unroll 4
+      for (int64_t i = threadIdx.x; i < q.n; i += kGsThreads) qj[i] /= nv;
+    }
     __syncthreads();
   }
 }
@@ -288,15 +296,21 @@ __global__ void unit_kernel(const __grid_constant__ Group<UnitJob> g) {
   for (int64_t j = threadIdx.x; j < q.count; j += blockDim.x) q.V[(int64_t)q.rows[j] + q.ldv * j] = 1.0;
 }
 
+static_assert(sizeof(Group<TnJob>) <= 32000 && sizeof(Group<TnReduceJob>) <= 32000 &&
+                  sizeof(Group<NnJob>) <= 32000 && sizeof(Group<NormJob>) <= 32000 &&
+                  sizeof(Group<ColJob>) <= 32000 && sizeof(Group<GsJob>) <= 32000 &&
+                  sizeof(Group<UnitJob>) <= 32000,
+              "grouped job lists must fit the kernel-parameter space");
+
 template <class Job, class Kernel>
 void launch_jobs(const std::vector<Job> &jobs, Kernel kernel, unsigned bx, bool grid_x_is_job,
-                 cudaStream_t s) {
+                 cudaStream_t s, int threads = kThreads) {
   std::unique_ptr<Group<Job>> g(new Group<Job>());
   for (size_t i = 0; i < jobs.size();) {
     g->n = 0;
     for (; i < jobs.size() && g->n < kJobs; ++i) g->j[g->n++] = jobs[i];
     const dim3 grid = grid_x_is_job ? dim3((unsigned)g->n) : dim3(bx, (unsigned)g->n);
-    kernel<<<grid, kThreads, 0, s>>>(*g);
+    kernel<<<grid, threads, 0, s>>>(*g);
     VGB_LAUNCH_CHECK();
   }
 }
@@ -542,7 +556,7 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
     M.chunks = ceil_div(M.n, (int64_t)kTnRows);
     M.T.assign(M.capc * M.capc, 0.0);
     M.evals.assign(neigen, 0.0);
-    pool_doubles += 2 * M.n * M.capc + M.n + 2 * M.n * M.needmax + 3 * M.capc + M.capc * M.capc +
+    pool_doubles += 2 * M.n * M.capc + 2 * M.n * M.needmax + 3 * M.capc + M.capc * M.capc +
                     M.chunks * M.capc * M.capc + 64;
     M.off_in = in_doubles;
     in_doubles += M.capc * M.needmax + M.needmax + 2 * M.capc + 8;  // U, lambdas, update lists
@@ -562,7 +576,6 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
       auto take = [&](int64_t cnt) { double *r = p; p += cnt; return r; };
       M.V = take(M.n * M.capc);
       M.AV = take(M.n * M.capc);
-      M.D = take(M.n);
       M.q = take(M.n * M.needmax);
       M.res = take(M.n * M.needmax);
       M.norms0 = take(M.capc);
@@ -622,10 +635,26 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
 
   // ---- diagonal and unit-vector guesses (setupInitialEigenvectors) ----
   {
+    // kept on the operator: a later solve with the same coefficients reads it again
     std::vector<BseOperator *> dops;
     std::vector<double *> dd;
-    for (Mol &M : mols) { dops.push_back(M.op); dd.push_back(M.D); }
+    for (Mol &M : mols) {
+      BseOperator &op = *M.op;
+      const bool same = op.diag_valid && op.diag_coef.cqp == coef.cqp && op.diag_coef.cx == coef.cx &&
+                        op.diag_coef.cd == coef.cd && op.diag_coef.cd2 == coef.cd2;
+      if (!same && std::find(dops.begin(), dops.end(), &op) == dops.end()) {
+        op.diag_valid = false;
+        op.diag_cache.resize(op.dim);
+        dops.push_back(&op);
+        dd.push_back(op.diag_cache.get());
+      }
+    }
     diagonal_grouped(coef, dops, dd, s);
+    for (BseOperator *op : dops) {
+      op->diag_coef = coef;
+      op->diag_valid = true;
+    }
+    for (Mol &M : mols) M.D = M.op->diag_cache.get();
   }
   for (Mol &M : mols)
     VGB_CUDA(cudaMemcpyAsync(hout + M.off_out, M.D, M.n * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -849,7 +878,7 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
         run_nn(nn, s);
         run_norms(nj, s);
         run_cols(sc, s);
-        launch_jobs(gs, gs_kernel, 1, true, s);
+        launch_jobs(gs, gs_kernel, 1, true, s, kGsThreads);
       }
       for (Mol *M : ext) M->ncols += M->nupdate;
     }

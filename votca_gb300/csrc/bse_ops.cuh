@@ -92,6 +92,10 @@ class BseOperator {
   int64_t m_v0 = 0, m_c0 = 0, n_v0 = 0, n_c0 = 0, msize = 0, nsize = 0;
   // scratch
   DeviceBuffer<double> S, Z, Xc, Ttmp;
+  // diagonal of the last coefficient set a batched solve used (the operator is immutable)
+  DeviceBuffer<double> diag_cache;
+  Coef diag_coef;
+  bool diag_valid = false;
   GemmWorkspace ws;
   int64_t s_budget_bytes = 4LL << 30;
   std::unique_ptr<MixedEngine> mixed;
