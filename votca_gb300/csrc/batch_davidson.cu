@@ -761,11 +761,14 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
       std::vector<NormJob> nj;
       const int64_t packed = pack(act, [](const Mol &M) { return std::min(M.needed, M.size_update); });
       for (Mol *M : act) {
-        nn.push_back({M->V, M->Ud, M->n, M->m, M->n, M->m, M->needed, M->q, M->n, 1.0, 0.0});
-        nn.push_back({M->AV, M->Ud, M->n, M->m, M->n, M->m, M->needed, M->res, M->n, 1.0, 0.0});
+        // only the first min(needed, size_update) pairs enter the convergence check and the
+        // corrections; the Ritz vectors a restart keeps are formed there
+        const int64_t pr = std::min(M->needed, M->size_update);
+        nn.push_back({M->V, M->Ud, M->n, M->m, M->n, M->m, pr, M->q, M->n, 1.0, 0.0});
+        nn.push_back({M->AV, M->Ud, M->n, M->m, M->n, M->m, pr, M->res, M->n, 1.0, 0.0});
         ColJob c;
         c.kind = 1; c.A = M->res; c.B = M->q; c.D = nullptr; c.v = M->lamd; c.cols = nullptr;
-        c.lda = M->n; c.ldb = M->n; c.n = M->n; c.p = M->needed;
+        c.lda = M->n; c.ldb = M->n; c.n = M->n; c.p = pr;
         cj.push_back(c);
         NormJob w;
         w.A = M->res; w.B = nullptr; w.lda = M->n; w.ldb = M->n; w.n = M->n;
@@ -889,11 +892,13 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
       if (M->ncols > M->max_space) rst.push_back(M);
     if (!rst.empty()) {
       std::vector<ColJob> keep, back, cq;
-      std::vector<NnJob> nn;
+      std::vector<NnJob> nn, qn;
       std::vector<ColJob> cav;
       for (Mol *M : rst) {
         const int64_t rs = M->restart_size, nv = M->nupdate;
         VGB_REQUIRE(rs <= M->needed, "DavidsonSolver: restart size exceeds the Ritz pairs");
+        // the kept Ritz vectors q = V[:, :m] U[:, :rs] (V's first m columns are unchanged)
+        qn.push_back({M->V, M->Ud, M->n, M->m, M->n, M->m, rs, M->q, M->n, 1.0, 0.0});
         // scratch: res holds the kept columns (nv <= needmax), q is copied into V
         VGB_REQUIRE(nv <= M->needmax, "batched Davidson: restart scratch too small");
         ColJob k;
@@ -915,6 +920,7 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
         bk.cols = nullptr; bk.lda = M->n; bk.ldb = M->n; bk.n = M->n; bk.p = nv;
         back.push_back(bk);
       }
+      run_nn(qn, s);
       run_cols(keep, s);
       run_cols(cq, s);
       run_nn(nn, s);
