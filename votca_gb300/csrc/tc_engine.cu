@@ -597,9 +597,12 @@ void MixedEngine::apply_dense_grouped(const Coef &c, const std::vector<GroupedIt
     j.hi = m.Xd.hi.get(); j.lo = m.Xd.lo.get(); j.ldo = m.Kd;
   }
   split_grouped(jobs, s);
-  // partials [split][j][I] of H X, then Y[I + j ldy] (+)= sum (the dense H holds Hx and Hd)
+  // Y[I + j ldy] (+)= (H X)(I, j).  With BN <= 64 a CTA runs all K splits of its tile and sums
+  // their FP32 chains in FP64 registers, writing Y directly; otherwise FP32 partials
+  // [split][j][I] are summed in FP64 by a reduction launch (the same sums in the same order).
   std::vector<TcProblem> pr(n);
   std::vector<int> ks(n, 0);
+  std::vector<char> direct(n, 0);
   GemmBuckets b;
   for (size_t i = 0; i < n; ++i) {
     Impl &m = *eng[i];
@@ -609,21 +612,34 @@ void MixedEngine::apply_dense_grouped(const Coef &c, const std::vector<GroupedIt
     q.A = m.mat(m.Hdense.hi.get(), m.Hdense.lo.get(), m.dim, m.Kd, 128, bk_for(bn));
     q.B = m.mat(m.Xd.hi.get(), m.Xd.lo.get(), (int64_t)m.Xd.hi.count / m.Kd, m.Kd, bn, bk_for(bn));
     q.shape.M = m.dim; q.shape.N = it.k; q.shape.K = m.Kd; q.shape.products = g_products;
-    q.shape.ksplit = pick_ksplit(ceil_div(m.dim, 128) * ceil_div(it.k, bn), m.Kd, g_dense_chain);
-    m.part.resize((size_t)q.shape.ksplit * m.dim * it.k);
-    q.epi.kind = TcEpilogue::STORE_F32;
-    q.epi.rd = m.dim; q.epi.ro2 = 1; q.epi.rlim = m.dim;
-    q.epi.cd = it.k; q.epi.co2 = m.dim; q.epi.clim = it.k;
-    q.epi.so = m.dim * it.k;
-    q.epi.out_f32 = m.part.get();
+    direct[i] = (g_kacc && bn <= 64) ? 1 : 0;
+    if (direct[i]) {
+      // in-CTA accumulation adds no parallelism: only the chain bound sets the splits
+      q.shape.ksplit = (int)ceil_div(m.Kd, g_dense_chain);
+      q.shape.kacc = true;
+      q.epi.kind = TcEpilogue::AXPBY_F64;
+      q.epi.rd = m.dim; q.epi.ro2 = 1; q.epi.rlim = m.dim;
+      q.epi.cd = it.k; q.epi.co2 = it.ldy; q.epi.clim = it.k;
+      q.epi.out_f64 = it.Y; q.epi.alpha = 1.0; q.epi.beta = accumulate ? 1.0 : 0.0;
+    } else {
+      q.shape.ksplit = pick_ksplit(ceil_div(m.dim, 128) * ceil_div(it.k, bn), m.Kd, g_dense_chain);
+      m.part.resize((size_t)q.shape.ksplit * m.dim * it.k);
+      q.epi.kind = TcEpilogue::STORE_F32;
+      q.epi.rd = m.dim; q.epi.ro2 = 1; q.epi.rlim = m.dim;
+      q.epi.cd = it.k; q.epi.co2 = m.dim; q.epi.clim = it.k;
+      q.epi.so = m.dim * it.k;
+      q.epi.out_f32 = m.part.get();
+    }
     b.add(&q, bn, i);
   }
   b.run(err, s, ks);
-  std::vector<ReduceJob> rj(n);
+  std::vector<ReduceJob> rj;
   for (size_t i = 0; i < n; ++i) {
+    if (direct[i]) continue;
     Impl &m = *eng[i];
     const GroupedItem &it = items[i];
-    ReduceJob &r = rj[i];
+    rj.emplace_back();
+    ReduceJob &r = rj.back();
     r.part = m.part.get(); r.M = it.k; r.N = m.dim; r.ksplit = ks[i];
     r.epi.kind = TcEpilogue::AXPBY_F64;
     r.epi.rd = it.k; r.epi.ro2 = it.ldy; r.epi.rlim = it.k;

@@ -139,14 +139,6 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// Next job of a CTA: the rest of the current run of `run` jobs, then the run gridDim.x
-// items further on.
-__device__ __forceinline__ int64_t next_job(int64_t t, int64_t &u, int64_t run) {
-  if (++u < run) return t + 1;
-  u = 0;
-  return t + 1 + (int64_t)(gridDim.x - 1) * run;
-}
-
 struct TileCoord {
   int64_t m, n, s, b;
 };
@@ -187,13 +179,21 @@ __device__ __forceinline__ void epi_store(const TcEpilogue &e, int64_t off, floa
   }
 }
 
+// Work items of the persistent kernel: an item is one tile job, or, for a problem with in-CTA K
+// accumulation (kacc), the ksplit consecutive jobs of one output tile; items are strided over
+// the CTAs and a CTA runs the jobs of its item in order.
+__host__ __device__ __forceinline__ int64_t item_count(const KParams &p) {
+  return p.kacc ? p.ntiles / p.ksplit : p.ntiles;
+}
+__device__ __forceinline__ int64_t item_len(const KParams &p) { return p.kacc ? p.ksplit : 1; }
+
 // Problem sources of the persistent kernel: one problem, or a group of up to
-// kGroupMax problems (same tile shape) whose tile lists are concatenated.  Both
+// kGroupMax problems (same tile shape) whose item lists are concatenated.  Both
 // live in the kernel parameter space, so every tensor map is a __grid_constant__.
 struct SingleSrc {
   CUtensorMap maps[4];  // A hi, A lo, B hi, B lo
   KParams p;
-  __device__ __forceinline__ int64_t total() const { return p.ntiles; }
+  __device__ __forceinline__ int64_t total() const { return item_count(p); }
   __device__ __forceinline__ int locate(int64_t t, int64_t &local, int &) const {
     local = t;
     return 0;
@@ -201,15 +201,13 @@ struct SingleSrc {
   __device__ __forceinline__ const KParams &params(int) const { return p; }
   __device__ __forceinline__ const CUtensorMap *map(int, int w) const { return &maps[w]; }
   __device__ __forceinline__ int *err() const { return p.err; }
-  // jobs run by a CTA in runs of run() consecutive indices (all K splits of a tile when kacc)
-  __device__ __forceinline__ int64_t run() const { return p.kacc ? p.ksplit : 1; }
 };
 
 constexpr int kGroupMax = 32;
 struct GroupSrc {
   CUtensorMap maps[4 * kGroupMax];
   KParams p[kGroupMax];
-  int64_t begin[kGroupMax + 1];  // first global tile of each problem; begin[n] = total
+  int64_t begin[kGroupMax + 1];  // first global item of each problem; begin[n] = total
   int n;
   int *err_ptr;
   __device__ __forceinline__ int64_t total() const { return begin[n]; }
@@ -222,7 +220,6 @@ struct GroupSrc {
   __device__ __forceinline__ const KParams &params(int i) const { return p[i]; }
   __device__ __forceinline__ const CUtensorMap *map(int i, int w) const { return &maps[4 * i + w]; }
   __device__ __forceinline__ int *err() const { return err_ptr; }
-  __device__ __forceinline__ int64_t run() const { return 1; }
 };
 static_assert(sizeof(GroupSrc) <= 32000, "grouped GEMM parameters exceed the kernel parameter space");
 
@@ -262,8 +259,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
   fence_after();
   const uint32_t tmem_base = *tmem_slot;
   int *const err = src.err();
-  const int64_t ntiles = src.total();
-  const int64_t run = src.run();  // job t = item * run + u, u < run, items strided over CTAs
+  const int64_t nitems = src.total();  // item R: jobs li * len + u, u < len (see item_len)
 
   if (warp == 0) {
     if (lane == 0) {
@@ -271,26 +267,29 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
       int stage = 0;
       uint32_t phase = 0;
       int hint = 0;
-      for (int64_t t = blockIdx.x * run, u = 0; t < ntiles; t = next_job(t, u, run)) {
-        int64_t lt;
-        const int pi = src.locate(t, lt, hint);
+      for (int64_t R = blockIdx.x; R < nitems; R += gridDim.x) {
+        int64_t li;
+        const int pi = src.locate(R, li, hint);
         const KParams p = src.params(pi);  // registers: no reloads behind the stores
-        const TileCoord tc = decode(p, lt);
-        const int kchunks = (int)(p.K / BK);
-        const int kb = (int)tc.s * p.kc_per, ke = min(kchunks, kb + p.kc_per);
-        const int ya = (int)(tc.b * p.a_brows + tc.m * BM);
-        const int yb = (int)(tc.b * p.b_brows + tc.n * BN);
+        const int64_t len = item_len(p);
         const CUtensorMap *mAhi = src.map(pi, 0), *mAlo = src.map(pi, 1);
         const CUtensorMap *mBhi = src.map(pi, 2), *mBlo = src.map(pi, 3);
-        for (int kc = kb; kc < ke; ++kc) {
-          if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, err, 1)) goto producer_done;
-          uint8_t *st = smem + stage * C::STAGE_BYTES;
-          mbar_expect_tx(&full[stage], (uint32_t)C::STAGE_BYTES);
-          tma_load_2d(smem_u32(st), mAhi, &full[stage], kc * BK, ya);
-          tma_load_2d(smem_u32(st + C::A_BYTES), mAlo, &full[stage], kc * BK, ya);
-          tma_load_2d(smem_u32(st + 2 * C::A_BYTES), mBhi, &full[stage], kc * BK, yb);
-          tma_load_2d(smem_u32(st + 2 * C::A_BYTES + C::B_BYTES), mBlo, &full[stage], kc * BK, yb);
-          if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
+        for (int64_t u = 0; u < len; ++u) {
+          const TileCoord tc = decode(p, li * len + u);
+          const int kchunks = (int)(p.K / BK);
+          const int kb = (int)tc.s * p.kc_per, ke = min(kchunks, kb + p.kc_per);
+          const int ya = (int)(tc.b * p.a_brows + tc.m * BM);
+          const int yb = (int)(tc.b * p.b_brows + tc.n * BN);
+          for (int kc = kb; kc < ke; ++kc) {
+            if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, err, 1)) goto producer_done;
+            uint8_t *st = smem + stage * C::STAGE_BYTES;
+            mbar_expect_tx(&full[stage], (uint32_t)C::STAGE_BYTES);
+            tma_load_2d(smem_u32(st), mAhi, &full[stage], kc * BK, ya);
+            tma_load_2d(smem_u32(st + C::A_BYTES), mAlo, &full[stage], kc * BK, ya);
+            tma_load_2d(smem_u32(st + 2 * C::A_BYTES), mBhi, &full[stage], kc * BK, yb);
+            tma_load_2d(smem_u32(st + 2 * C::A_BYTES + C::B_BYTES), mBlo, &full[stage], kc * BK, yb);
+            if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
+          }
         }
       }
       // drain: wait until the MMA warp has consumed every stage issued (bounded)
@@ -312,42 +311,44 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
       int buf = 0;
       uint32_t aphase = 0;
       int hint = 0;
-      for (int64_t t = blockIdx.x * run, u = 0; t < ntiles; t = next_job(t, u, run)) {
-        int64_t lt;
-        const KParams p = src.params(src.locate(t, lt, hint));
-        const TileCoord tc = decode(p, lt);
-        const int kchunks = (int)(p.K / BK);
-        const int kb = (int)tc.s * p.kc_per, ke = min(kchunks, kb + p.kc_per);
-        if (!mbar_wait(&acce[buf], aphase ^ 1, abort_flag, err, 2)) break;
-        fence_after();
-        const uint32_t d_tmem = tmem_base + (uint32_t)(buf * BN);
-        bool ok = true;
-        for (int kc = kb; kc < ke; ++kc) {
-          if (!mbar_wait(&full[stage], phase, abort_flag, err, 3)) { ok = false; break; }
+      for (int64_t R = blockIdx.x; R < nitems; R += gridDim.x) {
+        int64_t li;
+        const KParams p = src.params(src.locate(R, li, hint));
+        const int64_t len = item_len(p);
+        for (int64_t u = 0; u < len; ++u) {
+          const TileCoord tc = decode(p, li * len + u);
+          const int kchunks = (int)(p.K / BK);
+          const int kb = (int)tc.s * p.kc_per, ke = min(kchunks, kb + p.kc_per);
+          if (!mbar_wait(&acce[buf], aphase ^ 1, abort_flag, err, 2)) goto mma_done;
           fence_after();
-          const uint32_t st = smem_u32(smem + stage * C::STAGE_BYTES);
-          const uint32_t ahi = st, alo = st + C::A_BYTES;
-          const uint32_t bhi = st + 2 * C::A_BYTES, blo = bhi + C::B_BYTES;
+          const uint32_t d_tmem = tmem_base + (uint32_t)(buf * BN);
+          for (int kc = kb; kc < ke; ++kc) {
+            if (!mbar_wait(&full[stage], phase, abort_flag, err, 3)) goto mma_done;
+            fence_after();
+            const uint32_t st = smem_u32(smem + stage * C::STAGE_BYTES);
+            const uint32_t ahi = st, alo = st + C::A_BYTES;
+            const uint32_t bhi = st + 2 * C::A_BYTES, blo = bhi + C::B_BYTES;
 #pragma unroll
-          for (int kk = 0; kk < BK / 16; ++kk) {
-            const uint32_t koff = kk * 32;  // 16 bf16 = 32 bytes along K inside the swizzle row
-            const uint32_t acc0 = (kc > kb || kk > 0) ? 1u : 0u;
-            const uint64_t dah = sdesc(ahi + koff, C::SBO, C::LAYOUT);
-            const uint64_t dal = sdesc(alo + koff, C::SBO, C::LAYOUT);
-            const uint64_t dbh = sdesc(bhi + koff, C::SBO, C::LAYOUT);
-            const uint64_t dbl = sdesc(blo + koff, C::SBO, C::LAYOUT);
-            mma_bf16(d_tmem, dah, dbh, idesc, acc0);
-            mma_bf16(d_tmem, dah, dbl, idesc, 1u);
-            mma_bf16(d_tmem, dal, dbh, idesc, 1u);
-            if (p.products == 4) mma_bf16(d_tmem, dal, dbl, idesc, 1u);
+            for (int kk = 0; kk < BK / 16; ++kk) {
+              const uint32_t koff = kk * 32;  // 16 bf16 = 32 bytes along K inside the swizzle row
+              const uint32_t acc0 = (kc > kb || kk > 0) ? 1u : 0u;
+              const uint64_t dah = sdesc(ahi + koff, C::SBO, C::LAYOUT);
+              const uint64_t dal = sdesc(alo + koff, C::SBO, C::LAYOUT);
+              const uint64_t dbh = sdesc(bhi + koff, C::SBO, C::LAYOUT);
+              const uint64_t dbl = sdesc(blo + koff, C::SBO, C::LAYOUT);
+              mma_bf16(d_tmem, dah, dbh, idesc, acc0);
+              mma_bf16(d_tmem, dah, dbl, idesc, 1u);
+              mma_bf16(d_tmem, dal, dbh, idesc, 1u);
+              if (p.products == 4) mma_bf16(d_tmem, dal, dbl, idesc, 1u);
+            }
+            mma_commit(&empty[stage]);  // frees the smem stage when these MMAs complete
+            if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
           }
-          mma_commit(&empty[stage]);  // frees the smem stage when these MMAs complete
-          if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
+          mma_commit(&accf[buf]);  // accumulator ready for the epilogue
+          if (++buf == 2) { buf = 0; aphase ^= 1; }
         }
-        if (!ok) break;
-        mma_commit(&accf[buf]);  // accumulator ready for the epilogue
-        if (++buf == 2) { buf = 0; aphase ^= 1; }
       }
+    mma_done:;
     }
   } else {
     // ---------------- epilogue warps ----------------
@@ -364,13 +365,15 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
     int buf = 0;
     uint32_t aphase = 0;
     int hint = 0;
-    for (int64_t t = blockIdx.x * run, u = 0; t < ntiles; t = next_job(t, u, run)) {
-      int64_t lt;
+    for (int64_t R = blockIdx.x; R < nitems; R += gridDim.x) {
+      int64_t li;
       // a register copy: the stores below cannot alias it, so nothing is reloaded per element
-      const KParams p = src.params(src.locate(t, lt, hint));
+      const KParams p = src.params(src.locate(R, li, hint));
       const TcEpilogue &e = p.epi;
-      const TileCoord tc = decode(p, lt);
-      if (!mbar_wait(&accf[buf], aphase, abort_flag, err, 4)) break;
+      const int64_t len = item_len(p);
+      for (int64_t u = 0; u < len; ++u) {
+      const TileCoord tc = decode(p, li * len + u);
+      if (!mbar_wait(&accf[buf], aphase, abort_flag, err, 4)) goto epi_done;
       fence_after();
       const int64_t i = tc.m * BM + q * 32 + lane;
       const bool row_ok = i < p.M && (i % e.rd) < e.rlim;
@@ -461,7 +464,9 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
       __syncwarp();
       if (lane == 0) mbar_arrive(&acce[buf]);
       if (++buf == 2) { buf = 0; aphase ^= 1; }
+      }
     }
+  epi_done:;
   }
   fence_before();
   __syncthreads();
@@ -693,7 +698,7 @@ int tc_gemm(const TcMat &A, const TcMat &B, const TcShape &sh, const TcEpilogue 
   src.maps[2] = B.map_hi;
   src.maps[3] = B.map_lo;
   src.p = p;
-  launch_any(bn, A.bk, src, p.ntiles, s);
+  launch_any(bn, A.bk, src, item_count(p), s);
   return p.ksplit;
 }
 
@@ -708,7 +713,6 @@ void tc_gemm_grouped(const std::vector<const TcProblem *> &probs, int bn, int *e
     int64_t total = 0;
     for (; i < probs.size() && src->n < kGroupMax; ++i) {
       const TcProblem &q = *probs[i];
-      VGB_REQUIRE(!q.shape.kacc, "tc_gemm_grouped: in-CTA K accumulation is not grouped");
       const KParams p = make_params(q.A, q.B, q.shape, q.epi, bn, err);
       if (ksplit_out) ksplit_out[i] = p.ksplit;
       if (p.ntiles == 0) continue;
@@ -721,7 +725,7 @@ void tc_gemm_grouped(const std::vector<const TcProblem *> &probs, int bn, int *e
       src->maps[4 * g + 3] = q.B.map_lo;
       src->p[g] = p;
       src->begin[g] = total;
-      total += p.ntiles;
+      total += item_count(p);
     }
     if (src->n == 0) continue;
     src->begin[src->n] = total;
