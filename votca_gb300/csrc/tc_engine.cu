@@ -15,6 +15,7 @@
 //   S    [(j, c1)][Kg]         sum_c M(c1,c,P) X_j(v,c)       (Hd intermediate)
 //   U    [(j, v1)][Kg]         sum_c X_j(v,c) M(v1,c,P)       (Hd2 intermediate)
 //   Zs   [j][Kn]               sum_I M(I,P) X_j(I)            (Hx intermediate)
+#include <algorithm>
 #include "tc_engine.cuh"
 
 #include <cstdlib>
@@ -604,7 +605,12 @@ void MixedEngine::apply_dense_grouped(const Coef &c, const std::vector<GroupedIt
   std::vector<int> ks(n, 0);
   std::vector<char> direct(n, 0);
   GemmBuckets b;
-  for (size_t i = 0; i < n; ++i) {
+  // largest operators first: their long work items start early and the small ones fill the
+  // tail of each launch
+  std::vector<size_t> order(n);
+  for (size_t i = 0; i < n; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return eng[x]->dim > eng[y]->dim; });
+  for (size_t i : order) {
     Impl &m = *eng[i];
     const GroupedItem &it = items[i];
     const int bn = pick_bn(it.k);
