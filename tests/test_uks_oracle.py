@@ -119,3 +119,29 @@ def test_dense_full_bse_roots():
         np.testing.assert_allclose(H @ v, lam[j] * v, atol=1e-10)
         assert abs(X[:, j] @ X[:, j] - Y[:, j] @ Y[:, j] - 1.0) < 1e-12
         assert X[np.argmax(np.abs(X[:, j])), j] > 0
+
+
+def test_exciton_weights_uks():
+    """PrintWeightsUKS arithmetic (bse_uks.cc:520-595) on hand-made vectors (host only)."""
+    from votca_gb300.bse_operator_uks import BSEOperatorUKS_Options, exciton_weights_uks
+
+    opt = BSEOperatorUKS_Options(homo_alpha=3, homo_beta=2, rpamin=0, qpmin=0, vmin=1, cmax=6)
+    na, nb = 3 * 3, 2 * 4  # alpha: v 1..3, c 4..6; beta: v 1..2, c 3..6
+    X = np.zeros((na + nb, 2))
+    X[1 * 3 + 2, 0] = np.sqrt(0.6)        # alpha (v=1, c=2): level 2 -> level 6
+    X[na + 0 * 4 + 1, 0] = np.sqrt(0.3)   # beta  (v=0, c=1): level 1 -> level 4
+    X[na + 1 * 4 + 3, 0] = np.sqrt(0.1)
+    X[0, 1] = 1.0
+    Y = np.zeros_like(X)
+    Y[0, 1] = np.sqrt(0.2)
+    r = exciton_weights_uks(opt, X, min_print_weight=0.2)
+    assert abs(r[0]["alpha_weight"] - 0.6) < 1e-15 and abs(r[0]["beta_weight"] - 0.4) < 1e-15
+    top = r[0]["contributions"]
+    assert [(t.is_alpha, t.v, t.c) for t in top] == [(True, 1, 2), (False, 0, 1)]
+    assert (top[0].homo_minus, top[0].lumo_plus) == (3 - 2, 2)   # HOMO-1 -> LUMO+2 (alpha)
+    assert (top[1].homo_minus, top[1].lumo_plus) == (2 - 1, 1)   # HOMO-1 -> LUMO+1 (beta)
+    full = exciton_weights_uks(opt, X, Y, min_print_weight=0.5)
+    assert abs(full[1]["alpha_weight"] - 0.8) < 1e-15
+    assert [(t.v, t.c) for t in full[1]["contributions"]] == [(0, 0)]
+    many = exciton_weights_uks(opt, np.ones((na + nb, 1)) * 0.9, min_print_weight=0.5)
+    assert len(many[0]["contributions"]) == 8 and many[0]["more_above_threshold"] == na + nb - 8

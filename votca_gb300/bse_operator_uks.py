@@ -13,6 +13,9 @@ the solve drivers of BSE_UKS (xtp/src/libxtp/gwbse/bse_uks.cc).
   solve_excitons_uks_tda     BSE_UKS::Solve_excitons_uks_TDA, bse_uks.cc:218-231
   solve_excitons_uks_btda    BSE_UKS::Solve_excitons_uks_BTDA, bse_uks.cc:291-440 (dense
                              solve up to dim 128, else the HAM Davidson with the ranked guess)
+  exciton_weights_uks        the composition BSE_UKS::Analyze_excitons_uks reports per root
+                             (PrintWeightsUKS, bse_uks.cc:520-595, 597-638): sector weights and
+                             the largest transitions, as data instead of log lines
 
 Vectors are [x_alpha; x_beta]: alpha pairs first, pair index v * ctotal + c per channel.
 """
@@ -173,3 +176,53 @@ def solve_excitons_uks_btda(ctx: GpuBSEContextUKS, opt: DavidsonOptions):
     with np.errstate(invalid="ignore", divide="ignore"):
         s = np.sqrt(1.0 / (np.sum(X * X, axis=0) - np.sum(Y * Y, axis=0)))
     return evals, X * s, Y * s, ds
+
+
+@dataclass
+class UKSContribution:
+    weight: float
+    is_alpha: bool
+    v: int  # index in the spin block's occupied range (vmin + v is the level)
+    c: int  # index in the spin block's virtual range (homo + 1 + c is the level)
+    homo_minus: int  # HOMO-<homo_minus>
+    lumo_plus: int   # LUMO+<lumo_plus>
+
+
+def exciton_weights_uks(opt: BSEOperatorUKS_Options, X, Y=None, min_print_weight=0.5, max_print=8):
+    """Per root: (alpha-sector weight, beta-sector weight, the largest contributions).
+    weights = |X|^2 (TDA) or |X|^2 - |Y|^2 (full BSE) per pair; contributions with
+    |weight| > min_print_weight (the gwbse option print_weight, default 0.5), sorted by |weight|
+    and cut at max_print (8 in the reference); the number above the threshold that were cut is
+    returned too."""
+    X = np.asarray(X, dtype=np.float64)
+    if X.ndim == 1:
+        X = X[:, None]
+    w_all = X * X
+    if Y is not None:
+        Y = np.asarray(Y, dtype=np.float64).reshape(X.shape)
+        w_all = w_all - Y * Y
+    blocks = []
+    off = 0
+    for homo, alpha in ((opt.homo_alpha, True), (opt.homo_beta, False)):
+        vt, ct = homo - opt.vmin + 1, opt.cmax - homo
+        blocks.append((alpha, homo, vt, ct, off))
+        off += vt * ct
+    if off != X.shape[0]:
+        raise ValueError("exciton_weights_uks: vectors do not match the UKS window")
+    out = []
+    for k in range(X.shape[1]):
+        w = w_all[:, k]
+        sectors = []
+        contribs = []
+        for alpha, homo, vt, ct, o in blocks:
+            sectors.append(float(np.sum(w[o:o + vt * ct])))
+            for i in range(vt * ct):
+                if abs(w[o + i]) > min_print_weight:
+                    v, c = i // ct, i % ct
+                    contribs.append(UKSContribution(float(w[o + i]), alpha, v, c,
+                                                    homo - (opt.vmin + v), c))
+        contribs.sort(key=lambda t: abs(t.weight), reverse=True)
+        out.append({"alpha_weight": sectors[0], "beta_weight": sectors[1],
+                    "contributions": contribs[:max_print],
+                    "more_above_threshold": max(0, len(contribs) - max_print)})
+    return out
