@@ -1,5 +1,8 @@
 """Mirror of the BSE solve drivers of VOTCA-XTP (xtp/src/libxtp/gwbse/bse.cc).
 
+  adjust_hqp_size             BSE::AdjustHqpSize, bse.cc:147-186 (and BSE::configure's
+                              diagonal-only choice, bse.cc:53-57; per spin channel it is
+                              BSE_UKS::AdjustHqpSize, bse_uks.cc:92-133)
   solve_hermitian             BSE::solve_hermitian, bse.cc:266-293
   solve_nonhermitian_davidson BSE::Solve_nonhermitian_Davidson, bse.cc:315-360
   full_bse_ranked_guess       BuildFullBSEXRankedInitialGuess,
@@ -28,6 +31,43 @@ class DavidsonOptions:
     davidson_update: str = "safe"
     davidson_maxiter: int = 50
     nmax: int = 5
+
+
+def adjust_hqp_size(Hqp, rpa_input_energies, homo, vmin, cmax, qpmin, qpmax, rpamin,
+                    use_hqp_offdiag=False):
+    """The (vtotal + ctotal)^2 Hqp window the operator reads (occupied first): the QP
+    Hamiltonian (qpmin..qpmax) where the BSE window overlaps it, and the RPA input energies
+    (indexed from rpamin) on the diagonal of the levels outside the QP range.  Without
+    use_hqp_offdiag only the diagonal is kept."""
+    Hqp = np.asarray(Hqp, dtype=np.float64)
+    e = np.asarray(rpa_input_energies, dtype=np.float64)
+    vtotal, ctotal = homo - vmin + 1, cmax - homo
+    n = vtotal + ctotal
+    gwsize = qpmax - qpmin + 1
+    rpa_off = vmin - rpamin
+    if Hqp.shape != (gwsize, gwsize):
+        raise ValueError("adjust_hqp_size: Hqp must be (qpmax - qpmin + 1) square")
+    out = np.zeros((n, n))
+    if vmin >= qpmin:
+        start = vmin - qpmin
+        if cmax <= qpmax:
+            out[:, :] = Hqp[start:start + n, start:start + n]
+        else:
+            virt = gwsize - start
+            out[:virt, :virt] = Hqp[start:start + virt, start:start + virt]
+            extra = cmax - qpmax
+            out[np.arange(n - extra, n), np.arange(n - extra, n)] = e[rpa_off + virt:rpa_off + virt + extra]
+    else:
+        occ = qpmin - vmin
+        if occ + gwsize > n:
+            raise ValueError("adjust_hqp_size: the QP range extends beyond the BSE window")
+        out[np.arange(occ), np.arange(occ)] = e[rpa_off:rpa_off + occ]
+        out[occ:occ + gwsize, occ:occ + gwsize] = Hqp
+        if cmax > qpmax:
+            virt = occ + gwsize
+            extra = cmax - qpmax
+            out[np.arange(n - extra, n), np.arange(n - extra, n)] = e[rpa_off + virt:rpa_off + virt + extra]
+    return out if use_hqp_offdiag else np.diag(np.diag(out))
 
 
 def _solver(opt: DavidsonOptions):
