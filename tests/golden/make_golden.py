@@ -12,6 +12,13 @@ Writes bse_operator_hqp.npz:
 Writes davidson_kat.npz: the lowest 10 eigenvalues of init_matrix(N, 0.01)
 (test_davidson.cc:42-56) for N = 100, 400, from a dense symmetric eigensolver,
 the reference value its Davidson tests check against at 1e-6.
+Writes bse_operator_methane.npz (xtp/src/tests/DataFiles/bse_operator and .../bse, the inputs
+and golden outputs of xtp/src/tests/test_bse_operator.cc:37-147 besides those above):
+  basis_xml     the 3-21G basis file (bse/3-21G.xml, used as DFT and auxiliary basis)
+  elements, xyz the methane geometry in Angstrom (bse/molecule.xyz)
+  MOs           17x17 MO coefficients (bse_operator/MOs.mm)
+  rpa_op        17x17 matrix the filled Mmn is multiplied with (bse_operator/rpa_op.mm)
+  hx_ref, hd_ref, hd2_ref   HxOperator / HdOperator / Hd2Operator * Identity, 20x20
 Writes aomatrix.npz (xtp/src/tests/DataFiles/aomatrix, methane 3-21G; checked by
 xtp/src/tests/test_aomatrix.cc:43-123 at isApprox 1e-5):
   overlap, coulomb                 AOOverlap / AOCoulomb matrices (overlap_ref.mm, coulomb_ref.mm)
@@ -52,6 +59,21 @@ def main():
     for n in (100, 400):
         out[f"evals_{n}"] = np.linalg.eigvalsh(init_matrix(n, 0.01))[:10]
     np.savez(os.path.join(here, "davidson_kat.npz"), **out)
+    b = os.path.join(ref, "xtp/src/tests/DataFiles/bse")
+    elements, xyz = [], []
+    for line in open(os.path.join(b, "molecule.xyz")).read().splitlines()[2:]:
+        t = line.split()
+        if len(t) == 4:
+            elements.append(t[0])
+            xyz.append([float(x) for x in t[1:]])
+    np.savez(os.path.join(here, "bse_operator_methane.npz"),
+             basis_xml=np.array(open(os.path.join(b, "3-21G.xml")).read()),
+             elements=np.array(elements), xyz=np.array(xyz),
+             MOs=read_mm_array(os.path.join(d, "MOs.mm")),
+             rpa_op=read_mm_array(os.path.join(d, "rpa_op.mm")),
+             hx_ref=read_mm_array(os.path.join(d, "hx_ref.mm")),
+             hd_ref=read_mm_array(os.path.join(d, "hd_ref.mm")),
+             hd2_ref=read_mm_array(os.path.join(d, "hd2_ref.mm")))
     a = os.path.join(ref, "xtp/src/tests/DataFiles/aomatrix")
     np.savez(os.path.join(here, "aomatrix.npz"),
              overlap=read_mm_array(os.path.join(a, "overlap_ref.mm")),
