@@ -7,6 +7,10 @@ reference.  The product package (votca_gb300) never imports it.
   bse_oracle.c        restated BSE_OPERATOR loop nest + diagonal + factorised form
                       + HamiltonianOperator product (ctypes-loaded below)
   davidson_oracle.py  restated DavidsonSolver (SYMM Ritz and HAM harmonic Ritz)
+  rpa_oracle.py       restated RPA epsilon and the eigen-rotation screening
+  uks_oracle.py       restated BSE_OPERATOR_UKS blocks
+  threecenter_oracle.py   restated Fill3cMO and the auxiliary metrics
+  gaussian_integrals.py   McMurchie-Davidson AO integrals for the golden methane case
 """
 from __future__ import annotations
 
