@@ -19,6 +19,12 @@ and golden outputs of xtp/src/tests/test_bse_operator.cc:37-147 besides those ab
   MOs           17x17 MO coefficients (bse_operator/MOs.mm)
   rpa_op        17x17 matrix the filled Mmn is multiplied with (bse_operator/rpa_op.mm)
   hx_ref, hd_ref, hd2_ref   HxOperator / HdOperator / Hd2Operator * Identity, 20x20
+Writes threecenter_gwbse.npz (xtp/src/tests/DataFiles/threecenter_gwbse, the same methane
+geometry and 3-21G basis; checked by xtp/src/tests/test_threecenter_gwbse.cc:36-123 at
+isApprox 1e-5):
+  MOs                17x17 MO coefficients
+  ref0b, ref2b, ref4b  slices m = 0, 2, 4 (8 x 17: n = 0..7 by aux) of TCMatrix_gwbse::Fill
+                     over the window m 0..5, n 0..7
 Writes aomatrix.npz (xtp/src/tests/DataFiles/aomatrix, methane 3-21G; checked by
 xtp/src/tests/test_aomatrix.cc:43-123 at isApprox 1e-5):
   overlap, coulomb                 AOOverlap / AOCoulomb matrices (overlap_ref.mm, coulomb_ref.mm)
@@ -74,6 +80,12 @@ def main():
              hx_ref=read_mm_array(os.path.join(d, "hx_ref.mm")),
              hd_ref=read_mm_array(os.path.join(d, "hd_ref.mm")),
              hd2_ref=read_mm_array(os.path.join(d, "hd2_ref.mm")))
+    t = os.path.join(ref, "xtp/src/tests/DataFiles/threecenter_gwbse")
+    np.savez(os.path.join(here, "threecenter_gwbse.npz"),
+             MOs=read_mm_array(os.path.join(t, "MOs.mm")),
+             ref0b=read_mm_array(os.path.join(t, "ref0b.mm")),
+             ref2b=read_mm_array(os.path.join(t, "ref2b.mm")),
+             ref4b=read_mm_array(os.path.join(t, "ref4b.mm")))
     a = os.path.join(ref, "xtp/src/tests/DataFiles/aomatrix")
     np.savez(os.path.join(here, "aomatrix.npz"),
              overlap=read_mm_array(os.path.join(a, "overlap_ref.mm")),

@@ -39,3 +39,18 @@ def test_golden_operator_matrices(precision):
         assert np.linalg.norm(mat - ref) <= tol * np.linalg.norm(ref), cls.__name__
         assert is_approx(np.diag(mat), op.diagonal(), 1e-3), cls.__name__
     ctx.close()
+
+
+def test_golden_threecenter_slices():
+    """TCMatrix_gwbse::Fill on the device (window m 0..5, n 0..7) against the golden slices of
+    test_threecenter_gwbse.cc:36-123 (isApprox 1e-5)."""
+    from votca_gb300 import bse_operator as bo
+    from votca_gb300 import threecenter as tc
+
+    shells, _ = methane_shells()
+    S, V, A3 = gi.overlap(shells), gi.coulomb2(shells), gi.coulomb3(shells, shells)
+    t = np.load(os.path.join(GOLD, "threecenter_gwbse.npz"))
+    M = bo.TCMatrix_gwbse.Initialize(17, 0, 5, 0, 7)
+    assert tc.fill(M, A3, t["MOs"], S, V) == 0
+    for k in (0, 2, 4):
+        assert is_approx(M[k], t["ref%db" % k], 1e-5)

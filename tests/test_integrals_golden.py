@@ -69,3 +69,15 @@ def test_operator_chain_matches_golden(ao, name, ref):
     assert is_approx(mat, gold, 1e-3)
     assert np.linalg.norm(mat - gold) <= 2e-5 * np.linalg.norm(gold)
     assert is_approx(np.diag(mat), prob.diagonal(name), 1e-12)
+
+
+def test_fill_matches_threecenter_golden(ao):
+    """TCMatrix_gwbse::Fill over the window m 0..5, n 0..7 against the slices 0, 2, 4 of
+    test_threecenter_gwbse.cc:36-123 (isApprox 1e-5 there)."""
+    t = np.load(os.path.join(GOLD, "threecenter_gwbse.npz"))
+    M = fill_3c_mo(ao["A3"], t["MOs"], 0, 5, 0, 7)
+    inv, _ = pseudo_inv_sqrt_gwbse(ao["S"], ao["V"], 5e-7)
+    M = np.einsum("mpn,pq->mqn", M, inv)
+    for k in (0, 2, 4):
+        ref = t["ref%db" % k]           # Mmn_[k]: nsize x auxsize
+        assert is_approx(M[k].T, ref, 1e-5)
