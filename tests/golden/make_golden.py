@@ -19,6 +19,15 @@ and golden outputs of xtp/src/tests/test_bse_operator.cc:37-147 besides those ab
   MOs           17x17 MO coefficients (bse_operator/MOs.mm)
   rpa_op        17x17 matrix the filled Mmn is multiplied with (bse_operator/rpa_op.mm)
   hx_ref, hd_ref, hd2_ref   HxOperator / HdOperator / Hd2Operator * Identity, 20x20
+Writes bse_methane.npz (xtp/src/tests/DataFiles/bse; the inputs and golden outputs of
+xtp/src/tests/test_bse.cc:37-330):
+  MOs, Hqp                      17x17 MO coefficients and QP Hamiltonian (RPA energies =
+                                its diagonal)
+  singlets_nooffdiag_tda, singlets_tda, singlets_btda, triplets_tda   lowest roots
+  singlets_psi_nooffdiag_tda, singlets_psi_tda, singlets_psi_btda, singlets_psi_AR_btda,
+  triplets_psi_tda              eigenvectors (the reference compares subspace projections)
+  singlets_dynamic_TDA, singlets_dynamic_full, triplets_dynamic_TDA   perturbative dynamical
+                                screening
 Writes threecenter_gwbse.npz (xtp/src/tests/DataFiles/threecenter_gwbse, the same methane
 geometry and 3-21G basis; checked by xtp/src/tests/test_threecenter_gwbse.cc:36-123 at
 isApprox 1e-5):
@@ -80,6 +89,16 @@ def main():
              hx_ref=read_mm_array(os.path.join(d, "hx_ref.mm")),
              hd_ref=read_mm_array(os.path.join(d, "hd_ref.mm")),
              hd2_ref=read_mm_array(os.path.join(d, "hd2_ref.mm")))
+    keys = ["singlets_nooffdiag_tda", "singlets_tda", "singlets_btda", "triplets_tda",
+            "singlets_psi_nooffdiag_tda", "singlets_psi_tda", "singlets_psi_btda",
+            "singlets_psi_AR_btda", "triplets_psi_tda", "singlets_dynamic_TDA",
+            "singlets_dynamic_full", "triplets_dynamic_TDA"]
+    arrays = {k: read_mm_array(os.path.join(b, k + ".mm")) for k in keys}
+    for k in keys:
+        if "psi" not in k:
+            arrays[k] = arrays[k].reshape(-1)
+    np.savez(os.path.join(here, "bse_methane.npz"), MOs=read_mm_array(os.path.join(b, "MOs.mm")),
+             Hqp=read_mm_array(os.path.join(b, "Hqp.mm")), **arrays)
     t = os.path.join(ref, "xtp/src/tests/DataFiles/threecenter_gwbse")
     np.savez(os.path.join(here, "threecenter_gwbse.npz"),
              MOs=read_mm_array(os.path.join(t, "MOs.mm")),
