@@ -28,6 +28,10 @@ xtp/src/tests/test_bse.cc:37-330):
   triplets_psi_tda              eigenvectors (the reference compares subspace projections)
   singlets_dynamic_TDA, singlets_dynamic_full, triplets_dynamic_TDA   perturbative dynamical
                                 screening
+Writes rpa_methane.npz (xtp/src/tests/DataFiles/rpa; xtp/src/tests/test_rpa.cc:69-140 checks at
+isApprox 1e-4):
+  eigenvectors, eigenvals   MO coefficients and RPA input energies (same molecule and basis)
+  r_ref, r_complex_ref      RPA::calculate_epsilon_r at 0 and at 0.5 + 0.5i (homo 4, rpa 0..16)
 Writes threecenter_gwbse.npz (xtp/src/tests/DataFiles/threecenter_gwbse, the same methane
 geometry and 3-21G basis; checked by xtp/src/tests/test_threecenter_gwbse.cc:36-123 at
 isApprox 1e-5):
@@ -99,6 +103,12 @@ def main():
             arrays[k] = arrays[k].reshape(-1)
     np.savez(os.path.join(here, "bse_methane.npz"), MOs=read_mm_array(os.path.join(b, "MOs.mm")),
              Hqp=read_mm_array(os.path.join(b, "Hqp.mm")), **arrays)
+    r = os.path.join(ref, "xtp/src/tests/DataFiles/rpa")
+    np.savez(os.path.join(here, "rpa_methane.npz"),
+             eigenvectors=read_mm_array(os.path.join(r, "eigenvectors.mm")),
+             eigenvals=read_mm_array(os.path.join(r, "eigenvals.mm")).reshape(-1),
+             r_ref=read_mm_array(os.path.join(r, "r_ref.mm")),
+             r_complex_ref=read_mm_array(os.path.join(r, "r_complex_ref.mm")))
     t = os.path.join(ref, "xtp/src/tests/DataFiles/threecenter_gwbse")
     np.savez(os.path.join(here, "threecenter_gwbse.npz"),
              MOs=read_mm_array(os.path.join(t, "MOs.mm")),

@@ -54,3 +54,21 @@ def test_golden_threecenter_slices():
     assert tc.fill(M, A3, t["MOs"], S, V) == 0
     for k in (0, 2, 4):
         assert is_approx(M[k], t["ref%db" % k], 1e-5)
+
+
+def test_golden_rpa_epsilon():
+    """RPA::calculate_epsilon_r on the device at 0 and at 0.5 + 0.5i against the goldens of
+    test_rpa.cc:69-140 (isApprox 1e-4), from the device Fill."""
+    from votca_gb300 import bse_operator as bo
+    from votca_gb300 import threecenter as tc
+    from votca_gb300.screening import rpa_epsilon
+
+    shells, _ = methane_shells()
+    S, V, A3 = gi.overlap(shells), gi.coulomb2(shells), gi.coulomb3(shells, shells)
+    r = np.load(os.path.join(GOLD, "rpa_methane.npz"))
+    M = bo.TCMatrix_gwbse.Initialize(17, 0, 16, 0, 16)
+    assert tc.fill(M, A3, r["eigenvectors"], S, V) == 0
+    for freq, key in ((0.0, "r_ref"), (0.5 + 0.5j, "r_complex_ref")):
+        eps = rpa_epsilon(M, r["eigenvals"], 4, 0, 16, freq)
+        assert is_approx(eps, r[key], 1e-4)
+        assert np.linalg.norm(eps - r[key]) <= 1e-5 * np.linalg.norm(r[key])

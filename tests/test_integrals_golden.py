@@ -81,3 +81,16 @@ def test_fill_matches_threecenter_golden(ao):
     for k in (0, 2, 4):
         ref = t["ref%db" % k]           # Mmn_[k]: nsize x auxsize
         assert is_approx(M[k].T, ref, 1e-5)
+
+
+def test_rpa_epsilon_matches_golden(ao):
+    """RPA::calculate_epsilon_r at 0 and at 0.5 + 0.5i (test_rpa.cc:69-140, isApprox 1e-4)."""
+    from oracle.rpa_oracle import epsilon_r
+
+    r = np.load(os.path.join(GOLD, "rpa_methane.npz"))
+    M = fill_3c_mo(ao["A3"], r["eigenvectors"], 0, 16, 0, 16)
+    M = np.einsum("mpn,pq->mqn", M, pseudo_inv_sqrt_gwbse(ao["S"], ao["V"], 5e-7)[0])
+    for freq, key in ((0.0 + 0.0j, "r_ref"), (0.5 + 0.5j, "r_complex_ref")):
+        eps = epsilon_r(M, r["eigenvals"], 4, 0, 16, freq)
+        assert is_approx(eps, r[key], 1e-4)
+        assert np.linalg.norm(eps - r[key]) <= 1e-5 * np.linalg.norm(r[key])
