@@ -43,6 +43,24 @@ def test_host_only_entry_points_without_gpu():
     assert rc == 1 and b"null handle" in L.bse_last_error()
 
 
+def test_argument_errors_of_the_newer_entry_points_without_gpu():
+    """Null inputs and bad sizes are rejected before any device work (status 1)."""
+    from votca_gb300 import _lib
+
+    L = _lib.load()
+    h = ctypes.c_void_p()
+    o = _lib.bse_uks_options(3, 2, 0, 0, 0, 8)
+    assert L.bse_uks_op_create(None, None, None, None, None, None, 0, 0, None, 0, 0, ctypes.byref(o), 0,
+                               ctypes.byref(h)) == 1
+    assert L.bse_uks_op_create_dense_screening(None, None, None, None, None, None, 0, 0, None, 0, 0,
+                                               ctypes.byref(o), 0, ctypes.byref(h)) == 1
+    assert L.bse_mmn_fill_3c_mo(None, None, None, 4, None, 4, 4) == 1
+    removed = ctypes.c_int64()
+    assert L.bse_aux_pseudo_inv_sqrt(0, None, 0, 1e-7, None, 0, ctypes.byref(removed)) == 1
+    assert L.bse_aux_pseudo_inv_sqrt_gwbse(3, None, 3, None, 3, 1e-7, None, 3, ctypes.byref(removed)) == 1
+    assert b"bad arguments" in L.bse_last_error()
+
+
 def test_python_mirror_rejects_hd_and_hd2_together():
     from votca_gb300 import bse_operator as bo
     from votca_gb300._lib import BSEError

@@ -450,6 +450,7 @@ int bse_mmn_fill_3c_mo(const bse_mmn_desc *mmn, double *const *mmn_slices, const
 int bse_aux_pseudo_inv_sqrt(int64_t n, const double *V, int64_t ldv, double etol, double *out, int64_t ldo,
                             int64_t *removed) {
   return guarded([&] {
+    VGB_REQUIRE(n >= 1 && V && out && ldv >= n && ldo >= n, "bse_aux_pseudo_inv_sqrt: bad arguments");
     TmpStream ts;
     vgb::aux_pseudo_inv_sqrt(n, V, ldv, etol, out, ldo, removed, ts.s);
   });
@@ -458,6 +459,8 @@ int bse_aux_pseudo_inv_sqrt(int64_t n, const double *V, int64_t ldv, double etol
 int bse_aux_pseudo_inv_sqrt_gwbse(int64_t n, const double *S, int64_t lds, const double *V, int64_t ldv,
                                   double etol, double *out, int64_t ldo, int64_t *removed) {
   return guarded([&] {
+    VGB_REQUIRE(n >= 1 && S && V && out && lds >= n && ldv >= n && ldo >= n,
+                "bse_aux_pseudo_inv_sqrt_gwbse: bad arguments");
     TmpStream ts;
     vgb::aux_pseudo_inv_sqrt_gwbse(n, S, lds, V, ldv, etol, out, ldo, removed, ts.s);
   });
