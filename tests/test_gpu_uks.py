@@ -141,3 +141,35 @@ def test_errors():
         L = ctx._L
         _lib.check(L.bse_op_matmul_device_noalloc(ctx.handle, 1, 1, 1, 0, None, ctx.size, 1, None, ctx.size, None))
     ctx.close()
+
+
+def test_batched_uks_solves():
+    """UKS handles in the batched driver: independent solves on host threads agree with single
+    solves; the lockstep mode takes restricted operators only."""
+    from votca_gb300 import _lib
+    from votca_gb300.bse_operator_uks import ExcitonUKSOperator_TDA
+    from votca_gb300.davidson import DavidsonSolver
+
+    ctxs = [_setup(UKSProblem(5, 3, vmin=0, cmax=30, naux=36, nmo=34, seed=s))[0] for s in (31, 32)]
+    ops = [ExcitonUKSOperator_TDA(c) for c in ctxs]
+    ds = DavidsonSolver()
+    ds.set_tolerance(1e-9)
+    ds.set_max_search_space(40)
+    ev, info, _ = ds.solve_batch(ops, 4, nthreads=2)
+    assert info == ["Success", "Success"]
+    for m, op in enumerate(ops):
+        lam, _ = _single(op)
+        np.testing.assert_allclose(ev[m], lam, rtol=0, atol=1e-10)
+    with pytest.raises(_lib.BSEError):
+        ds.solve_batch(ops, 4, nthreads=0)
+    for c in ctxs:
+        c.close()
+
+
+def _single(op):
+    from votca_gb300.davidson import DavidsonSolver
+
+    ds = DavidsonSolver()
+    ds.set_tolerance(1e-9)
+    ds.set_max_search_space(40)
+    return ds.solve(op, 4)
