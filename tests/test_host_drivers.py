@@ -34,3 +34,21 @@ def test_ranked_guess_ties_and_sizes():
 def test_exchange_prefactor():
     assert exchange_prefactor("singlet") == 2.0
     assert exchange_prefactor("triplet") == 0.0
+
+
+def test_exciton_weights():
+    """PrintWeights (bse.cc:378-391): pairs above print_weight in pair order, HOMO-i -> LUMO+j."""
+    from votca_gb300.bse import exciton_weights
+
+    homo, vmin, cmax = 4, 1, 8          # v = 1..4, c = 5..8: 4 x 4 pairs
+    X = np.zeros((16, 2))
+    X[0 * 4 + 3, 0] = np.sqrt(0.3)      # v = 1, c = 8: HOMO-3 -> LUMO+3
+    X[3 * 4 + 0, 0] = np.sqrt(0.7)      # v = 4, c = 5: HOMO-0 -> LUMO+0
+    X[5, 1] = 1.0
+    Y = np.zeros_like(X)
+    Y[5, 1] = np.sqrt(0.6)              # full BSE: 1 - 0.6 = 0.4 < 0.5
+    r = exciton_weights(homo, vmin, cmax, X, min_print_weight=0.25)
+    assert [(a, b) for a, b, _ in r[0]] == [(3, 3), (0, 0)]       # pair order, not sorted
+    assert abs(r[0][1][2] - 0.7) < 1e-15
+    assert exciton_weights(homo, vmin, cmax, X, Y)[1] == []
+    assert exciton_weights(homo, vmin, cmax, X)[1] == [(2, 1, 1.0)]  # v = 2, c = 6

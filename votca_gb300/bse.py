@@ -7,6 +7,8 @@
   solve_nonhermitian_davidson BSE::Solve_nonhermitian_Davidson, bse.cc:315-360
   full_bse_ranked_guess       BuildFullBSEXRankedInitialGuess,
                               xtp/include/votca/xtp/bse_initialization.h:47-92
+  exciton_weights             the transitions BSE::Analyze_singlets / Analyze_triplets print
+                              per root (PrintWeights, bse.cc:378-391), as data
   expectation_value_operator  BSE::ExpectationValue_Operator, bse.cc:500-520
   analyze_eh_interaction      BSE::Analyze_eh_interaction, bse.cc:551-606 (with
                               ExchangePrefactor, bse.cc:136-145)
@@ -156,4 +158,29 @@ def analyze_eh_interaction(ctx, X, Y=None, spin="singlet"):
         out["exchange_contrib"] = xpref * (d + cr if Y is not None else d)
     else:
         out["exchange_contrib"] = np.zeros(direct.size)
+    return out
+
+
+def exciton_weights(homo, vmin, cmax, X, Y=None, min_print_weight=0.5):
+    """Per root, the pairs whose weight |X|^2 (TDA) or |X|^2 - |Y|^2 (full BSE) exceeds
+    min_print_weight (the gwbse option print_weight, default 0.5), in pair order, as
+    (HOMO-i, LUMO+j, weight) with i = homo - v and j = c - homo - 1 (vc2index levels
+    v = vmin + I // ctotal, c = homo + 1 + I % ctotal)."""
+    X = np.asarray(X, dtype=np.float64)
+    if X.ndim == 1:
+        X = X[:, None]
+    w = X * X
+    if Y is not None:
+        Yv = np.asarray(Y, dtype=np.float64).reshape(X.shape)
+        w = w - Yv * Yv
+    ctotal = cmax - homo
+    if X.shape[0] != (homo - vmin + 1) * ctotal:
+        raise ValueError("exciton_weights: vectors do not match the BSE window")
+    out = []
+    for k in range(X.shape[1]):
+        rows = []
+        for i in np.nonzero(w[:, k] > min_print_weight)[0]:
+            v, c = vmin + i // ctotal, homo + 1 + i % ctotal
+            rows.append((int(homo - v), int(c - homo - 1), float(w[i, k])))
+        out.append(rows)
     return out
