@@ -1,4 +1,4 @@
-"""CPU restatement of the Mmn producer (TEST INFRASTRUCTURE ONLY: tests/ use it as the checker).
+"""CPU restatement of the Mmn producer (TEST INFRASTRUCTURE ONLY: tests/ compare against it).
 
   fill_3c_mo             TCMatrix_gwbse::Fill3cMO (xtp/src/libxtp/libint2_calls.cc:595-651):
                          every aux function P: (dftn A_P) dftm with dftn = C[:, n-window]^T,

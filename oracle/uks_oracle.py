@@ -1,6 +1,6 @@
 """CPU restatement of the unrestricted (UKS) BSE operator (TEST INFRASTRUCTURE ONLY).
 
-Only tests/ may use this module, as the checker of the GPU UKS operator.  It restates
+Only tests/ may use this module, as the reference of the GPU UKS operator.  It restates
 BSE_OPERATOR_UKS<cqp, cx, cd, cd2> of xtp/src/libxtp/gwbse/bse_operator_uks.cc block by
 block, with the same loops over output pairs and the same Mmn slices and rows:
 
