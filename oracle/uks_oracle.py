@@ -16,9 +16,11 @@ block, with the same loops over output pairs and the same Mmn slices and rows:
 
 Index conventions follow the reference: slice m of Mmn is column-major [nn x naux]
 (M(m, n, P) = mmn[m, P, n] here), m and n counted from rpamin; a spin block's pair
-index is v * ctotal + c; the alpha block comes first.  Parity is unpinned against
-golden data (the reference has no UKS operator test); it is pinned by this loop-level
-restatement only.
+index is v * ctotal + c; the alpha block comes first.  The same-spin blocks equal the
+restricted BSE_OPERATOR of each channel (checked in tests/test_uks_oracle.py against the
+restricted oracle, which reproduces the reference's golden operator matrices); the cross-spin
+blocks have no golden data (the reference has no UKS operator test) and rest on this
+loop-level restatement alone.
 """
 from __future__ import annotations
 
