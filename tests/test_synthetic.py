@@ -57,3 +57,19 @@ def test_uks_problem(symmetric):
     sym = np.array_equal(p.mmn_alpha, p.mmn_alpha.transpose(2, 1, 0))
     assert sym == symmetric
     assert p.hqp_alpha.shape == (5 + 7, 5 + 7) and p.hqp_beta.shape == (3 + 9, 3 + 9)
+
+
+def test_mmn_tensor_torch_distribution():
+    """The large-size generator (torch's seeded generator; on the CPU here): the same symmetric
+    layout and entry distribution as mmn_tensor."""
+    naux, nmo = 96, 48
+    M = sy.mmn_tensor_torch(11, naux, nmo)
+    assert M.shape == (nmo, naux, nmo) and M.dtype == np.float64
+    np.testing.assert_array_equal(M, M.transpose(2, 1, 0))
+    m = np.arange(nmo)
+    decay = np.exp(-np.abs(m[:, None] - m[None, :]) / 40.0) * (0.1 / np.sqrt(naux))
+    z = M / decay[:, None, :]
+    iu = np.triu_indices(nmo)
+    upper = z[iu[0], :, iu[1]]
+    assert abs(upper.mean()) < 0.02 and abs(upper.std() - 1.0) < 0.02
+    np.testing.assert_array_equal(M, sy.mmn_tensor_torch(11, naux, nmo))
