@@ -69,3 +69,22 @@ def test_python_mirror_rejects_hd_and_hd2_together():
         size = 4
     with pytest.raises(BSEError):
         bo.BSE_OPERATOR(Fake(), 0, 0, 1, 1)
+
+
+@pytest.mark.parametrize("compiler,std", [("gcc", "-std=c99"), ("g++", "-std=c++11")])
+def test_header_is_plain_c_and_cxx(tmp_path, compiler, std):
+    """include/votca_gb300_bse.h compiles as C99 and C++11 on its own (what a cgo / JNI / ctypes
+    binding or a C++ adapter includes), and every declared function is callable from C."""
+    import shutil
+    import subprocess
+
+    if shutil.which(compiler) is None:
+        pytest.skip(f"{compiler} not available")
+    names = declared_functions()
+    src = tmp_path / ("use.c" if compiler == "gcc" else "use.cpp")
+    body = "\n".join(f"  (void)&{n};" for n in names)
+    src.write_text('#include "votca_gb300_bse.h"\nint main(void) {\n' + body + "\n  return 0;\n}\n")
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    r = subprocess.run([compiler, std, "-Wall", "-Wextra", "-Werror", "-pedantic", "-fsyntax-only", "-I", inc,
+                        str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
