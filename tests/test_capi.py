@@ -88,3 +88,20 @@ def test_header_is_plain_c_and_cxx(tmp_path, compiler, std):
     r = subprocess.run([compiler, std, "-Wall", "-Wextra", "-Werror", "-pedantic", "-fsyntax-only", "-I", inc,
                         str(src)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_ctypes_table_matches_header_arity():
+    """Every ctypes signature has as many arguments as the header's prototype."""
+    from votca_gb300 import _lib
+
+    src = ""
+    for f in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if f.endswith(".h"):
+            src += open(os.path.join(ROOT, "include", f)).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    protos = dict(re.findall(r"\b(bse_[a-z_0-9]+)\s*\(([^;{]*?)\)\s*;", src, flags=re.S))
+    assert len(protos) >= len(declared_functions())
+    for name, (_, argtypes) in _lib.SIGNATURES.items():
+        params = protos[name].strip()
+        n = 0 if params in ("", "void") else len([p for p in params.split(",") if p.strip()])
+        assert len(argtypes) == n, (name, len(argtypes), n)
