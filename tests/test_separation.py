@@ -31,3 +31,19 @@ def test_library_sources_do_not_reference_the_oracle():
         if re.search(r"oracle|bse_oracle", open(f).read()):
             bad.append(f)
     assert not bad, bad
+
+
+def test_no_batched_memcpy_calls():
+    """The batched memcpy entry points are closed on the GPU pool this library is tested on: no
+    source names them (the names are assembled here so that this file does not)."""
+    names = [p + "Memcpy" + d + "BatchAsync" for p in ("cuda", "cu") for d in ("", "3D")]
+    bad = []
+    for top in ("votca_gb300", "include", "oracle", "tests"):
+        for f in _files(top, (".py", ".cu", ".cuh", ".cpp", ".hpp", ".h", ".c")):
+            src = open(f, errors="ignore").read()
+            if any(n in src for n in names):
+                bad.append(f)
+    for f in ("bench.py", "__graft_entry__.py"):
+        if any(n in open(os.path.join(ROOT, f)).read() for n in names):
+            bad.append(f)
+    assert not bad, bad
