@@ -1,8 +1,8 @@
 """The reference's end-to-end BSE goldens for methane in 3-21G (xtp/src/tests/test_bse.cc:37-330)
 reproduced by the oracle chain on the CPU: AO integrals (oracle/gaussian_integrals.py) ->
 TCMatrix_gwbse::Fill -> RPA eps(0) from the QP energies -> eigen-rotated screening with
-1/lambda (BSE::SetupDirectInteractionOperator) -> restated BSE_OPERATOR -> dense eigenpairs, and
-the perturbative dynamical screening loop (BSE::Perturbative_DynamicalScreening).  Tolerances are
+1/lambda (BSE::SetupDirectInteractionOperator) -> restated BSE_OPERATOR -> dense eigenpairs and the
+restated DavidsonSolver with the reference test's settings, and the perturbative dynamical screening loop (BSE::Perturbative_DynamicalScreening).  Tolerances are
 the reference's (isApprox 1e-3 on energies, subspace projections 1 to 1e-5, 0.005 / 0.05 / 0.001
 for the dynamical singlet TDA / singlet full / triplet TDA energies)."""
 import os
@@ -76,6 +76,51 @@ def test_full_bse_singlets(chain):
     assert np.abs(lam - g["singlets_btda"]).max() < 2e-6
     np.testing.assert_allclose(_projection_norms(g["singlets_psi_btda"], X), 1.0, atol=1e-5)
     np.testing.assert_allclose(_projection_norms(g["singlets_psi_AR_btda"], Y), 1.0, atol=1e-5)
+
+
+def _davidson(A, nroots, guess=None):
+    """The restated DavidsonSolver with the settings of test_bse.cc:70-81 (DPR, lapack, safe,
+    50 iterations; max search space 10 * nmax as BSE::Solve_singlets sets it)."""
+    from oracle.davidson_oracle import DavidsonOracle
+
+    d = DavidsonOracle()
+    d.set_tolerance("lapack")
+    d.set_correction("DPR")
+    d.set_size_update("safe")
+    d.max_search_space = 10 * nroots
+    if guess is not None:
+        d.set_matrix_type("HAM")
+    lam, vec = d.solve(lambda X: A @ X, np.diag(A).copy(), nroots, initial_guess=guess)
+    assert d.info == "Success"
+    return lam, vec
+
+
+@pytest.mark.parametrize("offdiag,key,psi", [(False, "singlets_nooffdiag_tda", "singlets_psi_nooffdiag_tda"),
+                                             (True, "singlets_tda", "singlets_psi_tda")])
+def test_davidson_tda_singlets(chain, offdiag, key, psi):
+    """The matrix-free solve of the reference test (its TDA singlet Davidson) on the oracle
+    operator: the threefold lowest level converges and spans the golden subspace."""
+    g = chain["g"]
+    lam, vec = _davidson(chain["problem"](0.0, offdiag).dense("singlet"), 3)
+    assert is_approx(lam, g[key], 1e-3)
+    assert np.abs(lam - g[key]).max() < 2e-6
+    np.testing.assert_allclose(_projection_norms(g[psi], vec), 1.0, atol=1e-5)
+
+
+def test_davidson_triplet_and_full_bse(chain):
+    from votca_gb300.bse import full_bse_ranked_guess
+
+    g = chain["g"]
+    p = chain["problem"](0.0)
+    lt, _ = _davidson(p.dense("triplet"), 1)
+    assert is_approx(lt, g["triplets_tda"], 1e-3) and abs(lt[0] - g["triplets_tda"][0]) < 2e-6
+    A, B = p.dense("singlet"), p.dense("singlet_b")
+    n = A.shape[0]
+    lb, vec = _davidson(np.block([[A, B], [-B, -A]]), 3, full_bse_ranked_guess(np.diag(A), np.diag(B), 3))
+    assert is_approx(lb, g["singlets_btda"], 1e-3)
+    assert np.abs(lb - g["singlets_btda"]).max() < 2e-6
+    np.testing.assert_allclose(_projection_norms(g["singlets_psi_btda"], vec[:n]), 1.0, atol=1e-5)
+    np.testing.assert_allclose(_projection_norms(g["singlets_psi_AR_btda"], vec[n:]), 1.0, atol=1e-5)
 
 
 def _dynamical(chain, lam, X, Y=None, iters=10, tol=1e-5):
