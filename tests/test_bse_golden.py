@@ -1,10 +1,11 @@
 """The reference's end-to-end BSE goldens for methane in 3-21G (xtp/src/tests/test_bse.cc:37-330)
 reproduced by the oracle chain on the CPU: AO integrals (oracle/gaussian_integrals.py) ->
 TCMatrix_gwbse::Fill -> RPA eps(0) from the QP energies -> eigen-rotated screening with
-1/lambda (BSE::SetupDirectInteractionOperator) -> restated BSE_OPERATOR -> dense eigenpairs and the
-restated DavidsonSolver with the reference test's settings, and the perturbative dynamical screening loop (BSE::Perturbative_DynamicalScreening).  Tolerances are
-the reference's (isApprox 1e-3 on energies, subspace projections 1 to 1e-5, 0.005 / 0.05 / 0.001
-for the dynamical singlet TDA / singlet full / triplet TDA energies)."""
+1/lambda (BSE::SetupDirectInteractionOperator) -> restated BSE_OPERATOR -> dense eigenpairs and
+the restated DavidsonSolver with the reference test's settings, and the perturbative dynamical
+screening loop (BSE::Perturbative_DynamicalScreening).  Tolerances are the reference's
+(isApprox 1e-3 on energies, subspace projections 1 to 1e-5, 0.005 / 0.05 / 0.001 for the
+dynamical singlet TDA / singlet full / triplet TDA energies)."""
 import os
 
 import numpy as np
