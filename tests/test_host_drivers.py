@@ -1,6 +1,7 @@
 """Host logic of the BSE drivers (CPU): the ranked full-BSE guess
 (BuildFullBSEXRankedInitialGuess, xtp/include/votca/xtp/bse_initialization.h:47-92), the
-exchange prefactor (bse.cc:136-145) and the Davidson option presets."""
+exchange prefactor (bse.cc:136-145), the Davidson option presets, the exciton weights and the
+RPA input energies (RPA::UpdateRPAInputEnergies, rpa.cc:32-73; RPA_UKS, rpa_uks.cc:41-201)."""
 import numpy as np
 import pytest
 
@@ -52,3 +53,39 @@ def test_exciton_weights():
     assert abs(r[0][1][2] - 0.7) < 1e-15
     assert exciton_weights(homo, vmin, cmax, X, Y)[1] == []
     assert exciton_weights(homo, vmin, cmax, X)[1] == [(2, 1, 1.0)]  # v = 2, c = 6
+
+
+def test_rpa_input_energies_kat():
+    """test_rpa.cc:41-63 (rpa_calcenergies): configure(4, 0, 9), qpmin 1, isApprox 1e-4."""
+    from votca_gb300.screening import update_rpa_input_energies, update_rpa_input_energies_uks
+
+    dft = np.array([-0.5, -0.4, -0.3, -0.2, -0.2, -0.1, 0, 0.1, 0.2, 0.3])
+    gw = np.array([-0.15, -0.05, 0.05, 0.15, 0.45, 0.55, 0.65])
+    ref = np.array([-0.85, -0.15, -0.05, 0.05, 0.15, 0.45, 0.55, 0.65, 0.75, 0.85])
+    e = update_rpa_input_energies(dft, gw, 1, 4, 0, 9)
+    assert np.linalg.norm(e - ref) <= 1e-4 * min(np.linalg.norm(e), np.linalg.norm(ref))
+    np.testing.assert_allclose(e, ref, rtol=0, atol=1e-15)
+    ea, eb = update_rpa_input_energies_uks(dft, dft, gw, gw, 1, 4, 4, 0, 9)   # rpamin 0: same recipe
+    np.testing.assert_array_equal(ea, e)
+    np.testing.assert_array_equal(eb, e)
+
+
+def test_rpa_input_energies_window_offsets():
+    """rpamin > 0, worked by hand: the restricted form reads the RPA vector at the absolute level
+    index and shifts its first qpmin entries (rpa.cc:50-73); the unrestricted form indexes it from
+    rpamin (rpa_uks.cc:163-201).  Levels 0..7, rpa window 1..7, QP levels 2..5, HOMO 3."""
+    from votca_gb300.screening import update_rpa_input_energies, update_rpa_input_energies_uks
+
+    dft = 0.1 * np.arange(8)
+    gw = np.array([0.25, 0.33, 0.38, 0.60])
+    e = update_rpa_input_energies(dft, gw, 2, 3, 1, 7)
+    np.testing.assert_allclose(e, [-0.13, 0.02, 0.33, 0.38, 0.60, 0.9, 1.0], rtol=0, atol=1e-14)
+    ea, eb = update_rpa_input_energies_uks(dft, dft, gw, gw[:3], 2, 3, 2, 1, 7)
+    np.testing.assert_allclose(ea, [0.05, 0.25, 0.33, 0.38, 0.60, 0.7, 0.8], rtol=0, atol=1e-14)
+    # beta: QP levels 2..4, HOMO 2 -> occ correction |0.25 - 0.2|, virt max(|0.33-0.3|, |0.38-0.4|)
+    # on the DFT levels 5..7
+    np.testing.assert_allclose(eb, [0.05, 0.25, 0.33, 0.38, 0.53, 0.63, 0.73], rtol=0, atol=1e-14)
+    with pytest.raises(ValueError):
+        update_rpa_input_energies(dft, np.zeros(7), 2, 3, 1, 7)     # QP levels past rpamax
+    with pytest.raises(ValueError):
+        update_rpa_input_energies(dft, gw, 0, 3, 1, 7)              # qpmin below rpamin

@@ -1,6 +1,10 @@
 """Screening that feeds the direct term, and the perturbative dynamical screening of
 the excitation energies, on the GPU.
 
+  update_rpa_input_energies    RPA::UpdateRPAInputEnergies / ShiftUncorrectedEnergies
+                               (rpa.cc:32-73): the RPA input energies from DFT and QP levels
+                               (host arithmetic); update_rpa_input_energies_uks the same per
+                               spin channel (rpa_uks.cc:41-71, 163-201)
   rpa_epsilon                  RPA::calculate_epsilon_r (xtp/src/libxtp/gwbse/rpa.cc),
                                bse_rpa_epsilon
   cholesky_inverse             the inverse of a symmetric positive definite matrix,
@@ -42,6 +46,60 @@ def _desc_ptrs(Mmn: TCMatrix_gwbse):
     ptrs = (_lib.c_dp * Mmn.msize())(*[ctypes.cast(d.ctypes.data + m * d.strides[0], _lib.c_dp)
                                        for m in range(Mmn.msize())])
     return desc, ptrs
+
+
+def _rpa_input_energies(dft, gw, qpmin, homo, rpamin, rpamax, absolute_rpa_index):
+    dft = np.asarray(dft, dtype=np.float64)
+    gw = np.asarray(gw, dtype=np.float64)
+    rpatotal = rpamax - rpamin + 1
+    gwsize = gw.size
+    if rpamin < 0 or rpamax >= dft.size or rpatotal <= 0:
+        raise ValueError("update_rpa_input_energies: rpa window outside the DFT levels")
+    if qpmin < rpamin or qpmin - rpamin + gwsize > rpatotal:
+        raise ValueError("update_rpa_input_energies: QP levels outside the rpa window")
+    e = dft[rpamin:rpamax + 1].copy()
+    e[qpmin - rpamin:qpmin - rpamin + gwsize] = gw
+    qpmax = qpmin + gwsize - 1
+    # RPA::getMaxCorrection reads the RPA vector at the absolute level index and the DFT vector
+    # at index - rpamin; RPA_UKS::getMaxCorrection the other way round
+    ro, do = (0, -rpamin) if absolute_rpa_index else (-rpamin, 0)
+
+    def max_correction(lo, hi):
+        n = hi - lo + 1
+        if n <= 0:
+            return 0.0
+        if lo + ro < 0 or lo + ro + n > rpatotal or lo + do < 0 or lo + do + n > dft.size:
+            raise ValueError("update_rpa_input_energies: correction range outside the levels")
+        return float(np.max(np.abs(e[lo + ro:lo + ro + n] - dft[lo + do:lo + do + n])))
+
+    occ = max_correction(qpmin, homo)
+    virt = max_correction(homo + 1, qpmax)
+    e[:qpmin if absolute_rpa_index else qpmin - rpamin] -= occ
+    tail = rpamax - qpmax
+    if tail > 0:
+        e[rpatotal - tail:] += virt
+    return e
+
+
+def update_rpa_input_energies(dftenergies, gwaenergies, qpmin, homo, rpamin, rpamax):
+    """The energies eps(omega) is built from (rpamin..rpamax): DFT levels with the QP levels
+    (qpmin..qpmin + len(gwaenergies) - 1) put in, the levels below qpmin shifted down by the
+    largest |QP - DFT| correction among qpmin..homo and those above qpmax shifted up by the
+    largest among lumo..qpmax.  Index arithmetic as in RPA::UpdateRPAInputEnergies: the
+    corrections read the RPA vector at the absolute level index and the DFT vector at
+    index - rpamin, and the lower shift covers the first qpmin entries of the RPA vector (the
+    same as the unrestricted form for rpamin = 0, the GW-BSE default).  An empty correction
+    range contributes 0."""
+    return _rpa_input_energies(dftenergies, gwaenergies, qpmin, homo, rpamin, rpamax, True)
+
+
+def update_rpa_input_energies_uks(dft_alpha, dft_beta, gw_alpha, gw_beta, qpmin, homo_alpha, homo_beta,
+                                  rpamin, rpamax):
+    """RPA_UKS::UpdateRPAInputEnergies (rpa_uks.cc:41-71, 163-201): the restricted recipe per
+    spin channel with its own HOMO, indexing the RPA vector from rpamin throughout.
+    Returns (energies_alpha, energies_beta)."""
+    return (_rpa_input_energies(dft_alpha, gw_alpha, qpmin, homo_alpha, rpamin, rpamax, False),
+            _rpa_input_energies(dft_beta, gw_beta, qpmin, homo_beta, rpamin, rpamax, False))
 
 
 def rpa_epsilon(Mmn: TCMatrix_gwbse, rpa_energies, homo, rpamin, rpamax, frequency=0.0):
