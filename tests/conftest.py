@@ -13,6 +13,21 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "slow: long-running")
 
 
+def pytest_collection_modifyitems(config, items):
+    """Unit-level parity first, then the end-to-end methane chains (files named *golden*),
+    then the files named to run last (test_zz_*): under -x a failure in a long end-to-end
+    chain does not keep the unit parity results from being reported.  Order within each
+    group is the collection order."""
+
+    def group(item):
+        name = os.path.basename(str(item.fspath))
+        if name.startswith("test_zz_"):
+            return 2
+        return 1 if "golden" in name else 0
+
+    items[:] = sorted(items, key=group)
+
+
 def is_approx(a, b, prec):
     """Eigen's isApprox: ||a - b|| <= prec * min(||a||, ||b||)."""
     import numpy as np
