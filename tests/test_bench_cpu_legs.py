@@ -1,0 +1,29 @@
+"""The CPU legs of bench.py on a small problem (CPU): the factorised-oracle sample times the
+product on a slice of the aux index and scales it by Naux and by the waves of vectors, and the
+sliced problem is the same arithmetic as the full product with the other aux functions zeroed."""
+import numpy as np
+
+import bench
+import oracle
+from votca_gb300.synthetic import Problem
+
+
+def test_factorised_sample_scaling(monkeypatch):
+    monkeypatch.setattr(bench, "V", 3)
+    monkeypatch.setattr(bench, "C", 7)
+    monkeypatch.setattr(bench, "K", 5)
+    p = Problem(v=3, c=7, naux=16, nmo=10, seed=4)
+    oracle.set_threads(2)
+    t_full, desc = bench.cpu_factorised_sample(p.mmn, p.w, p.hqp, nthreads=2, p_slice=4)
+    assert t_full > 0.0
+    assert "4/16 aux functions for 2 vectors" in desc and "3 waves of 2" in desc
+
+
+def test_factorised_slice_is_partial_product():
+    p = Problem(v=3, c=7, naux=16, nmo=10, seed=5)
+    X = np.asfortranarray(np.random.default_rng(0).standard_normal((21, 2)))
+    sliced = oracle.BSEProblem(np.ascontiguousarray(p.mmn[:, :4, :]), p.w[:4], p.hqp, 3, 7)
+    zeroed = p.mmn.copy()
+    zeroed[:, 4:, :] = 0.0
+    full = oracle.BSEProblem(zeroed, p.w, p.hqp, 3, 7)
+    np.testing.assert_allclose(sliced.matmul_fact(X), full.matmul_fact(X), rtol=1e-13, atol=1e-13)
