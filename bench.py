@@ -182,10 +182,11 @@ def cpu_factorised_sample(mmn, w, hqp, nthreads, p_slice=64):
     return t_full, desc
 
 
-def cpu_baseline(mmn, w, hqp, seconds_target=20.0, factorised=False):
+def cpu_baseline(mmn, w, hqp, seconds_target=20.0, factorised=False, triplet=False):
     """The reference's CPU loop nest on a bounded sample of one singlet matvec at the
-    benchmark workload, with all host threads; with factorised, also the factorised FP64
-    oracle as an informational second CPU figure."""
+    benchmark workload, with all host threads; with triplet, also one triplet matvec (no Hx
+    stage); with factorised, also the factorised FP64 oracle as an informational second CPU
+    figure."""
     import oracle
 
     nthreads = os.cpu_count() or 1
@@ -197,6 +198,9 @@ def cpu_baseline(mmn, w, hqp, seconds_target=20.0, factorised=False):
         "value": F / t_full / 1e12, "unit": "TFLOP/s", "cores": nthreads, "kind": "port",
         "sample": desc, "seconds_per_matvec": t_full,
     }
+    if triplet:
+        t_trip, desc_t = sample_matvec(prob, V, C, K, "triplet", seconds_target / 2, nthreads)
+        out["triplet"] = {"seconds_per_matvec": t_trip, "sample": desc_t}
     if factorised:
         try:
             t_fact, desc_f = cpu_factorised_sample(mmn, w, hqp, nthreads)
@@ -205,6 +209,23 @@ def cpu_baseline(mmn, w, hqp, seconds_target=20.0, factorised=False):
         except Exception as exc:  # informational only: never costs the reference figure
             out["factorised_oracle"] = {"error": f"{type(exc).__name__}: {exc}"}
     return out
+
+
+def cpu_time_to_roots(roots, per_call):
+    """The reference CPU path's time-to-roots, extrapolated: the FP64 GPU solve runs the
+    reference's Davidson algorithm, so the CPU solve makes as many operator calls (one per
+    iteration, num_iterations() + 1), and a call of the reference loop nest costs the same for any block width up
+    to the 2 (vc)^2 k term (1.5 % at k = 30), so each call is charged the sampled k = 30
+    product time.  roots: the time_to_20_roots report; per_call: {"singlets": s, "triplets": s}."""
+    for kind, t_call in per_call.items():
+        rep = roots.get(kind, {}).get("fp64")
+        if not rep or t_call is None:
+            continue
+        n = int(rep["iterations"]) + 1  # num_iterations() is the index of the last iteration
+        roots[kind]["cpu_reference_extrapolated"] = {
+            "seconds": n * t_call, "operator_calls": n, "seconds_per_call": t_call,
+            "note": "operator calls of the FP64 solve x the sampled reference product time"}
+    return roots
 
 
 def ref_matvec_flops(v, c, naux, k):
@@ -759,7 +780,11 @@ def main():
     if rank == 0 and args.full_bse:
         line["full_bse"] = full_bse_report(check=args.full_bse_check, cpu=world == 1 and not args.no_cpu)
     if rank == 0 and world == 1 and not args.no_cpu:
-        cb = cpu_baseline(mmn, w, hqp, factorised=True)
+        cb = cpu_baseline(mmn, w, hqp, factorised=True, triplet="time_to_20_roots" in line)
+        if "time_to_20_roots" in line:
+            cpu_time_to_roots(line["time_to_20_roots"],
+                              {"singlets": cb["seconds_per_matvec"],
+                               "triplets": cb.get("triplet", {}).get("seconds_per_matvec")})
         cb.pop("seconds_per_matvec", None)
         line["cpu_baseline"] = cb
     if rank == 0:

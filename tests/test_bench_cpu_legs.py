@@ -27,3 +27,24 @@ def test_factorised_slice_is_partial_product():
     zeroed[:, 4:, :] = 0.0
     full = oracle.BSEProblem(zeroed, p.w, p.hqp, 3, 7)
     np.testing.assert_allclose(sliced.matmul_fact(X), full.matmul_fact(X), rtol=1e-13, atol=1e-13)
+
+
+def test_cpu_time_to_roots_counts_operator_calls():
+    roots = {"singlets": {"fp64": {"iterations": 3}, "mixed": {"iterations": 3}},
+             "triplets": {"fp64": {"iterations": 5}}}
+    out = bench.cpu_time_to_roots(roots, {"singlets": 47.0, "triplets": None})
+    rep = out["singlets"]["cpu_reference_extrapolated"]
+    assert rep["operator_calls"] == 4 and rep["seconds"] == 4 * 47.0
+    assert "cpu_reference_extrapolated" not in out["triplets"]          # no triplet sample
+    out = bench.cpu_time_to_roots({"singlets": {"mixed": {"iterations": 2}}}, {"singlets": 1.0})
+    assert "cpu_reference_extrapolated" not in out["singlets"]          # no FP64 solve
+
+
+def test_cpu_baseline_legs_small(monkeypatch):
+    for name, val in (("V", 3), ("C", 7), ("K", 5), ("NAUX", 16)):
+        monkeypatch.setattr(bench, name, val)
+    p = Problem(v=3, c=7, naux=16, nmo=10, seed=6)
+    cb = bench.cpu_baseline(p.mmn, p.w, p.hqp, seconds_target=0.2, factorised=True, triplet=True)
+    assert cb["kind"] == "port" and cb["seconds_per_matvec"] > 0 and cb["value"] > 0
+    assert cb["triplet"]["seconds_per_matvec"] > 0
+    assert cb["factorised_oracle"]["seconds_per_matvec"] > 0, cb["factorised_oracle"]
