@@ -36,7 +36,7 @@ def _rank(rank, world, port, out):
 def test_two_replicas_max_time_and_summed_throughput():
     world = 2
     port = _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:  # no fork of a process with OpenMP threads
         out = m.dict()
         mp.spawn(_rank, args=(world, port, out), nprocs=world, join=True)
         res = dict(out)
