@@ -145,3 +145,22 @@ def test_exciton_weights_uks():
     assert [(t.v, t.c) for t in full[1]["contributions"]] == [(0, 0)]
     many = exciton_weights_uks(opt, np.ones((na + nb, 1)) * 0.9, min_print_weight=0.5)
     assert len(many[0]["contributions"]) == 8 and many[0]["more_above_threshold"] == na + nb - 8
+
+
+def test_product_dense_full_bse_branch_matches_oracle():
+    """The product's host dense branch (used up to dim 128) against the oracle's restatement on
+    the same A, B: same roots, same phase and normalisation of X and Y."""
+    from oracle.uks_oracle import full_bse_dense_roots
+    from votca_gb300.bse_operator_uks import _dense_full_bse
+
+    for seed in (4, 9):
+        p = UKSProblem(3, 2, vmin=0, cmax=7, naux=8, nmo=8, seed=seed)
+        o = _oracle(p)
+        A, B = o.dense("tda"), o.dense("btda_b")
+        lam, X, Y = _dense_full_bse(A, B, 5)
+        lo, Xo, Yo = full_bse_dense_roots(A, B, 5)
+        np.testing.assert_allclose(lam, lo, rtol=0, atol=1e-12)
+        np.testing.assert_allclose(X, Xo, rtol=0, atol=1e-10)
+        np.testing.assert_allclose(Y, Yo, rtol=0, atol=1e-10)
+    with pytest.raises(RuntimeError):
+        _dense_full_bse(np.zeros((3, 3)), np.eye(3), 2)   # eigenvalues +-i: no real root
