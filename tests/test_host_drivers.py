@@ -89,3 +89,38 @@ def test_rpa_input_energies_window_offsets():
         update_rpa_input_energies(dft, np.zeros(7), 2, 3, 1, 7)     # QP levels past rpamax
     with pytest.raises(ValueError):
         update_rpa_input_energies(dft, gw, 0, 3, 1, 7)              # qpmin below rpamin
+
+
+def test_davidson_option_setters():
+    """DavidsonSolver's setters (davidsonsolver.cc:101-147): preset tolerances, the correction,
+    update and matrix-type names, the reference's error text for unknown names, and the option
+    struct handed to bse_davidson_solve; BSE::solve_hermitian's search space of 10 * nmax
+    (bse.cc:266-293)."""
+    from votca_gb300.bse import DavidsonOptions, _solver
+    from votca_gb300.davidson import DavidsonSolver
+
+    ds = DavidsonSolver()
+    o = ds._options()
+    assert (o.iter_max, o.tolerance, o.max_search_space, o.correction, o.update, o.matrix_type) == \
+        (50, 1e-4, 0, 0, 1, 0)                      # the reference's defaults
+    for name, tol in (("loose", 1e-3), ("normal", 1e-4), ("strict", 1e-5), ("lapack", 1e-9)):
+        ds.set_tolerance(name)
+        assert ds._options().tolerance == tol
+    ds.set_tolerance(3e-7)
+    ds.set_correction("OLSEN")
+    ds.set_size_update("max")
+    ds.set_matrix_type("HAM")
+    ds.set_iter_max(7)
+    ds.set_max_search_space(33)
+    o = ds._options()
+    assert (o.iter_max, o.tolerance, o.max_search_space, o.correction, o.update, o.matrix_type) == \
+        (7, 3e-7, 33, 1, 2, 1)
+    for setter, bad, text in ((ds.set_tolerance, "tight", "is not a valid Davidson tolerance"),
+                              (ds.set_correction, "dpr", "is not a valid Davidson correction method"),
+                              (ds.set_size_update, "SAFE", "is not a valid Davidson update"),
+                              (ds.set_matrix_type, "SYM", "is not a valid Davidson matrix type")):
+        with pytest.raises(RuntimeError, match=text):
+            setter(bad)
+    s = _solver(DavidsonOptions(davidson_correction="OLSEN", davidson_tolerance="strict",
+                                davidson_update="min", davidson_maxiter=12, nmax=4))._options()
+    assert (s.iter_max, s.tolerance, s.max_search_space, s.correction, s.update) == (12, 1e-5, 40, 1, 0)
