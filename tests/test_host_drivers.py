@@ -124,3 +124,20 @@ def test_davidson_option_setters():
     s = _solver(DavidsonOptions(davidson_correction="OLSEN", davidson_tolerance="strict",
                                 davidson_update="min", davidson_maxiter=12, nmax=4))._options()
     assert (s.iter_max, s.tolerance, s.max_search_space, s.correction, s.update) == (12, 1e-5, 40, 1, 0)
+
+
+def test_tcmatrix_container_mirror():
+    """TCMatrix_gwbse (threecenter.h:70-142, Initialize threecenter.cc:29-48): window accessors and
+    slice m as the [nsize x auxsize] matrix Mmn_[m] over the (msize, auxsize, nsize) storage."""
+    from votca_gb300.bse_operator import TCMatrix_gwbse
+
+    M = TCMatrix_gwbse.Initialize(5, 2, 6, 1, 4)
+    assert (M.msize(), M.nsize(), M.auxsize()) == (5, 4, 5)
+    assert (M.get_mmin(), M.get_mmax(), M.get_nmin(), M.get_nmax()) == (2, 6, 1, 4)
+    assert M.data.shape == (5, 5, 4) and not M.data.any()
+    M[3][2, 4] = 7.0                                   # Mmn_[3](n = 2, P = 4), a view
+    assert M.data[3, 4, 2] == 7.0 and M[3].shape == (4, 5)
+    d = np.arange(2 * 3 * 4, dtype=np.float64).reshape(2, 3, 4)
+    T = TCMatrix_gwbse(d, mmin=1, nmin=0)
+    np.testing.assert_array_equal(T[1], d[1].T)
+    assert (T.get_mmax(), T.get_nmax()) == (2, 3)
