@@ -62,49 +62,85 @@ void oracle_set_threads(int n) {
 #endif
 }
 
-/* row (ct x vt, column-major: row[c + ct*v]) += A (ct x naux, row-major a[c*naux+P])
- *                                                * B^T (B: vt x naux row-major)
- * Small register-blocked kernel; both operands P-contiguous. */
+/* Two doubles per vector register (SSE2 on x86-64, ASIMD on aarch64) through GCC's
+ * portable vector extensions: no target intrinsics, unaligned loads through memcpy.  The
+ * reference's CPU path runs Eigen's vectorised GEMM here; scalar dot products would
+ * understate it several-fold. */
+typedef double v2d __attribute__((vector_size(16)));
+static inline v2d ld2(const double *p) {
+  v2d r;
+  memcpy(&r, p, sizeof r);
+  return r;
+}
+static inline double hsum(v2d a) { return a[0] + a[1]; }
+
+/* sum_p a[p] b[p], four independent vector partial sums */
+static double dot(const double *a, const double *b, i64 n) {
+  v2d s0 = {0.0, 0.0}, s1 = s0, s2 = s0, s3 = s0;
+  i64 p = 0;
+  for (; p + 8 <= n; p += 8) {
+    s0 += ld2(a + p) * ld2(b + p);
+    s1 += ld2(a + p + 2) * ld2(b + p + 2);
+    s2 += ld2(a + p + 4) * ld2(b + p + 4);
+    s3 += ld2(a + p + 6) * ld2(b + p + 6);
+  }
+  double s = hsum((s0 + s1) + (s2 + s3));
+  for (; p < n; ++p) s += a[p] * b[p];
+  return s;
+}
+
+/* C (rows_a x rows_b, column-major, ldc) += A * B^T with A (rows_a x K) and B (rows_b x K)
+ * both row-major (K contiguous).  K is processed in chunks of KB so that a chunk of B stays in
+ * the core's cache while the 4 x 4 register blocks sweep A; within a block, 16 vector partial
+ * sums over K. */
+enum { KB = 128 };
 static void gemm_abt(i64 rows_a, i64 rows_b, i64 K, const double *A,
                      const double *B, double *C, i64 ldc) {
-  i64 i = 0;
-  for (; i + 4 <= rows_a; i += 4) {
-    const double *a0 = A + (i + 0) * K, *a1 = A + (i + 1) * K,
-                 *a2 = A + (i + 2) * K, *a3 = A + (i + 3) * K;
-    i64 j = 0;
-    for (; j + 2 <= rows_b; j += 2) {
-      const double *b0 = B + j * K, *b1 = B + (j + 1) * K;
-      double s00 = 0, s10 = 0, s20 = 0, s30 = 0, s01 = 0, s11 = 0, s21 = 0,
-             s31 = 0;
-      for (i64 p = 0; p < K; ++p) {
-        double x0 = b0[p], x1 = b1[p];
-        s00 += a0[p] * x0; s10 += a1[p] * x0; s20 += a2[p] * x0; s30 += a3[p] * x0;
-        s01 += a0[p] * x1; s11 += a1[p] * x1; s21 += a2[p] * x1; s31 += a3[p] * x1;
+  for (i64 k0 = 0; k0 < K; k0 += KB) {
+    const i64 kn = K - k0 < KB ? K - k0 : KB;
+    i64 i = 0;
+    for (; i + 4 <= rows_a; i += 4) {
+      const double *a0 = A + (i + 0) * K + k0, *a1 = A + (i + 1) * K + k0,
+                   *a2 = A + (i + 2) * K + k0, *a3 = A + (i + 3) * K + k0;
+      i64 j = 0;
+      for (; j + 4 <= rows_b; j += 4) {
+        const double *b0 = B + (j + 0) * K + k0, *b1 = B + (j + 1) * K + k0,
+                     *b2 = B + (j + 2) * K + k0, *b3 = B + (j + 3) * K + k0;
+        v2d c00 = {0.0, 0.0}, c01 = c00, c02 = c00, c03 = c00, c10 = c00, c11 = c00,
+            c12 = c00, c13 = c00, c20 = c00, c21 = c00, c22 = c00, c23 = c00, c30 = c00,
+            c31 = c00, c32 = c00, c33 = c00;
+        i64 p = 0;
+        for (; p + 2 <= kn; p += 2) {
+          const v2d x0 = ld2(a0 + p), x1 = ld2(a1 + p), x2 = ld2(a2 + p), x3 = ld2(a3 + p);
+          const v2d y0 = ld2(b0 + p), y1 = ld2(b1 + p), y2 = ld2(b2 + p), y3 = ld2(b3 + p);
+          c00 += x0 * y0; c01 += x0 * y1; c02 += x0 * y2; c03 += x0 * y3;
+          c10 += x1 * y0; c11 += x1 * y1; c12 += x1 * y2; c13 += x1 * y3;
+          c20 += x2 * y0; c21 += x2 * y1; c22 += x2 * y2; c23 += x2 * y3;
+          c30 += x3 * y0; c31 += x3 * y1; c32 += x3 * y2; c33 += x3 * y3;
+        }
+        double r[4][4] = {{hsum(c00), hsum(c01), hsum(c02), hsum(c03)},
+                          {hsum(c10), hsum(c11), hsum(c12), hsum(c13)},
+                          {hsum(c20), hsum(c21), hsum(c22), hsum(c23)},
+                          {hsum(c30), hsum(c31), hsum(c32), hsum(c33)}};
+        for (; p < kn; ++p) {
+          const double x[4] = {a0[p], a1[p], a2[p], a3[p]};
+          const double y[4] = {b0[p], b1[p], b2[p], b3[p]};
+          for (int ii = 0; ii < 4; ++ii)
+            for (int jj = 0; jj < 4; ++jj) r[ii][jj] += x[ii] * y[jj];
+        }
+        for (int jj = 0; jj < 4; ++jj)
+          for (int ii = 0; ii < 4; ++ii) C[(i + ii) + (j + jj) * ldc] += r[ii][jj];
       }
-      C[(i + 0) + j * ldc] += s00; C[(i + 1) + j * ldc] += s10;
-      C[(i + 2) + j * ldc] += s20; C[(i + 3) + j * ldc] += s30;
-      C[(i + 0) + (j + 1) * ldc] += s01; C[(i + 1) + (j + 1) * ldc] += s11;
-      C[(i + 2) + (j + 1) * ldc] += s21; C[(i + 3) + (j + 1) * ldc] += s31;
-    }
-    for (; j < rows_b; ++j) {
-      const double *b0 = B + j * K;
-      double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
-      for (i64 p = 0; p < K; ++p) {
-        s0 += a0[p] * b0[p]; s1 += a1[p] * b0[p];
-        s2 += a2[p] * b0[p]; s3 += a3[p] * b0[p];
+      for (; j < rows_b; ++j) {
+        const double *b0 = B + j * K + k0;
+        C[(i + 0) + j * ldc] += dot(a0, b0, kn);
+        C[(i + 1) + j * ldc] += dot(a1, b0, kn);
+        C[(i + 2) + j * ldc] += dot(a2, b0, kn);
+        C[(i + 3) + j * ldc] += dot(a3, b0, kn);
       }
-      C[(i + 0) + j * ldc] += s0; C[(i + 1) + j * ldc] += s1;
-      C[(i + 2) + j * ldc] += s2; C[(i + 3) + j * ldc] += s3;
     }
-  }
-  for (; i < rows_a; ++i) {
-    const double *a0 = A + i * K;
-    for (i64 j = 0; j < rows_b; ++j) {
-      const double *b0 = B + j * K;
-      double s = 0;
-      for (i64 p = 0; p < K; ++p) s += a0[p] * b0[p];
-      C[i + j * ldc] += s;
-    }
+    for (; i < rows_a; ++i)
+      for (i64 j = 0; j < rows_b; ++j) C[i + j * ldc] += dot(A + i * K + k0, B + j * K + k0, kn);
   }
 }
 
@@ -182,9 +218,7 @@ void oracle_bse_matmul_ref(const double *mmn, i64 nm, i64 nn, i64 naux,
         i64 I = ct * v1 + c1;
         for (i64 j = 0; j < k; ++j) {
           const double *xj = X + j * ldx;
-          double s = 0;
-          for (i64 q = 0; q < dim; ++q) s += row[q] * xj[q];
-          red[I + j * dim] = s;
+          red[I + j * dim] = dot(row, xj, dim);
         }
       }
     }
@@ -213,10 +247,7 @@ void oracle_bse_matmul_ref(const double *mmn, i64 nm, i64 nn, i64 naux,
             }
             if (v1 != v2) { /* r2 += blk^T * x1 */
               for (i64 cc = 0; cc < ct; ++cc) {
-                const double *bcol = blk + cc * ct;
-                double s = 0;
-                for (i64 c = 0; c < ct; ++c) s += bcol[c] * x1[c];
-                r2[cc] += s;
+                r2[cc] += dot(blk + cc * ct, x1, ct);
               }
             }
           }
