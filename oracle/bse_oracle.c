@@ -331,22 +331,17 @@ void oracle_bse_matmul_fact(const double *mmn, i64 nm, i64 nn, i64 naux,
       if (cx != 0) {
         double z = 0;
         for (i64 v = 0; v < vt; ++v)
-          for (i64 c = 0; c < ct; ++c)
-            z += mget(mmn, nn, naux, v + voff, c + coff, P) * x[ct * v + c];
+          z += dot(&mmn[(v + voff) * (nn * naux) + P * nn + coff], x + ct * v, ct);
         z *= cx;
         for (i64 v = 0; v < vt; ++v)
           for (i64 c = 0; c < ct; ++c)
             y[ct * v + c] += mget(mmn, nn, naux, v + voff, c + coff, P) * z;
       }
       if (cd != 0) {
-        /* t[v][c1] = sum_c M(c1,c,P) x[v][c] */
+        /* t[v][c1] = sum_c M(c1,c,P) x[v][c]  (row c1 of slice P contiguous in c) */
         for (i64 v = 0; v < vt; ++v)
-          for (i64 c1 = 0; c1 < ct; ++c1) {
-            double s = 0;
-            for (i64 c = 0; c < ct; ++c)
-              s += mget(mmn, nn, naux, c1 + coff, c + coff, P) * x[ct * v + c];
-            t[ct * v + c1] = s;
-          }
+          for (i64 c1 = 0; c1 < ct; ++c1)
+            t[ct * v + c1] = dot(&mmn[(c1 + coff) * (nn * naux) + P * nn + coff], x + ct * v, ct);
         double f = cd * w[P];
         for (i64 v1 = 0; v1 < vt; ++v1)
           for (i64 v = 0; v < vt; ++v) {
@@ -357,20 +352,12 @@ void oracle_bse_matmul_fact(const double *mmn, i64 nm, i64 nn, i64 naux,
       if (cd2 != 0) {
         /* u[v1][v] = sum_c M(v1,c,P) x[v][c] */
         for (i64 v1 = 0; v1 < vt; ++v1)
-          for (i64 v = 0; v < vt; ++v) {
-            double s = 0;
-            for (i64 c = 0; c < ct; ++c)
-              s += mget(mmn, nn, naux, v1 + voff, c + coff, P) * x[ct * v + c];
-            t[vt * v1 + v] = s;
-          }
+          for (i64 v = 0; v < vt; ++v)
+            t[vt * v1 + v] = dot(&mmn[(v1 + voff) * (nn * naux) + P * nn + coff], x + ct * v, ct);
         double f = cd2 * w[P];
         for (i64 v1 = 0; v1 < vt; ++v1)
-          for (i64 c1 = 0; c1 < ct; ++c1) {
-            double s = 0;
-            for (i64 v = 0; v < vt; ++v)
-              s += mget(mmn, nn, naux, c1 + coff, v + voff, P) * t[vt * v1 + v];
-            y[ct * v1 + c1] -= f * s;
-          }
+          for (i64 c1 = 0; c1 < ct; ++c1)
+            y[ct * v1 + c1] -= f * dot(&mmn[(c1 + coff) * (nn * naux) + P * nn + voff], t + vt * v1, vt);
       }
     }
     if (cqp != 0) {
