@@ -48,3 +48,16 @@ def test_cpu_baseline_legs_small(monkeypatch):
     assert cb["kind"] == "port" and cb["seconds_per_matvec"] > 0 and cb["value"] > 0
     assert cb["triplet"]["seconds_per_matvec"] > 0
     assert cb["factorised_oracle"]["seconds_per_matvec"] > 0, cb["factorised_oracle"]
+
+
+def test_batched_and_full_bse_cpu_legs_small():
+    """The C3 leg (the Davidson restatement on a sampled subset, scaled by the reference's flops)
+    and the C2 leg (one Hamiltonian application, sampled) finish on tiny inputs."""
+    shapes = [{"v": 2, "c": 6, "naux": 8, "nmo": 16, "seed": 1},
+              {"v": 3, "c": 5, "naux": 9, "nmo": 16, "seed": 2},
+              {"v": 2, "c": 7, "naux": 6, "nmo": 17, "seed": 3}]
+    out = bench.cpu_baseline_batched(shapes, roots=2, tol=1e-6, n_sample=2)
+    assert out["unit"] == "roots/s" and out["value"] > 0 and "2 of 3 molecules" in out["sample"]
+    p = Problem(v=3, c=7, naux=16, nmo=10, seed=7)
+    t, desc = bench.cpu_baseline_full_bse(p.mmn, p.w, p.hqp, 3, 7, 2, seconds_target=0.2)
+    assert t > 0 and desc.startswith("A: ") and "; B: " in desc
