@@ -15,7 +15,11 @@ e2e: the same product through the host-pointer C ABI call (bse_op_matmul):
 X copied host->device and Y device->host inside every timed step.
 
 Also reported once, outside the timed steps: time-to-20-roots of the full
-Davidson solve (tolerance 1e-7) for each precision built.
+Davidson solve (tolerance 1e-7) for each precision built, the C0 solve, the
+batched 256-molecule solve, and (N = 1) the CPU figures: the reference loop
+nest port on a bounded sample of one product (cpu_baseline; also one triplet
+product, from which the reference's time-to-20-roots is extrapolated), and the
+factorised FP64 oracle as an informational second figure.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|mixed]
   python bench.py --impl reference ...   # the reference CPU path (oracle port)
