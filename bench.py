@@ -239,10 +239,12 @@ def ref_matvec_flops(v, c, naux, k):
     return 2.0 * vc * vc * naux + v * (v + 1) * c * c * naux + 2.0 * vc * vc * k
 
 
-def cpu_baseline_batched(shapes, roots, tol, n_sample=6):
+def cpu_baseline_batched(shapes, roots, tol, n_sample=6, concurrent=True):
     """The reference CPU path (the DavidsonSolver restatement driving the reference
     loop nest on all host threads) on a seeded subset of the molecules, scaled to the
-    whole set by the reference algorithm's flops per product."""
+    whole set by the reference algorithm's flops per product; with concurrent, also one
+    molecule per single-threaded process on every core, and the faster of the two is the
+    figure."""
     import oracle
     from oracle.davidson_oracle import DavidsonOracle
     from votca_gb300.synthetic import qp_energies, screening_w
@@ -267,11 +269,85 @@ def cpu_baseline_batched(shapes, roots, tol, n_sample=6):
     cost_all = sum(ref_matvec_flops(s["v"], s["c"], s["naux"], 1) for s in shapes)
     t_all = t_sample * cost_all / cost_sample
     nroots = len(shapes) * roots
-    return {
+    out = {
         "value": nroots / t_all, "unit": "roots/s", "cores": nthreads, "kind": "port",
         "sample": (f"{n_sample} of {len(shapes)} molecules (evenly spaced) solved one after the other "
                    f"({t_sample:.1f} s, iterations {iters}), scaled by the reference algorithm's "
                    f"flops per product to all molecules: {t_all:.0f} s"),
+    }
+    if concurrent:
+        try:
+            conc = _cpu_batched_concurrent(shapes, roots, tol, nthreads)
+        except Exception as exc:  # the sequential figure stands
+            conc = {"error": f"{type(exc).__name__}: {exc}"}
+        out["concurrent"] = conc
+        if conc.get("value", 0.0) > out["value"]:
+            out["sequential_value"] = out["value"]
+            out["value"] = conc["value"]
+            out["cores"] = conc["cores"]
+            out["sample"] = conc["sample"] + "; one after the other: " + out["sample"]
+    return out
+
+
+def _solve_molecule_one_thread(task):
+    """Worker of the concurrent CPU leg: one molecule, one OpenMP thread (spawned process)."""
+    sh, roots, tol = task
+    import oracle
+    from oracle.davidson_oracle import DavidsonOracle
+    from votca_gb300.synthetic import mmn_tensor, qp_energies, screening_w
+
+    oracle.set_threads(1)
+    v, c, naux, seed = sh["v"], sh["c"], sh["naux"], sh["seed"]
+    prob = oracle.BSEProblem(mmn_tensor(seed, naux, sh["nmo"]), screening_w(seed, naux),
+                             np.diag(qp_energies(seed, v, c)), v, c)
+    d = DavidsonOracle()
+    d.set_tolerance(tol)
+    d.max_search_space = 10 * roots
+    t0 = time.perf_counter()
+    d.solve(lambda X: prob.matmul_ref(X, "singlet"), prob.diagonal("singlet"), roots)
+    return time.perf_counter() - t0, int(d.i_iter)
+
+
+def _cpu_batched_concurrent(shapes, roots, tol, nworkers):
+    """The reference run as it runs on many molecules, one molecule per process: nworkers
+    spawned single-threaded processes (OpenMP and BLAS at one thread) solve as many evenly
+    spaced molecules at once.  Scaled to the whole set as a queue over the workers: the busy
+    seconds of the sample per worker, times the reference flops of all molecules over those of
+    the sample.  The workers draw Mmn with the numpy generator (same distribution as the
+    one-after-the-other leg, other values)."""
+    import multiprocessing as mpr
+    from concurrent.futures import ProcessPoolExecutor
+
+    n = max(1, min(nworkers, len(shapes)))
+    pick = np.linspace(0, len(shapes) - 1, n).round().astype(int)
+    tasks = [(shapes[i], roots, tol) for i in pick]
+    keys = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")
+    saved = {k: os.environ.get(k) for k in keys}
+    os.environ.update({k: "1" for k in keys})  # inherited by the spawned workers
+    try:
+        # an executor, not a Pool: a worker that dies raises BrokenProcessPool instead of being
+        # replaced forever; every wait is bounded
+        with ProcessPoolExecutor(max_workers=n, mp_context=mpr.get_context("spawn")) as ex:
+            list(ex.map(abs, range(n), timeout=120))  # start the workers before the timed map
+            t0 = time.perf_counter()
+            res = list(ex.map(_solve_molecule_one_thread, tasks, timeout=600))
+            wall = time.perf_counter() - t0
+    finally:
+        for k, val in saved.items():
+            if val is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = val
+    busy = sum(t for t, _ in res)
+    cost_sample = sum(ref_matvec_flops(shapes[i]["v"], shapes[i]["c"], shapes[i]["naux"], 1) for i in pick)
+    cost_all = sum(ref_matvec_flops(s["v"], s["c"], s["naux"], 1) for s in shapes)
+    t_all = busy / n * cost_all / cost_sample
+    return {
+        "value": len(shapes) * roots / t_all, "unit": "roots/s", "cores": n, "kind": "port",
+        "sample": (f"{n} of {len(shapes)} molecules (evenly spaced) solved at once, one single-threaded "
+                   f"process each ({wall:.1f} s wall, {busy:.1f} busy seconds, iterations "
+                   f"{[it for _, it in res]}), scaled as a queue over {n} processes by the reference "
+                   f"algorithm's flops to all molecules: {t_all:.0f} s"),
     }
 
 

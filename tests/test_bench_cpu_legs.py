@@ -51,13 +51,21 @@ def test_cpu_baseline_legs_small(monkeypatch):
 
 
 def test_batched_and_full_bse_cpu_legs_small():
-    """The C3 leg (the Davidson restatement on a sampled subset, scaled by the reference's flops)
+    """The C3 leg (the Davidson restatement on a sampled subset, scaled by the reference's flops;
+    one after the other on all threads, and one molecule per spawned single-threaded process)
     and the C2 leg (one Hamiltonian application, sampled) finish on tiny inputs."""
     shapes = [{"v": 2, "c": 6, "naux": 8, "nmo": 16, "seed": 1},
               {"v": 3, "c": 5, "naux": 9, "nmo": 16, "seed": 2},
               {"v": 2, "c": 7, "naux": 6, "nmo": 17, "seed": 3}]
     out = bench.cpu_baseline_batched(shapes, roots=2, tol=1e-6, n_sample=2)
     assert out["unit"] == "roots/s" and out["value"] > 0 and "2 of 3 molecules" in out["sample"]
+    conc = out["concurrent"]                    # spawned single-threaded processes, one per molecule
+    assert "error" not in conc, conc
+    assert conc["value"] > 0 and "3 of 3 molecules (evenly spaced) solved at once" in conc["sample"]
+    if "sequential_value" in out:               # the concurrent figure won
+        assert out["value"] == conc["value"] > out["sequential_value"]
+    else:
+        assert out["value"] >= conc["value"]
     p = Problem(v=3, c=7, naux=16, nmo=10, seed=7)
     t, desc = bench.cpu_baseline_full_bse(p.mmn, p.w, p.hqp, 3, 7, 2, seconds_target=0.2)
     assert t > 0 and desc.startswith("A: ") and "; B: " in desc
