@@ -53,6 +53,7 @@ def lib():
         common = [P, I, I, I, P, P, I, I, I, I, I, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.oracle_bse_matmul_ref.argtypes = common + [P, I, I, P, I, I, I, I, I]
         L.oracle_bse_matmul_fact.argtypes = common + [P, I, I, P, I]
+        L.oracle_bse_matmul_rows.argtypes = common + [P, I, I, ctypes.POINTER(ctypes.c_longlong), I, P]
         L.oracle_bse_diagonal.argtypes = common + [P]
         L.oracle_ham_matmul.argtypes = [P, I, I, I, P, P, I, I, I, I, I,
                                         ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
@@ -111,6 +112,21 @@ class BSEProblem:
         k = X.shape[1]
         Y = np.zeros((self.dim, k), order="F")
         lib().oracle_bse_matmul_fact(*self._common(OPERATORS[op]), _p(X), self.dim, k, _p(Y), self.dim)
+        return Y
+
+    def matmul_rows(self, X, rows, op="singlet"):
+        """Rows `rows` (pair indices) of H X, each row built as the reference loop nest
+        builds it; returns a (len(rows), k) array."""
+        X = np.asfortranarray(X, dtype=np.float64)
+        if X.ndim == 1:
+            X = X.reshape(-1, 1, order="F")
+        k = X.shape[1]
+        r = np.ascontiguousarray(rows, dtype=np.int64)
+        if r.size and (r.min() < 0 or r.max() >= self.dim):
+            raise IndexError("matmul_rows: row index outside the operator")
+        Y = np.zeros((r.size, k), order="F")
+        lib().oracle_bse_matmul_rows(*self._common(OPERATORS[op]), _p(X), self.dim, k,
+                                     r.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)), r.size, _p(Y))
         return Y
 
     def diagonal(self, op="singlet"):

@@ -266,6 +266,61 @@ void oracle_bse_matmul_ref(const double *mmn, i64 nm, i64 nn, i64 naux,
   free(reduce);
 }
 
+/*
+ * Selected rows of the same product: Yr(r, j) = (H X)(rows[r], j) for r < nrows,
+ * Yr column-major nrows x k (ld nrows).  Each row is built as the reference builds
+ * it: the Hd (or Hd2) row from PrepareMatrix1/PrepareMatrix2 and the Hqp row
+ * (bse_operator.cc:61-93, openmp_cuda.cc:299-369), and the row of the Hx blocks
+ * that MultiplyBlocks applies (bse_operator.cc:98-116, openmp_cuda.cc:442-478:
+ * block (v1, v2) = cx Mmn[v1].middleRows(cmin, ct) Mmn[v2].middleRows(cmin, ct)^T,
+ * row c1 of it for v2 >= v1 and of its transpose for v2 < v1, the same numbers);
+ * then MultiplyRow's row^T X.  The cost per row is O(dim * naux), so rows of
+ * products far too large for the full loop nest can be checked.
+ */
+void oracle_bse_matmul_rows(const double *mmn, i64 nm, i64 nn, i64 naux,
+                            const double *w, const double *hqp, i64 ldh, i64 vt,
+                            i64 ct, i64 voff, i64 coff, int cqp, int cx, int cd,
+                            int cd2, const double *X, i64 ldx, i64 k,
+                            const i64 *rows, i64 nrows, double *Yr) {
+  (void)nm;
+  const i64 dim = vt * ct;
+#pragma omp parallel
+  {
+    double *row = (double *)malloc(sizeof(double) * dim);
+    double *temp = (double *)malloc(sizeof(double) * (ct > vt ? ct : vt) * naux);
+    double *mat2 = (double *)malloc(sizeof(double) * (ct > vt ? ct : vt) * naux);
+    double *m1 = (double *)malloc(sizeof(double) * naux);
+#pragma omp for schedule(dynamic)
+    for (i64 r = 0; r < nrows; ++r) {
+      const i64 I = rows[r], v1 = I / ct, c1 = I % ct;
+      memset(row, 0, sizeof(double) * dim);
+      if (cd != 0) {
+        slice_rows_T(mmn, nn, naux, c1 + coff, coff, ct, -(double)cd, w, temp);
+        slice_rows_T(mmn, nn, naux, v1 + voff, voff, vt, 1.0, NULL, mat2);
+        gemm_abt(ct, vt, naux, temp, mat2, row, ct);
+      }
+      if (cd2 != 0) {
+        slice_rows_T(mmn, nn, naux, c1 + coff, voff, vt, -(double)cd2, w, temp);
+        slice_rows_T(mmn, nn, naux, v1 + voff, coff, ct, 1.0, NULL, mat2);
+        gemm_abt(ct, vt, naux, mat2, temp, row, ct);
+      }
+      if (cqp != 0) {
+        for (i64 c = 0; c < ct; ++c) row[c + ct * v1] += cqp * hqp[(vt + c) + (vt + c1) * ldh];
+        for (i64 v = 0; v < vt; ++v) row[c1 + ct * v] -= cqp * hqp[v + v1 * ldh];
+      }
+      if (cx != 0) {
+        slice_rows_T(mmn, nn, naux, v1 + voff, coff + c1, 1, (double)cx, NULL, m1);
+        for (i64 v2 = 0; v2 < vt; ++v2) {
+          slice_rows_T(mmn, nn, naux, v2 + voff, coff, ct, 1.0, NULL, mat2);
+          gemm_abt(1, ct, naux, m1, mat2, row + ct * v2, 1);
+        }
+      }
+      for (i64 j = 0; j < k; ++j) Yr[r + j * nrows] = dot(row, X + j * ldx, dim);
+    }
+    free(row); free(temp); free(mat2); free(m1);
+  }
+}
+
 /* BSE_OPERATOR::diagonal, bse_operator.cc:133-175 */
 void oracle_bse_diagonal(const double *mmn, i64 nm, i64 nn, i64 naux,
                          const double *w, const double *hqp, i64 ldh, i64 vt,

@@ -44,10 +44,27 @@ def test_cpu_baseline_legs_small(monkeypatch):
     for name, val in (("V", 3), ("C", 7), ("K", 5), ("NAUX", 16)):
         monkeypatch.setattr(bench, name, val)
     p = Problem(v=3, c=7, naux=16, nmo=10, seed=6)
-    cb = bench.cpu_baseline(p.mmn, p.w, p.hqp, seconds_target=0.2, factorised=True, triplet=True)
+    cb = bench.cpu_baseline(p.mmn, p.w, p.hqp, factorised=True, triplet=True)
     assert cb["kind"] == "port" and cb["seconds_per_matvec"] > 0 and cb["value"] > 0
+    assert "not extrapolated" in cb["sample"]
     assert cb["triplet"]["seconds_per_matvec"] > 0
     assert cb["factorised_oracle"]["seconds_per_matvec"] > 0, cb["factorised_oracle"]
+
+
+def test_reference_arm_times_whole_products(monkeypatch, capsys):
+    """bench.py --impl reference: every timed step is one whole product of the reference loop
+    nest; one JSON line with the arm's fields."""
+    import argparse
+    import json
+
+    for name, val in (("V", 3), ("C", 7), ("K", 5), ("NAUX", 16), ("NMO", 10)):
+        monkeypatch.setattr(bench, name, val)
+    bench.reference_arm(argparse.Namespace(steps=2, warmup=1))
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["steps"] == 2 and line["value"] > 0
+    assert line["e2e"]["value"] == line["value"] and line["e2e"]["h2d_bytes_per_step"] == 0
+    assert line["cpu_baseline"]["value"] == line["value"]
+    assert "whole k=5 singlet products" in line["cpu_baseline"]["sample"]
 
 
 def test_batched_and_full_bse_cpu_legs_small():

@@ -49,6 +49,24 @@ def test_reference_loop_equals_factorised(small, op):
     assert np.allclose(a, b, rtol=1e-12, atol=1e-13)
 
 
+@pytest.mark.parametrize("op", list(oracle.OPERATORS))
+def test_row_evaluation_equals_reference_loop(op):
+    """oracle_bse_matmul_rows (rows built one at a time) against the full loop nest, with
+    off-diagonal Hqp and a window that starts above rpamin (voff, coff offsets)."""
+    p = Problem(v=7, c=9, naux=13, nmo=20, seed=5)
+    hqp = p.hqp.copy()
+    rng = np.random.default_rng(1)
+    off = 0.05 * rng.standard_normal(hqp.shape)
+    hqp = hqp + off + off.T
+    prob = oracle.BSEProblem(p.mmn, p.w, hqp[2:, 2:], vt=5, ct=9, voff=2, coff=7)
+    X = rng.standard_normal((prob.dim, 3))
+    full = prob.matmul_ref(X, op)
+    rows = np.array([0, 44, 3, prob.dim - 1, 17, 17])
+    np.testing.assert_allclose(prob.matmul_rows(X, rows, op), full[rows], rtol=1e-12, atol=1e-13)
+    with pytest.raises(IndexError):
+        prob.matmul_rows(X, [prob.dim], op)
+
+
 def test_operator_composition(small):
     eye = np.eye(small.dim)
     hqp, hx, hd, hd2 = (small.matmul_ref(eye, o) for o in ("hqp", "hx", "hd", "hd2"))
