@@ -186,17 +186,29 @@ def cpu_factorised_sample(mmn, w, hqp, nthreads, p_slice=64):
     return t_full, desc
 
 
-def cpu_baseline(mmn, w, hqp, seconds_target=20.0, factorised=False, triplet=False):
-    """The reference's CPU loop nest on a bounded sample of one singlet matvec at the
-    benchmark workload, with all host threads; with triplet, also one triplet matvec (no Hx
-    stage); with factorised, also the factorised FP64 oracle as an informational second CPU
-    figure."""
+def full_matvec(prob, v, c, k, op):
+    """One whole k-column product of the reference loop nest (oracle port of
+    bse_operator.cc:39-119 with the CPU branches of openmp_cuda.cc: every c1 row, every
+    v1 <= v2 Hx block) on all host threads.  Returns (seconds, description)."""
+    X = np.asfortranarray(np.random.default_rng(1).standard_normal((v * c, k)))
+    t0 = time.perf_counter()
+    prob.matmul_ref(X, op)
+    t = time.perf_counter() - t0
+    return t, (f"one whole k={k} {op} product of the reference loop nest (row-built Hd over all {c} c1 "
+               f"rows + all {v * (v + 1) // 2} v-pair Hx blocks): {t:.1f} s, not extrapolated")
+
+
+def cpu_baseline(mmn, w, hqp, factorised=False, triplet=False):
+    """The reference's CPU loop nest on one whole singlet matvec at the benchmark workload
+    (about 20 s on 16 cores), with all host threads; with triplet, also one whole triplet
+    matvec (no Hx stage); with factorised, also the factorised FP64 oracle as an
+    informational second CPU figure."""
     import oracle
 
     nthreads = os.cpu_count() or 1
     oracle.set_threads(nthreads)
     prob = oracle.BSEProblem(mmn, w, hqp, V, C)
-    t_full, desc = sample_matvec(prob, V, C, K, "singlet", seconds_target, nthreads)
+    t_full, desc = full_matvec(prob, V, C, K, "singlet")
     F = algorithmic_flops(V, C, NAUX, K)
     out = {
         "value": F / t_full / 1e12, "unit": "TFLOP/s", "cores": nthreads, "kind": "port",
@@ -204,7 +216,7 @@ def cpu_baseline(mmn, w, hqp, seconds_target=20.0, factorised=False, triplet=Fal
         "executed_tflops": ref_matvec_flops(V, C, NAUX, K) / t_full / 1e12,
     }
     if triplet:
-        t_trip, desc_t = sample_matvec(prob, V, C, K, "triplet", seconds_target / 2, nthreads)
+        t_trip, desc_t = full_matvec(prob, V, C, K, "triplet")
         out["triplet"] = {"seconds_per_matvec": t_trip, "sample": desc_t}
     if factorised:
         try:
@@ -370,18 +382,30 @@ def reference_arm(args):
         return
     from votca_gb300.synthetic import qp_energies, screening_w
 
+    import oracle
+
     mmn = make_mmn(1, NAUX, NMO)
     w = screening_w(1, NAUX)
     hqp = np.diag(qp_energies(1, V, C))
+    nthreads = os.cpu_count() or 1
+    oracle.set_threads(nthreads)
+    prob = oracle.BSEProblem(mmn, w, hqp, V, C)
+    X = np.asfortranarray(np.random.default_rng(1).standard_normal((V * C, K)))
+    # warm-up steps: one wave of c1 rows each (caches, page faults, thread pool); not timed
+    for _ in range(args.warmup):
+        prob.matmul_ref(X, "singlet", c1_range=(0, min(C, nthreads)), v1_range=(0, 0))
     times = []
-    cb = None
-    for step in range(args.warmup + args.steps):
-        cb = cpu_baseline(mmn, w, hqp, seconds_target=8.0)
-        if step >= args.warmup:
-            times.append(cb["seconds_per_matvec"])
-    t = float(np.median(times)) if times else cb["seconds_per_matvec"]
+    for _ in range(args.steps):  # every timed step is one whole product: nothing extrapolated
+        t0 = time.perf_counter()
+        prob.matmul_ref(X, "singlet")
+        times.append(time.perf_counter() - t0)
+    t = float(np.mean(times))
     F = algorithmic_flops(V, C, NAUX, K)
     val = F / t / 1e12
+    cb = {"cores": nthreads, "kind": "port",
+          "sample": (f"{args.steps} whole k={K} singlet products of the reference loop nest (every c1 row, "
+                     f"every v1 <= v2 Hx block), mean {t:.1f} s per product (min {min(times):.1f}, "
+                     f"max {max(times):.1f}); warm-up steps: one wave of {min(C, nthreads)} c1 rows each")}
     line = {
         "impl": "reference", "metric": "bse_matvec_tflops", "value": val, "unit": "TFLOP/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
@@ -514,7 +538,8 @@ def full_bse_report(roots=10, tol=1e-7, k=32, check=False, cpu=False):
     flops_a = 2.0 * naux * vc * (v + c) + 4.0 * naux * vc + 2.0 * vc
     flops_b = 4.0 * naux * v * v * c + 4.0 * naux * vc
     F = 2 * k * (flops_a + flops_b)
-    dopt = DavidsonOptions(davidson_tolerance=tol, nmax=roots)
+    # block Davidson with k trial vectors per iteration (the configuration's 32), FP64 polish on
+    dopt = DavidsonOptions(davidson_tolerance=tol, nmax=roots, davidson_block=k)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     lam, Xr, Yr, ds = solve_nonhermitian_davidson(A, B, dopt)
@@ -525,7 +550,11 @@ def full_bse_report(roots=10, tol=1e-7, k=32, check=False, cpu=False):
         "ham_matvec": {"k": k, "seconds": t_ham, "tflops": F / t_ham / 1e12,
                        "flops": F, "note": "host-pointer call, H2D/D2H of 2 x 2n x k doubles included"},
         "time_to_roots_seconds": t_solve, "iterations": int(ds.num_iterations()), "info": ds.info(),
+        "trial_vectors_per_iteration": k,
         "matvec_seconds": ds.result.seconds_matvec, "matvec_columns": int(ds.result.matvec_columns),
+        "max_residual": ds.result.max_residual,
+        "fp64_polish": {"applied": bool(ds.result.polished), "iterations": int(ds.result.polish_iterations),
+                        "fp64_columns": int(ds.result.fp64_columns), "seconds": ds.result.seconds_polish},
         "roots_eV": [round(float(x), 9) for x in lam],
     }
     ctx.close()
@@ -573,7 +602,7 @@ def roots_report(ctx, precision, w, Mmn, hqp, opt):
         except _lib.BSEError as e:
             out[pname] = {"unavailable": str(e)}
     for kind, cls in (("singlets", bo.SingletOperator_TDA), ("triplets", bo.TripletOperator_TDA)):
-        res, vecs = {}, {}
+        res, vecs, lams = {}, {}, {}
         for pname, c2 in ctxs.items():
             ds = DavidsonSolver()
             ds.set_tolerance(1e-7)
@@ -583,10 +612,15 @@ def roots_report(ctx, precision, w, Mmn, hqp, opt):
             lam, v = ds.solve(cls(c2), ROOTS)
             dt = time.perf_counter() - t0
             vecs[pname] = v
+            lams[pname] = lam
+            r = ds.result
             res[pname] = {"seconds": dt, "iterations": int(ds.num_iterations()), "info": ds.info(),
-                          "matvec_seconds": ds.result.seconds_matvec,
-                          "matvec_columns": int(ds.result.matvec_columns),
+                          "matvec_seconds": r.seconds_matvec, "matvec_columns": int(r.matvec_columns),
+                          "max_residual": r.max_residual,
                           "roots_eV": [round(float(x), 9) for x in lam]}
+            if r.polished:
+                res[pname]["fp64_polish"] = {"iterations": int(r.polish_iterations),
+                                             "fp64_columns": int(r.fp64_columns), "seconds": r.seconds_polish}
         if "fp64" in vecs and "mixed" in vecs:
             d = np.abs(np.array(res["fp64"]["roots_eV"]) - np.array(res["mixed"]["roots_eV"])) * 1e3
             res["max_abs_diff_meV"] = float(d.max())
@@ -595,6 +629,11 @@ def roots_report(ctx, precision, w, Mmn, hqp, opt):
             res["min_eigvec_overlap"] = float(ov.min())
             res["max_one_minus_overlap"] = float((1.0 - ov).max())
             res["speedup_mixed_vs_fp64"] = res["fp64"]["seconds"] / res["mixed"]["seconds"]
+            # residuals of the mixed roots under the FP64 operator (an FP64 product on the GPU)
+            lam_m = lams["mixed"]
+            xm = vecs["mixed"]
+            r64 = cls(ctxs["fp64"]).matmul(xm) - xm * lam_m
+            res["mixed"]["max_fp64_residual"] = float(np.max(np.linalg.norm(r64, axis=0)))
         out[kind] = res
         if kind == "singlets" and "fp64" in ctxs:
             # adjoint: d(sum_k g_k Omega_k)/d(Mmn, Hqp, w) for the 5 lowest singlets
