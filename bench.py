@@ -453,7 +453,9 @@ def batched_solve(n_molecules, nthreads, roots=5, tol=1e-7, cpu=False):
     t0 = time.perf_counter()
     ev, info, iters = ds.solve_batch(ops, roots, nthreads=0)  # lockstep, grouped launches
     t_solve = time.perf_counter() - t0
-    # the same molecules as independent solves on host threads (one stream each)
+    # the same molecules as independent solves on host threads (one stream each); like the
+    # lockstep mode, without the FP64 polish
+    ds.set_fp64_polish(False)
     t0 = time.perf_counter()
     evt, _, _ = ds.solve_batch(ops, roots, nthreads=nthreads)
     t_threads = time.perf_counter() - t0
@@ -632,8 +634,25 @@ def roots_report(ctx, precision, w, Mmn, hqp, opt):
             # residuals of the mixed roots under the FP64 operator (an FP64 product on the GPU)
             lam_m = lams["mixed"]
             xm = vecs["mixed"]
-            r64 = cls(ctxs["fp64"]).matmul(xm) - xm * lam_m
+            A64 = cls(ctxs["fp64"])
+            r64 = A64.matmul(xm) - xm * lam_m
             res["mixed"]["max_fp64_residual"] = float(np.max(np.linalg.norm(r64, axis=0)))
+            # for reference: the split-precision iteration alone (no FP64 polish), its roots judged
+            # against the FP64 operator the same way
+            ds = DavidsonSolver()
+            ds.set_tolerance(1e-7)
+            ds.set_max_search_space(10 * ROOTS)
+            ds.set_fp64_polish(False)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            lam_u, xu = ds.solve(cls(ctxs["mixed"]), ROOTS)
+            dt = time.perf_counter() - t0
+            ru = A64.matmul(xu) - xu * lam_u
+            res["mixed_without_polish"] = {
+                "seconds": dt, "iterations": int(ds.num_iterations()), "info": ds.info(),
+                "max_fp64_residual": float(np.max(np.linalg.norm(ru, axis=0))),
+                "max_abs_diff_meV_vs_fp64": float(np.max(np.abs(lam_u - lams["fp64"])) * 1e3),
+                "note": "split-precision residuals only; not a result at the 1e-7 FP64 tolerance"}
         out[kind] = res
         if kind == "singlets" and "fp64" in ctxs:
             # adjoint: d(sum_k g_k Omega_k)/d(Mmn, Hqp, w) for the 5 lowest singlets
@@ -707,6 +726,38 @@ def c0_report(cpu=True):
     return out
 
 
+def solve_only(args):
+    """The profiler workload: a warm-up solve, then one timed 20-singlet solve (tolerance 1e-7,
+    split precision with the FP64 polish) at the workload shape (--shape to change it)."""
+    import torch
+
+    from votca_gb300 import bse_operator as bo
+    from votca_gb300.davidson import DavidsonSolver
+    from votca_gb300.synthetic import qp_energies, screening_w
+
+    v, c, naux, nmo = V, C, NAUX, NMO
+    if args.shape:
+        v, c, naux, nmo = (int(x) for x in args.shape.split(","))
+    mmn = make_mmn(1, naux, nmo)
+    opt = bo.BSEOperator_Options(homo=v - 1, rpamin=0, qpmin=0, vmin=0, cmax=v + c - 1)
+    ctx = bo.GpuBSEContext(screening_w(1, naux), bo.TCMatrix_gwbse(mmn), np.diag(qp_energies(1, v, c)), opt,
+                           precision=bo.PRECISION_MIXED)
+    out = {}
+    for rep in ("warmup", "timed"):
+        ds = DavidsonSolver()
+        ds.set_tolerance(1e-7)
+        ds.set_max_search_space(10 * ROOTS)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ds.solve(bo.SingletOperator_TDA(ctx), ROOTS)
+        r = ds.result
+        out[rep] = {"seconds": time.perf_counter() - t0, "iterations": int(ds.num_iterations()),
+                    "polished": int(r.polished), "max_residual": r.max_residual,
+                    "polish_seconds": r.seconds_polish, "matvec_seconds": r.seconds_matvec}
+    ctx.close()
+    print(json.dumps({"workload": f"tda_singlet_v{v}_c{c}_naux{naux}_roots{ROOTS}_solve", **out}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -724,9 +775,14 @@ def main():
     ap.add_argument("--full-bse", action="store_true",
                     help="also run the full-BSE report (v=128, c=1024, Naux=4096; minutes, ~110 GB of HBM)")
     ap.add_argument("--full-bse-check", action="store_true", help="FP64 evaluation of the full-BSE roots")
+    ap.add_argument("--solve-only", action="store_true",
+                    help="one split-precision 20-singlet solve (with its FP64 polish) at the workload shape, "
+                         "after one warm-up solve, and nothing else (for profiler captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.solve_only:
+        return solve_only(args)
 
     import torch
 

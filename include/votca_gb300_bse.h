@@ -263,15 +263,34 @@ typedef struct bse_davidson_options {
   int32_t update;           /* 0 = min, 1 = safe, 2 = max */
   int32_t matrix_type;      /* 0 = SYMM (Ritz), 1 = HAM (harmonic Ritz) */
   int32_t verbose;          /* print one line per iteration to stderr */
+  /* Fields below have no counterpart in the reference; zero keeps its behaviour. */
+  int32_t fp64_polish;      /* split-precision (BSE_PRECISION_MIXED) operators only: once the
+                               split-precision iterations meet the tolerance (or their largest
+                               residual has not halved in three iterations, or iter_max is
+                               reached), the neigen Ritz vectors are re-applied with FP64
+                               products and the iteration continues on that basis until the
+                               residuals, formed from FP64 products of the Ritz vectors, meet
+                               the tolerance; the returned eigenvalues are those FP64 Rayleigh
+                               quotients.  Ignored for FP64 operators. */
+  int32_t reserved;
+  int64_t size_update;      /* trial vectors per iteration: 0 = getSizeUpdate of `update`
+                               (davidsonsolver.cc:149-170); > 0 = that many (>= neigen) */
+  int64_t initial_size;     /* without a guess: 0 = 2*neigen unit vectors (solve(A, neigen));
+                               > 0 = that many (solve(A, neigen, size_initial_guess),
+                               davidsonsolver.h:64-85) */
 } bse_davidson_options;
 
 typedef struct bse_davidson_result {
   int64_t iterations;      /* num_iterations() */
   int32_t info;            /* 0 = Success, 1 = NoConvergence (eigenpairs of unconverged roots zeroed) */
-  int32_t reserved;
+  int32_t polished;        /* 1 when the returned roots come from the FP64 polish */
   int64_t matvec_columns;  /* operator columns applied during the solve */
   double seconds_matvec;   /* device time in operator products */
   double seconds_total;    /* wall time of the solve */
+  double max_residual;     /* largest residual norm of the neigen roots at return */
+  int64_t fp64_columns;    /* columns applied with FP64 products by the polish */
+  int64_t polish_iterations; /* iterations spent in the polish */
+  double seconds_polish;   /* wall time of the polish */
 } bse_davidson_result;
 
 /*
@@ -321,12 +340,25 @@ int bse_op_profile_read(bse_handle *h, double *stage_ms, int64_t *stage_calls,
  * register-resident FMA loop: the roofline denominator of the FP64 path. */
 int bse_probe_fp64_tflops(double *tflops);
 
+/* The device solver of the Davidson Ritz problems, exposed on its own: the lowest nw[i]
+ * eigenpairs of each of njobs symmetric matrices, every matrix solved on the device in one
+ * launch (one CTA each; FP64 Householder tridiagonalisation, FP32 bisection, FP64 inverse
+ * iteration, back-transformation).  It takes the place of the Eigen::SelfAdjointEigenSolver
+ * that DavidsonSolver::getRitz calls (xtp/src/libxtp/davidsonsolver.cc:221-239).  Host
+ * pointers: T holds the matrices back to back (matrix i column-major m[i] x m[i], lower
+ * triangle read); evals receives sum nw[i] values (ascending per matrix); evecs the m[i] x nw[i]
+ * eigenvector blocks back to back (column-major, orthonormal columns, sign not fixed).
+ * 1 <= nw[i] <= m[i] <= 3000.  phase_cycles (may be NULL): njobs x 4 SM clock cycles spent in
+ * the tridiagonalisation, the bisection, the inverse iteration and the back-transformation. */
+int bse_small_sym_eig(int64_t njobs, const int64_t *m, const int64_t *nw, const double *T,
+                      double *evals, double *evecs, int64_t *phase_cycles);
+
 /* ---- Adjoint (no counterpart in the reference; its forward twin is the
  * expectation-value analysis x^T H_part x of xtp/src/libxtp/gwbse/bse.cc:490-520) ----
  *
  * Hellmann-Feynman gradient of sum_k weights[k] * Omega_k for normalised
  * eigenvectors X (column-major dim x nroots, ldx) of the TDA operator
- * H(cqp, cx, cd, 0):
+ * H(cqp, cx, cd, cd2) (for any coefficient set: the gradient of the quadratic forms):
  *   grad_mmn:       same layout as the Mmn slices given to bse_op_create
  *                   (msize x nsize x auxsize, slices back to back); entries
  *                   outside the BSE window are zero;
@@ -338,6 +370,40 @@ int bse_op_eig_gradient(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd,
                         int64_t nroots, const double *weights,
                         double *grad_mmn, double *grad_hqp,
                         double *grad_screening);
+
+/* Full (non-TDA) BSE: gradient of sum_k weights[k] * Omega_k for eigenvectors (X_k, Y_k) of
+ * [[A, B], [-B, -A]], A = H(a_coef), B = H(b_coef), normalised X^T X - Y^T Y = 1 (as
+ * BSE::Solve_nonhermitian_Davidson returns them, bse.cc:315-360).  Omega is stationary in
+ * z = (X, Y) for S z = Omega J z (S = [[A, B], [B, A]], J = diag(I, -I)), so
+ * dOmega = X^T dA X + Y^T dA Y + 2 X^T dB Y for a symmetric dB, the sum
+ * BSE::Analyze_eh_interaction forms for the full BSE (xtp/src/libxtp/gwbse/bse.cc:551-564); the
+ * gradient with respect to single Mmn entries (which perturb B unsymmetrically) is that of
+ * X^T (dB + dB^T) Y, the first-order change seen through the left eigenvector J z.
+ * X, Y: host, dim x nroots (ldx); outputs as
+ * bse_op_eig_gradient; grad_mmn also carries the entries M(c, v, P) that the Hd2 term of B reads.
+ * Computed in FP64 on the device. */
+int bse_op_eig_gradient_full(bse_handle *h, const int32_t a_coef[4], const int32_t b_coef[4],
+                             const double *X, const double *Y, int64_t ldx, int64_t nroots,
+                             const double *weights, double *grad_mmn, double *grad_hqp,
+                             double *grad_screening);
+
+/* The same gradients kept on the device in the operator's block layouts, so that a caller that
+ * needs only some blocks (or feeds them to further device work) does not move the Mmn-shaped
+ * gradient (8 * msize * nsize * auxsize bytes) to the host.  dX (and dY for the full BSE, NULL
+ * for TDA, in which case b_coef is ignored): device, dim x nroots, leading dimension ldx;
+ * weights: host.  Outputs (device, any may be NULL, overwritten):
+ *   d_grad_vc  [P][v][c]  = dsum/dM(vmin + v, homo + 1 + c, P)       auxsize * dim
+ *   d_grad_cv  [P][v][c]  = dsum/dM(homo + 1 + c, vmin + v, P)       auxsize * dim
+ *   d_grad_vv  [P][v1][v] = dsum/dM(vmin + v1, vmin + v, P)          auxsize * vt * vt
+ *   d_grad_cc  [P][c1][c] = dsum/dM(homo + 1 + c1, homo + 1 + c, P)  auxsize * ct * ct
+ * (M(m, n, P) is row n - nmin of slice m - mmin, aux column P, as in bse_op_create).
+ *   d_grad_hqp (vt + ct)^2 column-major window; d_grad_screening auxsize or auxsize^2.
+ * Stream-ordered on `stream`; returns after the work completed. */
+int bse_op_eig_gradient_device(bse_handle *h, const int32_t a_coef[4], const int32_t b_coef[4],
+                               const double *dX, const double *dY, int64_t ldx, int64_t nroots,
+                               const double *weights, double *d_grad_vc, double *d_grad_cv,
+                               double *d_grad_vv, double *d_grad_cc, double *d_grad_hqp,
+                               double *d_grad_screening, void *stream);
 
 /* Many independent molecules (one handle each, e.g. of uneven BSE dimension),
  * bse_davidson_solve semantics (no guess, eigenvalues only).

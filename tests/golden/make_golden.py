@@ -1,7 +1,8 @@
 """Regenerates the golden fixtures in this folder from the VOTCA-XTP test data.
 
-Run in a checkout that has the reference tree at REF (default /root/reference):
-    python tests/golden/make_golden.py [REF]
+Run where the reference tree (votca/votca) is available, giving its root as the argument or
+in the environment variable VOTCA_REFERENCE_ROOT:
+    python tests/golden/make_golden.py REF
 
 Writes bse_operator_hqp.npz:
   Hqp      17x17  xtp/src/tests/DataFiles/bse_operator/Hqp.mm   (operator input)
@@ -59,7 +60,9 @@ def read_mm_array(path):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("VOTCA_REFERENCE_ROOT")
+    if not ref:
+        sys.exit("usage: make_golden.py REF (the votca/votca source root), or set VOTCA_REFERENCE_ROOT")
     here = os.path.dirname(os.path.abspath(__file__))
     d = os.path.join(ref, "xtp/src/tests/DataFiles/bse_operator")
     eps_inv = np.array([

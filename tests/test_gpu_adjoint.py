@@ -144,3 +144,142 @@ def test_adjoint_dense_screening_finite_differences():
         fd = (f(wp) - f(wm)) / (2 * h)
         an = gW[P, Q] + (gW[Q, P] if P != Q else 0.0)
         assert abs(fd - an) <= fd_tolerance(fd, g, lam0, h), (P, Q, fd, an)
+
+
+def _dense_ab(mmn, hqp, w):
+    """The singlet A and B blocks from the oracle (symmetric parts, as in dense_eigs)."""
+    prob = oracle.BSEProblem(mmn, w, hqp, V, C)
+    A, B = prob.dense("singlet"), prob.dense("singlet_b")
+    return 0.5 * (A + A.T), 0.5 * (B + B.T)
+
+
+def full_eigs(mmn, hqp, w):
+    A, B = _dense_ab(mmn, hqp, w)
+    ev = np.linalg.eigvals(np.block([[A, B], [-B, -A]])).real
+    return np.sort(ev[ev > 0])[:NROOTS]
+
+
+def cpu_reference_gradient_full(mmn, hqp, w, X, Y, g):
+    """dOmega = X^T dA X + Y^T dA Y + X^T (dB + dB^T) Y with torch's CPU autograd in FP64 on the
+    operator assembled element by element from Mmn (Hx, Hd, Hd2 as bse_operator.cc defines them).
+    A single Mmn entry perturbs B unsymmetrically; the first-order change of an eigenvalue of
+    [[A, B], [-B, -A]] (left eigenvector J z) then sees the symmetric part, hence dB + dB^T
+    (2 X^T dB Y for a symmetric perturbation)."""
+    import torch
+
+    M = torch.tensor(mmn, requires_grad=True)
+    W = torch.tensor(w, requires_grad=True)
+    H = torch.tensor(hqp)
+    Mvc, Mvv = M[:V, :, V:V + C], M[:V, :, :V]
+    Mcc, Mcv = M[V:V + C, :, V:V + C], M[V:V + C, :, :V]
+    n = V * C
+    Hx = torch.einsum("vpc,wpd->vcwd", Mvc, Mvc).reshape(n, n)
+    Hd = torch.einsum("p,cpd,vpw->vcwd", W, Mcc, Mvv).reshape(n, n)
+    Hd2 = torch.einsum("p,vpd,cpw->vcwd", W, Mvc, Mcv).reshape(n, n)
+    Hqp = (torch.einsum("vw,cd->vcwd", torch.eye(V, dtype=H.dtype), H[V:, V:])
+           - torch.einsum("vw,cd->vcwd", H[:V, :V], torch.eye(C, dtype=H.dtype))).reshape(n, n)
+    A = Hqp + 2 * Hx - Hd
+    B = 2 * Hx - Hd2
+    Xt, Yt = torch.tensor(X), torch.tensor(Y)
+    om = (torch.einsum("ik,ij,jk->k", Xt, A, Xt) + torch.einsum("ik,ij,jk->k", Yt, A, Yt)
+          + torch.einsum("ik,ij,jk->k", Xt, B + B.T, Yt))
+    (om * torch.tensor(g)).sum().backward()
+    return om.detach().numpy(), M.grad.numpy(), W.grad.numpy()
+
+
+def test_full_bse_adjoint_matches_cpu_reference_and_finite_differences():
+    """Full BSE: the gradient of sum g_k Omega_k (bse_op_eig_gradient_full behind
+    torch.autograd) against the FP64 CPU autograd reference and central differences of the
+    dense [[A, B], [-B, -A]] eigenvalues (step 1e-5)."""
+    import torch
+
+    from votca_gb300.adjoint import BSEFullEigenvalues
+
+    p, opt, mmn, hqp, w = setup(seed=43)
+    hq = p.hqp[:V + C, :V + C].copy()
+    lam = BSEFullEigenvalues.apply(mmn, hqp, w, opt, NROOTS, (1, 2, 1, 0), (0, 2, 0, 1), 1e-10, 0)
+    ref = full_eigs(p.mmn, hq, p.w)
+    assert np.max(np.abs(lam.detach().numpy() - ref)) < 1e-10
+    g = np.array([0.9, -0.4, 1.7])
+    (lam * torch.tensor(g)).sum().backward()
+    gm, gw = mmn.grad.numpy(), w.grad.numpy()
+    # the CPU reference at the eigenvectors of the same solve
+    from votca_gb300 import bse_operator as bo
+    from votca_gb300.bse import DavidsonOptions, solve_nonhermitian_davidson
+
+    ctx = bo.GpuBSEContext(p.w, bo.TCMatrix_gwbse(p.mmn), hq, opt)
+    lam2, X, Y, _ = solve_nonhermitian_davidson(bo.SingletOperator_TDA(ctx), bo.SingletOperator_BTDA_B(ctx),
+                                                DavidsonOptions(davidson_tolerance=1e-10, nmax=NROOTS))
+    om, gm_ref, gw_ref = cpu_reference_gradient_full(p.mmn, hq, p.w, X, Y, g)
+    assert np.allclose(om, lam2, atol=1e-10)
+    assert np.allclose(gm, gm_ref, rtol=1e-8, atol=1e-11), np.abs(gm - gm_ref).max()
+    assert np.allclose(gw, gw_ref, rtol=1e-8, atol=1e-11), np.abs(gw - gw_ref).max()
+    # the cv block (read only by the Hd2 term of B) carries gradient
+    assert np.abs(gm[V:V + C, :, :V]).max() > 0
+    f = lambda mm, ww: float(g @ full_eigs(mm, hq, ww))
+    h = 1e-5
+    rng = np.random.default_rng(2)
+    idx = [(rng.integers(0, V + C), rng.integers(0, NAUX), rng.integers(0, V + C)) for _ in range(48)]
+    for (m, P, n) in idx:
+        mp, mm_ = p.mmn.copy(), p.mmn.copy()
+        mp[m, P, n] += h
+        mm_[m, P, n] -= h
+        fd = (f(mp, p.w) - f(mm_, p.w)) / (2 * h)
+        assert abs(fd - gm[m, P, n]) <= fd_tolerance(fd, g, ref, h), (m, P, n, fd, gm[m, P, n])
+    for P in rng.integers(0, NAUX, 8):
+        wp, wm = p.w.copy(), p.w.copy()
+        wp[P] += h
+        wm[P] -= h
+        fd = (f(p.mmn, wp) - f(p.mmn, wm)) / (2 * h)
+        assert abs(fd - gw[P]) <= fd_tolerance(fd, g, ref, h), (P, fd, gw[P])
+
+
+def test_device_gradient_blocks_match_host_gradient():
+    """bse_op_eig_gradient_device (block layouts on the device) against the Mmn-shaped host
+    gradient, for the TDA and the full-BSE forms."""
+    import ctypes
+
+    import torch
+
+    from votca_gb300 import _lib
+    from votca_gb300 import bse_operator as bo
+    from votca_gb300.bse import DavidsonOptions, solve_nonhermitian_davidson
+
+    p, opt, _, _, _ = setup(seed=47)
+    hq = p.hqp[:V + C, :V + C].copy()
+    ctx = bo.GpuBSEContext(p.w, bo.TCMatrix_gwbse(p.mmn), hq, opt)
+    L = ctx._L
+    lam, X, Y, _ = solve_nonhermitian_davidson(bo.SingletOperator_TDA(ctx), bo.SingletOperator_BTDA_B(ctx),
+                                               DavidsonOptions(davidson_tolerance=1e-10, nmax=NROOTS))
+    g = np.array([1.0, 2.0, -0.5])
+    a = (ctypes.c_int32 * 4)(1, 2, 1, 0)
+    b = (ctypes.c_int32 * 4)(0, 2, 0, 1)
+    n = V * C
+    for full in (False, True):
+        gm = np.zeros(p.mmn.shape)
+        gh = np.zeros((V + C, V + C), order="F")
+        gw = np.zeros(NAUX)
+        Xf, Yf = np.asfortranarray(X), np.asfortranarray(Y)
+        if full:
+            _lib.check(L.bse_op_eig_gradient_full(ctx.handle, a, b, bo._p(Xf), bo._p(Yf), n, NROOTS, bo._p(g),
+                                                  bo._p(gm), bo._p(gh), bo._p(gw)))
+        else:
+            _lib.check(L.bse_op_eig_gradient(ctx.handle, 1, 2, 1, 0, bo._p(Xf), n, NROOTS, bo._p(g), bo._p(gm),
+                                             bo._p(gh), bo._p(gw)))
+        dX = torch.from_numpy(Xf.T.copy()).cuda()
+        dY = torch.from_numpy(Yf.T.copy()).cuda()
+        outs = [torch.full((NAUX * sz,), float("nan"), dtype=torch.float64, device="cuda")
+                for sz in (n, n, V * V, C * C, (V + C) ** 2, 1)]
+        ptr = [ctypes.c_void_p(t.data_ptr()) for t in outs]
+        ptr[4] = ctypes.c_void_p(outs[4].data_ptr())
+        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        _lib.check(L.bse_op_eig_gradient_device(ctx.handle, a, b, ctypes.c_void_p(dX.data_ptr()),
+                                                ctypes.c_void_p(dY.data_ptr()) if full else None, n, NROOTS,
+                                                bo._p(g), *ptr, stream))
+        vc, cv, vv, cc, hh, ww = (t.cpu().numpy() for t in outs)
+        np.testing.assert_allclose(vc.reshape(NAUX, V, C), gm[:V, :, V:V + C].transpose(1, 0, 2), atol=1e-13)
+        np.testing.assert_allclose(cv.reshape(NAUX, V, C), gm[V:V + C, :, :V].transpose(1, 2, 0), atol=1e-13)
+        np.testing.assert_allclose(vv.reshape(NAUX, V, V), gm[:V, :, :V].transpose(1, 0, 2), atol=1e-13)
+        np.testing.assert_allclose(cc.reshape(NAUX, C, C), gm[V:V + C, :, V:V + C].transpose(1, 0, 2), atol=1e-13)
+        np.testing.assert_allclose(hh[:(V + C) ** 2].reshape((V + C, V + C), order="F"), gh, atol=1e-13)
+        np.testing.assert_allclose(ww[:NAUX], gw, atol=1e-13)

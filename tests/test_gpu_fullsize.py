@@ -4,10 +4,15 @@ oracle is too slow to be the reference:
 - v=64, c=512, Naux=2048 (dim 32768): mixed vs FP64 products; symmetry x^T H y = y^T H x;
   linearity; the diagonal against e_i^T H e_i; Singlet = Hqp + 2 Hx - Hd term by term.
 - v=128, c=1024, Naux=4096 (dim 131072 per block), full BSE: the Hamiltonian product
-  [[A, B], [-B, -A]] [x; y] against separate A and B products.
+  [[A, B], [-B, -A]] [x; y] against separate A and B products, and sampled rows of it against
+  the reference loop nest's rows (the oracle builds single rows at O(dim * Naux) each).
 """
+import os
+
 import numpy as np
 import pytest
+
+import oracle
 
 pytestmark = [pytest.mark.gpu, pytest.mark.slow]
 
@@ -61,9 +66,11 @@ def test_medium_workload_properties():
 
 def test_large_full_bse_hamiltonian_structure():
     from votca_gb300 import bse_operator as bo
+    from votca_gb300.synthetic import qp_energies, screening_w
 
     v, c, naux = 128, 1024, 4096
-    _, m = _context(v, c, naux, bo.PRECISION_MIXED, 2)
+    mmn, m = _context(v, c, naux, bo.PRECISION_MIXED, 2)
+    m_w, m_hqp = screening_w(2, naux), np.diag(qp_energies(2, v, c))
     n = v * c
     rng = np.random.default_rng(5)
     X = rng.standard_normal((2 * n, 3))
@@ -78,4 +85,22 @@ def test_large_full_bse_hamiltonian_structure():
     assert np.linalg.norm(H[n:] - bot) <= 2e-4 * np.linalg.norm(bot)
     # B is symmetric: y^T B x = x^T B y (to the split accuracy)
     assert abs(np.sum(y * Bx) - np.sum(x * By)) <= 1e-4 * np.linalg.norm(Bx) * np.linalg.norm(y)
+    # sampled rows of the Hamiltonian product against the reference loop nest's rows (each row of
+    # A and B built as bse_operator.cc:52-116 builds it, then [[A, B], [-B, -A]] assembled)
+    oracle.set_threads(os.cpu_count() or 1)
+    prob = oracle.BSEProblem(mmn, m_w, m_hqp, v, c)
+    rows = np.concatenate([[0, c - 1, n - 1], rng.choice(n, 13, replace=False)])
+    XY = np.asfortranarray(np.hstack([x, y]))
+    ra = prob.matmul_rows(XY, rows, "singlet")
+    rb = prob.matmul_rows(XY, rows, "singlet_b")
+    rq = prob.matmul_rows(XY, rows, "hqp")
+    k = X.shape[1]
+    top = ra[:, :k] + rb[:, k:]
+    bot = -rb[:, :k] - ra[:, k:]
+    inter_top = top - rq[:, :k]
+    inter_bot = bot + rq[:, k:]
+    e_top = np.linalg.norm(H[rows] - top) / np.linalg.norm(inter_top)
+    e_bot = np.linalg.norm(H[n + rows] - bot) / np.linalg.norm(inter_bot)
+    print(f"full BSE rows vs loop nest: top {e_top:.2e}, bottom {e_bot:.2e} (interaction part)")
+    assert e_top <= 5e-5 and e_bot <= 5e-5, (e_top, e_bot)
     m.close()

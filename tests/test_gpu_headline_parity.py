@@ -1,0 +1,123 @@
+"""The benchmark configuration itself against the oracle: v=64, c=512, Naux=2048, Nmo=576
+(dim 32768), the seeded inputs the benchmark measures.
+
+- FP64 products of the singlet, triplet and singlet-B operators against the factorised
+  FP64 oracle (all 32768 rows, 3 vectors) at 1e-11 normwise, and sampled rows against the
+  reference loop nest itself (each row built as bse_operator.cc:52-116 builds it);
+- the same products in split precision (BF16x3, FP32 accumulation) against both, at the
+  split tolerance on the interaction part;
+- the lowest 20 singlets and 20 triplets at residual 1e-7 in FP64 and in split precision:
+  every root within 0.1 meV of FP64 and every eigenvector overlap >= 1 - 1e-6 (the accuracy
+  bound of the mixed form), the residuals of the returned roots under the oracle's product
+  below the tolerance, and the FP64 residual of the split-precision roots below it as well.
+"""
+import concurrent.futures as cf
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = [pytest.mark.gpu, pytest.mark.slow]
+
+V, C, NAUX, NMO, SEED = 64, 512, 2048, 576, 1
+# split products: relative error of the interaction part (measured ~1e-5 at this size)
+MIXED_TOL = 5e-5
+OPS = ("singlet", "triplet", "singlet_b")
+
+
+@pytest.fixture(scope="module")
+def c1():
+    from votca_gb300 import bse_operator as bo
+    from votca_gb300.synthetic import mmn_tensor_torch, qp_energies, screening_w
+
+    oracle.set_threads(os.cpu_count() or 1)
+    mmn = mmn_tensor_torch(SEED, NAUX, NMO)
+    w = screening_w(SEED, NAUX)
+    hqp = np.diag(qp_energies(SEED, V, C))
+    opt = bo.BSEOperator_Options(homo=V - 1, rpamin=0, qpmin=0, vmin=0, cmax=V + C - 1)
+    Mmn = bo.TCMatrix_gwbse(mmn)
+    f = bo.GpuBSEContext(w, Mmn, hqp, opt, precision=bo.PRECISION_FP64)
+    m = bo.GpuBSEContext(w, Mmn, hqp, opt, precision=bo.PRECISION_MIXED)
+    prob = oracle.BSEProblem(mmn, w, hqp, V, C)
+    yield {"f": f, "m": m, "prob": prob}
+    f.close()
+    m.close()
+
+
+def _gpu(ctx, op, X):
+    from votca_gb300 import bse_operator as bo
+
+    return bo.BSE_OPERATOR(ctx, *oracle.OPERATORS[op]).matmul(X)
+
+
+def test_fp64_and_mixed_products_match_factorised_oracle(c1):
+    prob = c1["prob"]
+    X = np.asfortranarray(np.random.default_rng(11).standard_normal((V * C, 3)))
+    with cf.ThreadPoolExecutor(len(OPS)) as ex:  # the oracle releases the GIL
+        ref = dict(zip(OPS, ex.map(lambda op: prob.matmul_fact(X, op), OPS)))
+    hqp_part = prob.matmul_fact(X, "hqp")
+    for op in OPS:
+        y64 = _gpu(c1["f"], op, X)
+        err = np.linalg.norm(y64 - ref[op]) / np.linalg.norm(ref[op])
+        assert err <= 1e-11, (op, err)
+        inter = ref[op] - (hqp_part if oracle.OPERATORS[op][0] else 0.0)
+        ym = _gpu(c1["m"], op, X)
+        errm = np.linalg.norm(ym - ref[op]) / np.linalg.norm(inter)
+        print(f"{op}: fp64 vs oracle {err:.2e}, mixed vs oracle {errm:.2e} (interaction part)")
+        assert errm <= MIXED_TOL, (op, errm)
+
+
+def test_rows_match_reference_loop_nest(c1):
+    prob = c1["prob"]
+    rng = np.random.default_rng(12)
+    X = np.asfortranarray(rng.standard_normal((V * C, 4)))
+    rows = np.concatenate([[0, C - 1, C, V * C - 1], rng.choice(V * C, 28, replace=False)])
+    for op in OPS:
+        ref = prob.matmul_rows(X, rows, op)
+        y64 = _gpu(c1["f"], op, X)[rows]
+        err = np.linalg.norm(y64 - ref) / np.linalg.norm(ref)
+        assert err <= 1e-11, (op, err)
+        inter = ref - (prob.matmul_rows(X, rows, "hqp") if oracle.OPERATORS[op][0] else 0.0)
+        ym = _gpu(c1["m"], op, X)[rows]
+        errm = np.linalg.norm(ym - ref) / np.linalg.norm(inter)
+        print(f"{op} rows: fp64 vs loop nest {err:.2e}, mixed {errm:.2e}")
+        assert errm <= MIXED_TOL, (op, errm)
+
+
+@pytest.mark.parametrize("kind", ["singlet", "triplet"])
+def test_twenty_roots_mixed_against_fp64_and_oracle(c1, kind):
+    from votca_gb300 import bse_operator as bo
+    from votca_gb300.davidson import DavidsonSolver
+
+    cls = bo.SingletOperator_TDA if kind == "singlet" else bo.TripletOperator_TDA
+    out = {}
+    for name in ("f", "m"):
+        ds = DavidsonSolver()
+        ds.set_tolerance(1e-7)
+        ds.set_max_search_space(200)
+        lam, vec = ds.solve(cls(c1[name]), 20)
+        assert ds.info() == "Success", name
+        out[name] = (lam, vec, ds)
+    lam64, x64, _ = out["f"]
+    lamm, xm, dsm = out["m"]
+    dmev = np.abs(lamm - lam64) * 1e3
+    ov = np.abs(np.sum(x64 * xm, axis=0))
+    print(f"{kind}: max |mixed - fp64| {dmev.max():.2e} meV, max 1 - overlap {(1 - ov).max():.2e}")
+    assert dmev.max() <= 0.1, dmev
+    assert np.all(ov >= 1 - 1e-6), ov
+    # the FP64 residual of the split-precision roots (an FP64 product on the GPU)
+    A64 = cls(c1["f"])
+    r = A64.matmul(xm) - xm * lamm
+    res_m = np.linalg.norm(r, axis=0)
+    print(f"{kind}: FP64 residual of the mixed roots: max {res_m.max():.2e}")
+    assert res_m.max() <= 1e-7, res_m
+    # residuals under the oracle's product (eight roots of each precision: one oracle call)
+    sel = np.arange(8)
+    Z = np.asfortranarray(np.hstack([x64[:, sel], xm[:, sel]]))
+    HZ = c1["prob"].matmul_fact(Z, kind)
+    lamz = np.concatenate([lam64[sel], lamm[sel]])
+    res_o = np.linalg.norm(HZ - Z * lamz, axis=0)
+    print(f"{kind}: oracle residuals fp64 {res_o[:8].max():.2e}, mixed {res_o[8:].max():.2e}")
+    assert res_o.max() <= 1.01e-7, res_o

@@ -33,12 +33,15 @@ class bse_mmn_desc(ctypes.Structure):
 
 class bse_davidson_options(ctypes.Structure):
     _fields_ = [("iter_max", c_i64), ("tolerance", ctypes.c_double), ("max_search_space", c_i64),
-                ("correction", c_i32), ("update", c_i32), ("matrix_type", c_i32), ("verbose", c_i32)]
+                ("correction", c_i32), ("update", c_i32), ("matrix_type", c_i32), ("verbose", c_i32),
+                ("fp64_polish", c_i32), ("reserved", c_i32), ("size_update", c_i64), ("initial_size", c_i64)]
 
 
 class bse_davidson_result(ctypes.Structure):
-    _fields_ = [("iterations", c_i64), ("info", c_i32), ("reserved", c_i32), ("matvec_columns", c_i64),
-                ("seconds_matvec", ctypes.c_double), ("seconds_total", ctypes.c_double)]
+    _fields_ = [("iterations", c_i64), ("info", c_i32), ("polished", c_i32), ("matvec_columns", c_i64),
+                ("seconds_matvec", ctypes.c_double), ("seconds_total", ctypes.c_double),
+                ("max_residual", ctypes.c_double), ("fp64_columns", c_i64), ("polish_iterations", c_i64),
+                ("seconds_polish", ctypes.c_double)]
 
 
 # name -> (restype, argtypes); every symbol declared in include/votca_gb300_bse.h
@@ -73,6 +76,10 @@ SIGNATURES = {
                                          ctypes.POINTER(bse_davidson_options), c_i64, c_dp,
                                          ctypes.POINTER(c_i32), ctypes.POINTER(c_i64), c_i32]),
     "bse_op_eig_gradient": (c_i32, [c_vp, c_i32, c_i32, c_i32, c_i32, c_dp, c_i64, c_i64, c_dp, c_dp, c_dp, c_dp]),
+    "bse_op_eig_gradient_full": (c_i32, [c_vp, ctypes.POINTER(c_i32), ctypes.POINTER(c_i32), c_dp, c_dp, c_i64,
+                                         c_i64, c_dp, c_dp, c_dp, c_dp]),
+    "bse_op_eig_gradient_device": (c_i32, [c_vp, ctypes.POINTER(c_i32), ctypes.POINTER(c_i32), c_vp, c_vp, c_i64,
+                                           c_i64, c_dp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "bse_rpa_epsilon": (c_i32, [ctypes.POINTER(bse_mmn_desc), ctypes.POINTER(c_dp), c_dp, c_i64, c_i64, c_i64,
                                 c_i64, ctypes.c_double, ctypes.c_double, c_dp]),
     "bse_cholesky_inverse": (c_i32, [c_i64, c_dp, c_i64, c_dp, c_i64]),
@@ -86,6 +93,8 @@ SIGNATURES = {
     "bse_op_profile": (c_i32, [c_vp, c_i32]),
     "bse_op_profile_read": (c_i32, [c_vp, c_dp, ctypes.POINTER(c_i64), c_i32]),
     "bse_probe_fp64_tflops": (c_i32, [c_dp]),
+    "bse_small_sym_eig": (c_i32, [c_i64, ctypes.POINTER(c_i64), ctypes.POINTER(c_i64), c_dp, c_dp, c_dp,
+                                  ctypes.POINTER(c_i64)]),
     "bse_last_error": (ctypes.c_char_p, []),
     "bse_version": (ctypes.c_char_p, []),
 }

@@ -33,6 +33,10 @@ class DavidsonOptions:
     davidson_update: str = "safe"
     davidson_maxiter: int = 50
     nmax: int = 5
+    # no counterpart in gwbse.xml: trial vectors per iteration (0 = the davidson_update rule)
+    # and the FP64 polish of split-precision solves
+    davidson_block: int = 0
+    fp64_polish: bool = True
 
 
 def adjust_hqp_size(Hqp, rpa_input_energies, homo, vmin, cmax, qpmin, qpmax, rpamin,
@@ -79,6 +83,8 @@ def _solver(opt: DavidsonOptions):
     ds.set_size_update(opt.davidson_update)
     ds.set_iter_max(opt.davidson_maxiter)
     ds.set_max_search_space(10 * opt.nmax)
+    ds.set_block_size(opt.davidson_block)
+    ds.set_fp64_polish(opt.fp64_polish)
     return ds
 
 

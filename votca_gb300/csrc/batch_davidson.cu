@@ -7,9 +7,10 @@
 // iterating.  The operator products go through matmul_grouped (tensor-core
 // stages grouped across molecules), the FP64 projections, Ritz vectors,
 // corrections and Gram-Schmidt through the grouped kernels below, and the small
-// eigenproblems of all molecules are solved on the host between two packed
-// copies.  Per iteration the host synchronises three times, whatever the number
-// of molecules.
+// eigenproblems of all molecules in one launch of the device eigensolver
+// (small_eig.cu) on projected matrices that never leave HBM.  Per iteration the
+// host synchronises twice (residual norms and Ritz values; the Gram-Schmidt
+// flags ride with them), whatever the number of molecules.
 #include "batch_davidson.cuh"
 
 #include <algorithm>
@@ -27,7 +28,7 @@
 #include <thread>
 #include <unistd.h>
 
-#include "host_eig.hpp"
+#include "small_eig.cuh"
 #include "tc_engine.cuh"
 
 namespace vgb {
@@ -302,6 +303,21 @@ static_assert(sizeof(Group<TnJob>) <= 32000 && sizeof(Group<TnReduceJob>) <= 320
                   sizeof(Group<UnitJob>) <= 32000,
               "grouped job lists must fit the kernel-parameter space");
 
+// T[c0 + c, r] = T[r, c0 + c] for r < c0, c < nc (the lower block of the projected matrix)
+struct MirrorJob {
+  double *T;
+  int64_t ldt, c0, nc;
+};
+__global__ void mirror_kernel(const __grid_constant__ Group<MirrorJob> g) {
+  const MirrorJob q = g.j[blockIdx.y];
+  const int64_t total = q.c0 * q.nc;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = t % q.c0, c = t / q.c0;
+    q.T[(q.c0 + c) + q.ldt * r] = q.T[r + q.ldt * (q.c0 + c)];
+  }
+}
+
 template <class Job, class Kernel>
 void launch_jobs(const std::vector<Job> &jobs, Kernel kernel, unsigned bx, bool grid_x_is_job,
                  cudaStream_t s, int threads = kThreads) {
@@ -325,12 +341,12 @@ struct Mol {
   bool done = false;
   int info = 1;
   int64_t iterations = 0;
-  std::vector<double> T, lam, U, evals;
+  std::vector<double> lam, evals;
   std::vector<int64_t> upd;
   std::vector<double> upd_lam;
   // device (views into the pool)
-  double *V, *AV, *D, *q, *res, *Ud, *lamd, *cbuf, *norms0, *norms, *h, *part;
-  int *flag;
+  double *V, *AV, *D, *q, *res, *Ud, *lamd, *cbuf, *norms0, *norms, *h, *part, *Td, *eigw;
+  int *flag, *einfo;
   // packed host transfer offsets (doubles): off_in = [U (capc x needmax) | lambdas (needmax) |
   // correction columns (capc) | their lambdas (capc)] in din/hin; off_out in hout (diagonal);
   // off_pack = this step's block in dpack/hpack (every molecule's result of a step is packed
@@ -547,22 +563,30 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
     if (opt.update == 0) M.size_update = neigen;
     else if (opt.update == 1) M.size_update = neigen < 20 ? (int64_t)(1.5 * (double)neigen) : neigen + 10;
     else M.size_update = 2 * neigen;
-    M.restart_size = 2 * neigen;
+    if (opt.size_update > 0) {
+      VGB_REQUIRE(opt.size_update >= neigen, "DavidsonSolver: size_update smaller than neigen");
+      M.size_update = opt.size_update;
+    }
+    M.size_update = std::min(M.size_update, M.n);
+    VGB_REQUIRE(opt.initial_size == 0 || opt.initial_size >= neigen,
+                "DavidsonSolver: initial search space smaller than neigen");
+    M.restart_size = opt.initial_size > 0 ? opt.initial_size : 2 * neigen;
     M.ncols = M.restart_size;
     VGB_REQUIRE(M.ncols <= M.n, "DavidsonSolver: initial search space larger than the operator");
     const int64_t cap = std::max(M.ncols, max_space) + 2 * M.size_update + M.restart_size + 2;
     M.capc = std::min(cap, M.n + 2 * M.size_update + M.restart_size + 2);
     M.needmax = std::min(M.capc, std::max(M.restart_size, M.size_update));
     M.chunks = ceil_div(M.n, (int64_t)kTnRows);
-    M.T.assign(M.capc * M.capc, 0.0);
     M.evals.assign(neigen, 0.0);
     pool_doubles += 2 * M.n * M.capc + 2 * M.n * M.needmax + 3 * M.capc + M.capc * M.capc +
                     M.chunks * M.capc * M.capc + 64;
+    // projected matrix, Ritz coefficients and values, eigensolver scratch (device)
+    pool_doubles += M.capc * M.capc + M.capc * M.needmax + M.needmax + sym_eig_work_doubles(M.capc, M.needmax) + 64;
     M.off_in = in_doubles;
     in_doubles += M.capc * M.needmax + M.needmax + 2 * M.capc + 8;  // U, lambdas, update lists
     M.off_out = out_doubles;
     out_doubles += M.n + 8;                                           // diagonal
-    pack_doubles += M.capc * M.capc + 8;                              // T blocks or norms
+    pack_doubles += M.capc * M.capc + 2 * M.needmax + 8;              // T blocks, or norms + Ritz values
   }
   AllocStreamScope scope(s);
   DeviceBuffer<double> pool(pool_doubles);
@@ -582,6 +606,11 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
       M.norms = take(M.capc);
       M.h = take(M.capc + M.capc * M.capc);
       M.part = take(M.chunks * M.capc * M.capc);
+      p += 64;
+      M.Td = take(M.capc * M.capc);
+      M.Ud = take(M.capc * M.needmax);
+      M.lamd = take(M.needmax);
+      M.eigw = take(sym_eig_work_doubles(M.capc, M.needmax));
       p += 64;
     }
   }
@@ -615,12 +644,11 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
     MixedEngine::prepare_grouped(ops, kmax, s);
   }
   GroupScratch arena;  // Hd intermediates of the grouped products, shared by all molecules
-  DeviceBuffer<int> flags(nm);
-  VGB_CUDA(cudaMemsetAsync(flags.get(), 0, nm * sizeof(int), s));
-  for (size_t b = 0; b < nm; ++b) mols[b].flag = flags.get() + b;
-  for (Mol &M : mols) {  // the Ritz coefficients are read where the host staged them
-    M.Ud = din.get() + M.off_in;
-    M.lamd = M.Ud + M.capc * M.needmax;
+  DeviceBuffer<int> flags(2 * nm);  // Gram-Schmidt linear dependence, then eigensolver status
+  VGB_CUDA(cudaMemsetAsync(flags.get(), 0, 2 * nm * sizeof(int), s));
+  for (size_t b = 0; b < nm; ++b) {
+    mols[b].flag = flags.get() + b;
+    mols[b].einfo = flags.get() + nm + b;
   }
   // packs the given blocks back to back: off_pack and the device block of each molecule
   auto pack = [&](const std::vector<Mol *> &ms, const std::function<int64_t(const Mol &)> &size) {
@@ -704,7 +732,7 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
     {
       std::vector<GroupedItem> items;
       std::vector<TnReq> tn;
-      const int64_t packed = pack(act, [&](const Mol &M) { return M.ncols * (M.ncols - (it == 0 ? 0 : M.nav)); });
+      std::vector<MirrorJob> mj;
       for (Mol *M : act) {
         M->iterations = it;
         const int64_t old = (it == 0) ? 0 : M->nav, nvec = M->ncols - old;
@@ -712,54 +740,42 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
         gi.op = M->op; gi.X = M->V + old * M->n; gi.ldx = M->n; gi.k = nvec;
         gi.Y = M->AV + old * M->n; gi.ldy = M->n; gi.dense = M->dense; gi.diag = M->D;
         items.push_back(gi);
-        tn.push_back({M, M->V, M->AV + old * M->n, M->ncols, nvec, M->cbuf, M->ncols});
+        // T[:, old:ncols] = V^T AV_new straight into the device projected matrix
+        tn.push_back({M, M->V, M->AV + old * M->n, M->ncols, nvec, M->Td + M->capc * old, M->capc});
+        if (old > 0) mj.push_back({M->Td, M->capc, old, nvec});
+        M->nav = M->ncols;
       }
       matmul_grouped(coef, items, s, &arena);
       mark(0);
       run_tn(tn, s);
-      VGB_CUDA(cudaMemcpyAsync(hpack, dpack.get(), packed * sizeof(double), cudaMemcpyDeviceToHost, s));
-      std::vector<int> hflags(nm);
-      VGB_CUDA(cudaMemcpyAsync(hflags.data(), flags.get(), nm * sizeof(int), cudaMemcpyDeviceToHost, s));
-      VGB_CUDA(cudaStreamSynchronize(s));
-      act.front()->op->check_errors(s);  // grouped tensor-core stages report into the first engine
-      for (size_t b = 0; b < nm; ++b)
-        if (hflags[b]) fail(BSE_ERR_NUMERICAL, "molecule " + std::to_string(b) + ": Linear dependencies in Gram-Schmidt.");
-      for (Mol *M : act) {
-        const int64_t old = (it == 0) ? 0 : M->nav, nvec = M->ncols - old;
-        const double *blk = hpack + M->off_pack;
-        const int64_t ldT = M->capc;
-        for (int64_t c = 0; c < nvec; ++c)
-          for (int64_t r = 0; r < M->ncols; ++r) M->T[r + ldT * (old + c)] = blk[r + M->ncols * c];
-        for (int64_t c = 0; c < nvec; ++c)
-          for (int64_t r = 0; r < old; ++r) M->T[(old + c) + ldT * r] = M->T[r + ldT * (old + c)];
-        M->nav = M->ncols;
-      }
+      int64_t mx = 1;
+      for (const MirrorJob &j : mj) mx = std::max(mx, j.c0 * j.nc);
+      launch_jobs(mj, mirror_kernel, rows_blocks(mx), false, s);
     }
     mark(1);
-    // ---- getRitzEigenPairs: small symmetric eigenproblems on host threads ----
-    host_parallel(act.size(), [&](size_t i) {
-      Mol &M = *act[i];
-      const int64_t m = M.ncols;
-      M.m = m;
-      M.needed = std::min(m, std::max(M.restart_size, M.size_update));
-      std::vector<double> Tm(m * m), ev, evec;
-      for (int64_t c = 0; c < m; ++c)
-        for (int64_t r = 0; r < m; ++r) Tm[r + m * c] = M.T[r + M.capc * c];
-      if (!sym_eig(m, Tm.data(), ev, evec)) fail(BSE_ERR_NUMERICAL, "Small hermitian eigenvalue problem failed.");
-      M.lam.assign(ev.begin(), ev.begin() + M.needed);
-      M.U.assign(evec.begin(), evec.begin() + m * M.needed);
-      double *dst = hin + M.off_in;
-      std::copy(M.U.begin(), M.U.end(), dst);
-      std::copy(M.lam.begin(), M.lam.end(), dst + M.capc * M.needmax);
-    });
+    // ---- getRitzEigenPairs: every molecule's Ritz problem in one device launch ----
+    {
+      std::vector<SymEigJob> ej;
+      for (Mol *M : act) {
+        const int64_t m = M->ncols;
+        M->m = m;
+        M->needed = std::min(m, std::max(M->restart_size, M->size_update));
+        SymEigJob j;
+        j.T = M->Td; j.ldt = M->capc; j.m = m; j.nw = M->needed;
+        j.U = M->Ud; j.ldu = m; j.lam = M->lamd; j.work = M->eigw; j.info = M->einfo;
+        ej.push_back(j);
+      }
+      sym_eig_device(ej.data(), (int64_t)ej.size(), s);
+    }
     mark(2);
-    VGB_CUDA(cudaMemcpyAsync(din.get(), hin, in_doubles * sizeof(double), cudaMemcpyHostToDevice, s));
     // ---- Ritz vectors q = V U, residuals res = AV U - q Lambda, their norms ----
     {
       std::vector<NnJob> nn;
       std::vector<ColJob> cj;
       std::vector<NormJob> nj;
-      const int64_t packed = pack(act, [](const Mol &M) { return std::min(M.needed, M.size_update); });
+      std::vector<ColJob> lc;
+      const int64_t packed =
+          pack(act, [](const Mol &M) { return std::min(M.needed, M.size_update) + M.needed; });
       for (Mol *M : act) {
         // only the first min(needed, size_update) pairs enter the convergence check and the
         // corrections; the Ritz vectors a restart keeps are formed there
@@ -774,12 +790,28 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
         w.A = M->res; w.B = nullptr; w.lda = M->n; w.ldb = M->n; w.n = M->n;
         w.p = std::min(M->needed, M->size_update); w.out = M->cbuf;
         nj.push_back(w);
+        ColJob l;  // the Ritz values travel behind the norms
+        l.kind = 2; l.A = M->cbuf + pr; l.B = M->lamd; l.D = nullptr; l.v = nullptr; l.cols = nullptr;
+        l.lda = M->needed; l.ldb = M->needed; l.n = M->needed; l.p = 1;
+        lc.push_back(l);
       }
       run_nn(nn, s);
       run_cols(cj, s);
       run_norms(nj, s);
+      run_cols(lc, s);
       VGB_CUDA(cudaMemcpyAsync(hpack, dpack.get(), packed * sizeof(double), cudaMemcpyDeviceToHost, s));
+      std::vector<int> hflags(2 * nm);
+      VGB_CUDA(cudaMemcpyAsync(hflags.data(), flags.get(), 2 * nm * sizeof(int), cudaMemcpyDeviceToHost, s));
       VGB_CUDA(cudaStreamSynchronize(s));
+      act.front()->op->check_errors(s);  // grouped tensor-core stages report into the first engine
+      for (size_t b = 0; b < nm; ++b) {
+        if (hflags[b]) fail(BSE_ERR_NUMERICAL, "molecule " + std::to_string(b) + ": Linear dependencies in Gram-Schmidt.");
+        if (hflags[nm + b]) fail(BSE_ERR_NUMERICAL, "molecule " + std::to_string(b) + ": Small hermitian eigenvalue problem failed.");
+      }
+      for (Mol *M : act) {
+        const int64_t pr = std::min(M->needed, M->size_update);
+        M->lam.assign(hpack + M->off_pack + pr, hpack + M->off_pack + pr + M->needed);
+      }
     }
     mark(3);
     // ---- checkConvergence / storeEigenPairs / extendProjection (host) ----
@@ -926,19 +958,12 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
       run_nn(nn, s);
       run_cols(cav, s);
       run_cols(back, s);
-      std::vector<TnReq> tn;
-      const int64_t packed = pack(rst, [](const Mol &M) { return M.restart_size * M.restart_size; });
-      for (Mol *M : rst) tn.push_back({M, M->V, M->AV, M->restart_size, M->restart_size, M->cbuf, M->restart_size});
+      std::vector<TnReq> tn;  // T = V[:, :rs]^T AV[:, :rs], in the device projected matrix
+      for (Mol *M : rst) tn.push_back({M, M->V, M->AV, M->restart_size, M->restart_size, M->Td, M->capc});
       run_tn(tn, s);
-      VGB_CUDA(cudaMemcpyAsync(hpack, dpack.get(), packed * sizeof(double), cudaMemcpyDeviceToHost, s));
-      VGB_CUDA(cudaStreamSynchronize(s));
       for (Mol *M : rst) {
-        const int64_t rs = M->restart_size;
-        std::fill(M->T.begin(), M->T.end(), 0.0);
-        for (int64_t c = 0; c < rs; ++c)
-          for (int64_t r = 0; r < rs; ++r) M->T[r + M->capc * c] = hpack[M->off_pack + r + rs * c];
-        M->ncols = rs + M->nupdate;
-        M->nav = rs;
+        M->ncols = M->restart_size + M->nupdate;
+        M->nav = M->restart_size;
       }
     }
     mark(7);

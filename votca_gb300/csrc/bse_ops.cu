@@ -27,7 +27,7 @@ struct ScatterArgs {
   int64_t nsize, naux, vt, ct, dim;
   int64_t n_v0, n_c0;  // row index (in slice) of the first occupied / virtual BSE level
   const double *w;     // diagonal screening or nullptr (dense W applied later)
-  double *Bvc, *Mcc, *Gvv, *Mcv, *dcc;
+  double *Bvc, *Mcc, *Gvv, *Mcv, *Mcv0, *dcc;
 };
 
 __global__ void scatter_kernel(const ScatterArgs a) {
@@ -56,6 +56,7 @@ __global__ void scatter_kernel(const ScatterArgs a) {
       if (nl < a.vt) {
         const int64_t v = nl;
         a.Mcv[P * a.dim + v * a.ct + c1] = wp * val;
+        a.Mcv0[P * a.dim + v * a.ct + c1] = val;
       } else {
         const int64_t c = nl - a.vt;
         a.Mcc[(P * a.ct + c) * a.ct + c1] = val;
@@ -338,6 +339,7 @@ void BseOperator::stage(const bse_mmn_desc &desc, const double *const *slices, c
   Mcc.resize(naux * ct * ct);
   Gvv.resize(vt * naux * vt);
   Mcv.resize(naux * dim);
+  Mcv0.resize(naux * dim);
   dcc.resize(naux * ct);
   dvv.resize(naux * vt);
   Hcc.resize(ct * ct);
@@ -380,6 +382,7 @@ void BseOperator::stage(const bse_mmn_desc &desc, const double *const *slices, c
     a.Mcc = Mcc.get();
     a.Gvv = Gvv.get();
     a.Mcv = Mcv.get();
+    a.Mcv0 = Mcv0.get();
     a.dcc = dcc.get();
     scatter_kernel<<<grid_for(cnt * naux * nwin), 256, 0, s>>>(a);
     VGB_LAUNCH_CHECK();
@@ -565,7 +568,7 @@ void BseOperator::matmul(const Coef &c, const double *X, int64_t ldx, int64_t k,
   VGB_REQUIRE(!(c.cd != 0 && c.cd2 != 0), "Hamiltonian cannot contain Hd and Hd2 at the same time");
   bool acc = false;
   if (c.cqp != 0) { apply_hqp(c.cqp, X, ldx, k, Y, ldy, acc, s); acc = true; }
-  if (precision == BSE_PRECISION_MIXED && mixed) {
+  if (precision == BSE_PRECISION_MIXED && mixed && !force_fp64) {
     mixed->apply(*this, c, X, ldx, k, Y, ldy, acc, s);
     return;
   }

@@ -73,6 +73,13 @@ struct DeviceOperator {
   virtual void diagonal(double *D, cudaStream_t s) = 0;
   // raise if an asynchronous device-side failure was recorded (synchronises)
   virtual void check(cudaStream_t) {}
+  // true when apply() runs split-precision (tensor-core) products; apply_fp64 is then the
+  // same operator with every product in FP64 (the Davidson polish)
+  virtual bool split_precision() const { return false; }
+  virtual void apply_fp64(const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy,
+                          cudaStream_t s) {
+    apply(X, ldx, k, Y, ldy, s);
+  }
 };
 
 class MixedEngine;  // tensor-core contractions (tc_engine.cu)
@@ -82,11 +89,14 @@ class BseOperator {
   int64_t vt = 0, ct = 0, naux = 0, dim = 0;
   int precision = BSE_PRECISION_FP64;
   bool hqp_diagonal = true;
+  // set while a split-precision operator must run its FP64 path (FP64 blocks are always staged)
+  bool force_fp64 = false;
 
   // FP64 staged blocks (layouts documented in bse_ops.cu)
   DeviceBuffer<double> Bvc, Mcc, Gvv, Mcv, dcc, dvv, Hcc, Hvv;
-  // unscreened vv block [P][v1][v] and the screening (naux, or naux x naux when dense)
-  DeviceBuffer<double> Mvv, Wscr;
+  // unscreened vv block [P][v1][v], unscreened cv block [P][v][c1] = M(c1, v, P) (the Hd2
+  // adjoint), and the screening (naux, or naux x naux when dense)
+  DeviceBuffer<double> Mvv, Mcv0, Wscr;
   bool dense_screening = false;
   // index window of the staged blocks inside the caller's Mmn
   int64_t m_v0 = 0, m_c0 = 0, n_v0 = 0, n_c0 = 0, msize = 0, nsize = 0;
@@ -117,12 +127,13 @@ class BseOperator {
   void check_errors(cudaStream_t s);
   void stage_unscreened_vv(const bse_mmn_desc &desc, const double *const *slices,
                            const bse_options &opt, cudaStream_t s);
-  // Hellmann-Feynman gradients of sum_k g_k Omega_k (adjoint.cu); outputs are device
-  // buffers: gM* in the block layouts below, gH = Hqp window gradient ((vt+ct)^2),
-  // gW = screening gradient (naux, or naux^2 when dense).
-  void eig_gradient(const Coef &c, const double *X, int64_t ldx, int64_t nr, const double *g_host,
-                    double *gMvc, double *gMvv, double *gMcc, double *gH, double *gW,
-                    cudaStream_t s);
+  // Gradient of sum_i g_i u_i^T H(c) u_i (adjoint.cu) for any coefficient set, accumulated into
+  // device buffers (zeroed first unless accumulate): gMvc [P][v][c] (Bvc layout), gMcv [P][v][c1]
+  // (the cv block, Mcv0 layout), gMvv [P][v1][v], gMcc [P][c][c1], gH the Hqp window
+  // ((vt+ct)^2), gW the screening (naux, or naux^2 when dense).  Any output may be null.
+  void quad_gradient(const Coef &c, const double *U, int64_t ldu, int64_t nr, const double *g_host,
+                     double *gMvc, double *gMcv, double *gMvv, double *gMcc, double *gH, double *gW,
+                     bool accumulate, cudaStream_t s);
   // [[A, B], [-B, -A]] X, X and Y (2 dim) x k
   void ham_matmul(const Coef &a, const Coef &b, const double *X, int64_t ldx, int64_t k, double *Y,
                   int64_t ldy, cudaStream_t s);
@@ -151,8 +162,8 @@ void copy_cols(const double *X, int64_t ldx, int64_t rows, int64_t k, double *Y,
 
 // The Mmn-shaped gradient (the caller's slice layout, msize x naux x nsize, host memory) from the
 // block gradients of BseOperator::eig_gradient: scattered on the device, copied in chunks.
-void scatter_mmn_gradient(const BseOperator &op, const double *gMvc, const double *gMvv,
-                          const double *gMcc, double *host_out, cudaStream_t s);
+void scatter_mmn_gradient(const BseOperator &op, const double *gMvc, const double *gMcv,
+                          const double *gMvv, const double *gMcc, double *host_out, cudaStream_t s);
 
 // One molecule's share of a grouped product: Y = H(c) X on its own operator.
 struct GroupedItem {
@@ -179,6 +190,20 @@ void matmul_grouped(const Coef &c, const std::vector<GroupedItem> &items, cudaSt
 void diagonal_grouped(const Coef &c, const std::vector<BseOperator *> &ops,
                       const std::vector<double *> &D, cudaStream_t s);
 
+// Runs the operators' FP64 path for its lifetime (split-precision handles keep FP64 blocks).
+struct ForceFp64 {
+  BseOperator *a, *b;
+  bool sa, sb;
+  explicit ForceFp64(BseOperator *x, BseOperator *y = nullptr) : a(x), b(y), sa(x->force_fp64), sb(y ? y->force_fp64 : false) {
+    a->force_fp64 = true;
+    if (b) b->force_fp64 = true;
+  }
+  ~ForceFp64() {
+    a->force_fp64 = sa;
+    if (b) b->force_fp64 = sb;
+  }
+};
+
 struct BseApply : DeviceOperator {
   BseOperator *op;
   Coef coef;
@@ -190,6 +215,12 @@ struct BseApply : DeviceOperator {
   }
   void diagonal(double *D, cudaStream_t s) override { op->diagonal(coef, D, s); }
   void check(cudaStream_t s) override { op->check_errors(s); }
+  bool split_precision() const override { return op->precision == BSE_PRECISION_MIXED && op->mixed; }
+  void apply_fp64(const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy,
+                  cudaStream_t s) override {
+    ForceFp64 g(op);
+    op->matmul(coef, X, ldx, k, Y, ldy, s);
+  }
 };
 
 struct BseHamApply : DeviceOperator {
@@ -203,6 +234,12 @@ struct BseHamApply : DeviceOperator {
   }
   void diagonal(double *D, cudaStream_t s) override;
   void check(cudaStream_t s) override { op->check_errors(s); }
+  bool split_precision() const override { return op->precision == BSE_PRECISION_MIXED && op->mixed; }
+  void apply_fp64(const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy,
+                  cudaStream_t s) override {
+    ForceFp64 g(op);
+    op->ham_matmul(a, b, X, ldx, k, Y, ldy, s);
+  }
 };
 
 // Dense FP64 symmetric operator(s): A, optionally B for [[A, B], [-B, -A]].

@@ -11,6 +11,7 @@
 #include "bse_ops.cuh"
 #include "batch_davidson.cuh"
 #include "davidson.cuh"
+#include "small_eig.cuh"
 #include "uks_ops.cuh"
 
 struct bse_handle {
@@ -76,6 +77,78 @@ struct TmpStream {
 
 void create_stream(bse_handle *h) {
   VGB_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+}
+
+}  // namespace
+
+namespace {
+
+// P = X + Y, M = X - Y (dim x nr, leading dimensions ldx and dim)
+__global__ void plus_minus_kernel(const double *X, const double *Y, int64_t ldx, int64_t dim, int64_t nr,
+                                  double *P, double *M) {
+  const int64_t total = dim * nr;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t % dim, k = t / dim;
+    const double x = X[i + ldx * k], y = Y[i + ldx * k];
+    P[t] = x + y;
+    M[t] = x - y;
+  }
+}
+
+// The Hellmann-Feynman gradient of sum_k g_k Omega_k into device block buffers (any may be null):
+// TDA (Y == nullptr): quadratic forms of the eigenvectors X under H(a); full BSE: X^T dA X +
+// Y^T dA Y (weights g) plus 2 X^T dB Y as the quadratic forms of X + Y and X - Y under H(b)
+// (weights g/2 and -g/2).  X, Y device, leading dimension ldx.
+void eig_gradient_blocks(vgb::BseOperator &op, const vgb::Coef &a, const vgb::Coef *b, const double *X,
+                         const double *Y, int64_t ldx, int64_t nr, const double *g, double *gvc, double *gcv,
+                         double *gvv, double *gcc, double *gh, double *gw, cudaStream_t s) {
+  op.quad_gradient(a, X, ldx, nr, g, gvc, gcv, gvv, gcc, gh, gw, false, s);
+  if (!Y) return;
+  op.quad_gradient(a, Y, ldx, nr, g, gvc, gcv, gvv, gcc, gh, gw, true, s);
+  std::vector<double> half(2 * nr);
+  for (int64_t k = 0; k < nr; ++k) {
+    half[k] = 0.5 * g[k];
+    half[nr + k] = -0.5 * g[k];
+  }
+  vgb::DeviceBuffer<double> PM(2 * op.dim * nr);
+  plus_minus_kernel<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(vgb::ceil_div(op.dim * nr, 256), 2432)),
+                      256, 0, s>>>(X, Y, ldx, op.dim, nr, PM.get(), PM.get() + op.dim * nr);
+  VGB_LAUNCH_CHECK();
+  op.quad_gradient(*b, PM.get(), op.dim, 2 * nr, half.data(), gvc, gcv, gvv, gcc, gh, gw, true, s);
+}
+
+// Host-pointer gradient: the Mmn-shaped gradient, the Hqp window and the screening (any may be null).
+void eig_gradient_host(bse_handle *h, const vgb::Coef &a, const vgb::Coef *b, const double *X, const double *Y,
+                       int64_t ldx, int64_t nroots, const double *weights, double *grad_mmn, double *grad_hqp,
+                       double *grad_screening) {
+  vgb::BseOperator &op = *h->bse;
+  VGB_REQUIRE(ldx >= op.dim, "bse_op_eig_gradient: ldx smaller than the operator size");
+  cudaStream_t s = h->stream;
+  const int64_t vt = op.vt, ct = op.ct, naux = op.naux, dim = op.dim;
+  vgb::DeviceBuffer<double> dX(dim * nroots), dY, gMvc, gMcv, gMvv, gMcc, gH, gW;
+  VGB_CUDA(cudaMemcpy2DAsync(dX.get(), dim * sizeof(double), X, ldx * sizeof(double), dim * sizeof(double),
+                             nroots, cudaMemcpyHostToDevice, s));
+  if (Y) {
+    dY.resize(dim * nroots);
+    VGB_CUDA(cudaMemcpy2DAsync(dY.get(), dim * sizeof(double), Y, ldx * sizeof(double), dim * sizeof(double),
+                               nroots, cudaMemcpyHostToDevice, s));
+  }
+  if (grad_mmn) {
+    gMvc.resize(naux * dim);
+    gMcv.resize(naux * dim);
+    gMvv.resize(naux * vt * vt);
+    gMcc.resize(naux * ct * ct);
+  }
+  const int64_t nh = (vt + ct) * (vt + ct);
+  const int64_t nw = op.dense_screening ? naux * naux : naux;
+  if (grad_hqp) gH.resize(nh);
+  if (grad_screening) gW.resize(nw);
+  eig_gradient_blocks(op, a, b, dX.get(), Y ? dY.get() : nullptr, dim, nroots, weights, gMvc.get(), gMcv.get(),
+                      gMvv.get(), gMcc.get(), gH.get(), gW.get(), s);
+  if (grad_hqp) VGB_CUDA(cudaMemcpy(grad_hqp, gH.get(), nh * sizeof(double), cudaMemcpyDeviceToHost));
+  if (grad_screening) VGB_CUDA(cudaMemcpy(grad_screening, gW.get(), nw * sizeof(double), cudaMemcpyDeviceToHost));
+  if (grad_mmn) vgb::scatter_mmn_gradient(op, gMvc.get(), gMcv.get(), gMvv.get(), gMcc.get(), grad_mmn, s);
 }
 
 }  // namespace
@@ -361,10 +434,14 @@ int bse_davidson_solve(bse_handle *h, const int32_t a_coef[4], const int32_t b_c
     if (result) {
       result->iterations = o.iterations;
       result->info = o.info;
-      result->reserved = 0;
+      result->polished = o.polished;
       result->matvec_columns = o.matvec_columns;
       result->seconds_matvec = o.seconds_matvec;
       result->seconds_total = o.seconds_total;
+      result->max_residual = o.max_residual;
+      result->fp64_columns = o.fp64_columns;
+      result->polish_iterations = o.polish_iterations;
+      result->seconds_polish = o.seconds_polish;
     }
   });
 }
@@ -377,28 +454,44 @@ int bse_op_eig_gradient(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd, int3
     vgb::AllocStreamScope alloc_scope(h->stream);
     VGB_REQUIRE(h->kind == 0, "bse_op_eig_gradient: not a BSE operator");
     VGB_REQUIRE(X && weights && nroots >= 1, "bse_op_eig_gradient: null eigenvectors or weights");
+    eig_gradient_host(h, coef(cqp, cx, cd, cd2), nullptr, X, nullptr, ldx, nroots, weights, grad_mmn, grad_hqp,
+                      grad_screening);
+  });
+}
+
+int bse_op_eig_gradient_full(bse_handle *h, const int32_t a_coef[4], const int32_t b_coef[4], const double *X,
+                             const double *Y, int64_t ldx, int64_t nroots, const double *weights,
+                             double *grad_mmn, double *grad_hqp, double *grad_screening) {
+  return guarded([&] {
+    require_handle(h);
+    vgb::AllocStreamScope alloc_scope(h->stream);
+    VGB_REQUIRE(h->kind == 0, "bse_op_eig_gradient_full: not a BSE operator");
+    VGB_REQUIRE(a_coef && b_coef && X && Y && weights && nroots >= 1,
+                "bse_op_eig_gradient_full: null argument");
+    const vgb::Coef a = coef(a_coef[0], a_coef[1], a_coef[2], a_coef[3]);
+    const vgb::Coef b = coef(b_coef[0], b_coef[1], b_coef[2], b_coef[3]);
+    eig_gradient_host(h, a, &b, X, Y, ldx, nroots, weights, grad_mmn, grad_hqp, grad_screening);
+  });
+}
+
+int bse_op_eig_gradient_device(bse_handle *h, const int32_t a_coef[4], const int32_t b_coef[4],
+                               const double *dX, const double *dY, int64_t ldx, int64_t nroots,
+                               const double *weights, double *d_grad_vc, double *d_grad_cv, double *d_grad_vv,
+                               double *d_grad_cc, double *d_grad_hqp, double *d_grad_screening, void *stream) {
+  return guarded([&] {
+    require_handle(h);
+    VGB_REQUIRE(h->kind == 0, "bse_op_eig_gradient_device: not a BSE operator");
+    VGB_REQUIRE(a_coef && dX && weights && nroots >= 1, "bse_op_eig_gradient_device: null argument");
+    VGB_REQUIRE(!dY || b_coef, "bse_op_eig_gradient_device: full BSE needs the B coefficients");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    vgb::AllocStreamScope alloc_scope(s);
     vgb::BseOperator &op = *h->bse;
-    VGB_REQUIRE(ldx >= op.dim, "bse_op_eig_gradient: ldx smaller than the operator size");
-    cudaStream_t s = h->stream;
-    const int64_t vt = op.vt, ct = op.ct, naux = op.naux, dim = op.dim;
-    vgb::DeviceBuffer<double> dX(dim * nroots), gMvc, gMvv, gMcc, gH, gW;
-    VGB_CUDA(cudaMemcpy2DAsync(dX.get(), dim * sizeof(double), X, ldx * sizeof(double),
-                               dim * sizeof(double), nroots, cudaMemcpyHostToDevice, s));
-    if (grad_mmn) {
-      gMvc.resize(naux * dim);
-      gMvv.resize(naux * vt * vt);
-      gMcc.resize(naux * ct * ct);
-    }
-    const int64_t nh = (vt + ct) * (vt + ct);
-    const int64_t nw = op.dense_screening ? naux * naux : naux;
-    if (grad_hqp) gH.resize(nh);
-    if (grad_screening) gW.resize(nw);
-    op.eig_gradient(coef(cqp, cx, cd, cd2), dX.get(), dim, nroots, weights, gMvc.get(), gMvv.get(),
-                    gMcc.get(), gH.get(), gW.get(), s);
-    if (grad_hqp) VGB_CUDA(cudaMemcpy(grad_hqp, gH.get(), nh * sizeof(double), cudaMemcpyDeviceToHost));
-    if (grad_screening)
-      VGB_CUDA(cudaMemcpy(grad_screening, gW.get(), nw * sizeof(double), cudaMemcpyDeviceToHost));
-    if (grad_mmn) vgb::scatter_mmn_gradient(op, gMvc.get(), gMvv.get(), gMcc.get(), grad_mmn, s);
+    VGB_REQUIRE(ldx >= op.dim, "bse_op_eig_gradient_device: ldx smaller than the operator size");
+    const vgb::Coef a = coef(a_coef[0], a_coef[1], a_coef[2], a_coef[3]);
+    vgb::Coef b;
+    if (dY) b = coef(b_coef[0], b_coef[1], b_coef[2], b_coef[3]);
+    eig_gradient_blocks(op, a, dY ? &b : nullptr, dX, dY, ldx, nroots, weights, d_grad_vc, d_grad_cv, d_grad_vv,
+                        d_grad_cc, d_grad_hqp, d_grad_screening, s);
   });
 }
 
@@ -544,6 +637,51 @@ int bse_probe_fp64_tflops(double *tflops) {
   return guarded([&] {
     VGB_REQUIRE(tflops != nullptr, "bse_probe_fp64_tflops: null out");
     *tflops = vgb::probe_fp64_tflops();
+  });
+}
+
+int bse_small_sym_eig(int64_t njobs, const int64_t *m, const int64_t *nw, const double *T, double *evals,
+                      double *evecs, int64_t *phase_cycles) {
+  return guarded([&] {
+    VGB_REQUIRE(njobs >= 0 && (njobs == 0 || (m && nw && T && evals && evecs)), "bse_small_sym_eig: null argument");
+    int64_t nt = 0, nl = 0, nu = 0, wmax = 0;
+    for (int64_t i = 0; i < njobs; ++i) {
+      VGB_REQUIRE(m[i] >= 1 && m[i] <= vgb::kSymEigMaxM && nw[i] >= 1 && nw[i] <= m[i],
+                  "bse_small_sym_eig: sizes out of range");
+      nt += m[i] * m[i];
+      nl += nw[i];
+      nu += m[i] * nw[i];
+      wmax += vgb::sym_eig_work_doubles(m[i], nw[i]);
+    }
+    if (njobs == 0) return;
+    cudaStream_t s = nullptr;
+    vgb::DeviceBuffer<double> dT(nt), dl(nl), dU(nu), dw(wmax);
+    vgb::DeviceBuffer<int> dinfo(njobs);
+    vgb::DeviceBuffer<long long> dclk(phase_cycles ? 5 * njobs : 0);
+    VGB_CUDA(cudaMemcpyAsync(dT.get(), T, nt * sizeof(double), cudaMemcpyHostToDevice, s));
+    std::vector<vgb::SymEigJob> jobs(njobs);
+    int64_t ot = 0, ol = 0, ou = 0, ow = 0;
+    for (int64_t i = 0; i < njobs; ++i) {
+      vgb::SymEigJob &j = jobs[i];
+      j.T = dT.get() + ot; j.ldt = m[i]; j.m = m[i]; j.nw = nw[i];
+      j.U = dU.get() + ou; j.ldu = m[i]; j.lam = dl.get() + ol; j.work = dw.get() + ow; j.info = dinfo.get() + i;
+      if (phase_cycles) j.clocks = dclk.get() + 5 * i;
+      ot += m[i] * m[i]; ol += nw[i]; ou += m[i] * nw[i]; ow += vgb::sym_eig_work_doubles(m[i], nw[i]);
+    }
+    vgb::sym_eig_device(jobs.data(), njobs, s);
+    std::vector<int> info(njobs);
+    VGB_CUDA(cudaMemcpyAsync(evals, dl.get(), nl * sizeof(double), cudaMemcpyDeviceToHost, s));
+    VGB_CUDA(cudaMemcpyAsync(evecs, dU.get(), nu * sizeof(double), cudaMemcpyDeviceToHost, s));
+    VGB_CUDA(cudaMemcpyAsync(info.data(), dinfo.get(), njobs * sizeof(int), cudaMemcpyDeviceToHost, s));
+    std::vector<long long> clk(phase_cycles ? 5 * njobs : 0);
+    if (phase_cycles)
+      VGB_CUDA(cudaMemcpyAsync(clk.data(), dclk.get(), clk.size() * sizeof(long long), cudaMemcpyDeviceToHost, s));
+    VGB_CUDA(cudaStreamSynchronize(s));
+    for (int64_t i = 0; i < njobs; ++i)
+      if (info[i] != 0) vgb::fail(BSE_ERR_NUMERICAL, "Small hermitian eigenvalue problem failed.");
+    if (phase_cycles)
+      for (int64_t i = 0; i < njobs; ++i)
+        for (int p = 0; p < 4; ++p) phase_cycles[4 * i + p] = clk[5 * i + p + 1] - clk[5 * i + p];
   });
 }
 

@@ -20,6 +20,7 @@
 #include <cstdlib>
 
 #include "host_eig.hpp"
+#include "small_eig.cuh"
 
 namespace vgb {
 
@@ -133,6 +134,17 @@ __global__ void copy_block_kernel(const double *src, int64_t lds, double *dst, i
        t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = t % n, c = t / n;
     dst[c * ldd + i] = src[c * lds + i];
+  }
+}
+
+// T[c0 + c, r] = T[r, c0 + c] for r < c0, c < nc: the lower block of the projected matrix from
+// the columns just computed (updateProjection's bottomLeftCorner = topRightCorner^T)
+__global__ void mirror_block_kernel(double *T, int64_t ldt, int64_t c0, int64_t nc) {
+  const int64_t total = c0 * nc;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = t % c0, c = t / c0;
+    T[(c0 + c) + ldt * r] = T[r + ldt * (c0 + c)];
   }
 }
 
@@ -279,9 +291,9 @@ struct Ctx {
   }
   // C (m x nc, ldc) = alpha * A[:, a0:a0+m]^T B[:, b0:b0+nc] + beta C
   void gemm_tn(const double *A, int64_t lda, int64_t m, const double *B, int64_t ldb, int64_t nc,
-               double *C, int64_t ldc, double alpha, double beta) {
+               double *C, int64_t ldc, double alpha, double beta, int64_t rows = -1) {
     GemmDesc g;
-    g.M = m; g.N = nc; g.K = n;
+    g.M = m; g.N = nc; g.K = rows < 0 ? n : rows;
     g.a_colmajor(A, lda, true).b_colmajor(B, ldb, false).c_colmajor(C, ldc);
     g.alpha = alpha; g.beta = beta;
     dgemm(g, s, &ws);
@@ -389,6 +401,291 @@ std::vector<double> thin_q(int64_t m, int64_t r, const std::vector<double> &A) {
   return Q;
 }
 
+// Cholesky factor L (lower, column-major) of the symmetric m x m matrix S; false if S is not
+// positive definite.
+bool cholesky_lower(int64_t m, const std::vector<double> &S, std::vector<double> &L) {
+  L.assign(m * m, 0.0);
+  for (int64_t j = 0; j < m; ++j) {
+    double d = S[j + m * j];
+    for (int64_t k = 0; k < j; ++k) d -= L[j + m * k] * L[j + m * k];
+    if (!(d > 0.0)) return false;
+    const double ljj = std::sqrt(d);
+    L[j + m * j] = ljj;
+    for (int64_t i = j + 1; i < m; ++i) {
+      double t = S[i + m * j];
+      for (int64_t k = 0; k < j; ++k) t -= L[i + m * k] * L[j + m * k];
+      L[i + m * j] = t / ljj;
+    }
+  }
+  return true;
+}
+
+// Products of the Davidson operator, timed with events on the solve's stream.
+struct TimedApply {
+  DeviceOperator &A;
+  cudaStream_t s;
+  int64_t n;
+  DavidsonOutput &out;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double ms = 0.0;
+  TimedApply(DeviceOperator &a, cudaStream_t st, int64_t nn, DavidsonOutput &o) : A(a), s(st), n(nn), out(o) {
+    VGB_CUDA(cudaEventCreate(&ev0));
+    VGB_CUDA(cudaEventCreate(&ev1));
+  }
+  ~TimedApply() {
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+  }
+  void operator()(const double *X, int64_t k, double *Y, bool fp64 = false) {
+    if (k <= 0) return;
+    VGB_CUDA(cudaEventRecord(ev0, s));
+    if (fp64) A.apply_fp64(X, n, k, Y, n, s); else A.apply(X, n, k, Y, n, s);
+    VGB_CUDA(cudaEventRecord(ev1, s));
+    VGB_CUDA(cudaEventSynchronize(ev1));
+    A.check(s);
+    float t = 0.f;
+    VGB_CUDA(cudaEventElapsedTime(&t, ev0, ev1));
+    ms += t;
+    out.matvec_columns += k;
+    if (fp64) out.fp64_columns += k;
+  }
+};
+
+// FP64 polish of a split-precision solve (no counterpart in the reference).  The split
+// products agree with FP64 to about 1e-5 of the interaction part, which bounds how far the
+// Davidson residuals of the split operator say anything about the FP64 operator.  Here the
+// basis restarts from the neigen Ritz vectors q0 with FP64 products A V0; corrections
+// (DPR/Olsen of the residuals, as computeCorrectionVector) are added with split products.
+// The coupling of a correction t to the FP64 block is taken from the FP64 side,
+// t^T (A V0), and a correction enters a Ritz vector with a coefficient of the size of the
+// residual over the gap, so the split error reaches the residuals and Rayleigh quotients
+// only as that coefficient times 1e-5: they are FP64 quantities for every practical purpose.
+// SYMM: Rayleigh-Ritz on V^T A V.  HAM ([[A, B], [-B, -A]] = J S with S = [[A, B], [B, A]]
+// symmetric, J = diag(I, -I)): the projected pencil (V^T S V, V^T J V), reduced through the
+// Cholesky factor of V^T S V (positive definite for a stable BSE); the lowest positive roots.
+// Returns false (nothing changed) when that factor does not exist.
+bool fp64_polish(Ctx &x, TimedApply &apply, const double *Dd, const double *q0, int64_t neigen,
+                 bool ham, int correction, double tol, int64_t max_iter, double *evecs_dev,
+                 DavidsonOutput &out, int verbose) {
+  const int64_t n = x.n;
+  const int64_t np = std::min(neigen, n);
+  const int64_t cap = std::max<int64_t>(np, std::min<int64_t>(n, 9 * np));
+  const int64_t half = n / 2;
+  cudaStream_t s = x.s;
+  DeviceBuffer<double> V(n * cap), AV(n * cap), q(n * np), res(n * np), Ud, lamd, work, cbuf, tmp;
+  DeviceBuffer<int64_t> colsd(std::max<int64_t>(np, 64));
+  DeviceBuffer<int> flag(1), einfo(1);
+  DeviceBuffer<double> Td, eigw;              // SYMM: V^T A V on the device (ld cap)
+  std::vector<double> T, Jm;                  // HAM: V^T S V and V^T J V on the host
+  if (ham) {
+    T.assign(cap * cap, 0.0);
+    Jm.assign(cap * cap, 0.0);
+  } else {
+    Td.resize(cap * cap);
+  }
+  // C (r x c) = V[:, a0:a0+r]^T (J) W[:, 0:c]
+  auto proj = [&](const double *Va, int64_t r, const double *W, int64_t c, double *C, bool withJ) {
+    if (!withJ) {
+      x.gemm_tn(Va, n, r, W, n, c, C, r, 1.0, 0.0);
+    } else {
+      x.gemm_tn(Va, n, r, W, n, c, C, r, 1.0, 0.0, half);
+      x.gemm_tn(Va + half, n, r, W + half, n, c, C, r, -1.0, 1.0, half);
+    }
+  };
+  auto to_host = [&](const double *src, int64_t cnt) {
+    std::vector<double> h(cnt);
+    VGB_CUDA(cudaMemcpyAsync(h.data(), src, cnt * sizeof(double), cudaMemcpyDeviceToHost, s));
+    VGB_CUDA(cudaStreamSynchronize(s));
+    return h;
+  };
+  int64_t m = 0, old = 0;
+  auto start_basis = [&](const double *qsrc) {
+    x.copy_cols(qsrc, n, V.get(), n, np);
+    if (ham) gramschmidt(x, V.get(), 0, np, work, flag);  // harmonic Ritz vectors are not orthogonal
+    apply(V.get(), np, AV.get(), true);
+    m = np;
+    old = 0;
+  };
+  start_basis(q0);
+  std::vector<double> lam(np), U;
+  for (int64_t pit = 0; pit < max_iter; ++pit) {
+    out.polish_iterations = pit + 1;
+    // ---- projected matrices for the columns [old, m) ----
+    if (!ham) {  // lower triangle on the device: coupling from the FP64 side, V_new^T (A V_old)
+      const int64_t nv = m - old;
+      if (old > 0) x.gemm_tn(V.get() + old * n, n, nv, AV.get(), n, old, Td.get() + old, cap, 1.0, 0.0);
+      x.gemm_tn(V.get() + old * n, n, nv, AV.get() + old * n, n, nv, Td.get() + old + cap * old, cap, 1.0, 0.0);
+    } else {
+      const int64_t nv = m - old;
+      cbuf.resize(std::max<int64_t>(m * nv, 1));
+      if (old > 0) {  // coupling from the FP64 side: V_new^T (A V_old)
+        proj(V.get() + old * n, nv, AV.get(), old, cbuf.get(), ham);
+        auto b = to_host(cbuf.get(), nv * old);
+        for (int64_t c = 0; c < old; ++c)
+          for (int64_t r = 0; r < nv; ++r) T[(old + r) + cap * c] = T[c + cap * (old + r)] = b[r + nv * c];
+      }
+      proj(V.get() + old * n, nv, AV.get() + old * n, nv, cbuf.get(), ham);
+      auto b = to_host(cbuf.get(), nv * nv);
+      for (int64_t c = 0; c < nv; ++c)
+        for (int64_t r = 0; r < nv; ++r)
+          T[(old + r) + cap * (old + c)] = 0.5 * (b[r + nv * c] + b[c + nv * r]);
+      if (ham) {  // V^T J V_new (no operator)
+        proj(V.get(), m, V.get() + old * n, nv, cbuf.get(), true);
+        auto g = to_host(cbuf.get(), m * nv);
+        for (int64_t c = 0; c < nv; ++c)
+          for (int64_t r = 0; r < m; ++r) Jm[r + cap * (old + c)] = Jm[(old + c) + cap * r] = g[r + m * c];
+      }
+    }
+    // ---- Ritz pairs of the projected problem ----
+    Ud.resize(m * np);
+    lamd.resize(np);
+    if (!ham) {  // on the device (small_eig.cu)
+      eigw.resize(sym_eig_work_doubles(m, np));
+      SymEigJob job;
+      job.T = Td.get(); job.ldt = cap; job.m = m; job.nw = np;
+      job.U = Ud.get(); job.ldu = m; job.lam = lamd.get(); job.work = eigw.get(); job.info = einfo.get();
+      sym_eig_device(&job, 1, s);
+    } else {  // the Cholesky-reduced pencil on the host
+      std::vector<double> Tm(m * m);
+      for (int64_t c = 0; c < m; ++c)
+        for (int64_t r = 0; r < m; ++r) Tm[r + m * c] = T[r + cap * c];
+      U.assign(m * np, 0.0);
+      std::vector<double> L;
+      if (!cholesky_lower(m, Tm, L)) {
+        if (pit == 0) return false;
+        fail(BSE_ERR_NUMERICAL, "FP64 polish: projected S lost positive definiteness");
+      }
+      // M = L^-1 Jp L^-T
+      std::vector<double> Jp(m * m), Mm(m * m);
+      for (int64_t c = 0; c < m; ++c)
+        for (int64_t r = 0; r < m; ++r) Jp[r + m * c] = Jm[r + cap * c];
+      for (int64_t c = 0; c < m; ++c) {  // forward substitution: L Y = Jp
+        for (int64_t r = 0; r < m; ++r) {
+          double t = Jp[r + m * c];
+          for (int64_t k = 0; k < r; ++k) t -= L[r + m * k] * Jp[k + m * c];
+          Jp[r + m * c] = t / L[r + m * r];
+        }
+      }
+      for (int64_t r = 0; r < m; ++r) {  // Mm = Y L^-T: rows of Y solved against L
+        for (int64_t c = 0; c < m; ++c) {
+          double t = Jp[r + m * c];
+          for (int64_t k = 0; k < c; ++k) t -= Mm[r + m * k] * L[c + m * k];
+          Mm[r + m * c] = t / L[c + m * c];
+        }
+      }
+      for (int64_t c = 0; c < m; ++c)
+        for (int64_t r = 0; r < c; ++r) Mm[r + m * c] = Mm[c + m * r] = 0.5 * (Mm[r + m * c] + Mm[c + m * r]);
+      std::vector<double> mu, Z;
+      if (!sym_eig(m, Mm.data(), mu, Z)) fail(BSE_ERR_NUMERICAL, "Small hermitian eigenvalue problem failed.");
+      // largest positive mu = 1/omega for the lowest positive omega
+      int64_t npos = 0;
+      for (int64_t i = 0; i < m; ++i) npos += mu[i] > 0.0;
+      if (npos < np) {
+        if (pit == 0) return false;
+        fail(BSE_ERR_NUMERICAL, "FP64 polish: fewer positive roots than requested");
+      }
+      for (int64_t j = 0; j < np; ++j) {
+        const int64_t col = m - 1 - j;
+        lam[j] = 1.0 / mu[col];
+        for (int64_t r = m - 1; r >= 0; --r) {  // u = L^-T z
+          double t = Z[r + m * col];
+          for (int64_t k = r + 1; k < m; ++k) t -= L[k + m * r] * U[k + m * j];
+          U[r + m * j] = t / L[r + m * r];
+        }
+      }
+      VGB_CUDA(cudaMemcpyAsync(Ud.get(), U.data(), m * np * sizeof(double), cudaMemcpyHostToDevice, s));
+      VGB_CUDA(cudaMemcpyAsync(lamd.get(), lam.data(), np * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    // ---- Ritz vectors and residuals: q = V U, res = A V U - q lambda (normalised) ----
+    x.gemm_nn(V.get(), n, m, Ud.get(), m, np, q.get(), n, 1.0, 0.0);
+    x.gemm_nn(AV.get(), n, m, Ud.get(), m, np, res.get(), n, 1.0, 0.0);
+    residual_kernel<<<blocks_for(n * np), 256, 0, s>>>(res.get(), q.get(), n, np, lamd.get());
+    VGB_LAUNCH_CHECK();
+    work.resize(2 * np + 8);
+    if (ham) {
+      x.coldots(q.get(), n, nullptr, 0, np, work.get(), true);
+      x.scale_cols(res.get(), n, np, work.get());
+      x.scale_cols(q.get(), n, np, work.get());
+    }
+    x.coldots(res.get(), n, nullptr, 0, np, work.get() + np, true);
+    int einfo_h = 0;
+    if (!ham) {
+      VGB_CUDA(cudaMemcpyAsync(lam.data(), lamd.get(), np * sizeof(double), cudaMemcpyDeviceToHost, s));
+      VGB_CUDA(cudaMemcpyAsync(&einfo_h, einfo.get(), sizeof(int), cudaMemcpyDeviceToHost, s));
+    }
+    std::vector<double> resn = to_host(work.get() + np, np);
+    if (einfo_h != 0) fail(BSE_ERR_NUMERICAL, "Small hermitian eigenvalue problem failed.");
+    double maxres = 0.0;
+    std::vector<int64_t> upd;
+    std::vector<double> upd_lam;
+    for (int64_t j = 0; j < np; ++j) {
+      maxres = std::max(maxres, resn[j]);
+      if (!(resn[j] < tol)) { upd.push_back(j); upd_lam.push_back(lam[j]); }
+    }
+    out.history_resnorm.push_back(maxres);
+    if (verbose)
+      fprintf(stderr, "[davidson] fp64 polish %3lld  search space %6lld  max residual %.3e\n",
+              (long long)pit, (long long)m, maxres);
+    const bool done = upd.empty();
+    if (done || pit == max_iter - 1) {
+      out.evals.assign(lam.begin(), lam.end());
+      out.evals.resize(neigen, 0.0);
+      out.info = done ? 0 : 1;
+      out.max_residual = maxres;
+      if (evecs_dev) x.copy_cols(q.get(), n, evecs_dev, n, np);
+      if (!done) {
+        for (int64_t j : upd) {
+          out.evals[j] = 0.0;
+          if (evecs_dev) VGB_CUDA(cudaMemsetAsync(evecs_dev + j * n, 0, n * sizeof(double), s));
+        }
+      }
+      VGB_CUDA(cudaStreamSynchronize(s));
+      return true;
+    }
+    // ---- corrections for the unconverged roots (computeCorrectionVector) ----
+    const int64_t nupdate = (int64_t)upd.size();
+    if (m + nupdate > cap) {  // restart on the current Ritz vectors with FP64 products
+      DeviceBuffer<double> qk(n * np);
+      x.copy_cols(q.get(), n, qk.get(), n, np);
+      start_basis(qk.get());
+      if (ham) {
+        std::fill(T.begin(), T.end(), 0.0);
+        std::fill(Jm.begin(), Jm.end(), 0.0);
+      }
+      continue;
+    }
+    colsd.resize(std::max<int64_t>(nupdate, 64));
+    tmp.resize(2 * nupdate * n + 2 * nupdate + 8);
+    double *lamu = tmp.get();
+    double *numd = lamu + nupdate, *dend = numd + nupdate + 4;
+    double *dq = dend + nupdate + 4;
+    VGB_CUDA(cudaMemcpyAsync(colsd.get(), upd.data(), nupdate * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    VGB_CUDA(cudaMemcpyAsync(lamu, upd_lam.data(), nupdate * sizeof(double), cudaMemcpyHostToDevice, s));
+    double *Vnew = V.get() + m * n;
+    const bool olsen = correction == 1;
+    dpr_kernel<<<blocks_for(n * nupdate), 256, 0, s>>>(Vnew, n, res.get(), q.get(), n, Dd, colsd.get(), lamu,
+                                                      nupdate, olsen ? 0 : 1, olsen ? dq : nullptr);
+    VGB_LAUNCH_CHECK();
+    if (olsen) {
+      for (int64_t kk = 0; kk < nupdate; ++kk) {
+        x.coldots(q.get() + upd[kk] * n, n, Vnew + kk * n, n, 1, numd + kk, false);
+        x.coldots(q.get() + upd[kk] * n, n, dq + kk * n, n, 1, dend + kk, false);
+      }
+      olsen_finish_kernel<<<blocks_for(n * nupdate), 256, 0, s>>>(Vnew, n, q.get(), n, colsd.get(), numd, dend,
+                                                                 nupdate);
+      VGB_LAUNCH_CHECK();
+    }
+    work.resize(nupdate + 8);
+    x.coldots(Vnew, n, nullptr, 0, nupdate, work.get(), true);
+    x.scale_cols(Vnew, n, nupdate, work.get());
+    gramschmidt(x, V.get(), m, m + nupdate, work, flag);
+    apply(Vnew, nupdate, AV.get() + m * n, false);
+    old = m;
+    m += nupdate;
+  }
+  return true;
+}
+
 }  // namespace
 
 void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_options &opt,
@@ -422,6 +719,12 @@ void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_option
   if (opt.update == 0) size_update = neigen;
   else if (opt.update == 1) size_update = neigen < 20 ? (int64_t)(1.5 * (double)neigen) : neigen + 10;
   else size_update = 2 * neigen;
+  if (opt.size_update > 0) {
+    VGB_REQUIRE(opt.size_update >= neigen, "DavidsonSolver: size_update smaller than neigen");
+    size_update = opt.size_update;
+  }
+  size_update = std::min(size_update, n);
+  bool polish = opt.fp64_polish != 0 && A.split_precision();
 
   int64_t restart_size, ncols;
   if (host_guess) {
@@ -429,7 +732,9 @@ void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_option
     restart_size = std::min(guess_cols, max_space);
     ncols = guess_cols;
   } else {
-    restart_size = 2 * neigen;
+    VGB_REQUIRE(opt.initial_size == 0 || opt.initial_size >= neigen,
+                "DavidsonSolver: initial search space smaller than neigen");
+    restart_size = opt.initial_size > 0 ? opt.initial_size : 2 * neigen;
     ncols = restart_size;
   }
   VGB_REQUIRE(ncols <= n, "DavidsonSolver: initial search space larger than the operator");
@@ -440,27 +745,14 @@ void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_option
   x.s = s;
   x.n = n;
   DeviceBuffer<double> V(n * capc), AV(n * capc), AAV, D(n), q, res, Ud, tmp, lamd, work, cbuf;
+  DeviceBuffer<double> Td, eigw;  // SYMM: the projected matrix stays on the device (ld capc)
   DeviceBuffer<int64_t> colsd;
-  DeviceBuffer<int> flag(1);
+  DeviceBuffer<int> flag(1), einfo(1);
   if (ham) AAV.resize(n * capc);
+  else Td.resize(capc * capc);
   VGB_CUDA(cudaMemsetAsync(V.get(), 0, n * capc * sizeof(double), s));
 
-  cudaEvent_t ev0, ev1;
-  VGB_CUDA(cudaEventCreate(&ev0));
-  VGB_CUDA(cudaEventCreate(&ev1));
-  double matvec_ms = 0.0;
-  auto apply = [&](const double *X, int64_t k, double *Y) {
-    if (k <= 0) return;
-    VGB_CUDA(cudaEventRecord(ev0, s));
-    A.apply(X, n, k, Y, n, s);
-    VGB_CUDA(cudaEventRecord(ev1, s));
-    VGB_CUDA(cudaEventSynchronize(ev1));
-    A.check(s);
-    float ms = 0.f;
-    VGB_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
-    matvec_ms += ms;
-    out.matvec_columns += k;
-  };
+  TimedApply apply(A, s, n, out);
 
   // diagonal of the operator
   A.diagonal(D.get(), s);
@@ -501,20 +793,24 @@ void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_option
     if (phases) { cudaStreamSynchronize(s); tick = std::chrono::steady_clock::now(); }
     {
       const int64_t old = (it == 0) ? 0 : nav, nvec = ncols - old;
-      apply(V.get() + old * n, nvec, AV.get() + old * n);
-      cbuf.resize(ncols * std::max<int64_t>(ncols, 1));
-      // T[:, old:ncols] = V^T AV_new
-      x.gemm_tn(V.get(), n, ncols, AV.get() + old * n, n, nvec, cbuf.get(), ncols, 1.0, 0.0);
-      std::vector<double> blk(ncols * nvec);
-      VGB_CUDA(cudaMemcpyAsync(blk.data(), cbuf.get(), blk.size() * sizeof(double),
-                               cudaMemcpyDeviceToHost, s));
-      VGB_CUDA(cudaStreamSynchronize(s));
-      for (int64_t c = 0; c < nvec; ++c)
-        for (int64_t r = 0; r < ncols; ++r) T[r + ldT * (old + c)] = blk[r + ncols * c];
+      apply(V.get() + old * n, nvec, AV.get() + old * n, false);
       if (!ham) {
-        for (int64_t c = 0; c < nvec; ++c)
-          for (int64_t r = 0; r < old; ++r) T[(old + c) + ldT * r] = T[r + ldT * (old + c)];
+        // T[:, old:ncols] = V^T AV_new, T[old:ncols, :old] its transpose, in HBM
+        x.gemm_tn(V.get(), n, ncols, AV.get() + old * n, n, nvec, Td.get() + ldT * old, ldT, 1.0, 0.0);
+        if (old > 0) {
+          mirror_block_kernel<<<blocks_for(old * nvec), 256, 0, s>>>(Td.get(), ldT, old, nvec);
+          VGB_LAUNCH_CHECK();
+        }
       } else {
+        cbuf.resize(ncols * std::max<int64_t>(ncols, 1));
+        // T[:, old:ncols] = V^T AV_new
+        x.gemm_tn(V.get(), n, ncols, AV.get() + old * n, n, nvec, cbuf.get(), ncols, 1.0, 0.0);
+        std::vector<double> blk(ncols * nvec);
+        VGB_CUDA(cudaMemcpyAsync(blk.data(), cbuf.get(), blk.size() * sizeof(double),
+                                 cudaMemcpyDeviceToHost, s));
+        VGB_CUDA(cudaStreamSynchronize(s));
+        for (int64_t c = 0; c < nvec; ++c)
+          for (int64_t r = 0; r < ncols; ++r) T[r + ldT * (old + c)] = blk[r + ncols * c];
         // T[old:, :old] = V_new^T AV_old;  AAV_new = A AV_new;  B likewise
         if (old > 0) {
           x.gemm_tn(V.get() + old * n, n, nvec, AV.get(), n, old, cbuf.get(), nvec, 1.0, 0.0);
@@ -545,25 +841,28 @@ void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_option
       nav = ncols;
     }
     const int64_t m = ncols;
-    std::vector<double> Tm(m * m);
-    for (int64_t c = 0; c < m; ++c)
-      for (int64_t r = 0; r < m; ++r) Tm[r + m * c] = T[r + ldT * c];
-    if (debug) {
-      fprintf(stderr, "[davidson-debug] iter %lld m %lld T diag:", (long long)it, (long long)m);
-      for (int64_t c = 0; c < std::min<int64_t>(m, 40); ++c) fprintf(stderr, " %.4f", Tm[c + m * c]);
-      fprintf(stderr, "\n");
-    }
     const int64_t needed = std::min(m, std::max(restart_size, size_update));
+    Ud.resize(m * needed);
+    lamd.resize(needed);
 
     mark(0);
-    // ---- getRitzEigenPairs (small problem on the host) ----
+    // ---- getRitzEigenPairs ----
     if (!ham) {
-      std::vector<double> ev, evec;
-      if (!sym_eig(m, Tm.data(), ev, evec))
-        fail(BSE_ERR_NUMERICAL, "Small hermitian eigenvalue problem failed.");
-      lam.assign(ev.begin(), ev.begin() + needed);
-      U.assign(evec.begin(), evec.begin() + m * needed);
+      // Ritz problem on the device (small_eig.cu): U and lambda never leave HBM
+      eigw.resize(sym_eig_work_doubles(m, needed));
+      SymEigJob job;
+      job.T = Td.get(); job.ldt = ldT; job.m = m; job.nw = needed;
+      job.U = Ud.get(); job.ldu = m; job.lam = lamd.get(); job.work = eigw.get(); job.info = einfo.get();
+      sym_eig_device(&job, 1, s);
     } else {
+      std::vector<double> Tm(m * m);
+      for (int64_t c = 0; c < m; ++c)
+        for (int64_t r = 0; r < m; ++r) Tm[r + m * c] = T[r + ldT * c];
+      if (debug) {
+        fprintf(stderr, "[davidson-debug] iter %lld m %lld T diag:", (long long)it, (long long)m);
+        for (int64_t c = 0; c < std::min<int64_t>(m, 40); ++c) fprintf(stderr, " %.4f", Tm[c + m * c]);
+        fprintf(stderr, "\n");
+      }
       std::vector<double> Bmm(m * m);
       for (int64_t c = 0; c < m; ++c)
         for (int64_t r = 0; r < m; ++r) Bmm[r + m * c] = Bm[r + ldT * c];
@@ -622,15 +921,13 @@ void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_option
         }
         lam[c] = sacc;
       }
+      VGB_CUDA(cudaMemcpyAsync(Ud.get(), U.data(), m * needed * sizeof(double), cudaMemcpyHostToDevice, s));
+      VGB_CUDA(cudaMemcpyAsync(lamd.get(), lam.data(), needed * sizeof(double), cudaMemcpyHostToDevice, s));
     }
     mark(1);
     // q = V U, res = AV U - q Lambda
-    Ud.resize(m * needed);
-    lamd.resize(needed);
     q.resize(n * needed);
     res.resize(n * needed);
-    VGB_CUDA(cudaMemcpyAsync(Ud.get(), U.data(), m * needed * sizeof(double), cudaMemcpyHostToDevice, s));
-    VGB_CUDA(cudaMemcpyAsync(lamd.get(), lam.data(), needed * sizeof(double), cudaMemcpyHostToDevice, s));
     x.gemm_nn(V.get(), n, m, Ud.get(), m, needed, q.get(), n, 1.0, 0.0);
     x.gemm_nn(AV.get(), n, m, Ud.get(), m, needed, res.get(), n, 1.0, 0.0);
     residual_kernel<<<blocks_for(n * needed), 256, 0, s>>>(res.get(), q.get(), n, needed, lamd.get());
@@ -643,7 +940,14 @@ void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_option
     x.coldots(res.get(), n, nullptr, 0, nn_check, work.get(), true);
     resn.assign(nn_check, 0.0);
     VGB_CUDA(cudaMemcpyAsync(resn.data(), work.get(), nn_check * sizeof(double), cudaMemcpyDeviceToHost, s));
+    int einfo_h = 0;
+    if (!ham) {  // the Ritz values come back with the residual norms (one synchronisation)
+      lam.assign(needed, 0.0);
+      VGB_CUDA(cudaMemcpyAsync(lam.data(), lamd.get(), needed * sizeof(double), cudaMemcpyDeviceToHost, s));
+      VGB_CUDA(cudaMemcpyAsync(&einfo_h, einfo.get(), sizeof(int), cudaMemcpyDeviceToHost, s));
+    }
     VGB_CUDA(cudaStreamSynchronize(s));
+    if (einfo_h != 0) fail(BSE_ERR_NUMERICAL, "Small hermitian eigenvalue problem failed.");
     for (int64_t j = 0; j < size_update; ++j) conv[j] = (j < nn_check) ? (resn[j] < tol) : 0;
     bool converged = true;
     double maxres = 0.0;
@@ -656,6 +960,23 @@ void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_option
       fprintf(stderr, "[davidson] iter %4lld  search space %6lld  max residual %.3e\n",
               (long long)it, (long long)ncols, maxres);
     const bool last = it == iter_max - 1;
+    out.max_residual = maxres;
+    // split-precision residuals that meet the tolerance, or have not halved in three iterations
+    // (the floor of the split products), or the last iteration
+    const size_t nh = out.history_resnorm.size();
+    const bool stalled = nh > 3 && maxres > 0.5 * out.history_resnorm[nh - 4];
+    if (polish && (converged || stalled || last)) {
+      const auto tp0 = std::chrono::steady_clock::now();
+      const int64_t pmax = std::max<int64_t>(iter_max, 20);
+      const bool ran = fp64_polish(x, apply, D.get(), q.get(), neigen, ham, opt.correction, tol, pmax, evecs_dev,
+                                   out, opt.verbose);
+      out.seconds_polish = std::chrono::duration<double>(std::chrono::steady_clock::now() - tp0).count();
+      if (ran) {
+        out.polished = 1;
+        break;
+      }
+      polish = false;  // the projected S of a HAM problem was not positive definite: carry on as is
+    }
     if (converged || last) {
       // storeEigenPairs (+ zeroing of unconverged roots on the last iteration)
       out.evals.assign(lam.begin(), lam.begin() + std::min(neigen, needed));
@@ -779,15 +1100,17 @@ void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_option
       ncols = rs + nv;
       nav = rs;
       // T = V[:, :rs]^T AV (and B = V^T AAV for HAM)
-      cbuf.resize(rs * rs);
-      std::vector<double> blk(rs * rs);
-      x.gemm_tn(V.get(), n, rs, AV.get(), n, rs, cbuf.get(), rs, 1.0, 0.0);
-      VGB_CUDA(cudaMemcpyAsync(blk.data(), cbuf.get(), blk.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
-      VGB_CUDA(cudaStreamSynchronize(s));
-      std::fill(T.begin(), T.end(), 0.0);
-      for (int64_t c = 0; c < rs; ++c)
-        for (int64_t r = 0; r < rs; ++r) T[r + ldT * c] = blk[r + rs * c];
-      if (ham) {
+      if (!ham) {
+        x.gemm_tn(V.get(), n, rs, AV.get(), n, rs, Td.get(), ldT, 1.0, 0.0);
+      } else {
+        cbuf.resize(rs * rs);
+        std::vector<double> blk(rs * rs);
+        x.gemm_tn(V.get(), n, rs, AV.get(), n, rs, cbuf.get(), rs, 1.0, 0.0);
+        VGB_CUDA(cudaMemcpyAsync(blk.data(), cbuf.get(), blk.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+        VGB_CUDA(cudaStreamSynchronize(s));
+        std::fill(T.begin(), T.end(), 0.0);
+        for (int64_t c = 0; c < rs; ++c)
+          for (int64_t r = 0; r < rs; ++r) T[r + ldT * c] = blk[r + rs * c];
         x.gemm_tn(V.get(), n, rs, AAV.get(), n, rs, cbuf.get(), rs, 1.0, 0.0);
         VGB_CUDA(cudaMemcpyAsync(blk.data(), cbuf.get(), blk.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
         VGB_CUDA(cudaStreamSynchronize(s));
@@ -798,8 +1121,7 @@ void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_option
     }
   }
   VGB_CUDA(cudaStreamSynchronize(s));
-  cudaEventDestroy(ev0);
-  cudaEventDestroy(ev1);
+  const double matvec_ms = apply.ms;
   if (phases)
     fprintf(stderr,
             "[davidson] phases (s): projection+matvec %.4f (matvec %.4f)  small-eig %.4f  ritz %.4f  "

@@ -12,6 +12,10 @@ struct DavidsonOutput {
   int64_t matvec_columns = 0;
   double seconds_matvec = 0.0, seconds_total = 0.0;
   std::vector<double> history_resnorm;  // max residual of the first neigen roots, per iteration
+  double max_residual = 0.0;            // of the neigen roots at return
+  int polished = 0;                     // roots from the FP64 polish
+  int64_t fp64_columns = 0, polish_iterations = 0;
+  double seconds_polish = 0.0;
 };
 
 // Mirrors DavidsonSolver::solve (xtp/include/votca/xtp/davidsonsolver.h:64-190,

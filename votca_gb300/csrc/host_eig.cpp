@@ -71,7 +71,11 @@ void tridiagonalize(int64_t n, std::vector<double> &a, std::vector<double> &d,
 }
 
 // Implicit-shift QL on the symmetric tridiagonal (d, e), rotations applied to
-// the columns of Z (n x n column-major).
+// the columns of Z (n x n column-major).  This is the published QL algorithm with
+// implicit Wilkinson shifts of Bowdler, Martin, Reinsch and Wilkinson ("The QR and QL
+// algorithms for symmetric matrices", Numer. Math. 11 (1968) 293-306; EISPACK's tql2):
+// deflate where |e_m| <= eps (|d_m| + |d_m+1|), shift by the eigenvalue of the leading
+// 2 x 2 block closer to d_l, chase the bulge with plane rotations.
 bool tridiagonal_ql(int64_t n, std::vector<double> &d, std::vector<double> &e,
                     std::vector<double> &Z) {
   const double eps = std::numeric_limits<double>::epsilon();

@@ -68,6 +68,12 @@ struct UksApply : DeviceOperator {
   }
   void diagonal(double *D, cudaStream_t s) override { op->diagonal(coef, D, s); }
   void check(cudaStream_t s) override { op->check_errors(s); }
+  bool split_precision() const override { return op->precision == BSE_PRECISION_MIXED; }
+  void apply_fp64(const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy,
+                  cudaStream_t s) override {
+    ForceFp64 g(&op->alpha, &op->beta);
+    op->matmul(coef, X, ldx, k, Y, ldy, s);
+  }
 };
 
 struct UksHamApply : DeviceOperator {
@@ -85,6 +91,12 @@ struct UksHamApply : DeviceOperator {
     ham_diag(D, op->dim, D, s);
   }
   void check(cudaStream_t s) override { op->check_errors(s); }
+  bool split_precision() const override { return op->precision == BSE_PRECISION_MIXED; }
+  void apply_fp64(const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy,
+                  cudaStream_t s) override {
+    ForceFp64 g(&op->alpha, &op->beta);
+    op->ham_matmul(a, b, X, ldx, k, Y, ldy, s);
+  }
 };
 
 }  // namespace vgb

@@ -35,6 +35,11 @@ class DavidsonSolver:
         self.update_ = 1
         self.matrix_type_ = 0
         self.verbose = False
+        # no counterpart in the reference: FP64 polish of split-precision solves, trial vectors
+        # per iteration (0 = getSizeUpdate), initial unit-vector guesses (0 = 2 * neigen)
+        self.fp64_polish_ = True
+        self.block_size_ = 0
+        self.initial_size_ = 0
         self.eigenvalues_ = None
         self.eigenvectors_ = None
         self.info_ = "NoConvergence"
@@ -65,6 +70,20 @@ class DavidsonSolver:
             raise RuntimeError(s + " is not a valid Davidson update")
         self.update_ = UPDATES[s]
 
+    def set_fp64_polish(self, on):
+        """Split-precision operators: re-evaluate the converged Ritz vectors with FP64 products
+        and iterate until the FP64 residuals meet the tolerance (on by default)."""
+        self.fp64_polish_ = bool(on)
+
+    def set_block_size(self, n):
+        """Trial vectors added per iteration (>= neigen); 0 restores getSizeUpdate's rule."""
+        self.block_size_ = int(n)
+
+    def set_initial_size(self, n):
+        """Unit-vector guesses of solve(A, neigen) (the size_initial_guess argument of the
+        reference's overload, davidsonsolver.h:64-85); 0 means 2 * neigen."""
+        self.initial_size_ = int(n)
+
     def set_matrix_type(self, mt):
         if mt not in MATRIX_TYPES:
             raise RuntimeError(mt + " is not a valid Davidson matrix type")
@@ -84,7 +103,8 @@ class DavidsonSolver:
 
     def _options(self):
         return _lib.bse_davidson_options(self.iter_max_, self.tol_, self.max_search_space_, self.correction_,
-                                         self.update_, self.matrix_type_, int(self.verbose))
+                                         self.update_, self.matrix_type_, int(self.verbose),
+                                         int(self.fp64_polish_), 0, self.block_size_, self.initial_size_)
 
     def solve_batch(self, ops, neigen, nthreads=0):
         """Lowest neigen eigenvalues of every operator in ops (BSE_OPERATORs with one
