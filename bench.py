@@ -15,11 +15,14 @@ e2e: the same product through the host-pointer C ABI call (bse_op_matmul):
 X copied host->device and Y device->host inside every timed step.
 
 Also reported once, outside the timed steps: time-to-20-roots of the full
-Davidson solve (tolerance 1e-7) for each precision built, the C0 solve, the
-batched 256-molecule solve, and (N = 1) the CPU figures: the reference loop
-nest port on a bounded sample of one product (cpu_baseline; also one triplet
-product, from which the reference's time-to-20-roots is extrapolated), and the
-factorised FP64 oracle as an informational second figure.
+Davidson solve (tolerance 1e-7, split precision with its FP64 polish, and FP64)
+with the FP64 residuals of the returned roots, the C0 solve, the batched
+256-molecule solve, the full-BSE solve at v=128, c=1024, Naux=4096 (32 trial
+vectors per iteration, FP64 polish, an independent FP64 evaluation of its
+roots), and (N = 1) the CPU figures: the reference loop nest port on one whole
+product (cpu_baseline; also one whole triplet product, from which the
+reference's time-to-20-roots is computed), and the factorised FP64 oracle as an
+informational second figure.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|mixed]
   python bench.py --impl reference ...   # the reference CPU path (oracle port)
@@ -772,9 +775,11 @@ def main():
     ap.add_argument("--molecules", type=int, default=256,
                     help="batched independent molecules (0 skips the batched solve report)")
     ap.add_argument("--batch-threads", type=int, default=16, help="host threads of the batched solve")
-    ap.add_argument("--full-bse", action="store_true",
-                    help="also run the full-BSE report (v=128, c=1024, Naux=4096; minutes, ~110 GB of HBM)")
-    ap.add_argument("--full-bse-check", action="store_true", help="FP64 evaluation of the full-BSE roots")
+    ap.add_argument("--no-full-bse", dest="full_bse", action="store_false",
+                    help="skip the full-BSE report (v=128, c=1024, Naux=4096, 32 trial vectors per iteration, "
+                         "FP64 polish; about 1.5 minutes, ~110 GB of HBM)")
+    ap.add_argument("--no-full-bse-check", dest="full_bse_check", action="store_false",
+                    help="skip the independent FP64 evaluation of the full-BSE roots")
     ap.add_argument("--solve-only", action="store_true",
                     help="one split-precision 20-singlet solve (with its FP64 polish) at the workload shape, "
                          "after one warm-up solve, and nothing else (for profiler captures)")
