@@ -40,10 +40,17 @@ typedef enum bse_status {
 } bse_status;
 
 typedef enum bse_precision {
-  BSE_PRECISION_FP64 = 0,  /* every product in FP64 (the plain drop-in) */
-  BSE_PRECISION_MIXED = 1  /* Hx/Hd/Hd2 contractions as BF16x3 split products on
-                              tcgen05 tensor cores with FP32 accumulation;
-                              Hqp and all Davidson algebra in FP64 */
+  BSE_PRECISION_FP64 = 0,   /* every product in FP64 (the plain drop-in) */
+  BSE_PRECISION_MIXED = 1,  /* Hx/Hd/Hd2 contractions as BF16x3 split products on
+                               tcgen05 tensor cores with FP32 accumulation;
+                               Hqp and all Davidson algebra in FP64 */
+  BSE_PRECISION_SLICED = 2  /* Hx/Hd/Hd2 contractions as Ozaki slice products on the
+                               tcgen05 tensor cores: each FP64 operand cut into five 7-bit
+                               digit planes (power-of-two scale per run of <= 1024 K
+                               elements), every pair of digit levels up to the fifth
+                               accumulated exactly in FP32 over one run, runs and pairs
+                               summed in FP64, intermediates kept in FP64; agrees with the
+                               FP64 product to about 1e-11 of its scale */
 } bse_precision;
 
 /* BSEOperator_Options, xtp/include/votca/xtp/bse_operator.h:32-38 (absolute MO indices). */
@@ -267,11 +274,13 @@ typedef struct bse_davidson_options {
   int32_t fp64_polish;      /* split-precision (BSE_PRECISION_MIXED) operators only: once the
                                split-precision iterations meet the tolerance (or their largest
                                residual has not halved in three iterations, or iter_max is
-                               reached), the neigen Ritz vectors are re-applied with FP64
-                               products and the iteration continues on that basis until the
-                               residuals, formed from FP64 products of the Ritz vectors, meet
-                               the tolerance; the returned eigenvalues are those FP64 Rayleigh
-                               quotients.  Ignored for FP64 operators. */
+                               reached), the neigen Ritz vectors are re-applied with
+                               FP64-accurate products and the iteration continues on that
+                               basis until the residuals, formed from FP64-accurate products of
+                               the Ritz vectors, meet the tolerance; the returned eigenvalues
+                               are those Rayleigh quotients.  1: the FP64-accurate products are
+                               the Ozaki slice products of BSE_PRECISION_SLICED; 2: FP64
+                               DGEMM.  Ignored for FP64 and SLICED operators. */
   int32_t reserved;
   int64_t size_update;      /* trial vectors per iteration: 0 = getSizeUpdate of `update`
                                (davidsonsolver.cc:149-170); > 0 = that many (>= neigen) */
@@ -352,6 +361,17 @@ int bse_probe_fp64_tflops(double *tflops);
  * the tridiagonalisation, the bisection, the inverse iteration and the back-transformation. */
 int bse_small_sym_eig(int64_t njobs, const int64_t *m, const int64_t *nw, const double *T,
                       double *evals, double *evecs, int64_t *phase_cycles);
+
+/* The device solver of the harmonic-Ritz problem of the HAM Davidson, exposed on its own: the
+ * real generalized problem T u = theta B u (m x m, general, column-major host arrays), the
+ * reference's selection (the second member of each complex-conjugate pair dropped, an unpaired
+ * complex eigenvalue an error; the nw largest real parts first) and its outputs: evecs (m x nw)
+ * the real parts of the selected eigenvectors, each normalised, evals[c] = u_c^T T u_c.  It takes
+ * the place of Eigen::GeneralizedEigenSolver and the selection in DavidsonSolver::getHarmonicRitz
+ * (xtp/src/libxtp/davidsonsolver.cc:241-331).  Columns past the number of candidates are zero;
+ * *selected (may be NULL) receives that number.  1 <= nw <= m <= 1024. */
+int bse_small_gen_eig(int64_t m, int64_t nw, const double *T, const double *B, double *evals,
+                      double *evecs, int64_t *selected);
 
 /* ---- Adjoint (no counterpart in the reference; its forward twin is the
  * expectation-value analysis x^T H_part x of xtp/src/libxtp/gwbse/bse.cc:490-520) ----

@@ -154,9 +154,12 @@ def _dense_ab(mmn, hqp, w):
 
 
 def full_eigs(mmn, hqp, w):
+    """The lowest positive roots of [[A, B], [-B, -A]] through the symmetric form: with
+    A - B = L L^T, Omega^2 are the eigenvalues of L^T (A + B) L (similar to (A - B)(A + B));
+    a symmetric eigensolver keeps the finite differences at the rounding floor below."""
     A, B = _dense_ab(mmn, hqp, w)
-    ev = np.linalg.eigvals(np.block([[A, B], [-B, -A]])).real
-    return np.sort(ev[ev > 0])[:NROOTS]
+    L = np.linalg.cholesky(A - B)
+    return np.sqrt(np.linalg.eigvalsh(L.T @ (A + B) @ L))[:NROOTS]
 
 
 def cpu_reference_gradient_full(mmn, hqp, w, X, Y, g):

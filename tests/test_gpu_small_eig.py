@@ -98,3 +98,89 @@ def test_davidson_shaped_problem_phase_cycles():
     np.testing.assert_allclose(lam, np.linalg.eigvalsh(t)[:40], atol=1e-12 * 15)
     print("phase cycles (tridiagonal, bisection, inverse iteration, back-transform):", cyc.tolist())
     assert np.all(cyc > 0)
+
+
+def _gen_solve(T, B, nw):
+    from votca_gb300 import _lib
+
+    L = _lib.load()
+    m = T.shape[0]
+    ev = np.zeros(nw)
+    U = np.zeros(m * nw)
+    sel = ctypes.c_int64(0)
+    Tf = np.asfortranarray(T).ravel(order="F")
+    Bf = np.asfortranarray(B).ravel(order="F")
+    _lib.check(L.bse_small_gen_eig(m, nw, Tf.ctypes.data_as(_lib.c_dp), Bf.ctypes.data_as(_lib.c_dp),
+                                   ev.ctypes.data_as(_lib.c_dp), U.ctypes.data_as(_lib.c_dp), ctypes.byref(sel)))
+    return ev, U.reshape((m, nw), order="F"), sel.value
+
+
+def _reference_selection(w, nw):
+    """getHarmonicRitz's selection (davidsonsolver.cc:261-324) on eigenvalues w: the second
+    member of each conjugate pair dropped, a stable ascending sort by real part, reversed."""
+    pairs = []
+    for i, x in enumerate(w):
+        if x.imag == 0:
+            continue
+        for p in pairs:
+            if p[1] < 0 and abs(w[p[0]].real - x.real) < 1e-9 and abs(w[p[0]].imag + x.imag) < 1e-9:
+                p[1] = i
+                break
+        else:
+            pairs.append([i, -1])
+    seconds = {p[1] for p in pairs}
+    cand = [i for i in range(len(w)) if i not in seconds]
+    order = sorted(cand, key=lambda i: w[i].real)[::-1]
+    return order[:nw], len(cand)
+
+
+@pytest.mark.parametrize("m,nw,npairs", [(50, 20, 5), (10, 9, 3), (120, 40, 0), (7, 7, 0)])
+def test_harmonic_ritz_problem_matches_eig(m, nw, npairs):
+    """T u = theta B u with a known spectrum (T = B X D X^-1): real eigenvalues spread over
+    [-5, 5] and npairs complex pairs below them; the device selection and vectors against
+    numpy's eig with the reference's selection."""
+    rng = np.random.default_rng(m + nw)
+    B = rng.standard_normal((m, m)) + m ** 0.5 * np.eye(m)
+    X = rng.standard_normal((m, m)) + 2.0 * np.eye(m)
+    D = np.diag(np.sort(rng.uniform(-5, 5, m)))
+    for p in range(npairs):  # rotation blocks: a +- ib with a below every real eigenvalue
+        a, b = -10.0 + p, 0.5 + 0.1 * p
+        D[2 * p:2 * p + 2, 2 * p:2 * p + 2] = [[a, b], [-b, a]]
+    T = B @ X @ D @ np.linalg.inv(X)
+    lam, U, sel = _gen_solve(T, B, nw)
+    w, vr = np.linalg.eig(np.linalg.solve(B, T))
+    idx, ncand = _reference_selection(w, nw)
+    assert sel == min(ncand, nw) and ncand == m - npairs
+    for c, i in enumerate(idx):
+        u = U[:, c]
+        assert abs(np.linalg.norm(u) - 1.0) < 1e-12
+        if w[i].imag == 0:
+            v = vr[:, i].real / np.linalg.norm(vr[:, i].real)
+            assert abs(abs(u @ v) - 1.0) < 1e-9, (c, abs(u @ v))
+            assert abs(lam[c] - u @ T @ u) < 1e-9 * np.abs(T).max()
+    assert np.all(U[:, sel:] == 0) and np.all(lam[sel:] == 0)
+
+
+def test_harmonic_ritz_davidson_shape():
+    """The HAM Davidson's projected pencil T = V^T H V, B = V^T H H V for an orthonormal V and a
+    BSE-shaped H = [[A, Bc], [-Bc, -A]]: the largest theta (the smallest positive omega)."""
+    rng = np.random.default_rng(21)
+    k, m, nw = 150, 90, 30
+    A = np.diag(np.sort(rng.uniform(0.3, 1.5, k))) + 0.01 * rng.standard_normal((k, k))
+    A = 0.5 * (A + A.T)
+    Bc = 0.01 * rng.standard_normal((k, k))
+    Bc = 0.5 * (Bc + Bc.T)
+    H = np.block([[A, Bc], [-Bc, -A]])
+    V, _ = np.linalg.qr(rng.standard_normal((2 * k, m)))
+    HV = H @ V
+    T, B = V.T @ HV, V.T @ (H @ HV)
+    lam, U, sel = _gen_solve(T, B, nw)
+    w, vr = np.linalg.eig(np.linalg.solve(B, T))
+    idx, _ = _reference_selection(w, nw)
+    assert sel == nw
+    for c, i in enumerate(idx):
+        if w[i].imag != 0:
+            continue
+        v = vr[:, i].real / np.linalg.norm(vr[:, i].real)
+        assert abs(abs(U[:, c] @ v) - 1.0) < 1e-8, (c, abs(U[:, c] @ v))
+        assert abs(lam[c] - U[:, c] @ T @ U[:, c]) < 1e-10

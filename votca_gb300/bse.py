@@ -36,7 +36,7 @@ class DavidsonOptions:
     # no counterpart in gwbse.xml: trial vectors per iteration (0 = the davidson_update rule)
     # and the FP64 polish of split-precision solves
     davidson_block: int = 0
-    fp64_polish: bool = True
+    fp64_polish: object = True  # True / "sliced", "fp64" (FP64 DGEMM products) or False
 
 
 def adjust_hqp_size(Hqp, rpa_input_energies, homo, vmin, cmax, qpmin, qpmax, rpamin,

@@ -22,6 +22,7 @@ from . import _lib
 
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
+PRECISION_SLICED = 2
 
 
 @dataclass

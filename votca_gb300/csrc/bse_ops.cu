@@ -137,30 +137,31 @@ struct DiagArgs {
   double *D;
 };
 
+// sum_P x[P * sx] * y[P * sy] with four independent FMA chains (the FP64 pipe of GB300 has a long
+// latency: one chain per thread leaves it idle), combined in a fixed order
+__device__ __forceinline__ double strided_dot(const double *x, int64_t sx, const double *y, int64_t sy,
+                                              int64_t n) {
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  int64_t P = 0;
+  for (; P + 4 <= n; P += 4) {
+    s0 = fma(x[P * sx], y[P * sy], s0);
+    s1 = fma(x[(P + 1) * sx], y[(P + 1) * sy], s1);
+    s2 = fma(x[(P + 2) * sx], y[(P + 2) * sy], s2);
+    s3 = fma(x[(P + 3) * sx], y[(P + 3) * sy], s3);
+  }
+  for (; P < n; ++P) s0 = fma(x[P * sx], y[P * sy], s0);
+  return (s0 + s1) + (s2 + s3);
+}
+
 // BSE_OPERATOR::diagonal (bse_operator.cc:133-175), one thread per pair.
 __device__ __forceinline__ void diagonal_range(const DiagArgs &a, int64_t I0, int64_t step) {
   for (int64_t I = I0; I < a.dim; I += step) {
     const int64_t v = I / a.ct, c = I % a.ct;
     double entry = 0.0;
-    if (a.cx != 0.0) {
-      double s = 0.0;
-      for (int64_t P = 0; P < a.naux; ++P) {
-        const double x = a.Bvc[P * a.dim + I];
-        s = fma(x, x, s);
-      }
-      entry += a.cx * s;
-    }
+    if (a.cx != 0.0) entry += a.cx * strided_dot(a.Bvc + I, a.dim, a.Bvc + I, a.dim, a.naux);
     if (a.cqp != 0.0) entry += a.cqp * (a.Hcc[c + a.ct * c] - a.Hvv[v + a.vt * v]);
-    if (a.cd != 0.0) {
-      double s = 0.0;
-      for (int64_t P = 0; P < a.naux; ++P) s = fma(a.dcc[P * a.ct + c], a.dvv[P * a.vt + v], s);
-      entry -= a.cd * s;
-    }
-    if (a.cd2 != 0.0) {
-      double s = 0.0;
-      for (int64_t P = 0; P < a.naux; ++P) s = fma(a.Mcv[P * a.dim + I], a.Bvc[P * a.dim + I], s);
-      entry -= a.cd2 * s;
-    }
+    if (a.cd != 0.0) entry -= a.cd * strided_dot(a.dcc + c, a.ct, a.dvv + v, a.vt, a.naux);
+    if (a.cd2 != 0.0) entry -= a.cd2 * strided_dot(a.Mcv + I, a.dim, a.Bvc + I, a.dim, a.naux);
     a.D[I] = entry;
   }
 }
@@ -325,7 +326,7 @@ void BseOperator::stage(const bse_mmn_desc &desc, const double *const *slices, c
   VGB_REQUIRE(vt >= 1 && ct >= 1, "bse_op_create: empty BSE window (homo/vmin/cmax)");
   VGB_REQUIRE(naux >= 1, "bse_op_create: auxsize must be positive");
   VGB_REQUIRE(slices != nullptr && w != nullptr && hqp != nullptr, "bse_op_create: null input");
-  VGB_REQUIRE(prec == BSE_PRECISION_FP64 || prec == BSE_PRECISION_MIXED,
+  VGB_REQUIRE(prec == BSE_PRECISION_FP64 || prec == BSE_PRECISION_MIXED || prec == BSE_PRECISION_SLICED,
               "bse_op_create: unknown precision");
   const int64_t msize = desc.mmax - desc.mmin + 1, nsize = desc.nmax - desc.nmin + 1;
   VGB_REQUIRE(opt.vmin >= desc.mmin && opt.cmax <= desc.mmax,
@@ -443,9 +444,9 @@ void BseOperator::stage(const bse_mmn_desc &desc, const double *const *slices, c
   VGB_CUDA(cudaMemcpyAsync(Hvv.get(), hvv.data(), vt * vt * sizeof(double), cudaMemcpyHostToDevice, s));
   VGB_CUDA(cudaStreamSynchronize(s));
 
-  if (precision == BSE_PRECISION_MIXED) {
+  if (precision == BSE_PRECISION_MIXED || precision == BSE_PRECISION_SLICED) {
     mixed.reset(new MixedEngine());
-    mixed->stage(*this, s);
+    mixed->stage(*this, s, precision == BSE_PRECISION_MIXED);
   }
 }
 
@@ -568,6 +569,11 @@ void BseOperator::matmul(const Coef &c, const double *X, int64_t ldx, int64_t k,
   VGB_REQUIRE(!(c.cd != 0 && c.cd2 != 0), "Hamiltonian cannot contain Hd and Hd2 at the same time");
   bool acc = false;
   if (c.cqp != 0) { apply_hqp(c.cqp, X, ldx, k, Y, ldy, acc, s); acc = true; }
+  if (mixed && (precision == BSE_PRECISION_SLICED ||
+                (precision == BSE_PRECISION_MIXED && force_fp64 && fp64_products == 0))) {
+    mixed->apply_sliced(*this, c, X, ldx, k, Y, ldy, acc, s);
+    return;
+  }
   if (precision == BSE_PRECISION_MIXED && mixed && !force_fp64) {
     mixed->apply(*this, c, X, ldx, k, Y, ldy, acc, s);
     return;

@@ -74,8 +74,10 @@ struct DeviceOperator {
   // raise if an asynchronous device-side failure was recorded (synchronises)
   virtual void check(cudaStream_t) {}
   // true when apply() runs split-precision (tensor-core) products; apply_fp64 is then the
-  // same operator with every product in FP64 (the Davidson polish)
+  // same operator with FP64-accurate products (the Davidson polish): Ozaki slice products where
+  // the operator has a tensor-core engine and fp64_products == 0, else FP64 DGEMM
   virtual bool split_precision() const { return false; }
+  int fp64_products = 0;
   virtual void apply_fp64(const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy,
                           cudaStream_t s) {
     apply(X, ldx, k, Y, ldy, s);
@@ -89,8 +91,10 @@ class BseOperator {
   int64_t vt = 0, ct = 0, naux = 0, dim = 0;
   int precision = BSE_PRECISION_FP64;
   bool hqp_diagonal = true;
-  // set while a split-precision operator must run its FP64 path (FP64 blocks are always staged)
+  // set while a split-precision operator must run its FP64-accurate path (FP64 blocks are always
+  // staged): Ozaki slice products on the tensor cores (fp64_products 0) or FP64 DGEMM (1)
   bool force_fp64 = false;
+  int fp64_products = 0;
 
   // FP64 staged blocks (layouts documented in bse_ops.cu)
   DeviceBuffer<double> Bvc, Mcc, Gvv, Mcv, dcc, dvv, Hcc, Hvv;
@@ -190,17 +194,29 @@ void matmul_grouped(const Coef &c, const std::vector<GroupedItem> &items, cudaSt
 void diagonal_grouped(const Coef &c, const std::vector<BseOperator *> &ops,
                       const std::vector<double *> &D, cudaStream_t s);
 
-// Runs the operators' FP64 path for its lifetime (split-precision handles keep FP64 blocks).
+// Runs the operators' FP64-accurate path for its lifetime (split-precision handles keep FP64
+// blocks); mode: BseOperator::fp64_products.
 struct ForceFp64 {
   BseOperator *a, *b;
   bool sa, sb;
-  explicit ForceFp64(BseOperator *x, BseOperator *y = nullptr) : a(x), b(y), sa(x->force_fp64), sb(y ? y->force_fp64 : false) {
+  int ma, mb;
+  explicit ForceFp64(BseOperator *x, BseOperator *y = nullptr, int mode = 1)
+      : a(x), b(y), sa(x->force_fp64), sb(y ? y->force_fp64 : false), ma(x->fp64_products),
+        mb(y ? y->fp64_products : 0) {
     a->force_fp64 = true;
-    if (b) b->force_fp64 = true;
+    a->fp64_products = mode;
+    if (b) {
+      b->force_fp64 = true;
+      b->fp64_products = mode;
+    }
   }
   ~ForceFp64() {
     a->force_fp64 = sa;
-    if (b) b->force_fp64 = sb;
+    a->fp64_products = ma;
+    if (b) {
+      b->force_fp64 = sb;
+      b->fp64_products = mb;
+    }
   }
 };
 
@@ -218,7 +234,7 @@ struct BseApply : DeviceOperator {
   bool split_precision() const override { return op->precision == BSE_PRECISION_MIXED && op->mixed; }
   void apply_fp64(const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy,
                   cudaStream_t s) override {
-    ForceFp64 g(op);
+    ForceFp64 g(op, nullptr, fp64_products);
     op->matmul(coef, X, ldx, k, Y, ldy, s);
   }
 };
@@ -237,7 +253,7 @@ struct BseHamApply : DeviceOperator {
   bool split_precision() const override { return op->precision == BSE_PRECISION_MIXED && op->mixed; }
   void apply_fp64(const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy,
                   cudaStream_t s) override {
-    ForceFp64 g(op);
+    ForceFp64 g(op, nullptr, fp64_products);
     op->ham_matmul(a, b, X, ldx, k, Y, ldy, s);
   }
 };

@@ -685,4 +685,30 @@ int bse_small_sym_eig(int64_t njobs, const int64_t *m, const int64_t *nw, const 
   });
 }
 
+int bse_small_gen_eig(int64_t m, int64_t nw, const double *T, const double *B, double *evals, double *evecs,
+                      int64_t *selected) {
+  return guarded([&] {
+    VGB_REQUIRE(T && B && evals && evecs, "bse_small_gen_eig: null argument");
+    VGB_REQUIRE(m >= 1 && m <= vgb::kGenEigMaxM && nw >= 1 && nw <= m, "bse_small_gen_eig: sizes out of range");
+    cudaStream_t s = nullptr;
+    vgb::DeviceBuffer<double> dT(m * m), dB(m * m), dl(nw), dU(m * nw), dw(vgb::gen_eig_work_doubles(m, nw));
+    vgb::DeviceBuffer<int> dinfo(2);
+    VGB_CUDA(cudaMemcpyAsync(dT.get(), T, m * m * sizeof(double), cudaMemcpyHostToDevice, s));
+    VGB_CUDA(cudaMemcpyAsync(dB.get(), B, m * m * sizeof(double), cudaMemcpyHostToDevice, s));
+    vgb::GenEigJob j;
+    j.T = dT.get(); j.B = dB.get(); j.ldt = m; j.m = m; j.nw = nw;
+    j.U = dU.get(); j.ldu = m; j.lam = dl.get(); j.work = dw.get(); j.info = dinfo.get();
+    vgb::gen_eig_device(&j, 1, s);
+    int info[2] = {0, 0};
+    VGB_CUDA(cudaMemcpyAsync(evals, dl.get(), nw * sizeof(double), cudaMemcpyDeviceToHost, s));
+    VGB_CUDA(cudaMemcpyAsync(evecs, dU.get(), m * nw * sizeof(double), cudaMemcpyDeviceToHost, s));
+    VGB_CUDA(cudaMemcpyAsync(info, dinfo.get(), 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    VGB_CUDA(cudaStreamSynchronize(s));
+    if (info[0] == 4)
+      vgb::fail(BSE_ERR_NUMERICAL, "Eigenvalue:" + std::to_string(info[1]) + " is complex but has no partner.");
+    if (info[0] != 0) vgb::fail(BSE_ERR_NUMERICAL, "Small generalized eigenvalue problem failed.");
+    if (selected) *selected = info[1];
+  });
+}
+
 }  // extern "C"

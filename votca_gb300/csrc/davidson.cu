@@ -19,7 +19,6 @@
 #include <numeric>
 #include <cstdlib>
 
-#include "host_eig.hpp"
 #include "small_eig.cuh"
 
 namespace vgb {
@@ -364,62 +363,6 @@ void gramschmidt(Ctx &x, double *Q, int64_t nstart, int64_t ncols, DeviceBuffer<
   if (hflag[0]) fail(BSE_ERR_NUMERICAL, "Linear dependencies in Gram-Schmidt.");
 }
 
-// Householder QR, thin Q (m x r) of the m x r column-major matrix A (DavidsonSolver::qr)
-std::vector<double> thin_q(int64_t m, int64_t r, const std::vector<double> &A) {
-  std::vector<double> R(A), Q(m * r, 0.0);
-  std::vector<std::vector<double>> vs;
-  for (int64_t k = 0; k < r && k < m; ++k) {
-    std::vector<double> v(m, 0.0);
-    double nrm = 0.0;
-    for (int64_t i = k; i < m; ++i) nrm += R[i + m * k] * R[i + m * k];
-    nrm = std::sqrt(nrm);
-    if (nrm == 0.0) { vs.push_back(v); continue; }
-    const double alpha = R[k + m * k] >= 0 ? -nrm : nrm;
-    for (int64_t i = k; i < m; ++i) v[i] = R[i + m * k];
-    v[k] -= alpha;
-    double vn = 0.0;
-    for (int64_t i = k; i < m; ++i) vn += v[i] * v[i];
-    vn = std::sqrt(vn);
-    if (vn > 0)
-      for (int64_t i = k; i < m; ++i) v[i] /= vn;
-    for (int64_t c = k; c < r; ++c) {
-      double s = 0.0;
-      for (int64_t i = k; i < m; ++i) s += v[i] * R[i + m * c];
-      for (int64_t i = k; i < m; ++i) R[i + m * c] -= 2.0 * s * v[i];
-    }
-    vs.push_back(v);
-  }
-  for (int64_t c = 0; c < r; ++c) Q[c + m * c] = 1.0;
-  for (int64_t k = (int64_t)vs.size() - 1; k >= 0; --k) {
-    const auto &v = vs[k];
-    for (int64_t c = 0; c < r; ++c) {
-      double s = 0.0;
-      for (int64_t i = k; i < m; ++i) s += v[i] * Q[i + m * c];
-      for (int64_t i = k; i < m; ++i) Q[i + m * c] -= 2.0 * s * v[i];
-    }
-  }
-  return Q;
-}
-
-// Cholesky factor L (lower, column-major) of the symmetric m x m matrix S; false if S is not
-// positive definite.
-bool cholesky_lower(int64_t m, const std::vector<double> &S, std::vector<double> &L) {
-  L.assign(m * m, 0.0);
-  for (int64_t j = 0; j < m; ++j) {
-    double d = S[j + m * j];
-    for (int64_t k = 0; k < j; ++k) d -= L[j + m * k] * L[j + m * k];
-    if (!(d > 0.0)) return false;
-    const double ljj = std::sqrt(d);
-    L[j + m * j] = ljj;
-    for (int64_t i = j + 1; i < m; ++i) {
-      double t = S[i + m * j];
-      for (int64_t k = 0; k < j; ++k) t -= L[i + m * k] * L[j + m * k];
-      L[i + m * j] = t / ljj;
-    }
-  }
-  return true;
-}
-
 // Products of the Davidson operator, timed with events on the solve's stream.
 struct TimedApply {
   DeviceOperator &A;
@@ -474,23 +417,14 @@ bool fp64_polish(Ctx &x, TimedApply &apply, const double *Dd, const double *q0, 
   cudaStream_t s = x.s;
   DeviceBuffer<double> V(n * cap), AV(n * cap), q(n * np), res(n * np), Ud, lamd, work, cbuf, tmp;
   DeviceBuffer<int64_t> colsd(std::max<int64_t>(np, 64));
-  DeviceBuffer<int> flag(1), einfo(1);
-  DeviceBuffer<double> Td, eigw;              // SYMM: V^T A V on the device (ld cap)
-  std::vector<double> T, Jm;                  // HAM: V^T S V and V^T J V on the host
-  if (ham) {
-    T.assign(cap * cap, 0.0);
-    Jm.assign(cap * cap, 0.0);
-  } else {
-    Td.resize(cap * cap);
-  }
-  // C (r x c) = V[:, a0:a0+r]^T (J) W[:, 0:c]
-  auto proj = [&](const double *Va, int64_t r, const double *W, int64_t c, double *C, bool withJ) {
-    if (!withJ) {
-      x.gemm_tn(Va, n, r, W, n, c, C, r, 1.0, 0.0);
-    } else {
-      x.gemm_tn(Va, n, r, W, n, c, C, r, 1.0, 0.0, half);
-      x.gemm_tn(Va + half, n, r, W + half, n, c, C, r, -1.0, 1.0, half);
-    }
+  DeviceBuffer<int> flag(1), einfo(2);
+  // projected matrices on the device (ld cap): SYMM V^T A V; HAM V^T S V (= V^T J A V) and V^T J V
+  DeviceBuffer<double> Td(cap * cap), Jd, Wp, nud, Zd, eigw;
+  if (ham) Jd.resize(cap * cap);
+  // C (r x c, ldc) = V[:, a0:a0+r]^T J W[:, 0:c], J = diag(I, -I) on the two halves of the rows
+  auto projJ = [&](const double *Va, int64_t r, const double *W, int64_t c, double *C, int64_t ldc) {
+    x.gemm_tn(Va, n, r, W, n, c, C, ldc, 1.0, 0.0, half);
+    x.gemm_tn(Va + half, n, r, W + half, n, c, C, ldc, -1.0, 1.0, half);
   };
   auto to_host = [&](const double *src, int64_t cnt) {
     std::vector<double> h(cnt);
@@ -507,7 +441,7 @@ bool fp64_polish(Ctx &x, TimedApply &apply, const double *Dd, const double *q0, 
     old = 0;
   };
   start_basis(q0);
-  std::vector<double> lam(np), U;
+  std::vector<double> lam(np);
   for (int64_t pit = 0; pit < max_iter; ++pit) {
     out.polish_iterations = pit + 1;
     // ---- projected matrices for the columns [old, m) ----
@@ -515,86 +449,53 @@ bool fp64_polish(Ctx &x, TimedApply &apply, const double *Dd, const double *q0, 
       const int64_t nv = m - old;
       if (old > 0) x.gemm_tn(V.get() + old * n, n, nv, AV.get(), n, old, Td.get() + old, cap, 1.0, 0.0);
       x.gemm_tn(V.get() + old * n, n, nv, AV.get() + old * n, n, nv, Td.get() + old + cap * old, cap, 1.0, 0.0);
-    } else {
+    } else {  // S: lower triangle, coupling from the FP64 side; J: the new columns, mirrored
       const int64_t nv = m - old;
-      cbuf.resize(std::max<int64_t>(m * nv, 1));
-      if (old > 0) {  // coupling from the FP64 side: V_new^T (A V_old)
-        proj(V.get() + old * n, nv, AV.get(), old, cbuf.get(), ham);
-        auto b = to_host(cbuf.get(), nv * old);
-        for (int64_t c = 0; c < old; ++c)
-          for (int64_t r = 0; r < nv; ++r) T[(old + r) + cap * c] = T[c + cap * (old + r)] = b[r + nv * c];
-      }
-      proj(V.get() + old * n, nv, AV.get() + old * n, nv, cbuf.get(), ham);
-      auto b = to_host(cbuf.get(), nv * nv);
-      for (int64_t c = 0; c < nv; ++c)
-        for (int64_t r = 0; r < nv; ++r)
-          T[(old + r) + cap * (old + c)] = 0.5 * (b[r + nv * c] + b[c + nv * r]);
-      if (ham) {  // V^T J V_new (no operator)
-        proj(V.get(), m, V.get() + old * n, nv, cbuf.get(), true);
-        auto g = to_host(cbuf.get(), m * nv);
-        for (int64_t c = 0; c < nv; ++c)
-          for (int64_t r = 0; r < m; ++r) Jm[r + cap * (old + c)] = Jm[(old + c) + cap * r] = g[r + m * c];
+      if (old > 0) projJ(V.get() + old * n, nv, AV.get(), old, Td.get() + old, cap);
+      projJ(V.get() + old * n, nv, AV.get() + old * n, nv, Td.get() + old + cap * old, cap);
+      projJ(V.get(), m, V.get() + old * n, nv, Jd.get() + cap * old, cap);
+      if (old > 0) {
+        mirror_block_kernel<<<blocks_for(old * nv), 256, 0, s>>>(Jd.get(), cap, old, nv);
+        VGB_LAUNCH_CHECK();
       }
     }
-    // ---- Ritz pairs of the projected problem ----
+    // ---- Ritz pairs of the projected problem, on the device ----
     Ud.resize(m * np);
     lamd.resize(np);
-    if (!ham) {  // on the device (small_eig.cu)
+    if (!ham) {
       eigw.resize(sym_eig_work_doubles(m, np));
       SymEigJob job;
       job.T = Td.get(); job.ldt = cap; job.m = m; job.nw = np;
       job.U = Ud.get(); job.ldu = m; job.lam = lamd.get(); job.work = eigw.get(); job.info = einfo.get();
       sym_eig_device(&job, 1, s);
-    } else {  // the Cholesky-reduced pencil on the host
-      std::vector<double> Tm(m * m);
-      for (int64_t c = 0; c < m; ++c)
-        for (int64_t r = 0; r < m; ++r) Tm[r + m * c] = T[r + cap * c];
-      U.assign(m * np, 0.0);
-      std::vector<double> L;
-      if (!cholesky_lower(m, Tm, L)) {
+    } else {
+      // S = L L^T, eigenpairs of -L^-1 J L^-T: the np largest positive mu = 1 / omega
+      Wp.resize(3 * m * m);
+      nud.resize(np);
+      Zd.resize(m * np);
+      VGB_CUDA(cudaMemsetAsync(einfo.get(), 0, 2 * sizeof(int), s));
+      pencil_reduce_device(Td.get(), Jd.get(), cap, m, Wp.get(), einfo.get(), s);
+      int st = 0;
+      VGB_CUDA(cudaMemcpyAsync(&st, einfo.get(), sizeof(int), cudaMemcpyDeviceToHost, s));
+      VGB_CUDA(cudaStreamSynchronize(s));
+      if (st != 0) {
         if (pit == 0) return false;
         fail(BSE_ERR_NUMERICAL, "FP64 polish: projected S lost positive definiteness");
       }
-      // M = L^-1 Jp L^-T
-      std::vector<double> Jp(m * m), Mm(m * m);
-      for (int64_t c = 0; c < m; ++c)
-        for (int64_t r = 0; r < m; ++r) Jp[r + m * c] = Jm[r + cap * c];
-      for (int64_t c = 0; c < m; ++c) {  // forward substitution: L Y = Jp
-        for (int64_t r = 0; r < m; ++r) {
-          double t = Jp[r + m * c];
-          for (int64_t k = 0; k < r; ++k) t -= L[r + m * k] * Jp[k + m * c];
-          Jp[r + m * c] = t / L[r + m * r];
-        }
-      }
-      for (int64_t r = 0; r < m; ++r) {  // Mm = Y L^-T: rows of Y solved against L
-        for (int64_t c = 0; c < m; ++c) {
-          double t = Jp[r + m * c];
-          for (int64_t k = 0; k < c; ++k) t -= Mm[r + m * k] * L[c + m * k];
-          Mm[r + m * c] = t / L[c + m * c];
-        }
-      }
-      for (int64_t c = 0; c < m; ++c)
-        for (int64_t r = 0; r < c; ++r) Mm[r + m * c] = Mm[c + m * r] = 0.5 * (Mm[r + m * c] + Mm[c + m * r]);
-      std::vector<double> mu, Z;
-      if (!sym_eig(m, Mm.data(), mu, Z)) fail(BSE_ERR_NUMERICAL, "Small hermitian eigenvalue problem failed.");
-      // largest positive mu = 1/omega for the lowest positive omega
-      int64_t npos = 0;
-      for (int64_t i = 0; i < m; ++i) npos += mu[i] > 0.0;
-      if (npos < np) {
+      eigw.resize(sym_eig_work_doubles(m, np));
+      SymEigJob job;
+      job.T = Wp.get() + 2 * m * m; job.ldt = m; job.m = m; job.nw = np;
+      job.U = Zd.get(); job.ldu = m; job.lam = nud.get(); job.work = eigw.get(); job.info = einfo.get() + 1;
+      sym_eig_device(&job, 1, s);
+      pencil_finish_device(Wp.get(), m, nud.get(), Zd.get(), np, Ud.get(), lamd.get(), einfo.get(), s);
+      int st2[2] = {0, 0};
+      VGB_CUDA(cudaMemcpyAsync(st2, einfo.get(), 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+      VGB_CUDA(cudaStreamSynchronize(s));
+      if (st2[1] != 0) fail(BSE_ERR_NUMERICAL, "Small hermitian eigenvalue problem failed.");
+      if (st2[0] != 0) {
         if (pit == 0) return false;
         fail(BSE_ERR_NUMERICAL, "FP64 polish: fewer positive roots than requested");
       }
-      for (int64_t j = 0; j < np; ++j) {
-        const int64_t col = m - 1 - j;
-        lam[j] = 1.0 / mu[col];
-        for (int64_t r = m - 1; r >= 0; --r) {  // u = L^-T z
-          double t = Z[r + m * col];
-          for (int64_t k = r + 1; k < m; ++k) t -= L[k + m * r] * U[k + m * j];
-          U[r + m * j] = t / L[r + m * r];
-        }
-      }
-      VGB_CUDA(cudaMemcpyAsync(Ud.get(), U.data(), m * np * sizeof(double), cudaMemcpyHostToDevice, s));
-      VGB_CUDA(cudaMemcpyAsync(lamd.get(), lam.data(), np * sizeof(double), cudaMemcpyHostToDevice, s));
     }
     // ---- Ritz vectors and residuals: q = V U, res = A V U - q lambda (normalised) ----
     x.gemm_nn(V.get(), n, m, Ud.get(), m, np, q.get(), n, 1.0, 0.0);
@@ -609,10 +510,8 @@ bool fp64_polish(Ctx &x, TimedApply &apply, const double *Dd, const double *q0, 
     }
     x.coldots(res.get(), n, nullptr, 0, np, work.get() + np, true);
     int einfo_h = 0;
-    if (!ham) {
-      VGB_CUDA(cudaMemcpyAsync(lam.data(), lamd.get(), np * sizeof(double), cudaMemcpyDeviceToHost, s));
-      VGB_CUDA(cudaMemcpyAsync(&einfo_h, einfo.get(), sizeof(int), cudaMemcpyDeviceToHost, s));
-    }
+    VGB_CUDA(cudaMemcpyAsync(lam.data(), lamd.get(), np * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (!ham) VGB_CUDA(cudaMemcpyAsync(&einfo_h, einfo.get(), sizeof(int), cudaMemcpyDeviceToHost, s));
     std::vector<double> resn = to_host(work.get() + np, np);
     if (einfo_h != 0) fail(BSE_ERR_NUMERICAL, "Small hermitian eigenvalue problem failed.");
     double maxres = 0.0;
@@ -648,10 +547,6 @@ bool fp64_polish(Ctx &x, TimedApply &apply, const double *Dd, const double *q0, 
       DeviceBuffer<double> qk(n * np);
       x.copy_cols(q.get(), n, qk.get(), n, np);
       start_basis(qk.get());
-      if (ham) {
-        std::fill(T.begin(), T.end(), 0.0);
-        std::fill(Jm.begin(), Jm.end(), 0.0);
-      }
       continue;
     }
     colsd.resize(std::max<int64_t>(nupdate, 64));
@@ -725,6 +620,7 @@ void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_option
   }
   size_update = std::min(size_update, n);
   bool polish = opt.fp64_polish != 0 && A.split_precision();
+  A.fp64_products = opt.fp64_polish == 2 ? 1 : 0;
 
   int64_t restart_size, ncols;
   if (host_guess) {
@@ -745,11 +641,14 @@ void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_option
   x.s = s;
   x.n = n;
   DeviceBuffer<double> V(n * capc), AV(n * capc), AAV, D(n), q, res, Ud, tmp, lamd, work, cbuf;
-  DeviceBuffer<double> Td, eigw;  // SYMM: the projected matrix stays on the device (ld capc)
+  // the projected matrices stay on the device (ld capc): T = V^T A V and, for HAM, B = V^T A A V
+  DeviceBuffer<double> Td(capc * capc), Bd, eigw;
   DeviceBuffer<int64_t> colsd;
-  DeviceBuffer<int> flag(1), einfo(1);
-  if (ham) AAV.resize(n * capc);
-  else Td.resize(capc * capc);
+  DeviceBuffer<int> flag(1), einfo(2);
+  if (ham) {
+    AAV.resize(n * capc);
+    Bd.resize(capc * capc);
+  }
   VGB_CUDA(cudaMemsetAsync(V.get(), 0, n * capc * sizeof(double), s));
 
   TimedApply apply(A, s, n, out);
@@ -779,8 +678,6 @@ void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_option
     VGB_LAUNCH_CHECK();
   }
 
-  std::vector<double> T(capc * capc, 0.0), Bm;  // host projected matrices, ld capc
-  if (ham) Bm.assign(capc * capc, 0.0);
   const int64_t ldT = capc;
   int64_t nav = 0;  // columns of AV
   std::vector<double> lam, U, resn;
@@ -802,41 +699,12 @@ void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_option
           VGB_LAUNCH_CHECK();
         }
       } else {
-        cbuf.resize(ncols * std::max<int64_t>(ncols, 1));
-        // T[:, old:ncols] = V^T AV_new
-        x.gemm_tn(V.get(), n, ncols, AV.get() + old * n, n, nvec, cbuf.get(), ncols, 1.0, 0.0);
-        std::vector<double> blk(ncols * nvec);
-        VGB_CUDA(cudaMemcpyAsync(blk.data(), cbuf.get(), blk.size() * sizeof(double),
-                                 cudaMemcpyDeviceToHost, s));
-        VGB_CUDA(cudaStreamSynchronize(s));
-        for (int64_t c = 0; c < nvec; ++c)
-          for (int64_t r = 0; r < ncols; ++r) T[r + ldT * (old + c)] = blk[r + ncols * c];
-        // T[old:, :old] = V_new^T AV_old;  AAV_new = A AV_new;  B likewise
-        if (old > 0) {
-          x.gemm_tn(V.get() + old * n, n, nvec, AV.get(), n, old, cbuf.get(), nvec, 1.0, 0.0);
-          std::vector<double> b2(nvec * old);
-          VGB_CUDA(cudaMemcpyAsync(b2.data(), cbuf.get(), b2.size() * sizeof(double),
-                                   cudaMemcpyDeviceToHost, s));
-          VGB_CUDA(cudaStreamSynchronize(s));
-          for (int64_t c = 0; c < old; ++c)
-            for (int64_t r = 0; r < nvec; ++r) T[(old + r) + ldT * c] = b2[r + nvec * c];
-        }
+        // T[:, old:ncols] = V^T AV_new, T[old:, :old] = V_new^T AV_old (updateProjection, HAM)
+        x.gemm_tn(V.get(), n, ncols, AV.get() + old * n, n, nvec, Td.get() + ldT * old, ldT, 1.0, 0.0);
+        if (old > 0) x.gemm_tn(V.get() + old * n, n, nvec, AV.get(), n, old, Td.get() + old, ldT, 1.0, 0.0);
         apply(AV.get() + old * n, nvec, AAV.get() + old * n);
-        x.gemm_tn(V.get(), n, ncols, AAV.get() + old * n, n, nvec, cbuf.get(), ncols, 1.0, 0.0);
-        VGB_CUDA(cudaMemcpyAsync(blk.data(), cbuf.get(), blk.size() * sizeof(double),
-                                 cudaMemcpyDeviceToHost, s));
-        VGB_CUDA(cudaStreamSynchronize(s));
-        for (int64_t c = 0; c < nvec; ++c)
-          for (int64_t r = 0; r < ncols; ++r) Bm[r + ldT * (old + c)] = blk[r + ncols * c];
-        if (old > 0) {
-          x.gemm_tn(V.get() + old * n, n, nvec, AAV.get(), n, old, cbuf.get(), nvec, 1.0, 0.0);
-          std::vector<double> b2(nvec * old);
-          VGB_CUDA(cudaMemcpyAsync(b2.data(), cbuf.get(), b2.size() * sizeof(double),
-                                   cudaMemcpyDeviceToHost, s));
-          VGB_CUDA(cudaStreamSynchronize(s));
-          for (int64_t c = 0; c < old; ++c)
-            for (int64_t r = 0; r < nvec; ++r) Bm[(old + r) + ldT * c] = b2[r + nvec * c];
-        }
+        x.gemm_tn(V.get(), n, ncols, AAV.get() + old * n, n, nvec, Bd.get() + ldT * old, ldT, 1.0, 0.0);
+        if (old > 0) x.gemm_tn(V.get() + old * n, n, nvec, AAV.get(), n, old, Bd.get() + old, ldT, 1.0, 0.0);
       }
       nav = ncols;
     }
@@ -855,74 +723,12 @@ void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_option
       job.U = Ud.get(); job.ldu = m; job.lam = lamd.get(); job.work = eigw.get(); job.info = einfo.get();
       sym_eig_device(&job, 1, s);
     } else {
-      std::vector<double> Tm(m * m);
-      for (int64_t c = 0; c < m; ++c)
-        for (int64_t r = 0; r < m; ++r) Tm[r + m * c] = T[r + ldT * c];
-      if (debug) {
-        fprintf(stderr, "[davidson-debug] iter %lld m %lld T diag:", (long long)it, (long long)m);
-        for (int64_t c = 0; c < std::min<int64_t>(m, 40); ++c) fprintf(stderr, " %.4f", Tm[c + m * c]);
-        fprintf(stderr, "\n");
-      }
-      std::vector<double> Bmm(m * m);
-      for (int64_t c = 0; c < m; ++c)
-        for (int64_t r = 0; r < m; ++r) Bmm[r + m * c] = Bm[r + ldT * c];
-      std::vector<double> wr, wi, vr;
-      if (!gen_eig(m, Tm.data(), Bmm.data(), wr, wi, vr))
-        fail(BSE_ERR_NUMERICAL, "Small generalized eigenvalue problem failed.");
-      // complex partners (davidsonsolver.cc:261-291)
-      std::vector<std::pair<int64_t, int64_t>> pairs;
-      for (int64_t i = 0; i < m; ++i) {
-        if (wi[i] != 0.0) {
-          bool found = false;
-          for (auto &p : pairs) {
-            if (p.second > -1) continue;
-            if (std::fabs(wr[p.first] - wr[i]) < 1e-9 && std::fabs(wi[p.first] + wi[i]) < 1e-9) {
-              p.second = i;
-              found = true;
-            }
-          }
-          if (!found) pairs.emplace_back(i, -1);
-        }
-      }
-      for (auto &p : pairs)
-        if (p.second < 0)
-          fail(BSE_ERR_NUMERICAL, "Eigenvalue:" + std::to_string(p.first) + " is complex but has no partner.");
-      std::vector<double> evals;
-      std::vector<double> evecs;
-      for (int64_t i = 0; i < m; ++i) {
-        bool second = false;
-        for (auto &p : pairs) if (p.second == i) second = true;
-        if (second) continue;
-        evals.push_back(wr[i]);
-        // real part of eigenvector i (LAPACK packing: pair (i, i+1) shares columns)
-        std::vector<double> col(m);
-        for (int64_t r = 0; r < m; ++r) col[r] = vr[r + m * i];
-        double nn = 0.0;
-        for (double v : col) nn += v * v;
-        nn = std::sqrt(nn);
-        if (nn > 0) for (double &v : col) v /= nn;
-        evecs.insert(evecs.end(), col.begin(), col.end());
-      }
-      std::vector<int64_t> idx(evals.size());
-      std::iota(idx.begin(), idx.end(), 0);
-      std::stable_sort(idx.begin(), idx.end(), [&](int64_t a, int64_t b) { return evals[a] < evals[b]; });
-      std::reverse(idx.begin(), idx.end());
-      U.assign(m * needed, 0.0);
-      for (int64_t c = 0; c < needed; ++c)
-        std::copy(evecs.begin() + m * idx[c], evecs.begin() + m * (idx[c] + 1), U.begin() + m * c);
-      // lambda = diag(U^T T U)
-      lam.assign(needed, 0.0);
-      for (int64_t c = 0; c < needed; ++c) {
-        double sacc = 0.0;
-        for (int64_t a = 0; a < m; ++a) {
-          double tu = 0.0;
-          for (int64_t b = 0; b < m; ++b) tu += Tm[a + m * b] * U[b + m * c];
-          sacc += U[a + m * c] * tu;
-        }
-        lam[c] = sacc;
-      }
-      VGB_CUDA(cudaMemcpyAsync(Ud.get(), U.data(), m * needed * sizeof(double), cudaMemcpyHostToDevice, s));
-      VGB_CUDA(cudaMemcpyAsync(lamd.get(), lam.data(), needed * sizeof(double), cudaMemcpyHostToDevice, s));
+      // harmonic-Ritz pencil (T, B) on the device (gen_eig.cu)
+      eigw.resize(gen_eig_work_doubles(m, needed));
+      GenEigJob job;
+      job.T = Td.get(); job.B = Bd.get(); job.ldt = ldT; job.m = m; job.nw = needed;
+      job.U = Ud.get(); job.ldu = m; job.lam = lamd.get(); job.work = eigw.get(); job.info = einfo.get();
+      gen_eig_device(&job, 1, s);
     }
     mark(1);
     // q = V U, res = AV U - q Lambda
@@ -940,14 +746,16 @@ void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_option
     x.coldots(res.get(), n, nullptr, 0, nn_check, work.get(), true);
     resn.assign(nn_check, 0.0);
     VGB_CUDA(cudaMemcpyAsync(resn.data(), work.get(), nn_check * sizeof(double), cudaMemcpyDeviceToHost, s));
-    int einfo_h = 0;
-    if (!ham) {  // the Ritz values come back with the residual norms (one synchronisation)
-      lam.assign(needed, 0.0);
-      VGB_CUDA(cudaMemcpyAsync(lam.data(), lamd.get(), needed * sizeof(double), cudaMemcpyDeviceToHost, s));
-      VGB_CUDA(cudaMemcpyAsync(&einfo_h, einfo.get(), sizeof(int), cudaMemcpyDeviceToHost, s));
-    }
+    // the Ritz values come back with the residual norms (one synchronisation)
+    int einfo_h[2] = {0, 0};
+    lam.assign(needed, 0.0);
+    VGB_CUDA(cudaMemcpyAsync(lam.data(), lamd.get(), needed * sizeof(double), cudaMemcpyDeviceToHost, s));
+    VGB_CUDA(cudaMemcpyAsync(einfo_h, einfo.get(), (ham ? 2 : 1) * sizeof(int), cudaMemcpyDeviceToHost, s));
     VGB_CUDA(cudaStreamSynchronize(s));
-    if (einfo_h != 0) fail(BSE_ERR_NUMERICAL, "Small hermitian eigenvalue problem failed.");
+    if (!ham && einfo_h[0] != 0) fail(BSE_ERR_NUMERICAL, "Small hermitian eigenvalue problem failed.");
+    if (ham && einfo_h[0] == 4)
+      fail(BSE_ERR_NUMERICAL, "Eigenvalue:" + std::to_string(einfo_h[1]) + " is complex but has no partner.");
+    if (ham && einfo_h[0] != 0) fail(BSE_ERR_NUMERICAL, "Small generalized eigenvalue problem failed.");
     for (int64_t j = 0; j < size_update; ++j) conv[j] = (j < nn_check) ? (resn[j] < tol) : 0;
     bool converged = true;
     double maxres = 0.0;
@@ -1085,10 +893,9 @@ void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_option
         x.gemm_nn(AV.get(), n, nav, Ud.get(), m, rs, avn.get(), n, 1.0, 0.0);
         x.copy_cols(avn.get(), n, AV.get(), n, rs);
       } else {
-        std::vector<double> Ur(U.begin(), U.begin() + m * rs);
-        std::vector<double> O = thin_q(m, rs, Ur);
+        // DavidsonSolver::qr of the kept harmonic Ritz coefficients, on the device
         DeviceBuffer<double> Od(m * rs), vn(n * rs);
-        VGB_CUDA(cudaMemcpyAsync(Od.get(), O.data(), m * rs * sizeof(double), cudaMemcpyHostToDevice, s));
+        orthonormalise_device(Ud.get(), m, m, rs, Od.get(), m, s);
         x.gemm_nn(V.get(), n, nav, Od.get(), m, rs, vn.get(), n, 1.0, 0.0);
         x.gemm_nn(AV.get(), n, nav, Od.get(), m, rs, avn.get(), n, 1.0, 0.0);
         x.copy_cols(vn.get(), n, V.get(), n, rs);
@@ -1100,24 +907,8 @@ void davidson_solve(DeviceOperator &A, int64_t neigen, const bse_davidson_option
       ncols = rs + nv;
       nav = rs;
       // T = V[:, :rs]^T AV (and B = V^T AAV for HAM)
-      if (!ham) {
-        x.gemm_tn(V.get(), n, rs, AV.get(), n, rs, Td.get(), ldT, 1.0, 0.0);
-      } else {
-        cbuf.resize(rs * rs);
-        std::vector<double> blk(rs * rs);
-        x.gemm_tn(V.get(), n, rs, AV.get(), n, rs, cbuf.get(), rs, 1.0, 0.0);
-        VGB_CUDA(cudaMemcpyAsync(blk.data(), cbuf.get(), blk.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
-        VGB_CUDA(cudaStreamSynchronize(s));
-        std::fill(T.begin(), T.end(), 0.0);
-        for (int64_t c = 0; c < rs; ++c)
-          for (int64_t r = 0; r < rs; ++r) T[r + ldT * c] = blk[r + rs * c];
-        x.gemm_tn(V.get(), n, rs, AAV.get(), n, rs, cbuf.get(), rs, 1.0, 0.0);
-        VGB_CUDA(cudaMemcpyAsync(blk.data(), cbuf.get(), blk.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
-        VGB_CUDA(cudaStreamSynchronize(s));
-        std::fill(Bm.begin(), Bm.end(), 0.0);
-        for (int64_t c = 0; c < rs; ++c)
-          for (int64_t r = 0; r < rs; ++r) Bm[r + ldT * c] = blk[r + rs * c];
-      }
+      x.gemm_tn(V.get(), n, rs, AV.get(), n, rs, Td.get(), ldT, 1.0, 0.0);
+      if (ham) x.gemm_tn(V.get(), n, rs, AAV.get(), n, rs, Bd.get(), ldT, 1.0, 0.0);
     }
   }
   VGB_CUDA(cudaStreamSynchronize(s));

@@ -47,4 +47,38 @@ constexpr int64_t kSymEigMaxM = 3000;
 // Solve every job (one CTA each), stream-ordered on s.
 void sym_eig_device(const SymEigJob *jobs, int64_t njobs, cudaStream_t s);
 
+// The harmonic-Ritz problem of the HAM Davidson (gen_eig.cu): T u = theta B u for general m x m
+// T, B; the reference's selection (complex partners dropped, the nw largest real parts) and
+// its outputs: U = the real parts of those eigenvectors, normalised, lam = diag(U^T T U).
+struct GenEigJob {
+  const double *T = nullptr, *B = nullptr;  // column-major, leading dimension ldt
+  int64_t ldt = 0;
+  int64_t m = 0;
+  int64_t nw = 0;        // 1 <= nw <= m
+  double *U = nullptr;   // m x nw (leading dimension ldu >= m), output
+  int64_t ldu = 0;
+  double *lam = nullptr; // nw, output (zero past the number of candidates)
+  double *work = nullptr;  // gen_eig_work_doubles(m, nw) doubles
+  int *info = nullptr;   // two ints: [0] 0 ok, 1 invalid sizes, 2 B singular or B^-1 T not finite,
+                         // 3 QR iteration without convergence, 4 a complex eigenvalue without
+                         // partner (its index in [1]); on success [1] = pairs selected
+};
+constexpr int64_t kGenEigMaxM = 1024;
+int64_t gen_eig_work_doubles(int64_t m, int64_t nw);
+void gen_eig_device(const GenEigJob *jobs, int64_t njobs, cudaStream_t s);
+// O (m x r, ldo) = an orthonormal basis of the columns of U (modified Gram-Schmidt twice, one CTA);
+// the restart of the HAM Davidson (DavidsonSolver::qr, davidsonsolver.cc:480-488).
+void orthonormalise_device(const double *U, int64_t ldu, int64_t m, int64_t r, double *O, int64_t ldo,
+                           cudaStream_t s);
+// The FP64 polish of a HAM solve reduces its projected pencil (S, J) (S symmetric positive
+// definite, lower triangle read; J symmetric, full; ld) on the device: W (3 m^2 doubles) receives
+// L = chol(S), L^-1 J and Mneg = -L^-1 J L^-T (its leading m^2 x 3 block, each ld m); *status = 1
+// when S is not positive definite.  After sym_eig_device on Mneg (np lowest: the largest mu),
+// pencil_finish_device returns lam = 1 / mu and U = L^-T z (m x np, ld m); *status = 2 when fewer
+// than np of the mu are positive.
+void pencil_reduce_device(const double *S, const double *J, int64_t ld, int64_t m, double *W, int *status,
+                          cudaStream_t s);
+void pencil_finish_device(const double *W, int64_t m, const double *nu, const double *Z, int64_t np, double *U,
+                          double *lam, int *status, cudaStream_t s);
+
 }  // namespace vgb

@@ -49,6 +49,7 @@ struct SplitBuf {
   }
 };
 
+int g_slices = 5;  // Ozaki digits per operand (7 bits each; pairs up to the 5th digit level)
 int g_bk256 = 32;  // K box of the BN = 256 tiles (4-stage ring); 64 gives a 2-stage ring
 int bk_for(int bn) { return bn == 256 ? g_bk256 : 64; }
 
@@ -84,7 +85,36 @@ void read_tuning() {
     if (const char *e = getenv("VGB_TC_KACC")) g_kacc = atoi(e) != 0;
     if (const char *e = getenv("VGB_TC_S_BUDGET_GB")) g_s_budget = std::max(1LL, atoll(e)) << 30;
     if (const char *e = getenv("VGB_TC_DENSE_CHAIN")) g_dense_chain = std::max(64LL, atoll(e));
+    if (const char *e = getenv("VGB_TC_SLICES")) g_slices = std::max(2, std::min(5, atoi(e)));
   });
+}
+
+// Ozaki slice planes: nsl planes of rows x ld bf16 (plane t at t * rows * ld), zero-filled when
+// (re)allocated; a buffer keeps one ld, so its K padding stays zero.
+struct Planes {
+  DeviceBuffer<uint16_t> b;
+  int64_t rows = 0, ld = 0;
+  int nsl = 0;
+  void ensure(int64_t r, int64_t l, int n, cudaStream_t s) {
+    const int64_t need = r * l * n;
+    if (need > (int64_t)b.count || !b.get() || l != ld) {
+      b.resize(need);
+      VGB_CUDA(cudaMemsetAsync(b.get(), 0, need * sizeof(uint16_t), s));
+    }
+    rows = r;
+    ld = l;
+    nsl = n;
+  }
+  uint16_t *get() { return b.get(); }
+  int64_t plane() const { return rows * ld; }
+};
+
+// The largest multiple of 64 that divides K and is at most 1024: the run of one digit scale
+// and the longest exact FP32 chain of a slice pair.
+int64_t slice_chain(int64_t K) {
+  for (int64_t c = std::min<int64_t>(K, 1024) / 64 * 64; c >= 64; c -= 64)
+    if (K % c == 0) return c;
+  return 64;
 }
 
 }  // namespace
@@ -93,6 +123,9 @@ struct MixedEngine::Impl {
   int64_t vt = 0, ct = 0, naux = 0, dim = 0;
   int64_t Kc = 0, Kg = 0, Kn = 0, dimP = 0;
   SplitBuf Mcc2, G2, Bvc2, BvcT, McvT;
+  // Ozaki slice planes of the FP64-equivalent products (apply_sliced), built on first use
+  Planes pMcc, pG2, pBvc2, pBvcT, pMcvT, pX, pZ, pT;
+  DeviceBuffer<double> fZ, fT, gpart;
   SplitBuf Xs, S, U, Zs;
   DeviceBuffer<float> part;
   DeviceBuffer<int> err;
@@ -116,7 +149,7 @@ struct MixedEngine::Impl {
 MixedEngine::MixedEngine() : impl_(new Impl()) {}
 MixedEngine::~MixedEngine() { delete impl_; }
 
-void MixedEngine::stage(BseOperator &op, cudaStream_t s) {
+void MixedEngine::stage(BseOperator &op, cudaStream_t s, bool split_operands) {
   Impl &m = *impl_;
   m.vt = op.vt;
   m.ct = op.ct;
@@ -129,6 +162,10 @@ void MixedEngine::stage(BseOperator &op, cudaStream_t s) {
   const int64_t vt = m.vt, ct = m.ct, naux = m.naux, dim = m.dim;
   m.err.resize(1);
   VGB_CUDA(cudaMemsetAsync(m.err.get(), 0, sizeof(int), s));
+  if (!split_operands) {  // slice-product operators build their planes on first use
+    VGB_CUDA(cudaStreamSynchronize(s));
+    return;
+  }
   {  // Mcc2[(P, c1)][c] = Mcc[P*ct*ct + c*ct + c1]
     m.Mcc2.ensure(naux * ct, m.Kc, s);
     SplitMap sm;
@@ -349,6 +386,224 @@ void MixedEngine::apply(BseOperator &op, const Coef &c, const double *X, int64_t
   }
   if (!acc) {
     VGB_CUDA(cudaMemset2DAsync(Y, ldy * sizeof(double), 0, op.dim * sizeof(double), k, s));
+  }
+}
+
+namespace {
+
+// Pairs (a, b) of digit planes with a + b < nsl, by level: the products kept by the Ozaki
+// scheme (the dropped levels are below 2^(-7 nsl) of the row and column scales).
+void set_pairs(TcShape &sh, int nsl) {
+  sh.npairs = 0;
+  for (int l = 0; l < nsl; ++l)
+    for (int a = 0; a <= l; ++a) {
+      sh.pa[sh.npairs] = (uint8_t)a;
+      sh.pb[sh.npairs] = (uint8_t)(l - a);
+      ++sh.npairs;
+    }
+}
+
+// One slice-mode product: C (M x N) = sum over pairs of A planes (rows a_plane apart, K-major,
+// row stride K) times B planes, through the final FP64 epilogue fe.  When the tiles alone do
+// not fill the SMs, the K splits of a tile are shared by several CTAs whose FP64 partials are
+// added by a reduction launch.
+// chain: the run of one digit scale along K in both operands (a multiple of 64 dividing K).
+void sliced_gemm(const TcMat &A, int64_t a_plane, const TcMat &B, int64_t b_plane, int64_t M, int64_t N,
+                 int64_t K, int64_t chain, int nsl, int bn, const TcEpilogue &fe, DeviceBuffer<double> &gpart,
+                 int *err, cudaStream_t s) {
+  TcShape sh;
+  sh.M = M; sh.N = N; sh.K = K;
+  set_pairs(sh, nsl);
+  sh.a_plane = a_plane;
+  sh.b_plane = b_plane;
+  sh.chain = chain;
+  sh.kacc = true;
+  const int64_t tiles = ceil_div(M, 128) * ceil_div(N, bn);
+  const int64_t ksplit = sh.npairs * ceil_div(K / 64, sh.chain / 64);
+  int groups = 1;
+  for (int g = 2; g <= 64; ++g)
+    if (ksplit % g == 0 && tiles * g <= sm_count()) groups = g;
+  if (groups == 1) {
+    tc_gemm(A, B, sh, fe, bn, err, s);
+    return;
+  }
+  sh.kgroups = groups;
+  gpart.resize((size_t)groups * M * N);
+  TcEpilogue pe;  // FP64 partials, column-major per group
+  pe.kind = TcEpilogue::AXPBY_F64;
+  pe.rd = M; pe.ro2 = 1; pe.rlim = M;
+  pe.cd = N; pe.co2 = M; pe.clim = N;
+  pe.so = M * N;
+  pe.out_f64 = gpart.get();
+  pe.alpha = 1.0; pe.beta = 0.0;
+  tc_gemm(A, B, sh, pe, bn, err, s);
+  reduce_f64_groups(gpart.get(), M, N, groups, fe, s);
+}
+
+}  // namespace
+
+void MixedEngine::apply_sliced(BseOperator &op, const Coef &c, const double *X, int64_t ldx, int64_t k,
+                               double *Y, int64_t ldy, bool accumulate, cudaStream_t s) {
+  Impl &m = *impl_;
+  read_tuning();
+  const int nsl = g_slices;
+  const int64_t vt = m.vt, ct = m.ct, naux = m.naux, dim = m.dim;
+  const int64_t chc = slice_chain(m.Kc), chg = slice_chain(m.Kg), chn = slice_chain(m.Kn);
+  int *err = m.err.get();
+  bool acc = accumulate;
+  const bool hx = c.cx != 0, hd = c.cd != 0, hd2 = c.cd2 != 0;
+  if (!hx && !hd && !hd2) {
+    if (!acc) VGB_CUDA(cudaMemset2DAsync(Y, ldy * sizeof(double), 0, dim * sizeof(double), k, s));
+    return;
+  }
+  // operator planes, built once per operand from the FP64 staged blocks
+  op.timer.begin(STAGE_TC_SPLIT, s);
+  auto build = [&](Planes &P, const double *src, int64_t rows, int64_t cols, int64_t ld, const SplitMap &sm,
+                   int64_t chunk) {
+    if (P.nsl == nsl && P.rows == rows && P.ld == ld) return;
+    P.ensure(rows, ld, nsl, s);
+    slice_f64(src, rows, cols, sm, nsl, chunk, P.get(), ld, P.plane(), s);
+  };
+  if (hd) {
+    SplitMap a;  // Mcc planes [(P, c1)][c]
+    a.rdiv = ct; a.rs1 = ct * ct; a.rs2 = 1; a.cs = ct; a.rlim = ct;
+    build(m.pMcc, op.Mcc.get(), naux * ct, ct, m.Kc, a, chc);
+    SplitMap g;  // G planes [v1][(P, v)]
+    g.rdiv = vt; g.rs1 = 0; g.rs2 = naux * vt; g.cs = 1; g.rlim = vt;
+    build(m.pG2, op.Gvv.get(), vt, naux * vt, m.Kg, g, chg);
+  }
+  if (hx || hd2) {
+    SplitMap b;  // Bvc planes [(P, v)][c] (== [P][dimP] for Hx)
+    b.rdiv = vt; b.rs1 = dim; b.rs2 = ct; b.cs = 1; b.rlim = vt;
+    build(m.pBvc2, op.Bvc.get(), naux * vt, ct, m.Kc, b, chc);
+  }
+  if (hx) {
+    SplitMap t;  // BvcT planes [(v, c')][P]
+    t.rdiv = m.Kc; t.rs1 = ct; t.rs2 = 1; t.cs = dim; t.rlim = ct;
+    build(m.pBvcT, op.Bvc.get(), m.dimP, naux, m.Kn, t, chn);
+  }
+  if (hd2) {
+    SplitMap t;  // screened Mcv planes [c1][(P, v)]
+    t.rdiv = ct; t.rs1 = 0; t.rs2 = 1; t.cs = ct; t.rlim = ct;
+    build(m.pMcvT, op.Mcv.get(), ct, naux * vt, m.Kg, t, chg);
+  }
+  {  // X planes [(j, v)][c] (== [j][dimP] for Hx)
+    m.pX.ensure(k * vt, m.Kc, nsl, s);
+    SplitMap x;
+    x.rdiv = vt; x.rs1 = ldx; x.rs2 = ct; x.cs = 1; x.rlim = vt;
+    slice_f64(X, k * vt, ct, x, nsl, chc, m.pX.get(), m.Kc, m.pX.plane(), s);
+  }
+  op.timer.end(STAGE_TC_SPLIT, s);
+  const uint16_t *px = m.pX.get();
+  const int64_t xrows = nsl * k * vt;  // rows of the X planes as one matrix ([(j, v)] view)
+
+  if (hx) {
+    op.timer.begin(STAGE_TC_HX, s);
+    const TcMat &Ab = m.mat(m.pBvc2.get(), m.pBvc2.get(), nsl * naux, m.dimP, 128, 64);
+    m.fZ.resize(k * m.Kn);
+    for (int64_t j0 = 0; j0 < k; j0 += 64) {  // Z[j][P] = sum_I' Bvc[P][I'] X_j[I']
+      const int64_t kc = std::min<int64_t>(64, k - j0);
+      const int bn = kc > 32 ? 64 : 32;
+      TcMat Bx = make_tc_mat(px + j0 * m.dimP, px + j0 * m.dimP, nsl * k - j0, m.dimP, m.dimP, bn, 64);
+      TcEpilogue e;
+      e.kind = TcEpilogue::AXPBY_F64;
+      e.rd = naux; e.ro2 = 1; e.rlim = naux;
+      e.cd = kc; e.co2 = m.Kn; e.clim = kc;
+      e.out_f64 = m.fZ.get() + j0 * m.Kn; e.alpha = 1.0; e.beta = 0.0;
+      sliced_gemm(Ab, naux, Bx, k, naux, kc, m.dimP, chc, nsl, bn, e, m.gpart, err, s);
+    }
+    m.pZ.ensure(k, m.Kn, nsl, s);
+    SplitMap z;
+    z.rdiv = 1; z.rs1 = m.Kn; z.rs2 = 0; z.cs = 1; z.rlim = 1;
+    slice_f64(m.fZ.get(), k, naux, z, nsl, chn, m.pZ.get(), m.Kn, m.pZ.plane(), s);
+    const TcMat &At = m.mat(m.pBvcT.get(), m.pBvcT.get(), nsl * m.dimP, m.Kn, 128, 64);
+    for (int64_t j0 = 0; j0 < k; j0 += 64) {  // Y(I, j) (+)= cx sum_P BvcT[I'][P] Z[j][P]
+      const int64_t kc = std::min<int64_t>(64, k - j0);
+      const int bn = kc > 32 ? 64 : 32;
+      TcMat Bz = make_tc_mat(m.pZ.get() + j0 * m.Kn, m.pZ.get() + j0 * m.Kn, nsl * k - j0, m.Kn, m.Kn, bn, 64);
+      TcEpilogue e;
+      e.kind = TcEpilogue::AXPBY_F64;
+      e.rd = m.Kc; e.ro1 = ct; e.ro2 = 1; e.rlim = ct;
+      e.cd = kc; e.co2 = ldy; e.clim = kc;
+      e.out_f64 = Y + j0 * ldy; e.alpha = c.cx; e.beta = acc ? 1.0 : 0.0;
+      sliced_gemm(At, m.dimP, Bz, k, m.dimP, kc, m.Kn, chn, nsl, bn, e, m.gpart, err, s);
+    }
+    acc = true;
+    op.timer.end(STAGE_TC_HX, s);
+  }
+
+  for (int pass = 0; pass < 2; ++pass) {
+    const bool is_hd = pass == 0;
+    if (is_hd ? !hd : !hd2) continue;
+    const double alpha = is_hd ? -(double)c.cd : -(double)c.cd2;
+    const int64_t rows_per_vec = is_hd ? ct : vt;  // rows of the intermediate per vector
+    const int64_t per_vec = rows_per_vec * m.Kg * (8 + 2 * nsl);
+    const int64_t jmax = std::max<int64_t>(1, std::min<int64_t>(k, g_s_budget / per_vec));
+    const int64_t jc = ceil_div(k, ceil_div(k, jmax));
+    m.fT.resize(jc * rows_per_vec * m.Kg);
+    m.pT.ensure(jc * rows_per_vec, m.Kg, nsl, s);
+    const int64_t tplane = m.pT.plane() / m.Kg;  // rows per plane of the intermediate
+    for (int64_t j0 = 0; j0 < k; j0 += jc) {
+      const int64_t kc = std::min(jc, k - j0);
+      op.timer.begin(is_hd ? STAGE_TC_HD : STAGE_TC_HD2, s);
+      TcMat Ax = make_tc_mat(px + j0 * vt * m.Kc, px + j0 * vt * m.Kc, xrows - j0 * vt, m.Kc, m.Kc, 128, 64);
+      TcEpilogue e;  // stage 1 into the FP64 intermediate [(j, row)][(P, v)]
+      e.kind = TcEpilogue::AXPBY_F64;
+      e.rd = vt; e.ro2 = 1; e.rlim = vt;
+      e.ro1 = rows_per_vec * m.Kg;
+      e.cd = is_hd ? ct : vt; e.co1 = vt; e.co2 = m.Kg; e.clim = e.cd;
+      e.out_f64 = m.fT.get(); e.alpha = 1.0; e.beta = 0.0;
+      if (is_hd) {  // S[(j, c1)][(P, v)] = sum_c X_j(v, c) M(c1, c, P)
+        const TcMat &Bm = m.mat(m.pMcc.get(), m.pMcc.get(), nsl * naux * ct, m.Kc, 64, 64);
+        sliced_gemm(Ax, k * vt, Bm, naux * ct, kc * vt, naux * ct, m.Kc, chc, nsl, 64, e, m.gpart, err, s);
+      } else {      // U[(j, v1)][(P, v)] = sum_c X_j(v, c) M(v1, c, P)
+        const TcMat &Bm = m.mat(m.pBvc2.get(), m.pBvc2.get(), nsl * naux * vt, m.Kc, 64, 64);
+        sliced_gemm(Ax, k * vt, Bm, naux * vt, kc * vt, naux * vt, m.Kc, chc, nsl, 64, e, m.gpart, err, s);
+      }
+      SplitMap t;
+      t.rdiv = 1; t.rs1 = m.Kg; t.rs2 = 0; t.cs = 1; t.rlim = 1;
+      slice_f64(m.fT.get(), kc * rows_per_vec, naux * vt, t, nsl, chg, m.pT.get(), m.Kg, m.pT.plane(), s);
+      op.timer.end(is_hd ? STAGE_TC_HD : STAGE_TC_HD2, s);
+      op.timer.begin(is_hd ? STAGE_TC_HD_B : STAGE_TC_HD2_B, s);
+      if (is_hd) {  // Y_j(c1, v1) += alpha sum_{(P,v)} S[(j, c1)][(P,v)] G[v1][(P,v)]
+        TcMat As = make_tc_mat(m.pT.get(), m.pT.get(), nsl * tplane, m.Kg, m.Kg, 128, 64);
+        for (int64_t n0 = 0; n0 < vt; n0 += 64) {
+          const int64_t nn = std::min<int64_t>(64, vt - n0);
+          const int bn = nn > 32 ? 64 : 32;
+          TcMat Bg = make_tc_mat(m.pG2.get() + n0 * m.Kg, m.pG2.get() + n0 * m.Kg, nsl * vt - n0, m.Kg, m.Kg,
+                                 bn, 64);
+          TcEpilogue r;
+          r.kind = TcEpilogue::AXPBY_F64;
+          r.rd = ct; r.ro1 = ldy; r.ro2 = 1; r.rlim = ct;
+          r.cd = nn; r.co2 = ct; r.clim = nn;
+          r.out_f64 = Y + j0 * ldy + n0 * ct; r.alpha = alpha; r.beta = acc ? 1.0 : 0.0;
+          sliced_gemm(As, tplane, Bg, vt, kc * ct, nn, m.Kg, chg, nsl, bn, r, m.gpart, err, s);
+        }
+      } else {      // Y_j(c1, v1) += alpha sum_{(P,v)} McvT[c1][(P,v)] U[(j, v1)][(P,v)]
+        const TcMat &Am = m.mat(m.pMcvT.get(), m.pMcvT.get(), nsl * ct, m.Kg, 128, 64);
+        // column blocks of whole vectors (vt <= 64) or of 64 v1 of one vector
+        const int64_t nv = vt <= 64 ? std::max<int64_t>(1, 64 / vt) : 1;
+        for (int64_t j = 0; j < kc; j += nv) {
+          const int64_t vj = std::min(nv, kc - j);
+          for (int64_t v0 = 0; v0 < vt; v0 += 64) {
+            const int64_t nn = vt <= 64 ? vj * vt : std::min<int64_t>(64, vt - v0);
+            const int bn = nn > 32 ? 64 : 32;
+            const int64_t r0 = j * vt + v0;  // first intermediate row of the block
+            TcMat Bu = make_tc_mat(m.pT.get() + r0 * m.Kg, m.pT.get() + r0 * m.Kg, nsl * tplane - r0, m.Kg, m.Kg,
+                                   bn, 64);
+            TcEpilogue r;
+            r.kind = TcEpilogue::AXPBY_F64;
+            r.rd = ct; r.ro2 = 1; r.rlim = ct;
+            r.cd = vt <= 64 ? vt : nn; r.co1 = ldy; r.co2 = ct; r.clim = r.cd;
+            r.out_f64 = Y + (j0 + j) * ldy + v0 * ct; r.alpha = alpha; r.beta = acc ? 1.0 : 0.0;
+            sliced_gemm(Am, ct, Bu, tplane, ct, nn, m.Kg, chg, nsl, bn, r, m.gpart, err, s);
+            if (vt <= 64) break;
+          }
+        }
+      }
+      op.timer.end(is_hd ? STAGE_TC_HD_B : STAGE_TC_HD2_B, s);
+    }
+    acc = true;
   }
 }
 

@@ -9,11 +9,19 @@ class MixedEngine {
  public:
   MixedEngine();
   ~MixedEngine();
-  // Build the split (hi/lo) operand copies from the FP64 staged blocks.
-  void stage(BseOperator &op, cudaStream_t s);
+  // Build the split (hi/lo) operand copies from the FP64 staged blocks (split_operands false:
+  // only the sizes, for operators whose products all run as slice products).
+  void stage(BseOperator &op, cudaStream_t s, bool split_operands = true);
   // Y (+)= cx Hx X - cd Hd X - cd2 Hd2 X with tensor-core split products.
   void apply(BseOperator &op, const Coef &c, const double *X, int64_t ldx, int64_t k, double *Y,
              int64_t ldy, bool accumulate, cudaStream_t s);
+  // Y (+)= cx Hx X - cd Hd X - cd2 Hd2 X with Ozaki slice products on the tensor cores
+  // (slice_f64): every operand cut into 7-bit digit planes with power-of-two scales per run of
+  // at most 1024 K elements, each pair of digit planes accumulated exactly in FP32 over one run,
+  // the runs and pairs summed in FP64, the intermediates kept in FP64 and sliced again.  With
+  // five digits the result agrees with the FP64 product to about 1e-11 of its scale.
+  void apply_sliced(BseOperator &op, const Coef &c, const double *X, int64_t ldx, int64_t k, double *Y,
+                    int64_t ldy, bool accumulate, cudaStream_t s);
   // The same for many operators at once (GroupedItem.op->mixed engines), one grouped
   // launch per stage and tile shape; accumulate: Y already holds the Hqp term.
   static void apply_grouped(const Coef &c, const std::vector<GroupedItem> &items, bool accumulate,

@@ -31,11 +31,15 @@ struct Cfg {
 };
 
 struct KParams {
-  int64_t M, N, K;
-  int products;  // 3: hi.hi + hi.lo + lo.hi;  4: + lo.lo
+  int64_t M, N, K;  // slice mode: K of one slice
+  int products;  // 3: hi.hi + hi.lo + lo.hi;  4: + lo.lo;  1: slice mode (hi maps only)
   int64_t nbatch, a_brows, b_brows;
   int ksplit, kc_per;
-  int kacc;  // 1: one CTA runs all K splits of a tile and sums them in FP64 registers
+  int kacc;  // 1: one CTA runs K splits of a tile and sums them in FP64 registers
+  int spg;   // kacc: consecutive splits per work item (ksplit / spg groups per tile)
+  int npairs, cpp;        // slice mode: slice pairs, K splits per pair
+  uint64_t pa, pb;        // slice mode: A / B slice index of pair i in bits [4 i, 4 i + 4)
+  int64_t a_plane, b_plane;  // slice mode: operand rows between consecutive slice planes
   int64_t mt, nt, ntiles;
   TcEpilogue epi;
   int *err;
@@ -144,9 +148,12 @@ struct TileCoord {
 };
 __device__ __forceinline__ TileCoord decode(const KParams &p, int64_t t) {
   TileCoord c;
-  if (p.kacc) {  // the K splits of a tile are consecutive jobs of one CTA
-    c.s = t % p.ksplit;
-    t /= p.ksplit;
+  if (p.kacc) {  // the K splits of a (tile, group) item are consecutive jobs of one CTA
+    const int64_t u = t % p.spg;
+    t /= p.spg;
+    const int64_t groups = p.ksplit / p.spg;
+    c.s = (t % groups) * p.spg + u;
+    t /= groups;
     c.m = t % p.mt;
     t /= p.mt;
     c.n = t % p.nt;
@@ -183,9 +190,32 @@ __device__ __forceinline__ void epi_store(const TcEpilogue &e, int64_t off, floa
 // accumulation (kacc), the ksplit consecutive jobs of one output tile; items are strided over
 // the CTAs and a CTA runs the jobs of its item in order.
 __host__ __device__ __forceinline__ int64_t item_count(const KParams &p) {
-  return p.kacc ? p.ntiles / p.ksplit : p.ntiles;
+  return p.kacc ? p.ntiles / p.spg : p.ntiles;
 }
-__device__ __forceinline__ int64_t item_len(const KParams &p) { return p.kacc ? p.ksplit : 1; }
+__device__ __forceinline__ int64_t item_len(const KParams &p) { return p.kacc ? p.spg : 1; }
+
+// K blocks [kb, ke) of split s and, in slice mode, the row offsets of its A and B slice planes.
+struct KRange {
+  int kb, ke;
+  int ya, yb;
+};
+template <int BK>
+__device__ __forceinline__ KRange k_range(const KParams &p, int64_t s) {
+  KRange r;
+  const int kchunks = (int)(p.K / BK);
+  int sl = (int)s;
+  r.ya = 0;
+  r.yb = 0;
+  if (p.npairs) {
+    const int pr = sl / p.cpp;
+    sl -= pr * p.cpp;
+    r.ya = (int)((p.pa >> (4 * pr)) & 15) * (int)p.a_plane;
+    r.yb = (int)((p.pb >> (4 * pr)) & 15) * (int)p.b_plane;
+  }
+  r.kb = sl * p.kc_per;
+  r.ke = min(kchunks, r.kb + p.kc_per);
+  return r;
+}
 
 // Problem sources of the persistent kernel: one problem, or a group of up to
 // kGroupMax problems (same tile shape) whose item lists are concatenated.  Both
@@ -276,18 +306,23 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
         const CUtensorMap *mBhi = src.map(pi, 2), *mBlo = src.map(pi, 3);
         for (int64_t u = 0; u < len; ++u) {
           const TileCoord tc = decode(p, li * len + u);
-          const int kchunks = (int)(p.K / BK);
-          const int kb = (int)tc.s * p.kc_per, ke = min(kchunks, kb + p.kc_per);
+          const KRange kr = k_range<BK>(p, tc.s);
           const int ya = (int)(tc.b * p.a_brows + tc.m * BM);
           const int yb = (int)(tc.b * p.b_brows + tc.n * BN);
-          for (int kc = kb; kc < ke; ++kc) {
+          for (int kc = kr.kb; kc < kr.ke; ++kc) {
             if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, err, 1)) goto producer_done;
             uint8_t *st = smem + stage * C::STAGE_BYTES;
-            mbar_expect_tx(&full[stage], (uint32_t)C::STAGE_BYTES);
-            tma_load_2d(smem_u32(st), mAhi, &full[stage], kc * BK, ya);
-            tma_load_2d(smem_u32(st + C::A_BYTES), mAlo, &full[stage], kc * BK, ya);
-            tma_load_2d(smem_u32(st + 2 * C::A_BYTES), mBhi, &full[stage], kc * BK, yb);
-            tma_load_2d(smem_u32(st + 2 * C::A_BYTES + C::B_BYTES), mBlo, &full[stage], kc * BK, yb);
+            if (p.npairs) {  // slice mode: one A slice and one B slice per stage
+              mbar_expect_tx(&full[stage], (uint32_t)(C::A_BYTES + C::B_BYTES));
+              tma_load_2d(smem_u32(st), mAhi, &full[stage], kc * BK, ya + kr.ya);
+              tma_load_2d(smem_u32(st + 2 * C::A_BYTES), mBhi, &full[stage], kc * BK, yb + kr.yb);
+            } else {
+              mbar_expect_tx(&full[stage], (uint32_t)C::STAGE_BYTES);
+              tma_load_2d(smem_u32(st), mAhi, &full[stage], kc * BK, ya);
+              tma_load_2d(smem_u32(st + C::A_BYTES), mAlo, &full[stage], kc * BK, ya);
+              tma_load_2d(smem_u32(st + 2 * C::A_BYTES), mBhi, &full[stage], kc * BK, yb);
+              tma_load_2d(smem_u32(st + 2 * C::A_BYTES + C::B_BYTES), mBlo, &full[stage], kc * BK, yb);
+            }
             if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
           }
         }
@@ -317,8 +352,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
         const int64_t len = item_len(p);
         for (int64_t u = 0; u < len; ++u) {
           const TileCoord tc = decode(p, li * len + u);
-          const int kchunks = (int)(p.K / BK);
-          const int kb = (int)tc.s * p.kc_per, ke = min(kchunks, kb + p.kc_per);
+          const KRange kr = k_range<BK>(p, tc.s);
+          const int kb = kr.kb, ke = kr.ke;
           if (!mbar_wait(&acce[buf], aphase ^ 1, abort_flag, err, 2)) goto mma_done;
           fence_after();
           const uint32_t d_tmem = tmem_base + (uint32_t)(buf * BN);
@@ -337,9 +372,11 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
               const uint64_t dbh = sdesc(bhi + koff, C::SBO, C::LAYOUT);
               const uint64_t dbl = sdesc(blo + koff, C::SBO, C::LAYOUT);
               mma_bf16(d_tmem, dah, dbh, idesc, acc0);
-              mma_bf16(d_tmem, dah, dbl, idesc, 1u);
-              mma_bf16(d_tmem, dal, dbh, idesc, 1u);
-              if (p.products == 4) mma_bf16(d_tmem, dal, dbl, idesc, 1u);
+              if (p.products != 1) {
+                mma_bf16(d_tmem, dah, dbl, idesc, 1u);
+                mma_bf16(d_tmem, dal, dbh, idesc, 1u);
+                if (p.products == 4) mma_bf16(d_tmem, dal, dbl, idesc, 1u);
+              }
             }
             mma_commit(&empty[stage]);  // frees the smem stage when these MMAs complete
             if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
@@ -377,18 +414,40 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
       fence_after();
       const int64_t i = tc.m * BM + q * 32 + lane;
       const bool row_ok = i < p.M && (i % e.rd) < e.rlim;
+      // partial offset: the K split (F32 partials) or the split group (kacc groups)
       const int64_t rbase = (i / e.rd) * e.ro1 + (i % e.rd) * e.ro2 + tc.b * e.bo +
-                            (p.kacc ? 0 : tc.s * e.so);
+                            (p.kacc ? (tc.s / p.spg) * e.so : tc.s * e.so);
       if constexpr (BN <= 64) {
         if (p.kacc) {
           // this thread's 32 columns (cbeg == cend for the idle half of a BN = 32 tile)
           if (cbeg < cend) {
             uint32_t r[32];
             tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + cbeg), r);
+            const int64_t sg = tc.s % p.spg;  // position inside the split group
+            if (p.products == 1) {
+              // slice mode: each split's FP32 sum is exact; the splits are added as an unevaluated
+              // pair of floats (Knuth's TwoSum, error-free), held in the bits of kv[j] (hi, lo),
+              // which keeps the FP64 pipe out of the per-split work
 #pragma unroll
-            for (int j = 0; j < 32; ++j)
-              kv[j] = (tc.s == 0 ? 0.0 : kv[j]) + (double)__uint_as_float(r[j]);
-            if (row_ok && tc.s == p.ksplit - 1) {
+              for (int j = 0; j < 32; ++j) {
+                const float x = __uint_as_float(r[j]);
+                float hi = 0.f, lo = 0.f;
+                if (sg != 0) {
+                  hi = __int_as_float(__double2hiint(kv[j]));
+                  lo = __int_as_float(__double2loint(kv[j]));
+                }
+                const float sum = hi + x;
+                const float bb = sum - hi;
+                lo += (hi - (sum - bb)) + (x - bb);
+                kv[j] = (sg == p.spg - 1) ? (double)sum + (double)lo
+                                          : __hiloint2double(__float_as_int(sum), __float_as_int(lo));
+              }
+            } else {
+#pragma unroll
+              for (int j = 0; j < 32; ++j)
+                kv[j] = (sg == 0 ? 0.0 : kv[j]) + (double)__uint_as_float(r[j]);
+            }
+            if (row_ok && sg == p.spg - 1) {
               // the K splits summed in FP64 in split order, as the reduction kernel does
               int64_t n = tc.n * BN + cbeg, nq = n / e.cd, nr = n % e.cd;
 #pragma unroll
@@ -550,6 +609,52 @@ __global__ void reduce_partials_kernel(const float *__restrict__ part, int64_t M
                (int64_t)gridDim.x * blockDim.x);
 }
 
+// One warp per (row, run of chunk columns): the run's maximum, then its digits.
+__global__ void slice_kernel(const double *__restrict__ x, int64_t rows, int64_t cols, const SplitMap m,
+                             int nsl, int64_t chunk, uint16_t *__restrict__ out, int64_t ldo, int64_t plane) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nchunks = (cols + chunk - 1) / chunk;
+  const int64_t units = rows * nchunks;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t u = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; u < units; u += nwarps) {
+    const int64_t r = u / nchunks, q = u % nchunks;
+    const int64_t rq = r / m.rdiv, rr = r % m.rdiv;
+    if (rr >= m.rlim) continue;  // uniform over the warp
+    const double *xr = x + rq * m.rs1 + rr * m.rs2;
+    const int64_t c0 = q * chunk, c1 = min(cols, c0 + chunk);
+    double mx = 0.0;
+    for (int64_t c = c0 + lane; c < c1; c += 32) mx = fmax(mx, fabs(xr[c * m.cs]));
+#pragma unroll
+    for (int o = 16; o; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    int e = 0;
+    if (mx > 0.0) frexp(mx, &e);  // mx < 2^e: |x| / 2^e < 1
+    uint16_t *orow = out + r * ldo;
+    for (int64_t c = c0 + lane; c < c1; c += 32) {
+      double t = mx > 0.0 ? ldexp(xr[c * m.cs], -e) : 0.0;
+      for (int sl = 0; sl < nsl; ++sl) {
+        t = ldexp(t, 7);
+        const double d = rint(t);  // |d| <= 128 for the first digit, <= 64 after
+        t -= d;                    // exact: t and d are within a factor of two of each other or d = 0
+        orow[sl * plane + c] = __bfloat16_as_ushort(__double2bfloat16(ldexp(d, e - 7 * (sl + 1))));
+      }
+    }
+  }
+}
+
+__global__ void reduce_f64_kernel(const double *__restrict__ part, int64_t M, int64_t N, int G,
+                                  const TcEpilogue e) {
+  const int64_t total = M * N;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t % M, n = t / M;
+    if ((i % e.rd) >= e.rlim || (n % e.cd) >= e.clim) continue;
+    double acc = 0.0;
+    for (int g = 0; g < G; ++g) acc += part[g * total + t];
+    double *y = e.out_f64 + (i / e.rd) * e.ro1 + (i % e.rd) * e.ro2 + (n / e.cd) * e.co1 + (n % e.cd) * e.co2;
+    const double r = e.alpha * acc;
+    *y = (e.beta == 0.0) ? r : fma(e.beta, *y, r);
+  }
+}
+
 __global__ void reduce_group_kernel(const __grid_constant__ ReduceGroup g) {
   const ReduceJob q = g.j[blockIdx.y];
   reduce_range(q.part, q.M, q.N, q.ksplit, q.epi, blockIdx.x * (int64_t)blockDim.x + threadIdx.x,
@@ -653,6 +758,17 @@ KParams make_params(const TcMat &A, const TcMat &B, const TcShape &sh, const TcE
   VGB_REQUIRE(A.bk == B.bk, "tc_gemm: operands staged with different K boxes");
   const int BK = A.bk;
   VGB_REQUIRE(sh.K % BK == 0 && A.K >= sh.K && B.K >= sh.K, "tc_gemm: K not padded");
+  int64_t a_extra = 0, b_extra = 0;  // slice mode: rows of the highest slice plane addressed
+  if (sh.npairs > 0) {
+    VGB_REQUIRE(sh.npairs <= 16 && sh.chain >= BK && sh.chain % BK == 0 && sh.nbatch == 1,
+                "tc_gemm: bad slice pairs");
+    VGB_REQUIRE(sh.a_plane >= sh.M && sh.b_plane >= sh.N, "tc_gemm: slice planes smaller than the problem");
+    for (int i = 0; i < sh.npairs; ++i) {
+      VGB_REQUIRE(sh.pa[i] < 16 && sh.pb[i] < 16, "tc_gemm: slice index out of range");
+      a_extra = std::max(a_extra, (int64_t)sh.pa[i] * sh.a_plane);
+      b_extra = std::max(b_extra, (int64_t)sh.pb[i] * sh.b_plane);
+    }
+  }
   VGB_REQUIRE(epi.rd >= 1 && epi.cd >= 1, "tc_gemm: bad epilogue map");
   KParams p;
   p.ntiles = 0;
@@ -660,20 +776,42 @@ KParams make_params(const TcMat &A, const TcMat &B, const TcShape &sh, const TcE
   if (sh.M <= 0 || sh.N <= 0 || sh.nbatch <= 0) return p;
   // rows addressed by the last batch must exist in the operands (TMA fills beyond with zeros,
   // but row coordinates must stay within the int32 range of the descriptor)
-  VGB_REQUIRE((sh.nbatch - 1) * sh.a_batch_rows + sh.M <= A.rows + BM, "tc_gemm: A rows");
-  VGB_REQUIRE((sh.nbatch - 1) * sh.b_batch_rows + sh.N <= B.rows + bn, "tc_gemm: B rows");
+  VGB_REQUIRE((sh.nbatch - 1) * sh.a_batch_rows + a_extra + sh.M <= A.rows + BM, "tc_gemm: A rows");
+  VGB_REQUIRE((sh.nbatch - 1) * sh.b_batch_rows + b_extra + sh.N <= B.rows + bn, "tc_gemm: B rows");
   VGB_REQUIRE(A.rows < (1LL << 31) && B.rows < (1LL << 31), "tc_gemm: too many rows");
   p.M = sh.M; p.N = sh.N; p.K = sh.K;
-  p.products = sh.products == 4 ? 4 : 3;
+  p.products = sh.npairs > 0 ? 1 : (sh.products == 4 ? 4 : 3);
+  p.npairs = sh.npairs > 0 ? sh.npairs : 0;
+  p.a_plane = sh.a_plane;
+  p.b_plane = sh.b_plane;
+  p.pa = 0;
+  p.pb = 0;
+  for (int i = 0; i < p.npairs; ++i) {
+    p.pa |= (uint64_t)sh.pa[i] << (4 * i);
+    p.pb |= (uint64_t)sh.pb[i] << (4 * i);
+  }
   p.nbatch = sh.nbatch;
   p.a_brows = sh.a_batch_rows;
   p.b_brows = sh.b_batch_rows;
   const int kchunks = (int)(sh.K / BK);
   VGB_REQUIRE(kchunks >= 1, "tc_gemm: K must be positive");
-  int ks = std::max(1, std::min(sh.ksplit, kchunks));
-  p.kc_per = (int)ceil_div(kchunks, ks);
-  p.ksplit = (int)ceil_div(kchunks, p.kc_per);
-  p.kacc = (sh.kacc && p.ksplit > 1) ? 1 : 0;
+  if (p.npairs) {  // every split: one pair, at most chain K elements
+    p.kc_per = (int)std::min<int64_t>(kchunks, sh.chain / BK);
+    p.cpp = (int)ceil_div(kchunks, p.kc_per);
+    p.ksplit = p.npairs * p.cpp;
+    p.kacc = p.ksplit > 1 ? 1 : 0;
+  } else {
+    int ks = std::max(1, std::min(sh.ksplit, kchunks));
+    p.kc_per = (int)ceil_div(kchunks, ks);
+    p.ksplit = (int)ceil_div(kchunks, p.kc_per);
+    p.cpp = p.ksplit;
+    p.kacc = (sh.kacc && p.ksplit > 1) ? 1 : 0;
+  }
+  const int groups = p.kacc ? std::max(1, sh.kgroups) : 1;
+  VGB_REQUIRE(p.ksplit % groups == 0, "tc_gemm: split groups must divide the K splits");
+  VGB_REQUIRE(groups == 1 || (epi.kind == TcEpilogue::AXPBY_F64 && epi.beta == 0.0),
+              "tc_gemm: split groups write FP64 partials");
+  p.spg = p.ksplit / groups;
   VGB_REQUIRE(!p.kacc || (bn <= 64 && epi.kind != TcEpilogue::STORE_F32),
               "tc_gemm: in-CTA K accumulation needs BN <= 64 and a final (split or FP64) epilogue");
   VGB_REQUIRE(p.ksplit == 1 || p.kacc || epi.kind == TcEpilogue::STORE_F32,
@@ -783,6 +921,27 @@ void reduce_grouped(const std::vector<ReduceJob> &jobs, cudaStream_t s) {
     reduce_group_kernel<<<dim3(group_blocks(mx, g->n), (unsigned)g->n), 256, 0, s>>>(*g);
     VGB_LAUNCH_CHECK();
   }
+}
+
+void slice_f64(const double *x, int64_t rows, int64_t cols, const SplitMap &m, int nslices, int64_t chunk,
+               uint16_t *out, int64_t ldo, int64_t plane, cudaStream_t s) {
+  if (rows <= 0 || cols <= 0) return;
+  VGB_REQUIRE(m.rdiv >= 1 && nslices >= 1 && nslices <= 16 && chunk >= 1 && chunk <= 1024 && ldo >= cols &&
+                  plane >= rows * ldo,
+              "slice: bad map or sizes");
+  const int64_t warps = rows * ceil_div(cols, chunk);
+  const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(warps, 8), 64LL * sm_count()));
+  slice_kernel<<<blocks, 256, 0, s>>>(x, rows, cols, m, nslices, chunk, out, ldo, plane);
+  VGB_LAUNCH_CHECK();
+}
+
+void reduce_f64_groups(const double *part, int64_t M, int64_t N, int ngroups, const TcEpilogue &epi,
+                       cudaStream_t s) {
+  if (M <= 0 || N <= 0) return;
+  VGB_REQUIRE(epi.kind == TcEpilogue::AXPBY_F64 && ngroups >= 1 && epi.rd >= 1 && epi.cd >= 1,
+              "reduce_f64_groups: bad epilogue");
+  reduce_f64_kernel<<<grid_1d(M * N), 256, 0, s>>>(part, M, N, ngroups, epi);
+  VGB_LAUNCH_CHECK();
 }
 
 void reduce_partials(const float *partial, int64_t M, int64_t N, int ksplit, const TcEpilogue &epi,

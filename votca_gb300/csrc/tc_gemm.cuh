@@ -57,6 +57,19 @@ struct TcShape {
   // with ksplit > 1 and BN <= 64: one CTA runs all splits of a tile and sums them in FP64
   // registers (in split order) before the epilogue map; no partials, no reduction launch
   bool kacc = false;
+  // kacc: the splits of a tile shared out to kgroups CTAs (kgroups divides the split count);
+  // group g writes its FP64 sum through the epilogue map at offset g * epi.so (beta = 0), and
+  // reduce_f64_groups adds the groups
+  int kgroups = 1;
+  // slice mode (npairs > 0, nbatch 1): the operands hold bf16 slice planes stacked by rows
+  // (slice t of operand row r is row t * plane + r, see slice_f64); the product is the sum over
+  // pairs i of A slice pa[i] times B slice pb[i], one bf16 MMA per K step (hi maps only).
+  // Every K split covers one pair and at most `chain` K elements (the run of one digit scale),
+  // and the splits are summed in FP64 (kacc).
+  int npairs = 0;
+  uint8_t pa[16] = {}, pb[16] = {};
+  int64_t a_plane = 0, b_plane = 0;
+  int64_t chain = 1024;
 };
 
 // Launch the persistent GEMM; bn in {32, 64, 128, 256}.  err: device int set
@@ -88,6 +101,24 @@ struct SplitMap {
 };
 void split_f64_to_bf16(const double *x, int64_t rows, int64_t cols, const SplitMap &m, uint16_t *hi,
                        uint16_t *lo, int64_t ldo, cudaStream_t s);
+
+// Ozaki slices (Ozaki, Ogita, Oishi, Rump, Numer. Algorithms 59 (2012) 95-118; on tensor cores:
+// Mukunoki, Ozaki, Ogita, Imamura, ISC 2020) of the FP64 matrix x (element (r, c) through the map
+// as above): for every row and every run of `chunk` columns (c / chunk equal) a power of two
+// sigma >= max |x| over the run, and nslices digits d_t = the t-th base-2^7 digit of x / sigma
+// rounded to nearest (|d_1| <= 128, |d_t| <= 64 after), stored as the bf16 value
+// d_t sigma 2^(-7 t) at out[(t - 1) * plane + r * ldo + c].  The bf16 values are exact, and the
+// product of two digits is an integer times sigma_a sigma_b 2^(-7 (s + t)) below 2^14 of it, so
+// a sum of at most 1024 such products for one slice pair and one output element, with the
+// same sigmas, is exact in FP32.  Rows with (r % rdiv) >= rlim and columns >= cols are left
+// as they are (zero padding).
+void slice_f64(const double *x, int64_t rows, int64_t cols, const SplitMap &m, int nslices, int64_t chunk,
+               uint16_t *out, int64_t ldo, int64_t plane, cudaStream_t s);
+
+// Y = epi(sum over g < ngroups of part[g * M * N + n * M + i]) for the M x N partials of a
+// kgroups product (column-major per group), summed in FP64 in group order; epi: AXPBY_F64.
+void reduce_f64_groups(const double *part, int64_t M, int64_t N, int ngroups, const TcEpilogue &epi,
+                       cudaStream_t s);
 
 // Many independent splits / reductions in one launch per 96 jobs (one grid row per job).
 struct SplitJob {

@@ -71,7 +71,7 @@ struct UksApply : DeviceOperator {
   bool split_precision() const override { return op->precision == BSE_PRECISION_MIXED; }
   void apply_fp64(const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy,
                   cudaStream_t s) override {
-    ForceFp64 g(&op->alpha, &op->beta);
+    ForceFp64 g(&op->alpha, &op->beta, fp64_products);
     op->matmul(coef, X, ldx, k, Y, ldy, s);
   }
 };
@@ -94,7 +94,7 @@ struct UksHamApply : DeviceOperator {
   bool split_precision() const override { return op->precision == BSE_PRECISION_MIXED; }
   void apply_fp64(const double *X, int64_t ldx, int64_t k, double *Y, int64_t ldy,
                   cudaStream_t s) override {
-    ForceFp64 g(&op->alpha, &op->beta);
+    ForceFp64 g(&op->alpha, &op->beta, fp64_products);
     op->ham_matmul(a, b, X, ldx, k, Y, ldy, s);
   }
 };

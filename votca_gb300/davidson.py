@@ -37,7 +37,7 @@ class DavidsonSolver:
         self.verbose = False
         # no counterpart in the reference: FP64 polish of split-precision solves, trial vectors
         # per iteration (0 = getSizeUpdate), initial unit-vector guesses (0 = 2 * neigen)
-        self.fp64_polish_ = True
+        self.fp64_polish_ = 1
         self.block_size_ = 0
         self.initial_size_ = 0
         self.eigenvalues_ = None
@@ -71,9 +71,15 @@ class DavidsonSolver:
         self.update_ = UPDATES[s]
 
     def set_fp64_polish(self, on):
-        """Split-precision operators: re-evaluate the converged Ritz vectors with FP64 products
-        and iterate until the FP64 residuals meet the tolerance (on by default)."""
-        self.fp64_polish_ = bool(on)
+        """Split-precision operators: re-evaluate the converged Ritz vectors with FP64-accurate
+        products and iterate until those residuals meet the tolerance (on by default).  True or
+        "sliced": Ozaki slice products on the tensor cores; "fp64": FP64 DGEMM; False: off."""
+        if on == "fp64":
+            self.fp64_polish_ = 2
+        elif on == "sliced":
+            self.fp64_polish_ = 1
+        else:
+            self.fp64_polish_ = 1 if on else 0
 
     def set_block_size(self, n):
         """Trial vectors added per iteration (>= neigen); 0 restores getSizeUpdate's rule."""
