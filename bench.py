@@ -15,8 +15,9 @@ e2e: the same product through the host-pointer C ABI call (bse_op_matmul):
 X copied host->device and Y device->host inside every timed step.
 
 Also reported once, outside the timed steps: time-to-20-roots of the full
-Davidson solve (tolerance 1e-7, split precision with its FP64 polish, and FP64)
-with the FP64 residuals of the returned roots, the C0 solve, the batched
+Davidson solve (tolerance 1e-7; split precision with its FP64-accurate polish
+on Ozaki slice products, FP64, and slice products throughout) with the FP64
+residuals of the returned roots, the C0 solve, the batched
 256-molecule solve, the full-BSE solve at v=128, c=1024, Naux=4096 (32 trial
 vectors per iteration, FP64 polish, an independent FP64 evaluation of its
 roots), and (N = 1) the CPU figures: the reference loop nest port on one whole
@@ -601,7 +602,7 @@ def roots_report(ctx, precision, w, Mmn, hqp, opt):
 
     out = {}
     ctxs = {}
-    for pname, pr in (("fp64", bo.PRECISION_FP64), ("mixed", bo.PRECISION_MIXED)):
+    for pname, pr in (("fp64", bo.PRECISION_FP64), ("mixed", bo.PRECISION_MIXED), ("sliced", bo.PRECISION_SLICED)):
         try:
             ctxs[pname] = ctx if pr == precision else bo.GpuBSEContext(w, Mmn, hqp, opt, precision=pr)
         except _lib.BSEError as e:
@@ -625,7 +626,8 @@ def roots_report(ctx, precision, w, Mmn, hqp, opt):
                           "roots_eV": [round(float(x), 9) for x in lam]}
             if r.polished:
                 res[pname]["fp64_polish"] = {"iterations": int(r.polish_iterations),
-                                             "fp64_columns": int(r.fp64_columns), "seconds": r.seconds_polish}
+                                             "fp64_columns": int(r.fp64_columns), "seconds": r.seconds_polish,
+                                             "products": "sliced (Ozaki, tensor cores)"}
         if "fp64" in vecs and "mixed" in vecs:
             d = np.abs(np.array(res["fp64"]["roots_eV"]) - np.array(res["mixed"]["roots_eV"])) * 1e3
             res["max_abs_diff_meV"] = float(d.max())
@@ -634,6 +636,10 @@ def roots_report(ctx, precision, w, Mmn, hqp, opt):
             res["min_eigvec_overlap"] = float(ov.min())
             res["max_one_minus_overlap"] = float((1.0 - ov).max())
             res["speedup_mixed_vs_fp64"] = res["fp64"]["seconds"] / res["mixed"]["seconds"]
+            if "sliced" in vecs:
+                res["speedup_sliced_vs_fp64"] = res["fp64"]["seconds"] / res["sliced"]["seconds"]
+                res["sliced_max_abs_diff_meV"] = float(
+                    np.max(np.abs(np.array(res["fp64"]["roots_eV"]) - np.array(res["sliced"]["roots_eV"]))) * 1e3)
             # residuals of the mixed roots under the FP64 operator (an FP64 product on the GPU)
             lam_m = lams["mixed"]
             xm = vecs["mixed"]

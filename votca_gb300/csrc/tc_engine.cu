@@ -420,8 +420,8 @@ void sliced_gemm(const TcMat &A, int64_t a_plane, const TcMat &B, int64_t b_plan
   sh.kacc = true;
   const int64_t tiles = ceil_div(M, 128) * ceil_div(N, bn);
   const int64_t ksplit = sh.npairs * ceil_div(K / 64, sh.chain / 64);
-  int groups = 1;
-  for (int g = 2; g <= 64; ++g)
+  int groups = 1;  // float-pair outputs are written by the CTA that owns the tile
+  for (int g = 2; g <= 64 && fe.kind == TcEpilogue::AXPBY_F64; ++g)
     if (ksplit % g == 0 && tiles * g <= sm_count()) groups = g;
   if (groups == 1) {
     tc_gemm(A, B, sh, fe, bn, err, s);
@@ -547,12 +547,12 @@ void MixedEngine::apply_sliced(BseOperator &op, const Coef &c, const double *X, 
       const int64_t kc = std::min(jc, k - j0);
       op.timer.begin(is_hd ? STAGE_TC_HD : STAGE_TC_HD2, s);
       TcMat Ax = make_tc_mat(px + j0 * vt * m.Kc, px + j0 * vt * m.Kc, xrows - j0 * vt, m.Kc, m.Kc, 128, 64);
-      TcEpilogue e;  // stage 1 into the FP64 intermediate [(j, row)][(P, v)]
-      e.kind = TcEpilogue::AXPBY_F64;
+      TcEpilogue e;  // stage 1 into the intermediate [(j, row)][(P, v)], FP64 sums as float pairs
+      e.kind = TcEpilogue::PAIR_F32;
       e.rd = vt; e.ro2 = 1; e.rlim = vt;
       e.ro1 = rows_per_vec * m.Kg;
       e.cd = is_hd ? ct : vt; e.co1 = vt; e.co2 = m.Kg; e.clim = e.cd;
-      e.out_f64 = m.fT.get(); e.alpha = 1.0; e.beta = 0.0;
+      e.out_f32 = reinterpret_cast<float *>(m.fT.get());
       if (is_hd) {  // S[(j, c1)][(P, v)] = sum_c X_j(v, c) M(c1, c, P)
         const TcMat &Bm = m.mat(m.pMcc.get(), m.pMcc.get(), nsl * naux * ct, m.Kc, 64, 64);
         sliced_gemm(Ax, k * vt, Bm, naux * ct, kc * vt, naux * ct, m.Kc, chc, nsl, 64, e, m.gpart, err, s);
@@ -560,10 +560,13 @@ void MixedEngine::apply_sliced(BseOperator &op, const Coef &c, const double *X, 
         const TcMat &Bm = m.mat(m.pBvc2.get(), m.pBvc2.get(), nsl * naux * vt, m.Kc, 64, 64);
         sliced_gemm(Ax, k * vt, Bm, naux * vt, kc * vt, naux * vt, m.Kc, chc, nsl, 64, e, m.gpart, err, s);
       }
+      op.timer.end(is_hd ? STAGE_TC_HD : STAGE_TC_HD2, s);
+      op.timer.begin(STAGE_TC_SPLIT, s);
       SplitMap t;
       t.rdiv = 1; t.rs1 = m.Kg; t.rs2 = 0; t.cs = 1; t.rlim = 1;
-      slice_f64(m.fT.get(), kc * rows_per_vec, naux * vt, t, nsl, chg, m.pT.get(), m.Kg, m.pT.plane(), s);
-      op.timer.end(is_hd ? STAGE_TC_HD : STAGE_TC_HD2, s);
+      slice_pairs(reinterpret_cast<const float *>(m.fT.get()), kc * rows_per_vec, naux * vt, t, nsl, chg,
+                  m.pT.get(), m.Kg, m.pT.plane(), s);
+      op.timer.end(STAGE_TC_SPLIT, s);
       op.timer.begin(is_hd ? STAGE_TC_HD_B : STAGE_TC_HD2_B, s);
       if (is_hd) {  // Y_j(c1, v1) += alpha sum_{(P,v)} S[(j, c1)][(P,v)] G[v1][(P,v)]
         TcMat As = make_tc_mat(m.pT.get(), m.pT.get(), nsl * tplane, m.Kg, m.Kg, 128, 64);

@@ -304,18 +304,24 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
         const int64_t len = item_len(p);
         const CUtensorMap *mAhi = src.map(pi, 0), *mAlo = src.map(pi, 1);
         const CUtensorMap *mBhi = src.map(pi, 2), *mBlo = src.map(pi, 3);
-        for (int64_t u = 0; u < len; ++u) {
-          const TileCoord tc = decode(p, li * len + u);
+        // the jobs of an item share the tile; only the K split advances (decode once per item)
+        TileCoord tc = decode(p, li * len);
+        for (int64_t u = 0; u < len; ++u, ++tc.s) {
           const KRange kr = k_range<BK>(p, tc.s);
           const int ya = (int)(tc.b * p.a_brows + tc.m * BM);
           const int yb = (int)(tc.b * p.b_brows + tc.n * BN);
-          for (int kc = kr.kb; kc < kr.ke; ++kc) {
+          // slice mode: two K blocks per stage (the hi and lo slots), one A and one B plane each
+          for (int kc = kr.kb; kc < kr.ke; kc += p.npairs ? 2 : 1) {
             if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, err, 1)) goto producer_done;
             uint8_t *st = smem + stage * C::STAGE_BYTES;
-            if (p.npairs) {  // slice mode: one A slice and one B slice per stage
-              mbar_expect_tx(&full[stage], (uint32_t)(C::A_BYTES + C::B_BYTES));
-              tma_load_2d(smem_u32(st), mAhi, &full[stage], kc * BK, ya + kr.ya);
-              tma_load_2d(smem_u32(st + 2 * C::A_BYTES), mBhi, &full[stage], kc * BK, yb + kr.yb);
+            if (p.npairs) {
+              const int nblk = min(2, kr.ke - kc);
+              mbar_expect_tx(&full[stage], (uint32_t)(nblk * (C::A_BYTES + C::B_BYTES)));
+              for (int h = 0; h < nblk; ++h) {
+                tma_load_2d(smem_u32(st + h * C::A_BYTES), mAhi, &full[stage], (kc + h) * BK, ya + kr.ya);
+                tma_load_2d(smem_u32(st + 2 * C::A_BYTES + h * C::B_BYTES), mBhi, &full[stage], (kc + h) * BK,
+                            yb + kr.yb);
+              }
             } else {
               mbar_expect_tx(&full[stage], (uint32_t)C::STAGE_BYTES);
               tma_load_2d(smem_u32(st), mAhi, &full[stage], kc * BK, ya);
@@ -350,19 +356,35 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
         int64_t li;
         const KParams p = src.params(src.locate(R, li, hint));
         const int64_t len = item_len(p);
-        for (int64_t u = 0; u < len; ++u) {
-          const TileCoord tc = decode(p, li * len + u);
+        // the jobs of an item share the tile; only the K split advances (decode once per item)
+        TileCoord tc = decode(p, li * len);
+        for (int64_t u = 0; u < len; ++u, ++tc.s) {
           const KRange kr = k_range<BK>(p, tc.s);
           const int kb = kr.kb, ke = kr.ke;
           if (!mbar_wait(&acce[buf], aphase ^ 1, abort_flag, err, 2)) goto mma_done;
           fence_after();
           const uint32_t d_tmem = tmem_base + (uint32_t)(buf * BN);
-          for (int kc = kb; kc < ke; ++kc) {
+          for (int kc = kb; kc < ke; kc += p.npairs ? 2 : 1) {
             if (!mbar_wait(&full[stage], phase, abort_flag, err, 3)) goto mma_done;
             fence_after();
             const uint32_t st = smem_u32(smem + stage * C::STAGE_BYTES);
             const uint32_t ahi = st, alo = st + C::A_BYTES;
             const uint32_t bhi = st + 2 * C::A_BYTES, blo = bhi + C::B_BYTES;
+            if (p.npairs) {  // slice mode: K block kc in the hi slots, kc + 1 in the lo slots
+              const int nblk = min(2, ke - kc);
+              for (int h = 0; h < nblk; ++h) {
+#pragma unroll
+                for (int kk = 0; kk < BK / 16; ++kk) {
+                  const uint32_t koff = kk * 32;
+                  const uint32_t acc0 = (kc > kb || h > 0 || kk > 0) ? 1u : 0u;
+                  mma_bf16(d_tmem, sdesc((h ? alo : ahi) + koff, C::SBO, C::LAYOUT),
+                           sdesc((h ? blo : bhi) + koff, C::SBO, C::LAYOUT), idesc, acc0);
+                }
+              }
+              mma_commit(&empty[stage]);
+              if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
+              continue;
+            }
 #pragma unroll
             for (int kk = 0; kk < BK / 16; ++kk) {
               const uint32_t koff = kk * 32;  // 16 bf16 = 32 bytes along K inside the swizzle row
@@ -408,26 +430,28 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
       const KParams p = src.params(src.locate(R, li, hint));
       const TcEpilogue &e = p.epi;
       const int64_t len = item_len(p);
-      for (int64_t u = 0; u < len; ++u) {
-      const TileCoord tc = decode(p, li * len + u);
-      if (!mbar_wait(&accf[buf], aphase, abort_flag, err, 4)) goto epi_done;
-      fence_after();
+      // the jobs of an item share the tile and the split group: row terms once per item
+      TileCoord tc = decode(p, li * len);
       const int64_t i = tc.m * BM + q * 32 + lane;
       const bool row_ok = i < p.M && (i % e.rd) < e.rlim;
       // partial offset: the K split (F32 partials) or the split group (kacc groups)
       const int64_t rbase = (i / e.rd) * e.ro1 + (i % e.rd) * e.ro2 + tc.b * e.bo +
                             (p.kacc ? (tc.s / p.spg) * e.so : tc.s * e.so);
+      for (int64_t u = 0; u < len; ++u, ++tc.s) {
+      if (!mbar_wait(&accf[buf], aphase, abort_flag, err, 4)) goto epi_done;
+      fence_after();
       if constexpr (BN <= 64) {
         if (p.kacc) {
           // this thread's 32 columns (cbeg == cend for the idle half of a BN = 32 tile)
           if (cbeg < cend) {
             uint32_t r[32];
             tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + cbeg), r);
-            const int64_t sg = tc.s % p.spg;  // position inside the split group
-            if (p.products == 1) {
+            const int64_t sg = u;  // position inside the split group (an item is one group)
+            const bool pairs = p.products == 1;
+            if (pairs) {
               // slice mode: each split's FP32 sum is exact; the splits are added as an unevaluated
-              // pair of floats (Knuth's TwoSum, error-free), held in the bits of kv[j] (hi, lo),
-              // which keeps the FP64 pipe out of the per-split work
+              // pair of floats (Knuth's TwoSum, error-free), held in the bits of kv[j] (hi, lo):
+              // no FP64 instruction per split
 #pragma unroll
               for (int j = 0; j < 32; ++j) {
                 const float x = __uint_as_float(r[j]);
@@ -439,8 +463,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
                 const float sum = hi + x;
                 const float bb = sum - hi;
                 lo += (hi - (sum - bb)) + (x - bb);
-                kv[j] = (sg == p.spg - 1) ? (double)sum + (double)lo
-                                          : __hiloint2double(__float_as_int(sum), __float_as_int(lo));
+                kv[j] = __hiloint2double(__float_as_int(sum), __float_as_int(lo));
               }
             } else {
 #pragma unroll
@@ -448,18 +471,27 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
                 kv[j] = (sg == 0 ? 0.0 : kv[j]) + (double)__uint_as_float(r[j]);
             }
             if (row_ok && sg == p.spg - 1) {
-              // the K splits summed in FP64 in split order, as the reduction kernel does
+              // the K splits summed in FP64 (or as float pairs) in split order, as the reduction
+              // kernel does
               int64_t n = tc.n * BN + cbeg, nq = n / e.cd, nr = n % e.cd;
 #pragma unroll
               for (int j = 0; j < 32; ++j) {
                 if (n < p.N && nr < e.clim) {
                   const int64_t off = rbase + nq * e.co1 + nr * e.co2;
-                  if (e.kind == TcEpilogue::AXPBY_F64) {
-                    double *y = e.out_f64 + off;
-                    const double rv = e.alpha * kv[j];
-                    *y = (e.beta == 0.0) ? rv : fma(e.beta, *y, rv);
+                  if (e.kind == TcEpilogue::PAIR_F32) {
+                    reinterpret_cast<float2 *>(e.out_f32)[off] =
+                        make_float2(__int_as_float(__double2hiint(kv[j])), __int_as_float(__double2loint(kv[j])));
                   } else {
-                    epi_store(e, off, (float)kv[j]);
+                    const double val = pairs ? (double)__int_as_float(__double2hiint(kv[j])) +
+                                                   (double)__int_as_float(__double2loint(kv[j]))
+                                             : kv[j];
+                    if (e.kind == TcEpilogue::AXPBY_F64) {
+                      double *y = e.out_f64 + off;
+                      const double rv = e.alpha * val;
+                      *y = (e.beta == 0.0) ? rv : fma(e.beta, *y, rv);
+                    } else {
+                      epi_store(e, off, (float)val);
+                    }
                   }
                 }
                 ++n;
@@ -609,9 +641,66 @@ __global__ void reduce_partials_kernel(const float *__restrict__ part, int64_t M
                (int64_t)gridDim.x * blockDim.x);
 }
 
-// One warp per (row, run of chunk columns): the run's maximum, then its digits.
-__global__ void slice_kernel(const double *__restrict__ x, int64_t rows, int64_t cols, const SplitMap m,
-                             int nsl, int64_t chunk, uint16_t *__restrict__ out, int64_t ldo, int64_t plane) {
+// One warp per (row, run of chunk columns): the run's maximum, then its digits, all in integer
+// arithmetic on the FP64 bit patterns (the FP64 pipe of GB300 is slow; these are INT32/INT64
+// operations): the run scale is 2^e with e the frexp exponent of the largest |x|, an element is
+// m = round(x 2^(B - e)) with B = 7 nsl (|m| <= 2^B, a 64-bit integer from its mantissa), and the
+// digits are its balanced base-2^7 digits, d_t = round(r / 2^(B - 7t)), r -= d_t 2^(B - 7t).
+__device__ __forceinline__ long long fixed_point(unsigned long long bits, int e, int B) {
+  const int ef = (int)((bits >> 52) & 0x7FF);
+  if (ef == 0) return 0;  // zero or subnormal: below 2^-1022, far under the run scale
+  const long long mant = (long long)((bits & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull);
+  // value = mant 2^(ef - 1075), m = mant 2^(ef - 1075 + B - e): a right shift by sh >= 53 - B
+  const int sh = 1075 + e - ef - B;
+  long long m = 0;
+  if (sh < 63) m = (mant + (1LL << (sh - 1))) >> sh;
+  return (bits >> 63) ? -m : m;
+}
+
+// The same fixed point for a float given by its bits.
+__device__ __forceinline__ long long fixed_point_f32(unsigned bits, int e, int B) {
+  const int ef = (int)((bits >> 23) & 0xFF);
+  if (ef == 0) return 0;
+  const long long mant = (long long)((bits & 0x7FFFFFu) | 0x800000u);
+  // value = mant 2^(ef - 150), m = mant 2^(ef - 150 + B - e)
+  const int sh = 150 + e - ef - B;
+  long long m;
+  if (sh <= 0) m = mant << (-sh);  // |value| < 2^(e + 1): at most 2^(B + 1)
+  else m = sh < 40 ? (mant + (1LL << (sh - 1))) >> sh : 0;
+  return (bits >> 31) ? -m : m;
+}
+
+// Input element access of the slicer: FP64 values, or float pairs (hi, lo) with value hi + lo.
+struct F64In {
+  const unsigned long long *p;
+  __device__ __forceinline__ unsigned long long abs_bits(int64_t i) const {
+    return __ldg(p + i) & 0x7FFFFFFFFFFFFFFFull;
+  }
+  // frexp exponent of a maximum (abs_bits): mx < 2^e; subnormal maxima as 2^-1022
+  __device__ __forceinline__ static int exponent(unsigned long long mx) {
+    return mx == 0 ? 0 : max((int)(mx >> 52), 1) - 1022;
+  }
+  __device__ __forceinline__ long long fixed(int64_t i, int e, int B) const {
+    return fixed_point(__ldg(p + i), e, B);
+  }
+};
+struct PairIn {
+  const unsigned long long *p;  // float2 elements
+  __device__ __forceinline__ unsigned long long abs_bits(int64_t i) const {
+    return (unsigned long long)((unsigned)__ldg(p + i) & 0x7FFFFFFFu);  // |hi|; hi holds the sum
+  }
+  __device__ __forceinline__ static int exponent(unsigned long long mx) {
+    return mx == 0 ? 0 : max((int)(mx >> 23), 1) - 126;
+  }
+  __device__ __forceinline__ long long fixed(int64_t i, int e, int B) const {
+    const unsigned long long v = __ldg(p + i);  // little-endian float2: hi in the low word
+    return fixed_point_f32((unsigned)v, e, B) + fixed_point_f32((unsigned)(v >> 32), e, B);
+  }
+};
+
+template <class In>
+__global__ void slice_kernel(const In in, int64_t rows, int64_t cols, const SplitMap m, int nsl, int64_t chunk,
+                             uint16_t *__restrict__ out, int64_t ldo, int64_t plane) {
   const int lane = threadIdx.x & 31;
   const int64_t nchunks = (cols + chunk - 1) / chunk;
   const int64_t units = rows * nchunks;
@@ -620,22 +709,34 @@ __global__ void slice_kernel(const double *__restrict__ x, int64_t rows, int64_t
     const int64_t r = u / nchunks, q = u % nchunks;
     const int64_t rq = r / m.rdiv, rr = r % m.rdiv;
     if (rr >= m.rlim) continue;  // uniform over the warp
-    const double *xr = x + rq * m.rs1 + rr * m.rs2;
+    const int64_t base = rq * m.rs1 + rr * m.rs2;
     const int64_t c0 = q * chunk, c1 = min(cols, c0 + chunk);
-    double mx = 0.0;
-    for (int64_t c = c0 + lane; c < c1; c += 32) mx = fmax(mx, fabs(xr[c * m.cs]));
+    unsigned long long mx = 0;  // largest |x| as a bit pattern (ordered like the values)
+    for (int64_t c = c0 + lane; c < c1; c += 32) {
+      const unsigned long long a = in.abs_bits(base + c * m.cs);
+      mx = a > mx ? a : mx;
+    }
 #pragma unroll
-    for (int o = 16; o; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    int e = 0;
-    if (mx > 0.0) frexp(mx, &e);  // mx < 2^e: |x| / 2^e < 1
+    for (int o = 16; o; o >>= 1) {
+      const unsigned long long y = __shfl_xor_sync(0xffffffffu, mx, o);
+      mx = y > mx ? y : mx;
+    }
+    const int e = In::exponent(mx);
     uint16_t *orow = out + r * ldo;
     for (int64_t c = c0 + lane; c < c1; c += 32) {
-      double t = mx > 0.0 ? ldexp(xr[c * m.cs], -e) : 0.0;
+      long long rem = mx == 0 ? 0 : in.fixed(base + c * m.cs, e, 7 * nsl);
       for (int sl = 0; sl < nsl; ++sl) {
-        t = ldexp(t, 7);
-        const double d = rint(t);  // |d| <= 128 for the first digit, <= 64 after
-        t -= d;                    // exact: t and d are within a factor of two of each other or d = 0
-        orow[sl * plane + c] = __bfloat16_as_ushort(__double2bfloat16(ldexp(d, e - 7 * (sl + 1))));
+        const int shift = 7 * (nsl - 1 - sl);  // digit sl + 1 has weight 2^(B - 7 (sl + 1))
+        long long d = rem;                     // the last digit: the remaining |rem| <= 64
+        if (shift > 0) {
+          d = (rem + (1LL << (shift - 1))) >> shift;  // round half up (arithmetic shift: floor)
+          rem -= d << shift;
+        }
+        // the bf16 value d 2^(e - 7 (sl + 1)): |d| <= 128 is exact in bf16; tiny scales flush to 0
+        const int pe = e - 7 * (sl + 1) + 127;
+        float v = 0.f;
+        if (pe >= 1 && pe <= 254) v = (float)d * __int_as_float(pe << 23);
+        orow[sl * plane + c] = __bfloat16_as_ushort(__float2bfloat16_rn(v));
       }
     }
   }
@@ -814,6 +915,8 @@ KParams make_params(const TcMat &A, const TcMat &B, const TcShape &sh, const TcE
   p.spg = p.ksplit / groups;
   VGB_REQUIRE(!p.kacc || (bn <= 64 && epi.kind != TcEpilogue::STORE_F32),
               "tc_gemm: in-CTA K accumulation needs BN <= 64 and a final (split or FP64) epilogue");
+  VGB_REQUIRE(epi.kind != TcEpilogue::PAIR_F32 || (p.kacc && p.npairs > 0 && (int64_t)bn <= 64),
+              "tc_gemm: float-pair output needs slice mode with in-CTA K accumulation");
   VGB_REQUIRE(p.ksplit == 1 || p.kacc || epi.kind == TcEpilogue::STORE_F32,
               "tc_gemm: K split needs F32 partials or in-CTA accumulation");
   p.mt = ceil_div(sh.M, BM);
@@ -926,12 +1029,26 @@ void reduce_grouped(const std::vector<ReduceJob> &jobs, cudaStream_t s) {
 void slice_f64(const double *x, int64_t rows, int64_t cols, const SplitMap &m, int nslices, int64_t chunk,
                uint16_t *out, int64_t ldo, int64_t plane, cudaStream_t s) {
   if (rows <= 0 || cols <= 0) return;
-  VGB_REQUIRE(m.rdiv >= 1 && nslices >= 1 && nslices <= 16 && chunk >= 1 && chunk <= 1024 && ldo >= cols &&
+  VGB_REQUIRE(m.rdiv >= 1 && nslices >= 1 && nslices <= 7 && chunk >= 1 && chunk <= 1024 && ldo >= cols &&
                   plane >= rows * ldo,
               "slice: bad map or sizes");
   const int64_t warps = rows * ceil_div(cols, chunk);
   const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(warps, 8), 64LL * sm_count()));
-  slice_kernel<<<blocks, 256, 0, s>>>(x, rows, cols, m, nslices, chunk, out, ldo, plane);
+  slice_kernel<<<blocks, 256, 0, s>>>(F64In{reinterpret_cast<const unsigned long long *>(x)}, rows, cols, m,
+                                      nslices, chunk, out, ldo, plane);
+  VGB_LAUNCH_CHECK();
+}
+
+void slice_pairs(const float *x2, int64_t rows, int64_t cols, const SplitMap &m, int nslices, int64_t chunk,
+                 uint16_t *out, int64_t ldo, int64_t plane, cudaStream_t s) {
+  if (rows <= 0 || cols <= 0) return;
+  VGB_REQUIRE(((uintptr_t)x2 & 7) == 0 && m.rdiv >= 1 && nslices >= 1 && nslices <= 7 && chunk >= 1 &&
+                  chunk <= 1024 && ldo >= cols && plane >= rows * ldo,
+              "slice: bad map or sizes");
+  const int64_t warps = rows * ceil_div(cols, chunk);
+  const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(warps, 8), 64LL * sm_count()));
+  slice_kernel<<<blocks, 256, 0, s>>>(PairIn{reinterpret_cast<const unsigned long long *>(x2)}, rows, cols, m,
+                                       nslices, chunk, out, ldo, plane);
   VGB_LAUNCH_CHECK();
 }
 

@@ -37,7 +37,9 @@ TcMat make_tc_mat(const uint16_t *hi, const uint16_t *lo, int64_t rows, int64_t 
 //   (i / rd) * ro1 + (i % rd) * ro2 + (n / cd) * co1 + (n % cd) * co2 + b * bo + s * so
 // and is written only when i < M, n < N, (i % rd) < rlim, (n % cd) < clim.
 struct TcEpilogue {
-  enum Kind { SPLIT_BF16 = 0, STORE_F32 = 1, AXPBY_F64 = 2 };
+  // PAIR_F32 (slice mode with kacc only): the FP64 sum as an unevaluated pair of floats
+  // (hi, lo), stored as a float2 at out_f32 + 2 * offset
+  enum Kind { SPLIT_BF16 = 0, STORE_F32 = 1, AXPBY_F64 = 2, PAIR_F32 = 3 };
   int kind = AXPBY_F64;
   int64_t rd = 1, ro1 = 0, ro2 = 0, rlim = 1;
   int64_t cd = 1, co1 = 0, co2 = 0, clim = 1;
@@ -105,8 +107,8 @@ void split_f64_to_bf16(const double *x, int64_t rows, int64_t cols, const SplitM
 // Ozaki slices (Ozaki, Ogita, Oishi, Rump, Numer. Algorithms 59 (2012) 95-118; on tensor cores:
 // Mukunoki, Ozaki, Ogita, Imamura, ISC 2020) of the FP64 matrix x (element (r, c) through the map
 // as above): for every row and every run of `chunk` columns (c / chunk equal) a power of two
-// sigma >= max |x| over the run, and nslices digits d_t = the t-th base-2^7 digit of x / sigma
-// rounded to nearest (|d_1| <= 128, |d_t| <= 64 after), stored as the bf16 value
+// sigma >= max |x| over the run, and nslices (<= 7) digits d_t = the t-th balanced base-2^7
+// digit of x / sigma rounded to 7 nslices bits (|d_1| <= 128, |d_t| <= 64 after), stored as the bf16 value
 // d_t sigma 2^(-7 t) at out[(t - 1) * plane + r * ldo + c].  The bf16 values are exact, and the
 // product of two digits is an integer times sigma_a sigma_b 2^(-7 (s + t)) below 2^14 of it, so
 // a sum of at most 1024 such products for one slice pair and one output element, with the
@@ -114,6 +116,10 @@ void split_f64_to_bf16(const double *x, int64_t rows, int64_t cols, const SplitM
 // as they are (zero padding).
 void slice_f64(const double *x, int64_t rows, int64_t cols, const SplitMap &m, int nslices, int64_t chunk,
                uint16_t *out, int64_t ldo, int64_t plane, cudaStream_t s);
+// The same for a matrix held as float pairs (hi, lo) (element value hi + lo; PAIR_F32 output);
+// the map addresses float2 elements.
+void slice_pairs(const float *x2, int64_t rows, int64_t cols, const SplitMap &m, int nslices, int64_t chunk,
+                 uint16_t *out, int64_t ldo, int64_t plane, cudaStream_t s);
 
 // Y = epi(sum over g < ngroups of part[g * M * N + n * M + i]) for the M x N partials of a
 // kgroups product (column-major per group), summed in FP64 in group order; epi: AXPBY_F64.
