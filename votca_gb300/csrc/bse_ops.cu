@@ -166,8 +166,57 @@ __device__ __forceinline__ void diagonal_range(const DiagArgs &a, int64_t I0, in
   }
 }
 
-__global__ void diagonal_kernel(const DiagArgs a) {
-  diagonal_range(a, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, (int64_t)gridDim.x * blockDim.x);
+// One operator: 32 pairs per 256-thread block, the aux sum of each pair split over the block's 8
+// warps (P = w, w + 8, ...; lanes run over consecutive pairs, so every load is a coalesced 256-byte
+// row segment) and the 8 partial sums added in a fixed order: enough independent FMA chains per
+// SM to keep the FP64 pipe and the memory system busy.
+constexpr int kDiagSlices = 8;
+__global__ void __launch_bounds__(32 * kDiagSlices) diagonal_kernel(const DiagArgs a) {
+  __shared__ double part[kDiagSlices][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int64_t I0 = blockIdx.x * 32LL; I0 < a.dim; I0 += (int64_t)gridDim.x * 32) {
+    const int64_t I = I0 + lane;
+    double sx0 = 0.0, sx1 = 0.0, sd0 = 0.0, sd1 = 0.0, s20 = 0.0, s21 = 0.0;
+    if (I < a.dim) {
+      const int64_t v = I / a.ct, c = I % a.ct;
+      int64_t P = w;
+      for (; P + kDiagSlices < a.naux; P += 2 * kDiagSlices) {
+        const int64_t P1 = P + kDiagSlices;
+        if (a.cx != 0.0 || a.cd2 != 0.0) {
+          const double b0 = a.Bvc[P * a.dim + I], b1 = a.Bvc[P1 * a.dim + I];
+          sx0 = fma(b0, b0, sx0);
+          sx1 = fma(b1, b1, sx1);
+          if (a.cd2 != 0.0) {
+            s20 = fma(a.Mcv[P * a.dim + I], b0, s20);
+            s21 = fma(a.Mcv[P1 * a.dim + I], b1, s21);
+          }
+        }
+        if (a.cd != 0.0) {
+          sd0 = fma(a.dcc[P * a.ct + c], a.dvv[P * a.vt + v], sd0);
+          sd1 = fma(a.dcc[P1 * a.ct + c], a.dvv[P1 * a.vt + v], sd1);
+        }
+      }
+      for (; P < a.naux; P += kDiagSlices) {
+        if (a.cx != 0.0 || a.cd2 != 0.0) {
+          const double b0 = a.Bvc[P * a.dim + I];
+          sx0 = fma(b0, b0, sx0);
+          if (a.cd2 != 0.0) s20 = fma(a.Mcv[P * a.dim + I], b0, s20);
+        }
+        if (a.cd != 0.0) sd0 = fma(a.dcc[P * a.ct + c], a.dvv[P * a.vt + v], sd0);
+      }
+    }
+    part[w][lane] = a.cx * (sx0 + sx1) - a.cd * (sd0 + sd1) - a.cd2 * (s20 + s21);
+    __syncthreads();
+    if (w == 0 && I < a.dim) {
+      double entry = 0.0;
+#pragma unroll
+      for (int q = 0; q < kDiagSlices; ++q) entry += part[q][lane];
+      const int64_t v = I / a.ct, c = I % a.ct;
+      if (a.cqp != 0.0) entry += a.cqp * (a.Hcc[c + a.ct * c] - a.Hvv[v + a.vt * v]);
+      a.D[I] = entry;
+    }
+    __syncthreads();
+  }
 }
 
 constexpr int kDiagJobsMax = 192;
@@ -648,7 +697,7 @@ void BseOperator::diagonal(const Coef &c, double *D, cudaStream_t s) {
   a.vt = vt; a.ct = ct; a.naux = naux; a.dim = dim;
   a.Bvc = Bvc.get(); a.Mcv = Mcv.get(); a.dcc = dcc.get(); a.dvv = dvv.get();
   a.Hcc = Hcc.get(); a.Hvv = Hvv.get(); a.D = D;
-  diagonal_kernel<<<grid_for(dim, 128), 128, 0, s>>>(a);
+  diagonal_kernel<<<(unsigned)std::min<int64_t>(ceil_div(dim, 32), 64LL * sm_count()), 32 * kDiagSlices, 0, s>>>(a);
   VGB_LAUNCH_CHECK();
 }
 

@@ -313,6 +313,59 @@ struct Ctx {
   }
 };
 
+// Cholesky QR of a block of nb unit columns: G = W^T W = R^T R (R upper), Rinv = R^-1, one CTA.
+// W R^-1 is the Q of the column-wise classical Gram-Schmidt of the block (the QR factorisation
+// with a positive diagonal is unique).  ok = 0 when a pivot falls below 1e-10 of G_kk (the block
+// is too ill-conditioned for Cholesky QR: the caller runs the column kernel instead); chk: the
+// reference's second-pass test, r_kk <= 1e-12 of the column's original norm -> flag = 1.
+constexpr int kCholQrMax = 64;
+__global__ void __launch_bounds__(256) cholqr_kernel(const double *G, int nb, double *Rinv, const double *norms0,
+                                                     int chk, int *ok, int *flag) {
+  __shared__ double a[kCholQrMax * kCholQrMax];
+  __shared__ int bad;
+  const int tid = threadIdx.x;
+  for (int t = tid; t < nb * nb; t += blockDim.x) a[t] = G[t];
+  if (tid == 0) bad = 0;
+  __syncthreads();
+  for (int k = 0; k < nb; ++k) {
+    if (tid == 0) {
+      const double d = a[k + nb * k];
+      if (!(d > 1e-10 * G[k + nb * k])) {
+        bad = 1;
+      } else {
+        a[k + nb * k] = sqrt(d);
+        if (chk && k > 0 && a[k + nb * k] <= 1e-12 * norms0[k]) *flag = 1;
+      }
+    }
+    __syncthreads();
+    if (bad) break;
+    const double rkk = a[k + nb * k];
+    for (int j = k + 1 + tid; j < nb; j += blockDim.x) a[k + nb * j] /= rkk;
+    __syncthreads();
+    const int r = nb - k - 1;
+    for (int t = tid; t < r * r; t += blockDim.x) {
+      const int i = k + 1 + t % r, j = k + 1 + t / r;
+      if (i <= j) a[i + nb * j] -= a[k + nb * i] * a[k + nb * j];
+    }
+    __syncthreads();
+  }
+  if (bad) {
+    if (tid == 0) *ok = 0;
+    return;
+  }
+  for (int j = tid; j < nb; j += blockDim.x) {  // column j of R^-1 by back substitution
+    double *x = Rinv + (int64_t)nb * j;
+    for (int i = nb - 1; i > j; --i) x[i] = 0.0;
+    x[j] = 1.0 / a[j + nb * j];
+    for (int i = j - 1; i >= 0; --i) {
+      double t = 0.0;
+      for (int l = i + 1; l <= j; ++l) t += a[i + nb * l] * x[l];
+      x[i] = -t / a[i + nb * i];
+    }
+  }
+  if (tid == 0) *ok = 1;
+}
+
 // DavidsonSolver::gramschmidt on columns [nstart, ncols) of Q (ld n).
 void gramschmidt(Ctx &x, double *Q, int64_t nstart, int64_t ncols, DeviceBuffer<double> &work,
                  DeviceBuffer<int> &flag) {
@@ -324,6 +377,7 @@ void gramschmidt(Ctx &x, double *Q, int64_t nstart, int64_t ncols, DeviceBuffer<
   double *h = norms + nupdate + 8;        // projection coefficients
   x.coldots(Q + nstart * n, n, nullptr, 0, nupdate, norms0, true);
   VGB_CUDA(cudaMemsetAsync(flag.get(), 0, sizeof(int), x.s));
+  bool column_kernel_ran = false;
   for (int pass = 0; pass < 2; ++pass) {
     if (nstart > 0) {
       // Q_new -= Q_old (Q_old^T Q_new); normalise
@@ -331,6 +385,25 @@ void gramschmidt(Ctx &x, double *Q, int64_t nstart, int64_t ncols, DeviceBuffer<
       x.gemm_nn(Q, n, nstart, h, nstart, nupdate, Q + nstart * n, n, -1.0, 1.0);
       x.coldots(Q + nstart * n, n, nullptr, 0, nupdate, norms, true);
       x.scale_cols(Q + nstart * n, n, nupdate, norms);
+    }
+    if (nstart > 0 && nupdate > 1 && nupdate <= kCholQrMax) {
+      // the block's columns are unit vectors now: Cholesky QR of the block (two FP64 GEMMs and
+      // one small kernel instead of two grid barriers per column)
+      x.gs_part.resize(2 * nupdate * nupdate + n * nupdate + 8);
+      double *G = x.gs_part.get(), *Ri = G + nupdate * nupdate, *T = Ri + nupdate * nupdate;
+      x.gs_err.resize(2);
+      x.gemm_tn(Q + nstart * n, n, nupdate, Q + nstart * n, n, nupdate, G, nupdate, 1.0, 0.0);
+      cholqr_kernel<<<1, 256, 0, x.s>>>(G, (int)nupdate, Ri, norms0, pass == 1 ? 1 : 0, x.gs_err.get() + 1,
+                                        flag.get());
+      VGB_LAUNCH_CHECK();
+      int ok = 0;
+      VGB_CUDA(cudaMemcpyAsync(&ok, x.gs_err.get() + 1, sizeof(int), cudaMemcpyDeviceToHost, x.s));
+      VGB_CUDA(cudaStreamSynchronize(x.s));
+      if (ok) {
+        x.gemm_nn(Q + nstart * n, n, nupdate, Ri, nupdate, nupdate, T, n, 1.0, 0.0);
+        x.copy_cols(T, n, Q + nstart * n, n, nupdate);
+        continue;
+      }
     }
     if (ncols - nstart > 1) {
       VGB_REQUIRE(ncols - nstart <= kGsMaxRange, "Gram-Schmidt: too many new columns in one step");
@@ -352,11 +425,12 @@ void gramschmidt(Ctx &x, double *Q, int64_t nstart, int64_t ncols, DeviceBuffer<
       int *fl = flag.get(), *er = x.gs_err.get();
       void *args[] = {&Qp, &nn, &ns, &nc, &chk, &norms0, &pp, &np, &bc, &bg, &fl, &er};
       VGB_CUDA(cudaLaunchCooperativeKernel((void *)gs_columns_kernel, dim3(nb), dim3(kGsThreads), args, 0, x.s));
+      column_kernel_ran = true;
     }
   }
   int hflag[2] = {0, 0};
   VGB_CUDA(cudaMemcpyAsync(&hflag[0], flag.get(), sizeof(int), cudaMemcpyDeviceToHost, x.s));
-  if (ncols - nstart > 1)
+  if (column_kernel_ran)
     VGB_CUDA(cudaMemcpyAsync(&hflag[1], x.gs_err.get(), sizeof(int), cudaMemcpyDeviceToHost, x.s));
   VGB_CUDA(cudaStreamSynchronize(x.s));
   if (hflag[1]) fail(BSE_ERR_TIMEOUT, "Gram-Schmidt: grid barrier gave up");
