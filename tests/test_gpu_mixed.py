@@ -8,8 +8,10 @@ from votca_gb300.synthetic import Problem
 pytestmark = pytest.mark.gpu
 
 # BF16x3 split products with FP32 accumulation: ~1e-5 relative on the
-# interaction part of the product (Hx, Hd, Hd2); Hqp is exact FP64.
-REL_TOL = 2e-4
+# interaction part of the product (Hx, Hd, Hd2; measured 0.5-1.2e-5 on these shapes and at the
+# headline size); Hqp is exact FP64.  A few times the measured error, so that a regression of the
+# split arithmetic (a dropped product, a longer FP32 chain) fails.
+REL_TOL = 5e-5
 
 
 def contexts(p, vt, ct, voff=0):
@@ -43,6 +45,7 @@ def test_mixed_matches_fp64(v, c, naux, nmo, voff, seed):
         yf = bo.BSE_OPERATOR(f, *oracle.OPERATORS[op]).matmul(X)
         ym = bo.BSE_OPERATOR(m, *oracle.OPERATORS[op]).matmul(X)
         err = np.linalg.norm(ym - yf) / np.linalg.norm(yf)
+        print(f"mixed {op}: {err:.2e}")
         assert err < REL_TOL, (op, err)
     hq = bo.HqpOperator(f).matmul(X)
     for op in ("singlet", "triplet", "singlet_b"):
@@ -50,6 +53,7 @@ def test_mixed_matches_fp64(v, c, naux, nmo, voff, seed):
         ym = bo.BSE_OPERATOR(m, *oracle.OPERATORS[op]).matmul(X)
         inter = yf - (hq if oracle.OPERATORS[op][0] else 0)
         err = np.linalg.norm(ym - yf) / np.linalg.norm(inter)
+        print(f"mixed {op}: {err:.2e}")
         assert err < REL_TOL, (op, err)
 
 
@@ -83,6 +87,7 @@ def test_mixed_long_aux_products(v, c, naux, seed):
         ym = bo.BSE_OPERATOR(m, *oracle.OPERATORS[op]).matmul(X)
         inter = yf - (hq if oracle.OPERATORS[op][0] else 0)
         err = np.linalg.norm(ym - yf) / np.linalg.norm(inter)
+        print(f"mixed {op}: {err:.2e}")
         assert err < REL_TOL, (op, err)
 
 
