@@ -384,7 +384,10 @@ int bse_small_gen_eig(int64_t m, int64_t nw, const double *T, const double *B, d
  *                   outside the BSE window are zero;
  *   grad_hqp:       (vt+ct) x (vt+ct) column-major gradient of the Hqp window;
  *   grad_screening: auxsize (diagonal epsilon_0_inv) or auxsize^2 (dense W).
- * Any output may be NULL.  Computed in FP64 on the device. */
+ * Any output may be NULL.  Computed on the device: in FP64 for FP64 handles; handles with a
+ * tensor-core engine (BSE_PRECISION_MIXED / _SLICED) form the two cc-block contractions
+ * (2 Naux v c^2 flops per vector each) as FP64-accurate slice products (about 1e-10 of each
+ * gradient block's norm from the FP64 gradient), the rest in FP64. */
 int bse_op_eig_gradient(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd,
                         int32_t cd2, const double *X, int64_t ldx,
                         int64_t nroots, const double *weights,
@@ -401,7 +404,7 @@ int bse_op_eig_gradient(bse_handle *h, int32_t cqp, int32_t cx, int32_t cd,
  * X^T (dB + dB^T) Y, the first-order change seen through the left eigenvector J z.
  * X, Y: host, dim x nroots (ldx); outputs as
  * bse_op_eig_gradient; grad_mmn also carries the entries M(c, v, P) that the Hd2 term of B reads.
- * Computed in FP64 on the device. */
+ * Computed on the device, with the precision rule of bse_op_eig_gradient. */
 int bse_op_eig_gradient_full(bse_handle *h, const int32_t a_coef[4], const int32_t b_coef[4],
                              const double *X, const double *Y, int64_t ldx, int64_t nroots,
                              const double *weights, double *grad_mmn, double *grad_hqp,

@@ -286,3 +286,41 @@ def test_device_gradient_blocks_match_host_gradient():
         np.testing.assert_allclose(cc.reshape(NAUX, C, C), gm[V:V + C, :, V:V + C].transpose(1, 0, 2), atol=1e-13)
         np.testing.assert_allclose(hh[:(V + C) ** 2].reshape((V + C, V + C), order="F"), gh, atol=1e-13)
         np.testing.assert_allclose(ww[:NAUX], gw, atol=1e-13)
+
+
+@pytest.mark.parametrize("prec", ["mixed", "sliced"])
+def test_tensor_core_adjoint_matches_fp64(prec):
+    """Handles with a tensor-core engine form the two cc-block contractions of the gradient as
+    FP64-accurate slice products: the same gradient as the FP64 handle to about 1e-10 of each
+    block's scale (singlet and triplet coefficient sets, 4 vectors, dense enough to exercise the
+    chunking of the vectors)."""
+    from votca_gb300 import bse_operator as bo
+
+    v, c, naux = 12, 80, 150
+    p = Problem(v=v, c=c, naux=naux, nmo=v + c, seed=17)
+    opt = bo.BSEOperator_Options(homo=v - 1, rpamin=0, qpmin=0, vmin=0, cmax=v + c - 1)
+    M = bo.TCMatrix_gwbse(p.mmn)
+    f = bo.GpuBSEContext(p.w, M, p.hqp, opt, precision=bo.PRECISION_FP64)
+    t = bo.GpuBSEContext(p.w, M, p.hqp, opt,
+                         precision=bo.PRECISION_MIXED if prec == "mixed" else bo.PRECISION_SLICED)
+    rng = np.random.default_rng(3)
+    X = np.asfortranarray(rng.standard_normal((v * c, 4)))
+    X /= np.linalg.norm(X, axis=0)
+    g = np.array([1.0, -0.5, 0.7, 0.3])
+    nh = v + c
+    for coef in ((1, 2, 1, 0), (1, 0, 1, 0)):
+        out = []
+        for ctx in (f, t):
+            gm = np.zeros(p.mmn.shape)
+            gh = np.zeros((nh, nh), order="F")
+            gw = np.zeros(p.w.shape)
+            from votca_gb300 import _lib
+            _lib.check(ctx._L.bse_op_eig_gradient(ctx.handle, *coef, bo._p(X), X.shape[0], 4, bo._p(g),
+                                                  bo._p(gm), bo._p(gh), bo._p(gw)))
+            out.append((gm, gh, gw))
+        for a, b, name in zip(out[0], out[1], ("mmn", "hqp", "w")):
+            err = np.linalg.norm(b - a) / max(np.linalg.norm(a), 1e-300)
+            print(f"{prec} {coef} {name}: {err:.2e}")
+            assert err < 1e-9, (coef, name, err)
+    f.close()
+    t.close()

@@ -32,6 +32,7 @@
 #include <vector>
 
 #include "bse_ops.cuh"
+#include "tc_engine.cuh"
 
 namespace vgb {
 
@@ -194,22 +195,44 @@ void BseOperator::quad_gradient(const Coef &c, const double *X, int64_t ldx, int
     o.alpha = 2.0 * c.cx; o.beta = 1.0;
     dgemm(o, s, &ws);
   }
+  // Handles with a tensor-core engine (split-precision or slice-product handles) run the two
+  // contractions of the cc block, 2 Naux v c^2 flops per vector each, as FP64-accurate slice
+  // products (about 2e-10 of their scale); FP64 handles keep FP64 throughout.
+  const bool sliced = mixed != nullptr;
+  // vectors per slice-product chunk: the intermediates (Naux dim doubles per vector) within 4 GB
+  const int64_t kch = std::max<int64_t>(1, std::min<int64_t>(nr, (4LL << 30) / (naux * dim * 8)));
   if (c.cd != 0 && (gMvv || gMcc || gW)) {
     const double cd = c.cd;
-    DeviceBuffer<double> Sk(naux * dim), Q(naux * vt * vt);
+    DeviceBuffer<double> Sk(sliced ? kch * naux * dim : naux * dim), Q(naux * vt * vt);
     // ---- Q^P = sum_k g_k X_k S_k^P^T ----
     for (int64_t k = 0; k < nr; ++k) {
-      GemmDesc a;  // S_k[P](c1, v) = sum_c Mcc_P(c1, c) X_k(c, v)
-      a.M = ct; a.N = vt; a.K = ct;
-      a.A = Mcc.get(); a.a_rs = 1; a.a_cs = ct;
-      a.B = X + k * ldx; a.b_rs = 1; a.b_cs = ct;
-      a.C = Sk.get(); a.c_rs = 1; a.c_cs = ct;
-      a.nb1 = naux; a.a_b1 = ct * ct; a.c_b1 = dim;
-      dgemm(a, s, &ws);
+      const double *Skp = Sk.get();
+      if (!sliced) {
+        GemmDesc a;  // S_k[P](c1, v) = sum_c Mcc_P(c1, c) X_k(c, v)
+        a.M = ct; a.N = vt; a.K = ct;
+        a.A = Mcc.get(); a.a_rs = 1; a.a_cs = ct;
+        a.B = X + k * ldx; a.b_rs = 1; a.b_cs = ct;
+        a.C = Sk.get(); a.c_rs = 1; a.c_cs = ct;
+        a.nb1 = naux; a.a_b1 = ct * ct; a.c_b1 = dim;
+        dgemm(a, s, &ws);
+      } else {
+        if (k % kch == 0) {  // S of the next kch vectors, [k][P][v][c1], as one slice product
+          const int64_t kc = std::min(kch, nr - k);
+          SplitMap xm;  // rows (k, v), columns c
+          xm.rdiv = vt; xm.rs1 = ldx; xm.rs2 = ct; xm.cs = 1; xm.rlim = vt;
+          TcEpilogue e;
+          e.kind = TcEpilogue::AXPBY_F64;
+          e.rd = vt; e.ro1 = naux * dim; e.ro2 = ct; e.rlim = vt;
+          e.cd = ct; e.co1 = dim; e.co2 = 1; e.clim = ct;
+          e.out_f64 = Sk.get(); e.alpha = 1.0; e.beta = 0.0;
+          mixed->gemm_sliced(*this, X + k * ldx, xm, kc * vt, nullptr, SplitMap(), naux * ct, ct, true, e, s);
+        }
+        Skp = Sk.get() + (k % kch) * naux * dim;
+      }
       GemmDesc q;  // Q[P](v, v') += g_k sum_c X_k(v, c) S_k[P](c, v')
       q.M = vt; q.N = vt; q.K = ct;
       q.A = X + k * ldx; q.a_rs = ct; q.a_cs = 1;
-      q.B = Sk.get(); q.b_rs = 1; q.b_cs = ct; q.b_b1 = dim;
+      q.B = Skp; q.b_rs = 1; q.b_cs = ct; q.b_b1 = dim;
       q.C = Q.get(); q.c_rs = vt; q.c_cs = 1; q.c_b1 = vt * vt;
       q.nb1 = naux; q.alpha = gh[k]; q.beta = k > 0 ? 1.0 : 0.0;
       dgemm(q, s, &ws);
@@ -244,7 +267,36 @@ void BseOperator::quad_gradient(const Coef &c, const double *X, int64_t ldx, int
         dgemm(d, s, &ws);
       }
     }
-    if (gMcc) {
+    if (gMcc && sliced) {
+      // gMcc[(P, c)][c'] += -cd sum_{(k, v)} (g_k X_k(v, c)) T[(P, c')][(k, v)] as one slice product
+      // per chunk of vectors, T = G^P X_k from FP64 GEMMs
+      for (int64_t k0 = 0; k0 < nr; k0 += kch) {
+        const int64_t kc = std::min(kch, nr - k0), Kt = kc * vt;
+        DeviceBuffer<double> T(naux * ct * Kt), Xg(Kt * ct);
+        for (int64_t k = k0; k < k0 + kc; ++k) {
+          GemmDesc t;  // T[(P, c')][(k, v)] = sum_v' Gvv[v][P][v'] X_k(v', c')
+          t.M = vt; t.N = ct; t.K = vt;
+          t.A = Gvv.get(); t.a_rs = naux * vt; t.a_cs = 1; t.a_b1 = vt;
+          t.B = X + k * ldx; t.b_rs = ct; t.b_cs = 1;
+          t.C = T.get() + (k - k0) * vt; t.c_rs = 1; t.c_cs = Kt; t.c_b1 = ct * Kt;
+          t.nb1 = naux;
+          dgemm(t, s, &ws);
+        }
+        copy_cols(X + k0 * ldx, ldx, dim, kc, Xg.get(), dim, s);  // Xg[(k, v)][c] = g_k X_k(v, c)
+        scale_cols_by_kernel<<<gfor(dim * kc), 256, 0, s>>>(Xg.get(), dim, dim, kc, g.get() + k0);
+        VGB_LAUNCH_CHECK();
+        SplitMap tm;  // rows (P, c'), columns (k, v)
+        tm.rdiv = 1; tm.rs1 = Kt; tm.rs2 = 0; tm.cs = 1; tm.rlim = 1;
+        SplitMap xm;  // rows c, columns (k, v): Xg[(k, v) ct + c]
+        xm.rdiv = 1; xm.rs1 = 1; xm.rs2 = 0; xm.cs = ct; xm.rlim = 1;
+        TcEpilogue e;  // gMcc[(P ct + c) ct + c'] for row (P, c'), column c
+        e.kind = TcEpilogue::AXPBY_F64;
+        e.rd = ct; e.ro1 = ct * ct; e.ro2 = 1; e.rlim = ct;
+        e.cd = ct; e.co2 = ct; e.clim = ct;
+        e.out_f64 = gMcc; e.alpha = -cd; e.beta = 1.0;
+        mixed->gemm_sliced(*this, T.get(), tm, naux * ct, Xg.get(), xm, ct, Kt, false, e, s);
+      }
+    } else if (gMcc) {
       // gMcc[P][c][c'] += -cd sum_k g_k sum_v X_k(v, c) T_k[P](v, c'),  T_k[P] = G^P X_k
       for (int64_t k = 0; k < nr; ++k) {
         GemmDesc t;  // T[P](v, c') = sum_v' Gvv[v][P][v'] X_k(v', c')

@@ -124,7 +124,7 @@ struct MixedEngine::Impl {
   int64_t Kc = 0, Kg = 0, Kn = 0, dimP = 0;
   SplitBuf Mcc2, G2, Bvc2, BvcT, McvT;
   // Ozaki slice planes of the FP64-equivalent products (apply_sliced), built on first use
-  Planes pMcc, pG2, pBvc2, pBvcT, pMcvT, pX, pZ, pT;
+  Planes pMcc, pG2, pBvc2, pBvcT, pMcvT, pX, pZ, pT, pA, pB;
   DeviceBuffer<double> fZ, fT, gpart;
   SplitBuf Xs, S, U, Zs;
   DeviceBuffer<float> part;
@@ -608,6 +608,41 @@ void MixedEngine::apply_sliced(BseOperator &op, const Coef &c, const double *X, 
     }
     acc = true;
   }
+}
+
+void MixedEngine::gemm_sliced(BseOperator &op, const double *A, const SplitMap &am, int64_t M, const double *B,
+                              const SplitMap &bm, int64_t N, int64_t K, bool mcc_as_b, const TcEpilogue &e,
+                              cudaStream_t s) {
+  Impl &m = *impl_;
+  read_tuning();
+  if (M <= 0 || N <= 0 || K <= 0) return;
+  VGB_REQUIRE(e.kind == TcEpilogue::AXPBY_F64, "gemm_sliced: FP64 epilogue expected");
+  const int nsl = g_slices;
+  const int64_t Kp = pad64(K), chain = slice_chain(Kp);
+  const uint16_t *bp;
+  int64_t bplane;
+  if (mcc_as_b) {
+    VGB_REQUIRE(K == m.ct && N == m.naux * m.ct, "gemm_sliced: cc block shape");
+    if (!(m.pMcc.nsl == nsl && m.pMcc.rows == m.naux * m.ct && m.pMcc.ld == m.Kc)) {
+      SplitMap a;  // Mcc planes [(P, c1)][c]
+      a.rdiv = m.ct; a.rs1 = m.ct * m.ct; a.rs2 = 1; a.cs = m.ct; a.rlim = m.ct;
+      m.pMcc.ensure(m.naux * m.ct, m.Kc, nsl, s);
+      slice_f64(op.Mcc.get(), m.naux * m.ct, m.ct, a, nsl, chain, m.pMcc.get(), m.Kc, m.pMcc.plane(), s);
+    }
+    bp = m.pMcc.get();
+    bplane = m.naux * m.ct;
+  } else {
+    m.pB.ensure(N, Kp, nsl, s);
+    slice_f64(B, N, K, bm, nsl, chain, m.pB.get(), Kp, m.pB.plane(), s);
+    bp = m.pB.get();
+    bplane = N;
+  }
+  m.pA.ensure(M, Kp, nsl, s);
+  slice_f64(A, M, K, am, nsl, chain, m.pA.get(), Kp, m.pA.plane(), s);
+  const int bn = N > 32 ? 64 : 32;
+  TcMat Am = make_tc_mat(m.pA.get(), m.pA.get(), nsl * M, Kp, Kp, 128, 64);
+  TcMat Bm = make_tc_mat(bp, bp, nsl * bplane, Kp, Kp, bn, 64);
+  sliced_gemm(Am, M, Bm, bplane, M, N, Kp, chain, nsl, bn, e, m.gpart, m.err.get(), s);
 }
 
 namespace {

@@ -2,6 +2,7 @@
 #pragma once
 
 #include "bse_ops.cuh"
+#include "tc_gemm.cuh"
 
 namespace vgb {
 
@@ -22,6 +23,13 @@ class MixedEngine {
   // five digits the result agrees with the FP64 product to about 1e-11 of its scale.
   void apply_sliced(BseOperator &op, const Coef &c, const double *X, int64_t ldx, int64_t k, double *Y,
                     int64_t ldy, bool accumulate, cudaStream_t s);
+  // FP64-accurate GEMM of FP64 operands on the tensor cores (the slice products of
+  // apply_sliced): C(i, n) = sum_q A(i, q) B(n, q) for i < M, n < N, q < K, elements read through
+  // the split maps (row i of A at am, row n of B at bm, column q), result through the FP64
+  // epilogue e (AXPBY_F64).  mcc_as_b: B is the operator's cc block [(P, c1)][c] (its digit planes
+  // are built once and kept; bm is then ignored).
+  void gemm_sliced(BseOperator &op, const double *A, const SplitMap &am, int64_t M, const double *B,
+                   const SplitMap &bm, int64_t N, int64_t K, bool mcc_as_b, const TcEpilogue &e, cudaStream_t s);
   // The same for many operators at once (GroupedItem.op->mixed engines), one grouped
   // launch per stage and tile shape; accumulate: Y already holds the Hqp term.
   static void apply_grouped(const Coef &c, const std::vector<GroupedItem> &items, bool accumulate,
