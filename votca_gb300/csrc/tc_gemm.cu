@@ -418,7 +418,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
     constexpr int COLS = BN >= 64 ? BN / 2 : BN;
     const int cbeg = (BN >= 64 || half == 0) ? half * COLS : BN;
     const int cend = (BN >= 64 || half == 0) ? cbeg + COLS : BN;
-    // FP64 sums over the K splits of a tile (kacc; BN <= 64: at most 32 columns per thread)
+    // float-pair sums over the K splits of a tile (kacc; BN <= 64: at most 32 columns per thread)
     constexpr int KACC = BN <= 64 ? 32 : 1;
     double kv[KACC];
     int buf = 0;
@@ -447,32 +447,26 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
             uint32_t r[32];
             tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + cbeg), r);
             const int64_t sg = u;  // position inside the split group (an item is one group)
-            const bool pairs = p.products == 1;
-            if (pairs) {
-              // slice mode: each split's FP32 sum is exact; the splits are added as an unevaluated
-              // pair of floats (Knuth's TwoSum, error-free), held in the bits of kv[j] (hi, lo):
-              // no FP64 instruction per split
+            // The splits' FP32 sums are added as an unevaluated pair of floats (Knuth's TwoSum,
+            // error-free; about 48 significant bits), held in the bits of kv[j] (hi, lo): no FP64
+            // instruction per split (the FP64 pipe of GB300 runs at 2 operations per clock and
+            // SM).  In slice mode every split sum is exact, so the result is the exact sum of
+            // the splits to that precision.
 #pragma unroll
-              for (int j = 0; j < 32; ++j) {
-                const float x = __uint_as_float(r[j]);
-                float hi = 0.f, lo = 0.f;
-                if (sg != 0) {
-                  hi = __int_as_float(__double2hiint(kv[j]));
-                  lo = __int_as_float(__double2loint(kv[j]));
-                }
-                const float sum = hi + x;
-                const float bb = sum - hi;
-                lo += (hi - (sum - bb)) + (x - bb);
-                kv[j] = __hiloint2double(__float_as_int(sum), __float_as_int(lo));
+            for (int j = 0; j < 32; ++j) {
+              const float x = __uint_as_float(r[j]);
+              float hi = 0.f, lo = 0.f;
+              if (sg != 0) {
+                hi = __int_as_float(__double2hiint(kv[j]));
+                lo = __int_as_float(__double2loint(kv[j]));
               }
-            } else {
-#pragma unroll
-              for (int j = 0; j < 32; ++j)
-                kv[j] = (sg == 0 ? 0.0 : kv[j]) + (double)__uint_as_float(r[j]);
+              const float sum = hi + x;
+              const float bb = sum - hi;
+              lo += (hi - (sum - bb)) + (x - bb);
+              kv[j] = __hiloint2double(__float_as_int(sum), __float_as_int(lo));
             }
             if (row_ok && sg == p.spg - 1) {
-              // the K splits summed in FP64 (or as float pairs) in split order, as the reduction
-              // kernel does
+              // the K splits summed in split order
               int64_t n = tc.n * BN + cbeg, nq = n / e.cd, nr = n % e.cd;
 #pragma unroll
               for (int j = 0; j < 32; ++j) {
@@ -482,9 +476,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
                     reinterpret_cast<float2 *>(e.out_f32)[off] =
                         make_float2(__int_as_float(__double2hiint(kv[j])), __int_as_float(__double2loint(kv[j])));
                   } else {
-                    const double val = pairs ? (double)__int_as_float(__double2hiint(kv[j])) +
-                                                   (double)__int_as_float(__double2loint(kv[j]))
-                                             : kv[j];
+                    const double val = (double)__int_as_float(__double2hiint(kv[j])) +
+                                       (double)__int_as_float(__double2loint(kv[j]));
                     if (e.kind == TcEpilogue::AXPBY_F64) {
                       double *y = e.out_f64 + off;
                       const double rv = e.alpha * val;
