@@ -24,7 +24,10 @@ struct Cfg {
   static constexpr int B_BYTES = BN * BK * 2;
   static constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
   static constexpr int STAGES = kSmemRing / STAGE_BYTES > 8 ? 8 : kSmemRing / STAGE_BYTES;
-  static constexpr int TMEM_COLS = 2 * BN < 32 ? 32 : 2 * BN;  // two accumulators
+  // accumulator buffers in TMEM: four for the narrow tiles (short K splits: the epilogue of a
+  // split may lag the MMAs of the next three), two for the wide ones
+  static constexpr int NBUF = BN <= 64 ? 4 : 2;
+  static constexpr int TMEM_COLS = NBUF * BN < 32 ? 32 : NBUF * BN;
   static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
   static constexpr uint32_t SBO = BK == 64 ? 1024 : 512;     // 8 rows of one swizzle atom
   static constexpr uint64_t LAYOUT = BK == 64 ? 2 : 4;       // SWIZZLE_128B / SWIZZLE_64B
@@ -261,8 +264,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
   uint64_t *full = (uint64_t *)(smem + C::STAGES * C::STAGE_BYTES);
   uint64_t *empty = full + C::STAGES;
   uint64_t *accf = empty + C::STAGES;
-  uint64_t *acce = accf + 2;
-  uint32_t *tmem_slot = (uint32_t *)(acce + 2);
+  uint64_t *acce = accf + C::NBUF;
+  uint32_t *tmem_slot = (uint32_t *)(acce + C::NBUF);
   volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
@@ -271,7 +274,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
       mbar_init(&full[i], 1);
       mbar_init(&empty[i], 1);
     }
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < C::NBUF; ++i) {
       mbar_init(&accf[i], 1);
       mbar_init(&acce[i], kEpiWarps);  // one arrive per epilogue warp
     }
@@ -404,7 +407,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
             if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
           }
           mma_commit(&accf[buf]);  // accumulator ready for the epilogue
-          if (++buf == 2) { buf = 0; aphase ^= 1; }
+          if (++buf == C::NBUF) { buf = 0; aphase ^= 1; }
         }
       }
     mma_done:;
@@ -495,7 +498,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
           fence_before();
           __syncwarp();
           if (lane == 0) mbar_arrive(&acce[buf]);
-          if (++buf == 2) { buf = 0; aphase ^= 1; }
+          if (++buf == C::NBUF) { buf = 0; aphase ^= 1; }
           continue;
         }
       }
@@ -547,7 +550,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
       fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&acce[buf]);
-      if (++buf == 2) { buf = 0; aphase ^= 1; }
+      if (++buf == C::NBUF) { buf = 0; aphase ^= 1; }
       }
     }
   epi_done:;
