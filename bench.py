@@ -493,10 +493,28 @@ def batched_solve(n_molecules, nthreads, roots=5, tol=1e-7, cpu=False):
         "lockstep_vs_threads_max_abs_diff_eV": float(np.max(np.abs(ev - evt))),
         "threads_match_one_thread": bool(np.array_equal(evt[:ns], ev1)),
         "dims": [int(s["v"] * s["c"]) for s in shapes[:4]] + ["..."],
+        "autotune": autotune_table(),
+        "autotune_note": "launch shapes of the grouped dense products, chosen by timing every candidate "
+                         "([K box, operators per launch, ms]) on the first solve's first product round "
+                         "(included in first_solve_seconds)",
     }
     if cpu:
         out["cpu_baseline"] = cpu_baseline_batched(shapes, roots, tol)
     return out
+
+
+def autotune_table():
+    """The launch shapes the library's autotuner chose in this process (bse_autotune_report)."""
+    import ctypes
+
+    from votca_gb300 import _lib
+
+    L = _lib.load()
+    need = ctypes.c_int64(0)
+    _lib.check(L.bse_autotune_report(None, 0, ctypes.byref(need)))
+    buf = ctypes.create_string_buffer(max(int(need.value), 1))
+    _lib.check(L.bse_autotune_report(buf, len(buf), None))
+    return json.loads(buf.value.decode() or "[]")
 
 
 def full_bse_report(roots=10, tol=1e-7, k=32, check=False, cpu=False):

@@ -373,6 +373,14 @@ int bse_small_sym_eig(int64_t njobs, const int64_t *m, const int64_t *nw, const 
 int bse_small_gen_eig(int64_t m, int64_t nw, const double *T, const double *B, double *evals,
                       double *evecs, int64_t *selected);
 
+/* The launch shapes the autotuner has chosen in this process (no counterpart in the reference):
+ * a JSON array, one object per tuned kernel and tile width, with the chosen shape and every
+ * candidate's measured time ([K box, operators per launch, ms]).  The grouped dense products of
+ * the lockstep batch are tuned on their first product round with at least 16 operators
+ * (environment VGB_TC_AUTOTUNE=0 keeps the fixed shape).  buf (may be NULL) receives at most
+ * cap - 1 characters and a terminating zero; *needed (may be NULL) the full length + 1. */
+int bse_autotune_report(char *buf, int64_t cap, int64_t *needed);
+
 /* ---- Adjoint (no counterpart in the reference; its forward twin is the
  * expectation-value analysis x^T H_part x of xtp/src/libxtp/gwbse/bse.cc:490-520) ----
  *

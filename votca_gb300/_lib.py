@@ -96,6 +96,7 @@ SIGNATURES = {
     "bse_small_sym_eig": (c_i32, [c_i64, ctypes.POINTER(c_i64), ctypes.POINTER(c_i64), c_dp, c_dp, c_dp,
                                   ctypes.POINTER(c_i64)]),
     "bse_small_gen_eig": (c_i32, [c_i64, c_i64, c_dp, c_dp, c_dp, c_dp, ctypes.POINTER(c_i64)]),
+    "bse_autotune_report": (c_i32, [ctypes.c_char_p, c_i64, ctypes.POINTER(c_i64)]),
     "bse_last_error": (ctypes.c_char_p, []),
     "bse_version": (ctypes.c_char_p, []),
 }

@@ -12,6 +12,7 @@
 #include "batch_davidson.cuh"
 #include "davidson.cuh"
 #include "small_eig.cuh"
+#include "tc_engine.cuh"
 #include "uks_ops.cuh"
 
 struct bse_handle {
@@ -682,6 +683,18 @@ int bse_small_sym_eig(int64_t njobs, const int64_t *m, const int64_t *nw, const 
     if (phase_cycles)
       for (int64_t i = 0; i < njobs; ++i)
         for (int p = 0; p < 4; ++p) phase_cycles[4 * i + p] = clk[5 * i + p + 1] - clk[5 * i + p];
+  });
+}
+
+int bse_autotune_report(char *buf, int64_t cap, int64_t *needed) {
+  return guarded([&] {
+    const std::string r = vgb::autotune_report();
+    if (needed) *needed = (int64_t)r.size() + 1;
+    if (buf && cap > 0) {
+      const size_t n = std::min<size_t>((size_t)cap - 1, r.size());
+      memcpy(buf, r.data(), n);
+      buf[n] = 0;
+    }
   });
 }
 

@@ -19,7 +19,9 @@
 #include "tc_engine.cuh"
 
 #include <cstdlib>
+#include <array>
 #include <map>
+#include <string>
 #include <tuple>
 #include <mutex>
 
@@ -50,6 +52,7 @@ struct SplitBuf {
 };
 
 int g_slices = 5;  // Ozaki digits per operand (7 bits each; pairs up to the 5th digit level)
+int g_autotune = 1;  // VGB_TC_AUTOTUNE=0: grouped dense products with the fixed shape (K box 64, 32 per launch)
 int g_bk256 = 32;  // K box of the BN = 256 tiles (4-stage ring); 64 gives a 2-stage ring
 int bk_for(int bn) { return bn == 256 ? g_bk256 : 64; }
 
@@ -86,6 +89,7 @@ void read_tuning() {
     if (const char *e = getenv("VGB_TC_S_BUDGET_GB")) g_s_budget = std::max(1LL, atoll(e)) << 30;
     if (const char *e = getenv("VGB_TC_DENSE_CHAIN")) g_dense_chain = std::max(64LL, atoll(e));
     if (const char *e = getenv("VGB_TC_SLICES")) g_slices = std::max(2, std::min(5, atoi(e)));
+    if (const char *e = getenv("VGB_TC_AUTOTUNE")) g_autotune = atoi(e) != 0;
   });
 }
 
@@ -657,10 +661,10 @@ struct GemmBuckets {
     owner[key].push_back(item);
   }
   // launches every bucket; ks[item] = K splits of that item's problem
-  void run(int *err, cudaStream_t s, std::vector<int> &ks) {
+  void run(int *err, cudaStream_t s, std::vector<int> &ks, int group_max = 32) {
     for (auto &kv : by_shape) {
       std::vector<int> k(kv.second.size(), 0);
-      tc_gemm_grouped(kv.second, kv.first / 1000, err, s, k.data());
+      tc_gemm_grouped(kv.second, kv.first / 1000, err, s, k.data(), group_max);
       const auto &own = owner[kv.first];
       for (size_t i = 0; i < own.size(); ++i) ks[own[i]] = k[i];
     }
@@ -869,8 +873,49 @@ void MixedEngine::build_dense_grouped(const std::vector<BseOperator *> &ops, con
   }
 }
 
+namespace {
+
+// Empirical choice of the launch shape of the grouped dense products (the dominant launch of
+// the lockstep batch): on the first product round with at least 16 operators of a tile width,
+// every candidate (K box 32 or 64 bf16 elements, 8, 16 or 32 operators per launch) runs the
+// whole round twice into scratch outputs and the second run is timed with events; the fastest
+// is kept for the process.  The candidates compute identical numbers (the same FP32 chains in
+// the same order), so the choice affects time only.
+struct DenseTuning {
+  bool done = false;
+  int bk = 64, group = 32;
+  std::vector<std::array<double, 3>> table;  // bk, group, ms
+};
+std::mutex g_tune_mu;
+std::map<int, DenseTuning> g_dense_tuning;  // by tile width
+
+}  // namespace
+
+std::string autotune_report() {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  std::string out = "[";
+  bool first = true;
+  for (const auto &kv : g_dense_tuning) {
+    if (!kv.second.done) continue;
+    if (!first) out += ", ";
+    first = false;
+    out += "{\"kernel\": \"grouped dense product\", \"bn\": " + std::to_string(kv.first) +
+           ", \"chosen\": {\"bk\": " + std::to_string(kv.second.bk) + ", \"operators_per_launch\": " +
+           std::to_string(kv.second.group) + "}, \"candidates_ms\": [";
+    for (size_t i = 0; i < kv.second.table.size(); ++i) {
+      const auto &t = kv.second.table[i];
+      char buf[96];
+      snprintf(buf, sizeof(buf), "%s[%d, %d, %.4f]", i ? ", " : "", (int)t[0], (int)t[1], t[2]);
+      out += buf;
+    }
+    out += "]}";
+  }
+  return out + "]";
+}
+
 void MixedEngine::apply_dense_grouped(const Coef &c, const std::vector<GroupedItem> &items, bool accumulate,
                                       cudaStream_t s) {
+  read_tuning();
   const size_t n = items.size();
   if (n == 0) return;
   std::vector<Impl *> eng(n);
@@ -892,46 +937,107 @@ void MixedEngine::apply_dense_grouped(const Coef &c, const std::vector<GroupedIt
   }
   split_grouped(jobs, s);
   // Y[I + j ldy] (+)= (H X)(I, j).  With BN <= 64 a CTA runs all K splits of its tile and sums
-  // their FP32 chains in FP64 registers, writing Y directly; otherwise FP32 partials
-  // [split][j][I] are summed in FP64 by a reduction launch (the same sums in the same order).
+  // their FP32 chains on the CTA, writing Y directly; otherwise FP32 partials [split][j][I] are
+  // summed in FP64 by a reduction launch.
   std::vector<TcProblem> pr(n);
   std::vector<int> ks(n, 0);
   std::vector<char> direct(n, 0);
-  GemmBuckets b;
   // largest operators first: their long work items start early and the small ones fill the
   // tail of each launch
   std::vector<size_t> order(n);
   for (size_t i = 0; i < n; ++i) order[i] = i;
   std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return eng[x]->dim > eng[y]->dim; });
-  for (size_t i : order) {
-    Impl &m = *eng[i];
-    const GroupedItem &it = items[i];
-    const int bn = pick_bn(it.k);
-    TcProblem &q = pr[i];
-    q.A = m.mat(m.Hdense.hi.get(), m.Hdense.lo.get(), m.dim, m.Kd, 128, bk_for(bn));
-    q.B = m.mat(m.Xd.hi.get(), m.Xd.lo.get(), (int64_t)m.Xd.hi.count / m.Kd, m.Kd, bn, bk_for(bn));
-    q.shape.M = m.dim; q.shape.N = it.k; q.shape.K = m.Kd; q.shape.products = g_products;
-    direct[i] = (g_kacc && bn <= 64) ? 1 : 0;
-    if (direct[i]) {
-      // in-CTA accumulation adds no parallelism: only the chain bound sets the splits
-      q.shape.ksplit = (int)ceil_div(m.Kd, g_dense_chain);
-      q.shape.kacc = true;
-      q.epi.kind = TcEpilogue::AXPBY_F64;
-      q.epi.rd = m.dim; q.epi.ro2 = 1; q.epi.rlim = m.dim;
-      q.epi.cd = it.k; q.epi.co2 = it.ldy; q.epi.clim = it.k;
-      q.epi.out_f64 = it.Y; q.epi.alpha = 1.0; q.epi.beta = accumulate ? 1.0 : 0.0;
-    } else {
-      q.shape.ksplit = pick_ksplit(ceil_div(m.dim, 128) * ceil_div(it.k, bn), m.Kd, g_dense_chain);
-      m.part.resize((size_t)q.shape.ksplit * m.dim * it.k);
-      q.epi.kind = TcEpilogue::STORE_F32;
-      q.epi.rd = m.dim; q.epi.ro2 = 1; q.epi.rlim = m.dim;
-      q.epi.cd = it.k; q.epi.co2 = m.dim; q.epi.clim = it.k;
-      q.epi.so = m.dim * it.k;
-      q.epi.out_f32 = m.part.get();
-    }
-    b.add(&q, bn, i);
+  int bn_all = 0;  // the tile width when every item has the same one and accumulates on the CTA
+  bool tunable = g_autotune && n >= 16;
+  for (size_t i = 0; i < n; ++i) {
+    const int bn = pick_bn(items[i].k);
+    tunable = tunable && g_kacc && bn <= 64 && (bn_all == 0 || bn == bn_all);
+    bn_all = bn;
   }
-  b.run(err, s, ks);
+  int use_bk = 0, use_group = 32;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_dense_tuning.find(bn_all);
+    if (it != g_dense_tuning.end() && it->second.done) {
+      use_bk = it->second.bk;
+      use_group = it->second.group;
+      tunable = false;
+    }
+  }
+  // problems of one round; Ys: per-item outputs (scratch for the tuning runs)
+  auto build = [&](int bk_override, const std::vector<double *> *Ys, GemmBuckets &b) {
+    for (size_t i : order) {
+      Impl &m = *eng[i];
+      const GroupedItem &it = items[i];
+      const int bn = pick_bn(it.k);
+      const int bk = bk_override ? bk_override : bk_for(bn);
+      TcProblem &q = pr[i];
+      q = TcProblem();
+      q.A = m.mat(m.Hdense.hi.get(), m.Hdense.lo.get(), m.dim, m.Kd, 128, bk);
+      q.B = m.mat(m.Xd.hi.get(), m.Xd.lo.get(), (int64_t)m.Xd.hi.count / m.Kd, m.Kd, bn, bk);
+      q.shape.M = m.dim; q.shape.N = it.k; q.shape.K = m.Kd; q.shape.products = g_products;
+      direct[i] = (g_kacc && bn <= 64) ? 1 : 0;
+      if (direct[i]) {
+        // in-CTA accumulation adds no parallelism: only the chain bound sets the splits
+        q.shape.ksplit = (int)ceil_div(m.Kd, g_dense_chain);
+        q.shape.kacc = true;
+        q.epi.kind = TcEpilogue::AXPBY_F64;
+        q.epi.rd = m.dim; q.epi.ro2 = 1; q.epi.rlim = m.dim;
+        q.epi.cd = it.k; q.epi.clim = it.k;
+        if (Ys) {
+          q.epi.co2 = m.dim; q.epi.out_f64 = (*Ys)[i]; q.epi.alpha = 1.0; q.epi.beta = 0.0;
+        } else {
+          q.epi.co2 = it.ldy; q.epi.out_f64 = it.Y; q.epi.alpha = 1.0; q.epi.beta = accumulate ? 1.0 : 0.0;
+        }
+      } else {
+        q.shape.ksplit = pick_ksplit(ceil_div(m.dim, 128) * ceil_div(it.k, bn), m.Kd, g_dense_chain);
+        m.part.resize((size_t)q.shape.ksplit * m.dim * it.k);
+        q.epi.kind = TcEpilogue::STORE_F32;
+        q.epi.rd = m.dim; q.epi.ro2 = 1; q.epi.rlim = m.dim;
+        q.epi.cd = it.k; q.epi.co2 = m.dim; q.epi.clim = it.k;
+        q.epi.so = m.dim * it.k;
+        q.epi.out_f32 = m.part.get();
+      }
+      b.add(&q, bn, i);
+    }
+  };
+  if (tunable) {
+    DenseTuning t;
+    int64_t tot = 0;
+    for (size_t i = 0; i < n; ++i) tot += eng[i]->dim * items[i].k;
+    DeviceBuffer<double> scratch(tot);
+    std::vector<double *> Ys(n);
+    for (size_t i = 0, off = 0; i < n; off += eng[i]->dim * items[i].k, ++i) Ys[i] = scratch.get() + off;
+    cudaEvent_t e0, e1;
+    VGB_CUDA(cudaEventCreate(&e0));
+    VGB_CUDA(cudaEventCreate(&e1));
+    double best = 1e30;
+    for (int bk : {32, 64})
+      for (int group : {8, 16, 32}) {
+        float ms = 0.f;
+        for (int rep = 0; rep < 2; ++rep) {
+          GemmBuckets tb;
+          build(bk, &Ys, tb);
+          VGB_CUDA(cudaEventRecord(e0, s));
+          tb.run(err, s, ks, group);
+          VGB_CUDA(cudaEventRecord(e1, s));
+          VGB_CUDA(cudaEventSynchronize(e1));
+          VGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        }
+        t.table.push_back({(double)bk, (double)group, (double)ms});
+        if (ms < best) { best = ms; t.bk = bk; t.group = group; }
+      }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    t.done = true;
+    use_bk = t.bk;
+    use_group = t.group;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_dense_tuning[bn_all] = t;
+  }
+  GemmBuckets b;
+  build(use_bk, nullptr, b);
+  b.run(err, s, ks, use_group);
   std::vector<ReduceJob> rj;
   for (size_t i = 0; i < n; ++i) {
     if (direct[i]) continue;

@@ -1,10 +1,15 @@
 // Mixed-precision (tensor-core) contractions of the BSE product.
 #pragma once
 
+#include <string>
+
 #include "bse_ops.cuh"
 #include "tc_gemm.cuh"
 
 namespace vgb {
+
+// The launch shapes chosen by the autotuner so far, with the candidates' times (JSON).
+std::string autotune_report();
 
 class MixedEngine {
  public:

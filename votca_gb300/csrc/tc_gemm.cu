@@ -940,15 +940,16 @@ int tc_gemm(const TcMat &A, const TcMat &B, const TcShape &sh, const TcEpilogue 
 }
 
 void tc_gemm_grouped(const std::vector<const TcProblem *> &probs, int bn, int *err, cudaStream_t s,
-                     int *ksplit_out) {
+                     int *ksplit_out, int group_max) {
   std::unique_ptr<GroupSrc> src(new GroupSrc());
+  const int gmax = std::max(1, std::min(group_max, kGroupMax));
   int bk = 0;
   size_t i = 0;
   while (i < probs.size()) {
     src->n = 0;
     src->err_ptr = err;
     int64_t total = 0;
-    for (; i < probs.size() && src->n < kGroupMax; ++i) {
+    for (; i < probs.size() && src->n < gmax; ++i) {
       const TcProblem &q = *probs[i];
       const KParams p = make_params(q.A, q.B, q.shape, q.epi, bn, err);
       if (ksplit_out) ksplit_out[i] = p.ksplit;
