@@ -395,17 +395,9 @@ void MixedEngine::apply(BseOperator &op, const Coef &c, const double *X, int64_t
 
 namespace {
 
-// Pairs (a, b) of digit planes with a + b < nsl, by level: the products kept by the Ozaki
-// scheme (the dropped levels are below 2^(-7 nsl) of the row and column scales).
-void set_pairs(TcShape &sh, int nsl) {
-  sh.npairs = 0;
-  for (int l = 0; l < nsl; ++l)
-    for (int a = 0; a <= l; ++a) {
-      sh.pa[sh.npairs] = (uint8_t)a;
-      sh.pb[sh.npairs] = (uint8_t)(l - a);
-      ++sh.npairs;
-    }
-}
+// All pairs (a, b) of digit planes with a + b < nsl: the products kept by the Ozaki scheme (the
+// dropped levels are below 2^(-7 nsl) of the row and column scales).
+void set_pairs(TcShape &sh, int nsl) { sh.nslices = nsl; }
 
 // One slice-mode product: C (M x N) = sum over pairs of A planes (rows a_plane apart, K-major,
 // row stride K) times B planes, through the final FP64 epilogue fe.  When the tiles alone do
@@ -423,10 +415,10 @@ void sliced_gemm(const TcMat &A, int64_t a_plane, const TcMat &B, int64_t b_plan
   sh.chain = chain;
   sh.kacc = true;
   const int64_t tiles = ceil_div(M, 128) * ceil_div(N, bn);
-  const int64_t ksplit = sh.npairs * ceil_div(K / 64, sh.chain / 64);
+  const int64_t runs = ceil_div(K / 64, sh.chain / 64);
   int groups = 1;  // float-pair outputs are written by the CTA that owns the tile
   for (int g = 2; g <= 64 && fe.kind == TcEpilogue::AXPBY_F64; ++g)
-    if (ksplit % g == 0 && tiles * g <= sm_count()) groups = g;
+    if (runs % g == 0 && tiles * g <= sm_count()) groups = g;
   if (groups == 1) {
     tc_gemm(A, B, sh, fe, bn, err, s);
     return;

@@ -18,15 +18,19 @@ constexpr int kSmemRing = 196608;                     // bytes of operand ring p
 
 // BK = bf16 elements of K per stage row: 64 -> 128-byte rows (SWIZZLE_128B),
 // 32 -> 64-byte rows (SWIZZLE_64B, half the stage size, twice the stages).
-template <int BN, int BK>
+// SLICE: the slice-mode kernel (Ozaki digit planes): a stage holds one A plane and up to
+// kMaxDigits B planes of one K block.
+constexpr int kMaxDigits = 5;
+template <int BN, int BK, bool SLICE = false>
 struct Cfg {
-  static constexpr int A_BYTES = BM * BK * 2;            // one of hi / lo
+  static constexpr int A_BYTES = BM * BK * 2;            // one of hi / lo (one plane)
   static constexpr int B_BYTES = BN * BK * 2;
-  static constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
+  static constexpr int STAGE_BYTES = SLICE ? A_BYTES + kMaxDigits * B_BYTES : 2 * A_BYTES + 2 * B_BYTES;
   static constexpr int STAGES = kSmemRing / STAGE_BYTES > 8 ? 8 : kSmemRing / STAGE_BYTES;
   // accumulator buffers in TMEM: four for the narrow tiles (short K splits: the epilogue of a
-  // split may lag the MMAs of the next three), two for the wide ones
-  static constexpr int NBUF = BN <= 64 ? 4 : 2;
+  // split may lag the MMAs of the next three), two for the wide ones; slice mode: eight (up to
+  // kMaxDigits splits are accumulated at once)
+  static constexpr int NBUF = SLICE ? 8 : (BN <= 64 ? 4 : 2);
   static constexpr int TMEM_COLS = NBUF * BN < 32 ? 32 : NBUF * BN;
   static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
   static constexpr uint32_t SBO = BK == 64 ? 1024 : 512;     // 8 rows of one swizzle atom
@@ -34,15 +38,16 @@ struct Cfg {
 };
 
 struct KParams {
-  int64_t M, N, K;  // slice mode: K of one slice
+  int64_t M, N, K;
   int products;  // 3: hi.hi + hi.lo + lo.hi;  4: + lo.lo;  1: slice mode (hi maps only)
   int64_t nbatch, a_brows, b_brows;
   int ksplit, kc_per;
   int kacc;  // 1: one CTA runs K splits of a tile and sums them in FP64 registers
   int spg;   // kacc: consecutive splits per work item (ksplit / spg groups per tile)
-  int npairs, cpp;        // slice mode: slice pairs, K splits per pair
-  uint64_t pa, pb;        // slice mode: A / B slice index of pair i in bits [4 i, 4 i + 4)
-  int64_t a_plane, b_plane;  // slice mode: operand rows between consecutive slice planes
+  // slice mode: digit planes per operand, K runs, runs per split group; the splits of a group are
+  // (a, q, b) for A plane a, run q, B plane b < nsl - a (pairs up to digit level nsl - 1)
+  int nsl, cpr, rpg;
+  int64_t a_plane, b_plane;  // slice mode: operand rows between consecutive digit planes
   int64_t mt, nt, ntiles;
   TcEpilogue epi;
   int *err;
@@ -197,25 +202,15 @@ __host__ __device__ __forceinline__ int64_t item_count(const KParams &p) {
 }
 __device__ __forceinline__ int64_t item_len(const KParams &p) { return p.kacc ? p.spg : 1; }
 
-// K blocks [kb, ke) of split s and, in slice mode, the row offsets of its A and B slice planes.
+// K blocks [kb, ke) of split s.
 struct KRange {
   int kb, ke;
-  int ya, yb;
 };
 template <int BK>
 __device__ __forceinline__ KRange k_range(const KParams &p, int64_t s) {
   KRange r;
   const int kchunks = (int)(p.K / BK);
-  int sl = (int)s;
-  r.ya = 0;
-  r.yb = 0;
-  if (p.npairs) {
-    const int pr = sl / p.cpp;
-    sl -= pr * p.cpp;
-    r.ya = (int)((p.pa >> (4 * pr)) & 15) * (int)p.a_plane;
-    r.yb = (int)((p.pb >> (4 * pr)) & 15) * (int)p.b_plane;
-  }
-  r.kb = sl * p.kc_per;
+  r.kb = (int)s * p.kc_per;
   r.ke = min(kchunks, r.kb + p.kc_per);
   return r;
 }
@@ -256,9 +251,9 @@ struct GroupSrc {
 };
 static_assert(sizeof(GroupSrc) <= 32000, "grouped GEMM parameters exceed the kernel parameter space");
 
-template <int BN, int BK, class Src>
+template <int BN, int BK, class Src, bool SLICE = false>
 __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_constant__ Src src) {
-  using C = Cfg<BN, BK>;
+  using C = Cfg<BN, BK, SLICE>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t *full = (uint64_t *)(smem + C::STAGES * C::STAGE_BYTES);
@@ -309,30 +304,42 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
         const CUtensorMap *mBhi = src.map(pi, 2), *mBlo = src.map(pi, 3);
         // the jobs of an item share the tile; only the K split advances (decode once per item)
         TileCoord tc = decode(p, li * len);
-        for (int64_t u = 0; u < len; ++u, ++tc.s) {
-          const KRange kr = k_range<BK>(p, tc.s);
-          const int ya = (int)(tc.b * p.a_brows + tc.m * BM);
-          const int yb = (int)(tc.b * p.b_brows + tc.n * BN);
-          // slice mode: two K blocks per stage (the hi and lo slots), one A and one B plane each
-          for (int kc = kr.kb; kc < kr.ke; kc += p.npairs ? 2 : 1) {
-            if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, err, 1)) goto producer_done;
-            uint8_t *st = smem + stage * C::STAGE_BYTES;
-            if (p.npairs) {
-              const int nblk = min(2, kr.ke - kc);
-              mbar_expect_tx(&full[stage], (uint32_t)(nblk * (C::A_BYTES + C::B_BYTES)));
-              for (int h = 0; h < nblk; ++h) {
-                tma_load_2d(smem_u32(st + h * C::A_BYTES), mAhi, &full[stage], (kc + h) * BK, ya + kr.ya);
-                tma_load_2d(smem_u32(st + 2 * C::A_BYTES + h * C::B_BYTES), mBhi, &full[stage], (kc + h) * BK,
-                            yb + kr.yb);
+        const int ya = (int)(tc.b * p.a_brows + tc.m * BM);
+        const int yb = (int)(tc.b * p.b_brows + tc.n * BN);
+        if constexpr (SLICE) {
+          // the item's split group g: runs [q0, q0 + rpg); per A plane a and run q, each K block is
+          // one stage with A plane a and B planes 0 .. nsl - 1 - a
+          const int kchunks = (int)(p.K / BK);
+          const int q0 = (int)(tc.s / p.spg) * p.rpg;
+          for (int a = 0; a < p.nsl; ++a) {
+            const int nb = p.nsl - a;
+            for (int qr = q0; qr < q0 + p.rpg; ++qr) {
+              const int kb = qr * p.kc_per, ke = min(kchunks, kb + p.kc_per);
+              for (int kc = kb; kc < ke; ++kc) {
+                if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, err, 1)) goto producer_done;
+                uint8_t *st = smem + stage * C::STAGE_BYTES;
+                mbar_expect_tx(&full[stage], (uint32_t)(C::A_BYTES + nb * C::B_BYTES));
+                tma_load_2d(smem_u32(st), mAhi, &full[stage], kc * BK, ya + a * (int)p.a_plane);
+                for (int b = 0; b < nb; ++b)
+                  tma_load_2d(smem_u32(st + C::A_BYTES + b * C::B_BYTES), mBhi, &full[stage], kc * BK,
+                              yb + b * (int)p.b_plane);
+                if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
               }
-            } else {
+            }
+          }
+        } else {
+          for (int64_t u = 0; u < len; ++u, ++tc.s) {
+            const KRange kr = k_range<BK>(p, tc.s);
+            for (int kc = kr.kb; kc < kr.ke; ++kc) {
+              if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, err, 1)) goto producer_done;
+              uint8_t *st = smem + stage * C::STAGE_BYTES;
               mbar_expect_tx(&full[stage], (uint32_t)C::STAGE_BYTES);
               tma_load_2d(smem_u32(st), mAhi, &full[stage], kc * BK, ya);
               tma_load_2d(smem_u32(st + C::A_BYTES), mAlo, &full[stage], kc * BK, ya);
               tma_load_2d(smem_u32(st + 2 * C::A_BYTES), mBhi, &full[stage], kc * BK, yb);
               tma_load_2d(smem_u32(st + 2 * C::A_BYTES + C::B_BYTES), mBlo, &full[stage], kc * BK, yb);
+              if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
             }
-            if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
           }
         }
       }
@@ -361,33 +368,57 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
         const int64_t len = item_len(p);
         // the jobs of an item share the tile; only the K split advances (decode once per item)
         TileCoord tc = decode(p, li * len);
+        if constexpr (SLICE) {
+          // splits (a, q, b), b fastest: the nb = nsl - a accumulators of (a, q) are filled together
+          // from the stages of run q, then handed to the epilogue in split order
+          const int kchunks = (int)(p.K / BK);
+          const int q0 = (int)(tc.s / p.spg) * p.rpg;
+          for (int a = 0; a < p.nsl; ++a) {
+            const int nb = p.nsl - a;
+            for (int qr = q0; qr < q0 + p.rpg; ++qr) {
+              const int kb = qr * p.kc_per, ke = min(kchunks, kb + p.kc_per);
+              uint32_t dt[kMaxDigits];
+              int bufs[kMaxDigits];
+              for (int b = 0; b < nb; ++b) {  // acquire nb accumulators in ring order
+                if (!mbar_wait(&acce[buf], aphase ^ 1, abort_flag, err, 2)) goto mma_done;
+                bufs[b] = buf;
+                dt[b] = tmem_base + (uint32_t)(buf * BN);
+                if (++buf == C::NBUF) { buf = 0; aphase ^= 1; }
+              }
+              fence_after();
+              for (int kc = kb; kc < ke; ++kc) {
+                if (!mbar_wait(&full[stage], phase, abort_flag, err, 3)) goto mma_done;
+                fence_after();
+                const uint32_t st = smem_u32(smem + stage * C::STAGE_BYTES);
+                for (int b = 0; b < nb; ++b) {
+#pragma unroll
+                  for (int kk = 0; kk < BK / 16; ++kk) {
+                    const uint32_t koff = kk * 32;
+                    mma_bf16(dt[b], sdesc(st + koff, C::SBO, C::LAYOUT),
+                             sdesc(st + C::A_BYTES + b * C::B_BYTES + koff, C::SBO, C::LAYOUT), idesc,
+                             (kc > kb || kk > 0) ? 1u : 0u);
+                  }
+                }
+                mma_commit(&empty[stage]);
+                if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
+              }
+              for (int b = 0; b < nb; ++b) mma_commit(&accf[bufs[b]]);
+            }
+          }
+          continue;
+        }
         for (int64_t u = 0; u < len; ++u, ++tc.s) {
           const KRange kr = k_range<BK>(p, tc.s);
           const int kb = kr.kb, ke = kr.ke;
           if (!mbar_wait(&acce[buf], aphase ^ 1, abort_flag, err, 2)) goto mma_done;
           fence_after();
           const uint32_t d_tmem = tmem_base + (uint32_t)(buf * BN);
-          for (int kc = kb; kc < ke; kc += p.npairs ? 2 : 1) {
+          for (int kc = kb; kc < ke; ++kc) {
             if (!mbar_wait(&full[stage], phase, abort_flag, err, 3)) goto mma_done;
             fence_after();
             const uint32_t st = smem_u32(smem + stage * C::STAGE_BYTES);
             const uint32_t ahi = st, alo = st + C::A_BYTES;
             const uint32_t bhi = st + 2 * C::A_BYTES, blo = bhi + C::B_BYTES;
-            if (p.npairs) {  // slice mode: K block kc in the hi slots, kc + 1 in the lo slots
-              const int nblk = min(2, ke - kc);
-              for (int h = 0; h < nblk; ++h) {
-#pragma unroll
-                for (int kk = 0; kk < BK / 16; ++kk) {
-                  const uint32_t koff = kk * 32;
-                  const uint32_t acc0 = (kc > kb || h > 0 || kk > 0) ? 1u : 0u;
-                  mma_bf16(d_tmem, sdesc((h ? alo : ahi) + koff, C::SBO, C::LAYOUT),
-                           sdesc((h ? blo : bhi) + koff, C::SBO, C::LAYOUT), idesc, acc0);
-                }
-              }
-              mma_commit(&empty[stage]);
-              if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
-              continue;
-            }
 #pragma unroll
             for (int kk = 0; kk < BK / 16; ++kk) {
               const uint32_t koff = kk * 32;  // 16 bf16 = 32 bytes along K inside the swizzle row
@@ -397,11 +428,9 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
               const uint64_t dbh = sdesc(bhi + koff, C::SBO, C::LAYOUT);
               const uint64_t dbl = sdesc(blo + koff, C::SBO, C::LAYOUT);
               mma_bf16(d_tmem, dah, dbh, idesc, acc0);
-              if (p.products != 1) {
-                mma_bf16(d_tmem, dah, dbl, idesc, 1u);
-                mma_bf16(d_tmem, dal, dbh, idesc, 1u);
-                if (p.products == 4) mma_bf16(d_tmem, dal, dbl, idesc, 1u);
-              }
+              mma_bf16(d_tmem, dah, dbl, idesc, 1u);
+              mma_bf16(d_tmem, dal, dbh, idesc, 1u);
+              if (p.products == 4) mma_bf16(d_tmem, dal, dbl, idesc, 1u);
             }
             mma_commit(&empty[stage]);  // frees the smem stage when these MMAs complete
             if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
@@ -792,16 +821,16 @@ void encode(CUtensorMap *m, const uint16_t *base, int64_t rows, int64_t K, int64
   if (r != CUDA_SUCCESS) fail(BSE_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
 }
 
-template <int BN, int BK, class Src>
+template <int BN, int BK, class Src, bool SLICE = false>
 void launch_src(const Src &src, int64_t ntiles, cudaStream_t s) {
-  using C = Cfg<BN, BK>;
+  using C = Cfg<BN, BK, SLICE>;
   static std::once_flag attr;
   std::call_once(attr, [] {
-    VGB_CUDA(cudaFuncSetAttribute(tc_gemm_kernel<BN, BK, Src>,
+    VGB_CUDA(cudaFuncSetAttribute(tc_gemm_kernel<BN, BK, Src, SLICE>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
   });
   const int64_t grid = std::min<int64_t>(ntiles, sm_count());
-  tc_gemm_kernel<BN, BK, Src><<<(unsigned)grid, kThreads, C::SMEM, s>>>(src);
+  tc_gemm_kernel<BN, BK, Src, SLICE><<<(unsigned)grid, kThreads, C::SMEM, s>>>(src);
   VGB_LAUNCH_CHECK();
 }
 
@@ -855,16 +884,15 @@ KParams make_params(const TcMat &A, const TcMat &B, const TcShape &sh, const TcE
   VGB_REQUIRE(A.bk == B.bk, "tc_gemm: operands staged with different K boxes");
   const int BK = A.bk;
   VGB_REQUIRE(sh.K % BK == 0 && A.K >= sh.K && B.K >= sh.K, "tc_gemm: K not padded");
-  int64_t a_extra = 0, b_extra = 0;  // slice mode: rows of the highest slice plane addressed
-  if (sh.npairs > 0) {
-    VGB_REQUIRE(sh.npairs <= 16 && sh.chain >= BK && sh.chain % BK == 0 && sh.nbatch == 1,
-                "tc_gemm: bad slice pairs");
+  int64_t a_extra = 0, b_extra = 0;  // slice mode: rows of the highest digit plane addressed
+  if (sh.nslices > 0) {
+    VGB_REQUIRE(sh.nslices <= kMaxDigits && sh.chain >= BK && sh.chain % BK == 0 && sh.nbatch == 1 &&
+                    BK == 64 && bn <= 64,
+                "tc_gemm: bad slice-mode shape");
     VGB_REQUIRE(sh.a_plane >= sh.M && sh.b_plane >= sh.N, "tc_gemm: slice planes smaller than the problem");
-    for (int i = 0; i < sh.npairs; ++i) {
-      VGB_REQUIRE(sh.pa[i] < 16 && sh.pb[i] < 16, "tc_gemm: slice index out of range");
-      a_extra = std::max(a_extra, (int64_t)sh.pa[i] * sh.a_plane);
-      b_extra = std::max(b_extra, (int64_t)sh.pb[i] * sh.b_plane);
-    }
+    VGB_REQUIRE((int64_t)sh.nslices * std::max(sh.a_plane, sh.b_plane) < (1LL << 31), "tc_gemm: planes too large");
+    a_extra = (sh.nslices - 1) * sh.a_plane;
+    b_extra = (sh.nslices - 1) * sh.b_plane;
   }
   VGB_REQUIRE(epi.rd >= 1 && epi.cd >= 1, "tc_gemm: bad epilogue map");
   KParams p;
@@ -877,41 +905,41 @@ KParams make_params(const TcMat &A, const TcMat &B, const TcShape &sh, const TcE
   VGB_REQUIRE((sh.nbatch - 1) * sh.b_batch_rows + b_extra + sh.N <= B.rows + bn, "tc_gemm: B rows");
   VGB_REQUIRE(A.rows < (1LL << 31) && B.rows < (1LL << 31), "tc_gemm: too many rows");
   p.M = sh.M; p.N = sh.N; p.K = sh.K;
-  p.products = sh.npairs > 0 ? 1 : (sh.products == 4 ? 4 : 3);
-  p.npairs = sh.npairs > 0 ? sh.npairs : 0;
+  p.products = sh.nslices > 0 ? 1 : (sh.products == 4 ? 4 : 3);
+  p.nsl = sh.nslices > 0 ? sh.nslices : 0;
   p.a_plane = sh.a_plane;
   p.b_plane = sh.b_plane;
-  p.pa = 0;
-  p.pb = 0;
-  for (int i = 0; i < p.npairs; ++i) {
-    p.pa |= (uint64_t)sh.pa[i] << (4 * i);
-    p.pb |= (uint64_t)sh.pb[i] << (4 * i);
-  }
   p.nbatch = sh.nbatch;
   p.a_brows = sh.a_batch_rows;
   p.b_brows = sh.b_batch_rows;
   const int kchunks = (int)(sh.K / BK);
   VGB_REQUIRE(kchunks >= 1, "tc_gemm: K must be positive");
-  if (p.npairs) {  // every split: one pair, at most chain K elements
+  const int npairs = p.nsl * (p.nsl + 1) / 2;
+  int groups = 1;
+  if (p.nsl) {  // every split: one digit pair on one run of at most chain K elements
     p.kc_per = (int)std::min<int64_t>(kchunks, sh.chain / BK);
-    p.cpp = (int)ceil_div(kchunks, p.kc_per);
-    p.ksplit = p.npairs * p.cpp;
-    p.kacc = p.ksplit > 1 ? 1 : 0;
+    p.cpr = (int)ceil_div(kchunks, p.kc_per);
+    p.ksplit = npairs * p.cpr;
+    p.kacc = 1;
+    groups = std::max(1, sh.kgroups);
+    VGB_REQUIRE(p.cpr % groups == 0, "tc_gemm: split groups must divide the K runs");
+    p.rpg = p.cpr / groups;
   } else {
     int ks = std::max(1, std::min(sh.ksplit, kchunks));
     p.kc_per = (int)ceil_div(kchunks, ks);
     p.ksplit = (int)ceil_div(kchunks, p.kc_per);
-    p.cpp = p.ksplit;
+    p.cpr = p.ksplit;
+    p.rpg = 0;
     p.kacc = (sh.kacc && p.ksplit > 1) ? 1 : 0;
+    groups = p.kacc ? std::max(1, sh.kgroups) : 1;
+    VGB_REQUIRE(p.ksplit % groups == 0, "tc_gemm: split groups must divide the K splits");
   }
-  const int groups = p.kacc ? std::max(1, sh.kgroups) : 1;
-  VGB_REQUIRE(p.ksplit % groups == 0, "tc_gemm: split groups must divide the K splits");
   VGB_REQUIRE(groups == 1 || (epi.kind == TcEpilogue::AXPBY_F64 && epi.beta == 0.0),
               "tc_gemm: split groups write FP64 partials");
   p.spg = p.ksplit / groups;
   VGB_REQUIRE(!p.kacc || (bn <= 64 && epi.kind != TcEpilogue::STORE_F32),
               "tc_gemm: in-CTA K accumulation needs BN <= 64 and a final (split or FP64) epilogue");
-  VGB_REQUIRE(epi.kind != TcEpilogue::PAIR_F32 || (p.kacc && p.npairs > 0 && (int64_t)bn <= 64),
+  VGB_REQUIRE(epi.kind != TcEpilogue::PAIR_F32 || (p.kacc && p.nsl > 0 && (int64_t)bn <= 64),
               "tc_gemm: float-pair output needs slice mode with in-CTA K accumulation");
   VGB_REQUIRE(p.ksplit == 1 || p.kacc || epi.kind == TcEpilogue::STORE_F32,
               "tc_gemm: K split needs F32 partials or in-CTA accumulation");
@@ -935,7 +963,12 @@ int tc_gemm(const TcMat &A, const TcMat &B, const TcShape &sh, const TcEpilogue 
   src.maps[2] = B.map_hi;
   src.maps[3] = B.map_lo;
   src.p = p;
-  launch_any(bn, A.bk, src, item_count(p), s);
+  if (p.nsl) {  // slice mode (validated: K box 64, BN <= 64)
+    if (bn == 32) launch_src<32, 64, SingleSrc, true>(src, item_count(p), s);
+    else launch_src<64, 64, SingleSrc, true>(src, item_count(p), s);
+  } else {
+    launch_any(bn, A.bk, src, item_count(p), s);
+  }
   return p.ksplit;
 }
 
@@ -951,6 +984,7 @@ void tc_gemm_grouped(const std::vector<const TcProblem *> &probs, int bn, int *e
     int64_t total = 0;
     for (; i < probs.size() && src->n < gmax; ++i) {
       const TcProblem &q = *probs[i];
+      VGB_REQUIRE(q.shape.nslices == 0, "tc_gemm_grouped: slice mode runs through tc_gemm");
       const KParams p = make_params(q.A, q.B, q.shape, q.epi, bn, err);
       if (ksplit_out) ksplit_out[i] = p.ksplit;
       if (p.ntiles == 0) continue;

@@ -63,13 +63,15 @@ struct TcShape {
   // group g writes its FP64 sum through the epilogue map at offset g * epi.so (beta = 0), and
   // reduce_f64_groups adds the groups
   int kgroups = 1;
-  // slice mode (npairs > 0, nbatch 1): the operands hold bf16 slice planes stacked by rows
-  // (slice t of operand row r is row t * plane + r, see slice_f64); the product is the sum over
-  // pairs i of A slice pa[i] times B slice pb[i], one bf16 MMA per K step (hi maps only).
-  // Every K split covers one pair and at most `chain` K elements (the run of one digit scale),
-  // and the splits are summed in FP64 (kacc).
-  int npairs = 0;
-  uint8_t pa[16] = {}, pb[16] = {};
+  // slice mode (nslices > 0, nbatch 1, K box 64, BN <= 64): the operands hold nslices bf16 digit
+  // planes stacked by rows (digit t of operand row r is row t * plane + r, see slice_f64); the
+  // product is the sum of A plane a times B plane b over all a + b < nslices, one bf16 MMA per K
+  // step.  Every K split covers one digit pair on one run of at most `chain` K elements (the run
+  // of one digit scale), its FP32 accumulator is exact, and the splits are summed on the CTA.
+  // A pipeline stage holds A plane a and B planes 0 .. nslices - 1 - a of one K block, whose
+  // products go to separate accumulators (one A load for up to nslices pairs).  kgroups must
+  // divide the number of runs.
+  int nslices = 0;
   int64_t a_plane = 0, b_plane = 0;
   int64_t chain = 1024;
 };
