@@ -30,7 +30,8 @@ struct Cfg {
   // accumulator buffers in TMEM: four for the narrow tiles (short K splits: the epilogue of a
   // split may lag the MMAs of the next three), two for the wide ones; slice mode: eight (up to
   // kMaxDigits splits are accumulated at once)
-  static constexpr int NBUF = SLICE ? 8 : (BN <= 64 ? 4 : 2);
+  static constexpr int NBUF = SLICE ? 8 : (BN <= 64 ? 4 : 2);  // a power of two
+  static_assert((NBUF & (NBUF - 1)) == 0, "accumulator ring size");
   static constexpr int TMEM_COLS = NBUF * BN < 32 ? 32 : NBUF * BN;
   static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
   static constexpr uint32_t SBO = BK == 64 ? 1024 : 512;     // 8 rows of one swizzle atom
@@ -377,12 +378,12 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
             const int nb = p.nsl - a;
             for (int qr = q0; qr < q0 + p.rpg; ++qr) {
               const int kb = qr * p.kc_per, ke = min(kchunks, kb + p.kc_per);
-              uint32_t dt[kMaxDigits];
-              int bufs[kMaxDigits];
-              for (int b = 0; b < nb; ++b) {  // acquire nb accumulators in ring order
+              // acquire nb accumulators in ring order: buffers buf0, buf0 + 1, ... (mod NBUF); the
+              // indices are computed, not stored (an indexed array would live in local memory on
+              // the MMA thread's critical path)
+              const int buf0 = buf;
+              for (int b = 0; b < nb; ++b) {
                 if (!mbar_wait(&acce[buf], aphase ^ 1, abort_flag, err, 2)) goto mma_done;
-                bufs[b] = buf;
-                dt[b] = tmem_base + (uint32_t)(buf * BN);
                 if (++buf == C::NBUF) { buf = 0; aphase ^= 1; }
               }
               fence_after();
@@ -390,19 +391,21 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
                 if (!mbar_wait(&full[stage], phase, abort_flag, err, 3)) goto mma_done;
                 fence_after();
                 const uint32_t st = smem_u32(smem + stage * C::STAGE_BYTES);
-                for (int b = 0; b < nb; ++b) {
+                const uint32_t acc = kc > kb ? 1u : 0u;
+                // descriptors are linear in the address (bits 0-13 hold addr >> 4): one per plane,
+                // plus 2 per 16-element K step
+                const uint64_t da = sdesc(st, C::SBO, C::LAYOUT);
+                uint64_t db = sdesc(st + C::A_BYTES, C::SBO, C::LAYOUT);
+                for (int b = 0; b < nb; ++b, db += C::B_BYTES >> 4) {
+                  const uint32_t dtb = tmem_base + (uint32_t)(((buf0 + b) & (C::NBUF - 1)) * BN);
+                  mma_bf16(dtb, da, db, idesc, acc);
 #pragma unroll
-                  for (int kk = 0; kk < BK / 16; ++kk) {
-                    const uint32_t koff = kk * 32;
-                    mma_bf16(dt[b], sdesc(st + koff, C::SBO, C::LAYOUT),
-                             sdesc(st + C::A_BYTES + b * C::B_BYTES + koff, C::SBO, C::LAYOUT), idesc,
-                             (kc > kb || kk > 0) ? 1u : 0u);
-                  }
+                  for (int kk = 1; kk < BK / 16; ++kk) mma_bf16(dtb, da + 2 * kk, db + 2 * kk, idesc, 1u);
                 }
                 mma_commit(&empty[stage]);
                 if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
               }
-              for (int b = 0; b < nb; ++b) mma_commit(&accf[bufs[b]]);
+              for (int b = 0; b < nb; ++b) mma_commit(&accf[(buf0 + b) & (C::NBUF - 1)]);
             }
           }
           continue;
@@ -417,16 +420,16 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
             if (!mbar_wait(&full[stage], phase, abort_flag, err, 3)) goto mma_done;
             fence_after();
             const uint32_t st = smem_u32(smem + stage * C::STAGE_BYTES);
-            const uint32_t ahi = st, alo = st + C::A_BYTES;
-            const uint32_t bhi = st + 2 * C::A_BYTES, blo = bhi + C::B_BYTES;
+            // descriptors are linear in the address: + 2 per 16 bf16 (32 bytes) along K
+            const uint64_t dah0 = sdesc(st, C::SBO, C::LAYOUT);
+            const uint64_t dal0 = dah0 + (C::A_BYTES >> 4);
+            const uint64_t dbh0 = dah0 + ((2 * C::A_BYTES) >> 4);
+            const uint64_t dbl0 = dbh0 + (C::B_BYTES >> 4);
 #pragma unroll
             for (int kk = 0; kk < BK / 16; ++kk) {
-              const uint32_t koff = kk * 32;  // 16 bf16 = 32 bytes along K inside the swizzle row
               const uint32_t acc0 = (kc > kb || kk > 0) ? 1u : 0u;
-              const uint64_t dah = sdesc(ahi + koff, C::SBO, C::LAYOUT);
-              const uint64_t dal = sdesc(alo + koff, C::SBO, C::LAYOUT);
-              const uint64_t dbh = sdesc(bhi + koff, C::SBO, C::LAYOUT);
-              const uint64_t dbl = sdesc(blo + koff, C::SBO, C::LAYOUT);
+              const uint64_t dah = dah0 + 2 * kk, dal = dal0 + 2 * kk;
+              const uint64_t dbh = dbh0 + 2 * kk, dbl = dbl0 + 2 * kk;
               mma_bf16(d_tmem, dah, dbh, idesc, acc0);
               mma_bf16(d_tmem, dah, dbl, idesc, 1u);
               mma_bf16(d_tmem, dal, dbh, idesc, 1u);
