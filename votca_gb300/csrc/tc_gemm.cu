@@ -18,21 +18,24 @@ constexpr int kSmemRing = 196608;                     // bytes of operand ring p
 
 // BK = bf16 elements of K per stage row: 64 -> 128-byte rows (SWIZZLE_128B),
 // 32 -> 64-byte rows (SWIZZLE_64B, half the stage size, twice the stages).
-// SLICE: the slice-mode kernel (Ozaki digit planes): a stage holds one A plane and up to
-// kMaxDigits B planes of one K block.
+// SLICE: the slice-mode kernel (Ozaki digit planes).  A unit is one A plane a and up to UNIT
+// B planes b0 .. b0 + nb - 1 (pairs of one digit level or less): a stage holds the unit's planes
+// of one K block, and one MMA of width nb * BN multiplies the A plane by the stacked B planes
+// into nb adjacent accumulators (A is read once per K step for nb pairs).
 constexpr int kMaxDigits = 5;
 template <int BN, int BK, bool SLICE = false>
 struct Cfg {
   static constexpr int A_BYTES = BM * BK * 2;            // one of hi / lo (one plane)
   static constexpr int B_BYTES = BN * BK * 2;
-  static constexpr int STAGE_BYTES = SLICE ? A_BYTES + kMaxDigits * B_BYTES : 2 * A_BYTES + 2 * B_BYTES;
+  static constexpr int UNIT = 256 / BN < kMaxDigits ? 256 / BN : kMaxDigits;  // B planes per unit
+  static constexpr int STAGE_BYTES = SLICE ? A_BYTES + UNIT * B_BYTES : 2 * A_BYTES + 2 * B_BYTES;
   static constexpr int STAGES = kSmemRing / STAGE_BYTES > 8 ? 8 : kSmemRing / STAGE_BYTES;
   // accumulator buffers in TMEM: four for the narrow tiles (short K splits: the epilogue of a
-  // split may lag the MMAs of the next three), two for the wide ones; slice mode: eight (up to
-  // kMaxDigits splits are accumulated at once)
-  static constexpr int NBUF = SLICE ? 8 : (BN <= 64 ? 4 : 2);  // a power of two
-  static_assert((NBUF & (NBUF - 1)) == 0, "accumulator ring size");
-  static constexpr int TMEM_COLS = NBUF * BN < 32 ? 32 : NBUF * BN;
+  // split may lag the MMAs of the next three), two for the wide ones; slice mode: two unit
+  // buffers of 256 columns
+  static constexpr int NBUF = SLICE ? 2 : (BN <= 64 ? 4 : 2);
+  static constexpr int BUFW = SLICE ? 256 : BN;  // TMEM columns per buffer
+  static constexpr int TMEM_COLS = NBUF * BUFW < 32 ? 32 : NBUF * BUFW;
   static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
   static constexpr uint32_t SBO = BK == 64 ? 1024 : 512;     // 8 rows of one swizzle atom
   static constexpr uint64_t LAYOUT = BK == 64 ? 2 : 4;       // SWIZZLE_128B / SWIZZLE_64B
@@ -195,6 +198,53 @@ __device__ __forceinline__ void epi_store(const TcEpilogue &e, int64_t off, floa
   }
 }
 
+// The K splits' FP32 sums of a tile are added as an unevaluated pair of floats (Knuth's TwoSum,
+// error-free; about 48 significant bits), held in the bits of kv[j] (hi, lo): no FP64 instruction
+// per split (the FP64 pipe of GB300 runs at 2 operations per clock and SM).  In slice mode every
+// split sum is exact, so the result is the exact sum of the splits to that precision.
+__device__ __forceinline__ void pair_add(double (&kv)[32], const uint32_t (&r)[32], bool first) {
+#pragma unroll
+  for (int j = 0; j < 32; ++j) {
+    const float x = __uint_as_float(r[j]);
+    float hi = 0.f, lo = 0.f;
+    if (!first) {
+      hi = __int_as_float(__double2hiint(kv[j]));
+      lo = __int_as_float(__double2loint(kv[j]));
+    }
+    const float sum = hi + x;
+    const float bb = sum - hi;
+    lo += (hi - (sum - bb)) + (x - bb);
+    kv[j] = __hiloint2double(__float_as_int(sum), __float_as_int(lo));
+  }
+}
+
+// Writes a thread's 32 float-pair sums (columns n0 ..) of row base rbase through the epilogue map.
+__device__ __forceinline__ void pair_write(const double (&kv)[32], const TcEpilogue &e, int64_t N, int64_t n0,
+                                           int64_t rbase) {
+  int64_t n = n0, nq = n / e.cd, nr = n % e.cd;
+#pragma unroll
+  for (int j = 0; j < 32; ++j) {
+    if (n < N && nr < e.clim) {
+      const int64_t off = rbase + nq * e.co1 + nr * e.co2;
+      const float hi = __int_as_float(__double2hiint(kv[j])), lo = __int_as_float(__double2loint(kv[j]));
+      if (e.kind == TcEpilogue::PAIR_F32) {
+        reinterpret_cast<float2 *>(e.out_f32)[off] = make_float2(hi, lo);
+      } else {
+        const double val = (double)hi + (double)lo;
+        if (e.kind == TcEpilogue::AXPBY_F64) {
+          double *y = e.out_f64 + off;
+          const double rv = e.alpha * val;
+          *y = (e.beta == 0.0) ? rv : fma(e.beta, *y, rv);
+        } else {
+          epi_store(e, off, (float)val);
+        }
+      }
+    }
+    ++n;
+    if (++nr == e.cd) { nr = 0; ++nq; }
+  }
+}
+
 // Work items of the persistent kernel: an item is one tile job, or, for a problem with in-CTA K
 // accumulation (kacc), the ksplit consecutive jobs of one output tile; items are strided over
 // the CTAs and a CTA runs the jobs of its item in order.
@@ -308,26 +358,26 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
         const int ya = (int)(tc.b * p.a_brows + tc.m * BM);
         const int yb = (int)(tc.b * p.b_brows + tc.n * BN);
         if constexpr (SLICE) {
-          // the item's split group g: runs [q0, q0 + rpg); per A plane a and run q, each K block is
-          // one stage with A plane a and B planes 0 .. nsl - 1 - a
+          // the item's split group g: runs [q0, q0 + rpg); units (a, run, b0) in order, each K
+          // block of a unit one stage with A plane a and B planes b0 .. b0 + nb - 1
           const int kchunks = (int)(p.K / BK);
           const int q0 = (int)(tc.s / p.spg) * p.rpg;
-          for (int a = 0; a < p.nsl; ++a) {
-            const int nb = p.nsl - a;
-            for (int qr = q0; qr < q0 + p.rpg; ++qr) {
-              const int kb = qr * p.kc_per, ke = min(kchunks, kb + p.kc_per);
-              for (int kc = kb; kc < ke; ++kc) {
-                if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, err, 1)) goto producer_done;
-                uint8_t *st = smem + stage * C::STAGE_BYTES;
-                mbar_expect_tx(&full[stage], (uint32_t)(C::A_BYTES + nb * C::B_BYTES));
-                tma_load_2d(smem_u32(st), mAhi, &full[stage], kc * BK, ya + a * (int)p.a_plane);
-                for (int b = 0; b < nb; ++b)
-                  tma_load_2d(smem_u32(st + C::A_BYTES + b * C::B_BYTES), mBhi, &full[stage], kc * BK,
-                              yb + b * (int)p.b_plane);
-                if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
+          for (int a = 0; a < p.nsl; ++a)
+            for (int qr = q0; qr < q0 + p.rpg; ++qr)
+              for (int b0 = 0; b0 < p.nsl - a; b0 += C::UNIT) {
+                const int nb = min(C::UNIT, p.nsl - a - b0);
+                const int kb = qr * p.kc_per, ke = min(kchunks, kb + p.kc_per);
+                for (int kc = kb; kc < ke; ++kc) {
+                  if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, err, 1)) goto producer_done;
+                  uint8_t *st = smem + stage * C::STAGE_BYTES;
+                  mbar_expect_tx(&full[stage], (uint32_t)(C::A_BYTES + nb * C::B_BYTES));
+                  tma_load_2d(smem_u32(st), mAhi, &full[stage], kc * BK, ya + a * (int)p.a_plane);
+                  for (int b = 0; b < nb; ++b)
+                    tma_load_2d(smem_u32(st + C::A_BYTES + b * C::B_BYTES), mBhi, &full[stage], kc * BK,
+                                yb + (b0 + b) * (int)p.b_plane);
+                  if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
+                }
               }
-            }
-          }
         } else {
           for (int64_t u = 0; u < len; ++u, ++tc.s) {
             const KRange kr = k_range<BK>(p, tc.s);
@@ -370,44 +420,36 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
         // the jobs of an item share the tile; only the K split advances (decode once per item)
         TileCoord tc = decode(p, li * len);
         if constexpr (SLICE) {
-          // splits (a, q, b), b fastest: the nb = nsl - a accumulators of (a, q) are filled together
-          // from the stages of run q, then handed to the epilogue in split order
+          // units (a, run, b0) in the producer's order: one accumulator buffer per unit, nb
+          // adjacent accumulators of BN columns filled by one MMA of width nb * BN per K step
           const int kchunks = (int)(p.K / BK);
           const int q0 = (int)(tc.s / p.spg) * p.rpg;
-          for (int a = 0; a < p.nsl; ++a) {
-            const int nb = p.nsl - a;
-            for (int qr = q0; qr < q0 + p.rpg; ++qr) {
-              const int kb = qr * p.kc_per, ke = min(kchunks, kb + p.kc_per);
-              // acquire nb accumulators in ring order: buffers buf0, buf0 + 1, ... (mod NBUF); the
-              // indices are computed, not stored (an indexed array would live in local memory on
-              // the MMA thread's critical path)
-              const int buf0 = buf;
-              for (int b = 0; b < nb; ++b) {
+          for (int a = 0; a < p.nsl; ++a)
+            for (int qr = q0; qr < q0 + p.rpg; ++qr)
+              for (int b0 = 0; b0 < p.nsl - a; b0 += C::UNIT) {
+                const int nb = min(C::UNIT, p.nsl - a - b0);
+                const int kb = qr * p.kc_per, ke = min(kchunks, kb + p.kc_per);
+                const uint32_t idesc_u = (idesc & ~(0x3Fu << 17)) | ((uint32_t)((nb * BN) >> 3) << 17);
                 if (!mbar_wait(&acce[buf], aphase ^ 1, abort_flag, err, 2)) goto mma_done;
+                fence_after();
+                const uint32_t dtu = tmem_base + (uint32_t)(buf * C::BUFW);
+                for (int kc = kb; kc < ke; ++kc) {
+                  if (!mbar_wait(&full[stage], phase, abort_flag, err, 3)) goto mma_done;
+                  fence_after();
+                  const uint32_t st = smem_u32(smem + stage * C::STAGE_BYTES);
+                  // descriptors are linear in the address (bits 0-13 hold addr >> 4): + 2 per
+                  // 16-element K step; the B planes of the unit are one stacked operand
+                  const uint64_t da = sdesc(st, C::SBO, C::LAYOUT);
+                  const uint64_t db = sdesc(st + C::A_BYTES, C::SBO, C::LAYOUT);
+                  mma_bf16(dtu, da, db, idesc_u, kc > kb ? 1u : 0u);
+#pragma unroll
+                  for (int kk = 1; kk < BK / 16; ++kk) mma_bf16(dtu, da + 2 * kk, db + 2 * kk, idesc_u, 1u);
+                  mma_commit(&empty[stage]);
+                  if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
+                }
+                mma_commit(&accf[buf]);
                 if (++buf == C::NBUF) { buf = 0; aphase ^= 1; }
               }
-              fence_after();
-              for (int kc = kb; kc < ke; ++kc) {
-                if (!mbar_wait(&full[stage], phase, abort_flag, err, 3)) goto mma_done;
-                fence_after();
-                const uint32_t st = smem_u32(smem + stage * C::STAGE_BYTES);
-                const uint32_t acc = kc > kb ? 1u : 0u;
-                // descriptors are linear in the address (bits 0-13 hold addr >> 4): one per plane,
-                // plus 2 per 16-element K step
-                const uint64_t da = sdesc(st, C::SBO, C::LAYOUT);
-                uint64_t db = sdesc(st + C::A_BYTES, C::SBO, C::LAYOUT);
-                for (int b = 0; b < nb; ++b, db += C::B_BYTES >> 4) {
-                  const uint32_t dtb = tmem_base + (uint32_t)(((buf0 + b) & (C::NBUF - 1)) * BN);
-                  mma_bf16(dtb, da, db, idesc, acc);
-#pragma unroll
-                  for (int kk = 1; kk < BK / 16; ++kk) mma_bf16(dtb, da + 2 * kk, db + 2 * kk, idesc, 1u);
-                }
-                mma_commit(&empty[stage]);
-                if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
-              }
-              for (int b = 0; b < nb; ++b) mma_commit(&accf[(buf0 + b) & (C::NBUF - 1)]);
-            }
-          }
           continue;
         }
         for (int64_t u = 0; u < len; ++u, ++tc.s) {
@@ -472,6 +514,32 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
       // partial offset: the K split (F32 partials) or the split group (kacc groups)
       const int64_t rbase = (i / e.rd) * e.ro1 + (i % e.rd) * e.ro2 + tc.b * e.bo +
                             (p.kacc ? (tc.s / p.spg) * e.so : tc.s * e.so);
+      if constexpr (SLICE) {
+        // the units of the item in the MMA's order; each buffer holds nb adjacent accumulators
+        const int q0 = (int)(tc.s / p.spg) * p.rpg;
+        bool first = true;
+        for (int a = 0; a < p.nsl; ++a)
+          for (int qr = q0; qr < q0 + p.rpg; ++qr)
+            for (int b0 = 0; b0 < p.nsl - a; b0 += C::UNIT) {
+              const int nb = min(C::UNIT, p.nsl - a - b0);
+              if (!mbar_wait(&accf[buf], aphase, abort_flag, err, 4)) goto epi_done;
+              fence_after();
+              if (cbeg < cend) {
+                for (int j = 0; j < nb; ++j) {
+                  uint32_t r[32];
+                  tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * C::BUFW + j * BN + cbeg), r);
+                  pair_add(kv, r, first);
+                  first = false;
+                }
+              }
+              fence_before();
+              __syncwarp();
+              if (lane == 0) mbar_arrive(&acce[buf]);
+              if (++buf == C::NBUF) { buf = 0; aphase ^= 1; }
+            }
+        if (row_ok && cbeg < cend) pair_write(kv, e, p.N, tc.n * BN + cbeg, rbase);
+        continue;
+      }
       for (int64_t u = 0; u < len; ++u, ++tc.s) {
       if (!mbar_wait(&accf[buf], aphase, abort_flag, err, 4)) goto epi_done;
       fence_after();
@@ -480,52 +548,10 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
           // this thread's 32 columns (cbeg == cend for the idle half of a BN = 32 tile)
           if (cbeg < cend) {
             uint32_t r[32];
-            tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + cbeg), r);
+            tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * C::BUFW + cbeg), r);
             const int64_t sg = u;  // position inside the split group (an item is one group)
-            // The splits' FP32 sums are added as an unevaluated pair of floats (Knuth's TwoSum,
-            // error-free; about 48 significant bits), held in the bits of kv[j] (hi, lo): no FP64
-            // instruction per split (the FP64 pipe of GB300 runs at 2 operations per clock and
-            // SM).  In slice mode every split sum is exact, so the result is the exact sum of
-            // the splits to that precision.
-#pragma unroll
-            for (int j = 0; j < 32; ++j) {
-              const float x = __uint_as_float(r[j]);
-              float hi = 0.f, lo = 0.f;
-              if (sg != 0) {
-                hi = __int_as_float(__double2hiint(kv[j]));
-                lo = __int_as_float(__double2loint(kv[j]));
-              }
-              const float sum = hi + x;
-              const float bb = sum - hi;
-              lo += (hi - (sum - bb)) + (x - bb);
-              kv[j] = __hiloint2double(__float_as_int(sum), __float_as_int(lo));
-            }
-            if (row_ok && sg == p.spg - 1) {
-              // the K splits summed in split order
-              int64_t n = tc.n * BN + cbeg, nq = n / e.cd, nr = n % e.cd;
-#pragma unroll
-              for (int j = 0; j < 32; ++j) {
-                if (n < p.N && nr < e.clim) {
-                  const int64_t off = rbase + nq * e.co1 + nr * e.co2;
-                  if (e.kind == TcEpilogue::PAIR_F32) {
-                    reinterpret_cast<float2 *>(e.out_f32)[off] =
-                        make_float2(__int_as_float(__double2hiint(kv[j])), __int_as_float(__double2loint(kv[j])));
-                  } else {
-                    const double val = (double)__int_as_float(__double2hiint(kv[j])) +
-                                       (double)__int_as_float(__double2loint(kv[j]));
-                    if (e.kind == TcEpilogue::AXPBY_F64) {
-                      double *y = e.out_f64 + off;
-                      const double rv = e.alpha * val;
-                      *y = (e.beta == 0.0) ? rv : fma(e.beta, *y, rv);
-                    } else {
-                      epi_store(e, off, (float)val);
-                    }
-                  }
-                }
-                ++n;
-                if (++nr == e.cd) { nr = 0; ++nq; }
-              }
-            }
+            pair_add(kv, r, sg == 0);
+            if (row_ok && sg == p.spg - 1) pair_write(kv, e, p.N, tc.n * BN + cbeg, rbase);  // split order
           }
           fence_before();
           __syncwarp();
@@ -537,7 +563,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
 #pragma unroll 1
       for (int c0 = cbeg; c0 < cend; c0 += 32) {
         uint32_t r[32];
-        tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + c0), r);
+        tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * C::BUFW + c0), r);
         if (!row_ok) continue;
         const int64_t n0 = tc.n * BN + c0;
         const int64_t nq0 = n0 / e.cd, nr0 = n0 % e.cd;
