@@ -737,6 +737,18 @@ struct F64In {
   __device__ __forceinline__ long long fixed(int64_t i, int e, int B) const {
     return fixed_point(__ldg(p + i), e, B);
   }
+  // four consecutive elements (32-byte aligned): raw words, |x| bits, fixed point of a word
+  __device__ __forceinline__ void load4(int64_t i, unsigned long long (&w)[4]) const {
+    const ulonglong2 a = __ldg(reinterpret_cast<const ulonglong2 *>(p + i));
+    const ulonglong2 b = __ldg(reinterpret_cast<const ulonglong2 *>(p + i) + 1);
+    w[0] = a.x; w[1] = a.y; w[2] = b.x; w[3] = b.y;
+  }
+  __device__ __forceinline__ static unsigned long long abs_word(unsigned long long w) {
+    return w & 0x7FFFFFFFFFFFFFFFull;
+  }
+  __device__ __forceinline__ static long long fixed_word(unsigned long long w, int e, int B) {
+    return fixed_point(w, e, B);
+  }
 };
 struct PairIn {
   const unsigned long long *p;  // float2 elements
@@ -747,14 +759,52 @@ struct PairIn {
     return mx == 0 ? 0 : max((int)(mx >> 23), 1) - 126;
   }
   __device__ __forceinline__ long long fixed(int64_t i, int e, int B) const {
-    const unsigned long long v = __ldg(p + i);  // little-endian float2: hi in the low word
+    return fixed_word(__ldg(p + i), e, B);
+  }
+  __device__ __forceinline__ void load4(int64_t i, unsigned long long (&w)[4]) const {
+    const ulonglong2 a = __ldg(reinterpret_cast<const ulonglong2 *>(p + i));
+    const ulonglong2 b = __ldg(reinterpret_cast<const ulonglong2 *>(p + i) + 1);
+    w[0] = a.x; w[1] = a.y; w[2] = b.x; w[3] = b.y;
+  }
+  __device__ __forceinline__ static unsigned long long abs_word(unsigned long long w) {
+    return (unsigned long long)((unsigned)w & 0x7FFFFFFFu);
+  }
+  __device__ __forceinline__ static long long fixed_word(unsigned long long v, int e, int B) {
+    // little-endian float2: hi in the low word
     return fixed_point_f32((unsigned)v, e, B) + fixed_point_f32((unsigned)(v >> 32), e, B);
   }
 };
 
-template <class In>
-__global__ void slice_kernel(const In in, int64_t rows, int64_t cols, const SplitMap m, int nsl, int64_t chunk,
+// The bf16 bits of digit d (|d| <= 128) of a run with scale exponent e at digit position t >= 1:
+// d 2^(e - 7 t), exact; scales below the FP32 normal range flush to 0.
+__device__ __forceinline__ uint16_t digit_bits(long long d, int e, int t) {
+  const int pe = e - 7 * t + 127;
+  float v = 0.f;
+  if (pe >= 1 && pe <= 254) v = (float)(int)d * __int_as_float(pe << 23);
+  return __bfloat16_as_ushort(__float2bfloat16_rn(v));
+}
+
+// The digits of one element (fixed point rem of B = 7 nsl bits) into d[0 .. nsl).
+__device__ __forceinline__ void digits(long long rem, int nsl, long long (&d)[kMaxDigits]) {
+#pragma unroll
+  for (int sl = 0; sl < kMaxDigits; ++sl) {
+    const int shift = 7 * (nsl - 1 - sl);  // digit sl + 1 has weight 2^(B - 7 (sl + 1))
+    long long v = sl < nsl ? rem : 0;      // the last digit: the remaining |rem| <= 64
+    if (shift > 0) {
+      v = (rem + (1LL << (shift - 1))) >> shift;  // round half up (arithmetic shift: floor)
+      rem -= v << shift;
+    }
+    d[sl] = v;
+  }
+}
+
+// VEC = 4: a lane handles 4 consecutive columns (one 32-byte load, one 8-byte store per plane);
+// needs unit column stride, runs and row bases aligned to 4 elements.
+// NSL > 0: the digit count as a compile-time constant (constant shifts); 0: nsl at run time.
+template <class In, int VEC, int NSL>
+__global__ void slice_kernel(const In in, int64_t rows, int64_t cols, const SplitMap m, int nsl_rt, int64_t chunk,
                              uint16_t *__restrict__ out, int64_t ldo, int64_t plane) {
+  const int nsl = NSL > 0 ? NSL : nsl_rt;
   const int lane = threadIdx.x & 31;
   const int64_t nchunks = (cols + chunk - 1) / chunk;
   const int64_t units = rows * nchunks;
@@ -766,9 +816,28 @@ __global__ void slice_kernel(const In in, int64_t rows, int64_t cols, const Spli
     const int64_t base = rq * m.rs1 + rr * m.rs2;
     const int64_t c0 = q * chunk, c1 = min(cols, c0 + chunk);
     unsigned long long mx = 0;  // largest |x| as a bit pattern (ordered like the values)
-    for (int64_t c = c0 + lane; c < c1; c += 32) {
-      const unsigned long long a = in.abs_bits(base + c * m.cs);
-      mx = a > mx ? a : mx;
+    if constexpr (VEC == 4) {
+      for (int64_t c = c0 + 4 * lane; c < c1; c += 128) {
+        if (c + 4 <= c1) {
+          unsigned long long w[4];
+          in.load4(base + c, w);
+#pragma unroll
+          for (int v = 0; v < 4; ++v) {
+            const unsigned long long a = In::abs_word(w[v]);
+            mx = a > mx ? a : mx;
+          }
+        } else {
+          for (int64_t cc = c; cc < c1; ++cc) {
+            const unsigned long long a = In::abs_word(__ldg(in.p + base + cc));
+            mx = a > mx ? a : mx;
+          }
+        }
+      }
+    } else {
+      for (int64_t c = c0 + lane; c < c1; c += 32) {
+        const unsigned long long a = in.abs_bits(base + c * m.cs);
+        mx = a > mx ? a : mx;
+      }
     }
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
@@ -777,20 +846,46 @@ __global__ void slice_kernel(const In in, int64_t rows, int64_t cols, const Spli
     }
     const int e = In::exponent(mx);
     uint16_t *orow = out + r * ldo;
-    for (int64_t c = c0 + lane; c < c1; c += 32) {
-      long long rem = mx == 0 ? 0 : in.fixed(base + c * m.cs, e, 7 * nsl);
-      for (int sl = 0; sl < nsl; ++sl) {
-        const int shift = 7 * (nsl - 1 - sl);  // digit sl + 1 has weight 2^(B - 7 (sl + 1))
-        long long d = rem;                     // the last digit: the remaining |rem| <= 64
-        if (shift > 0) {
-          d = (rem + (1LL << (shift - 1))) >> shift;  // round half up (arithmetic shift: floor)
-          rem -= d << shift;
+    if constexpr (VEC == 4) {
+      for (int64_t c = c0 + 4 * lane; c < c1; c += 128) {
+        const int nv = (int)min((int64_t)4, c1 - c);
+        unsigned long long w[4] = {0, 0, 0, 0};
+        if (nv == 4) {
+          in.load4(base + c, w);
+        } else {
+#pragma unroll
+          for (int v = 0; v < 4; ++v)
+            if (v < nv) w[v] = __ldg(in.p + base + c + v);
         }
-        // the bf16 value d 2^(e - 7 (sl + 1)): |d| <= 128 is exact in bf16; tiny scales flush to 0
-        const int pe = e - 7 * (sl + 1) + 127;
-        float v = 0.f;
-        if (pe >= 1 && pe <= 254) v = (float)d * __int_as_float(pe << 23);
-        orow[sl * plane + c] = __bfloat16_as_ushort(__float2bfloat16_rn(v));
+        long long d[4][kMaxDigits];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) digits((v < nv && mx != 0) ? In::fixed_word(w[v], e, 7 * nsl) : 0, nsl, d[v]);
+#pragma unroll
+        for (int sl = 0; sl < kMaxDigits; ++sl) {
+          if (sl >= nsl) break;
+          uint16_t *o = orow + sl * plane + c;
+          if (nv == 4) {
+            const unsigned long long bits = (unsigned long long)digit_bits(d[0][sl], e, sl + 1) |
+                                            ((unsigned long long)digit_bits(d[1][sl], e, sl + 1) << 16) |
+                                            ((unsigned long long)digit_bits(d[2][sl], e, sl + 1) << 32) |
+                                            ((unsigned long long)digit_bits(d[3][sl], e, sl + 1) << 48);
+            *reinterpret_cast<unsigned long long *>(o) = bits;
+          } else {
+#pragma unroll
+            for (int v = 0; v < 4; ++v)
+              if (v < nv) o[v] = digit_bits(d[v][sl], e, sl + 1);
+          }
+        }
+      }
+    } else {
+      for (int64_t c = c0 + lane; c < c1; c += 32) {
+        long long d[kMaxDigits];
+        digits(mx == 0 ? 0 : in.fixed(base + c * m.cs, e, 7 * nsl), nsl, d);
+#pragma unroll
+        for (int sl = 0; sl < kMaxDigits; ++sl) {
+          if (sl >= nsl) break;
+          orow[sl * plane + c] = digit_bits(d[sl], e, sl + 1);
+        }
       }
     }
   }
@@ -1089,26 +1184,38 @@ void reduce_grouped(const std::vector<ReduceJob> &jobs, cudaStream_t s) {
 void slice_f64(const double *x, int64_t rows, int64_t cols, const SplitMap &m, int nslices, int64_t chunk,
                uint16_t *out, int64_t ldo, int64_t plane, cudaStream_t s) {
   if (rows <= 0 || cols <= 0) return;
-  VGB_REQUIRE(m.rdiv >= 1 && nslices >= 1 && nslices <= 7 && chunk >= 1 && chunk <= 1024 && ldo >= cols &&
-                  plane >= rows * ldo,
+  VGB_REQUIRE(m.rdiv >= 1 && nslices >= 1 && nslices <= kMaxDigits && chunk >= 1 && chunk <= 1024 &&
+                  ldo >= cols && plane >= rows * ldo,
               "slice: bad map or sizes");
   const int64_t warps = rows * ceil_div(cols, chunk);
   const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(warps, 8), 64LL * sm_count()));
-  slice_kernel<<<blocks, 256, 0, s>>>(F64In{reinterpret_cast<const unsigned long long *>(x)}, rows, cols, m,
-                                      nslices, chunk, out, ldo, plane);
+  const F64In in{reinterpret_cast<const unsigned long long *>(x)};
+  if (m.cs == 1 && chunk % 4 == 0 && m.rs1 % 4 == 0 && m.rs2 % 4 == 0 && ldo % 4 == 0 && plane % 4 == 0 &&
+      ((uintptr_t)x & 31) == 0 && ((uintptr_t)out & 7) == 0) {
+    if (nslices == 5) slice_kernel<F64In, 4, 5><<<blocks, 256, 0, s>>>(in, rows, cols, m, nslices, chunk, out, ldo, plane);
+    else slice_kernel<F64In, 4, 0><<<blocks, 256, 0, s>>>(in, rows, cols, m, nslices, chunk, out, ldo, plane);
+  } else {
+    slice_kernel<F64In, 1, 0><<<blocks, 256, 0, s>>>(in, rows, cols, m, nslices, chunk, out, ldo, plane);
+  }
   VGB_LAUNCH_CHECK();
 }
 
 void slice_pairs(const float *x2, int64_t rows, int64_t cols, const SplitMap &m, int nslices, int64_t chunk,
                  uint16_t *out, int64_t ldo, int64_t plane, cudaStream_t s) {
   if (rows <= 0 || cols <= 0) return;
-  VGB_REQUIRE(((uintptr_t)x2 & 7) == 0 && m.rdiv >= 1 && nslices >= 1 && nslices <= 7 && chunk >= 1 &&
+  VGB_REQUIRE(((uintptr_t)x2 & 7) == 0 && m.rdiv >= 1 && nslices >= 1 && nslices <= kMaxDigits && chunk >= 1 &&
                   chunk <= 1024 && ldo >= cols && plane >= rows * ldo,
               "slice: bad map or sizes");
   const int64_t warps = rows * ceil_div(cols, chunk);
   const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(warps, 8), 64LL * sm_count()));
-  slice_kernel<<<blocks, 256, 0, s>>>(PairIn{reinterpret_cast<const unsigned long long *>(x2)}, rows, cols, m,
-                                       nslices, chunk, out, ldo, plane);
+  const PairIn in{reinterpret_cast<const unsigned long long *>(x2)};
+  if (m.cs == 1 && chunk % 4 == 0 && m.rs1 % 4 == 0 && m.rs2 % 4 == 0 && ldo % 4 == 0 && plane % 4 == 0 &&
+      ((uintptr_t)x2 & 31) == 0 && ((uintptr_t)out & 7) == 0) {
+    if (nslices == 5) slice_kernel<PairIn, 4, 5><<<blocks, 256, 0, s>>>(in, rows, cols, m, nslices, chunk, out, ldo, plane);
+    else slice_kernel<PairIn, 4, 0><<<blocks, 256, 0, s>>>(in, rows, cols, m, nslices, chunk, out, ldo, plane);
+  } else {
+    slice_kernel<PairIn, 1, 0><<<blocks, 256, 0, s>>>(in, rows, cols, m, nslices, chunk, out, ldo, plane);
+  }
   VGB_LAUNCH_CHECK();
 }
 
