@@ -816,6 +816,38 @@ def solve_only(args):
     print(json.dumps({"workload": f"tda_singlet_v{v}_c{c}_naux{naux}_roots{ROOTS}_solve", **out}))
 
 
+def product_only(args):
+    """A profiler workload: the Hd product (cd = 1 only) of one precision applied twice to k
+    vectors at the workload shape (--shape), the second application timed."""
+    import torch
+
+    from votca_gb300 import bse_operator as bo
+    from votca_gb300.synthetic import qp_energies, screening_w
+
+    v, c, naux, nmo = V, C, NAUX, NMO
+    if args.shape:
+        v, c, naux, nmo = (int(x) for x in args.shape.split(","))
+    prec = {"mixed": bo.PRECISION_MIXED, "sliced": bo.PRECISION_SLICED, "fp64": bo.PRECISION_FP64}[args.product_only]
+    k = args.columns
+    mmn = make_mmn(1, naux, nmo)
+    opt = bo.BSEOperator_Options(homo=v - 1, rpamin=0, qpmin=0, vmin=0, cmax=v + c - 1)
+    ctx = bo.GpuBSEContext(screening_w(1, naux), bo.TCMatrix_gwbse(mmn), np.diag(qp_energies(1, v, c)), opt,
+                           precision=prec)
+    n = v * c
+    X = torch.randn((k, n), dtype=torch.float64, device="cuda")
+    Y = torch.empty((k, n), dtype=torch.float64, device="cuda")
+    op = bo.HdOperator(ctx)
+    ms = []
+    for _ in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        op.matmul_device(X.data_ptr(), n, k, Y.data_ptr(), n, torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        ms.append((time.perf_counter() - t0) * 1e3)
+    ctx.close()
+    print(json.dumps({"workload": f"hd_product_{args.product_only}_v{v}_c{c}_naux{naux}_k{k}", "ms": ms}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -835,12 +867,17 @@ def main():
                          "FP64 polish; about 1.5 minutes, ~110 GB of HBM)")
     ap.add_argument("--no-full-bse-check", dest="full_bse_check", action="store_false",
                     help="skip the independent FP64 evaluation of the full-BSE roots")
+    ap.add_argument("--product-only", default=None, choices=["mixed", "sliced", "fp64"],
+                    help="profiler workload: the Hd product of that precision, twice, at the workload shape")
+    ap.add_argument("--columns", type=int, default=8, help="vectors of --product-only")
     ap.add_argument("--solve-only", action="store_true",
                     help="one split-precision 20-singlet solve (with its FP64 polish) at the workload shape, "
                          "after one warm-up solve, and nothing else (for profiler captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.product_only:
+        return product_only(args)
     if args.solve_only:
         return solve_only(args)
 

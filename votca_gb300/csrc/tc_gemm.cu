@@ -199,34 +199,38 @@ __device__ __forceinline__ void epi_store(const TcEpilogue &e, int64_t off, floa
 }
 
 // The K splits' FP32 sums of a tile are added as an unevaluated pair of floats (Knuth's TwoSum,
-// error-free; about 48 significant bits), held in the bits of kv[j] (hi, lo): no FP64 instruction
-// per split (the FP64 pipe of GB300 runs at 2 operations per clock and SM).  In slice mode every
-// split sum is exact, so the result is the exact sum of the splits to that precision.
-__device__ __forceinline__ void pair_add(double (&kv)[32], const uint32_t (&r)[32], bool first) {
+// error-free; about 48 significant bits) in kh[j] + kl[j]: no FP64 instruction per split (the
+// FP64 pipe of GB300 runs at 2 operations per clock and SM).  In slice mode every split sum is
+// exact, so the result is the exact sum of the splits to that precision.
+__device__ __forceinline__ void pair_add(float (&kh)[32], float (&kl)[32], const uint32_t (&r)[32], bool first) {
+  if (first) {
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+      kh[j] = __uint_as_float(r[j]);
+      kl[j] = 0.f;
+    }
+    return;
+  }
 #pragma unroll
   for (int j = 0; j < 32; ++j) {
-    const float x = __uint_as_float(r[j]);
-    float hi = 0.f, lo = 0.f;
-    if (!first) {
-      hi = __int_as_float(__double2hiint(kv[j]));
-      lo = __int_as_float(__double2loint(kv[j]));
-    }
+    const float x = __uint_as_float(r[j]), hi = kh[j];
     const float sum = hi + x;
     const float bb = sum - hi;
-    lo += (hi - (sum - bb)) + (x - bb);
-    kv[j] = __hiloint2double(__float_as_int(sum), __float_as_int(lo));
+    kl[j] += (hi - (sum - bb)) + (x - bb);
+    kh[j] = sum;
   }
 }
 
 // Writes a thread's 32 float-pair sums (columns n0 ..) of row base rbase through the epilogue map.
-__device__ __forceinline__ void pair_write(const double (&kv)[32], const TcEpilogue &e, int64_t N, int64_t n0,
+__device__ __forceinline__ void pair_write(const float (&kh)[32], const float (&kl)[32], const TcEpilogue &e,
+                                           int64_t N, int64_t n0,
                                            int64_t rbase) {
   int64_t n = n0, nq = n / e.cd, nr = n % e.cd;
 #pragma unroll
   for (int j = 0; j < 32; ++j) {
     if (n < N && nr < e.clim) {
       const int64_t off = rbase + nq * e.co1 + nr * e.co2;
-      const float hi = __int_as_float(__double2hiint(kv[j])), lo = __int_as_float(__double2loint(kv[j]));
+      const float hi = kh[j], lo = kl[j];
       if (e.kind == TcEpilogue::PAIR_F32) {
         reinterpret_cast<float2 *>(e.out_f32)[off] = make_float2(hi, lo);
       } else {
@@ -497,7 +501,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
     const int cend = (BN >= 64 || half == 0) ? cbeg + COLS : BN;
     // float-pair sums over the K splits of a tile (kacc; BN <= 64: at most 32 columns per thread)
     constexpr int KACC = BN <= 64 ? 32 : 1;
-    double kv[KACC];
+    float kh[KACC], kl[KACC];
     int buf = 0;
     uint32_t aphase = 0;
     int hint = 0;
@@ -528,7 +532,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
                 for (int j = 0; j < nb; ++j) {
                   uint32_t r[32];
                   tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * C::BUFW + j * BN + cbeg), r);
-                  pair_add(kv, r, first);
+                  pair_add(kh, kl, r, first);
                   first = false;
                 }
               }
@@ -537,7 +541,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
               if (lane == 0) mbar_arrive(&acce[buf]);
               if (++buf == C::NBUF) { buf = 0; aphase ^= 1; }
             }
-        if (row_ok && cbeg < cend) pair_write(kv, e, p.N, tc.n * BN + cbeg, rbase);
+        if (row_ok && cbeg < cend) pair_write(kh, kl, e, p.N, tc.n * BN + cbeg, rbase);
         continue;
       }
       for (int64_t u = 0; u < len; ++u, ++tc.s) {
@@ -550,8 +554,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
             uint32_t r[32];
             tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * C::BUFW + cbeg), r);
             const int64_t sg = u;  // position inside the split group (an item is one group)
-            pair_add(kv, r, sg == 0);
-            if (row_ok && sg == p.spg - 1) pair_write(kv, e, p.N, tc.n * BN + cbeg, rbase);  // split order
+            pair_add(kh, kl, r, sg == 0);
+            if (row_ok && sg == p.spg - 1) pair_write(kh, kl, e, p.N, tc.n * BN + cbeg, rbase);  // split order
           }
           fence_before();
           __syncwarp();
