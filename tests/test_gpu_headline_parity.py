@@ -5,7 +5,8 @@
   FP64 oracle (all 32768 rows, 3 vectors) at 1e-11 normwise, and sampled rows against the
   reference loop nest itself (each row built as bse_operator.cc:52-116 builds it);
 - the same products in split precision (BF16x3, FP32 accumulation) against both, at the
-  split tolerance on the interaction part;
+  split tolerance on the interaction part, and as Ozaki slice products against the factorised
+  oracle at 5e-10 of the interaction part (measured 2.6-2.9e-10);
 - the lowest 20 singlets and 20 triplets at residual 1e-7 in FP64 and in split precision:
   every root within 0.1 meV of FP64 and every eigenvector overlap >= 1 - 1e-6 (the accuracy
   bound of the mixed form), the residuals of the returned roots under the oracle's product
@@ -24,6 +25,8 @@ pytestmark = [pytest.mark.gpu, pytest.mark.slow]
 V, C, NAUX, NMO, SEED = 64, 512, 2048, 576, 1
 # split products: relative error of the interaction part (measured ~1e-5 at this size)
 MIXED_TOL = 5e-5
+# Ozaki slice products (five 7-bit digits): 2.6-2.9e-10 of the interaction part measured here
+SLICED_TOL = 5e-10
 OPS = ("singlet", "triplet", "singlet_b")
 
 
@@ -40,10 +43,12 @@ def c1():
     Mmn = bo.TCMatrix_gwbse(mmn)
     f = bo.GpuBSEContext(w, Mmn, hqp, opt, precision=bo.PRECISION_FP64)
     m = bo.GpuBSEContext(w, Mmn, hqp, opt, precision=bo.PRECISION_MIXED)
+    sl = bo.GpuBSEContext(w, Mmn, hqp, opt, precision=bo.PRECISION_SLICED)
     prob = oracle.BSEProblem(mmn, w, hqp, V, C)
-    yield {"f": f, "m": m, "prob": prob}
+    yield {"f": f, "m": m, "s": sl, "prob": prob}
     f.close()
     m.close()
+    sl.close()
 
 
 def _gpu(ctx, op, X):
@@ -65,8 +70,12 @@ def test_fp64_and_mixed_products_match_factorised_oracle(c1):
         inter = ref[op] - (hqp_part if oracle.OPERATORS[op][0] else 0.0)
         ym = _gpu(c1["m"], op, X)
         errm = np.linalg.norm(ym - ref[op]) / np.linalg.norm(inter)
-        print(f"{op}: fp64 vs oracle {err:.2e}, mixed vs oracle {errm:.2e} (interaction part)")
+        ys = _gpu(c1["s"], op, X)
+        errs = np.linalg.norm(ys - ref[op]) / np.linalg.norm(inter)
+        print(f"{op}: fp64 vs oracle {err:.2e}, mixed vs oracle {errm:.2e}, "
+              f"slice products vs oracle {errs:.2e} (interaction part)")
         assert errm <= MIXED_TOL, (op, errm)
+        assert errs <= SLICED_TOL, (op, errs)
 
 
 def test_rows_match_reference_loop_nest(c1):
