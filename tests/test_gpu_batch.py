@@ -189,3 +189,42 @@ def test_batch_reports_failing_molecule():
 def test_batch_empty():
     ev, info, iters = _solver().solve_batch([], 5)
     assert ev.shape == (0, 5) and info == [] and iters.size == 0
+
+
+def test_lockstep_autotuned_launch_shapes():
+    """With at least 16 operators in a dense product round the launch shape of the grouped dense
+    products is chosen by timing every candidate; the report lists the candidates and the choice,
+    and the roots are those of the FP64 dense eigenproblems."""
+    import json
+
+    from votca_gb300 import _lib
+    from votca_gb300 import bse_operator as bo
+    from bench import autotune_table
+
+    ctxs, dense = [], []
+    for i in range(20):
+        v, c, naux, seed = SHAPES[i % len(SHAPES)]
+        p = Problem(v=v, c=c, naux=naux, nmo=v + c + 8, seed=100 + i)
+        opt = bo.BSEOperator_Options(homo=v - 1, rpamin=0, qpmin=0, vmin=0, cmax=v + c - 1)
+        ctx = bo.GpuBSEContext(p.w, bo.TCMatrix_gwbse(p.mmn), p.hqp[:v + c, :v + c], opt, precision=1)
+        c64 = bo.GpuBSEContext(p.w, bo.TCMatrix_gwbse(p.mmn), p.hqp[:v + c, :v + c], opt, precision=0)
+        op64 = bo.SingletOperator_TDA(c64)
+        H = op64.matmul(np.eye(op64.rows()))
+        dense.append(np.linalg.eigvalsh(0.5 * (H + H.T))[:5])
+        c64.close()
+        ctxs.append(ctx)
+    ops = [bo.SingletOperator_TDA(ctx) for ctx in ctxs]
+    ev, info, _ = _solver().solve_batch(ops, 5, nthreads=0)
+    assert all(i == "Success" for i in info)
+    np.testing.assert_allclose(ev, np.array(dense), rtol=0, atol=1e-6)
+    table = autotune_table()
+    dense_rows = [t for t in table if t["kernel"] == "grouped dense product"]
+    assert dense_rows, table
+    for t in dense_rows:
+        assert t["chosen"]["bk"] in (32, 64) and t["chosen"]["operators_per_launch"] in (8, 16, 32)
+        assert len(t["candidates_ms"]) == 6 and all(c[2] > 0 for c in t["candidates_ms"])
+        best = min(t["candidates_ms"], key=lambda c: c[2])
+        assert [best[0], best[1]] == [t["chosen"]["bk"], t["chosen"]["operators_per_launch"]]
+    json.dumps(table)
+    for ctx in ctxs:
+        ctx.close()
