@@ -664,7 +664,7 @@ def roots_report(ctx, precision, w, Mmn, hqp, opt):
             A64 = cls(ctxs["fp64"])
             r64 = A64.matmul(xm) - xm * lam_m
             res["mixed"]["max_fp64_residual"] = float(np.max(np.linalg.norm(r64, axis=0)))
-            # for reference: the split-precision iteration alone (no FP64 polish), its roots judged
+            # for reference: the split-precision iteration alone (no FP64 polish), its roots evaluated
             # against the FP64 operator the same way
             ds = DavidsonSolver()
             ds.set_tolerance(1e-7)
