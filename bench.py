@@ -495,8 +495,8 @@ def batched_solve(n_molecules, nthreads, roots=5, tol=1e-7, cpu=False):
         "dims": [int(s["v"] * s["c"]) for s in shapes[:4]] + ["..."],
         "autotune": autotune_table(),
         "autotune_note": "launch shapes of the grouped dense products, chosen by timing every candidate "
-                         "([K box, operators per launch, ms]) on the first solve's first product round "
-                         "(included in first_solve_seconds)",
+                         "([K box, operators per launch, streams, ms]) on the first solve's first product "
+                         "round (included in first_solve_seconds)",
     }
     if cpu:
         out["cpu_baseline"] = cpu_baseline_batched(shapes, roots, tol)

@@ -375,7 +375,7 @@ int bse_small_gen_eig(int64_t m, int64_t nw, const double *T, const double *B, d
 
 /* The launch shapes the autotuner has chosen in this process (no counterpart in the reference):
  * a JSON array, one object per tuned kernel and tile width, with the chosen shape and every
- * candidate's measured time ([K box, operators per launch, ms]).  The grouped dense products of
+ * candidate's measured time ([K box, operators per launch, streams, ms]).  The grouped dense products of
  * the lockstep batch are tuned on their first product round with at least 16 operators
  * (environment VGB_TC_AUTOTUNE=0 keeps the fixed shape).  buf (may be NULL) receives at most
  * cap - 1 characters and a terminating zero; *needed (may be NULL) the full length + 1. */

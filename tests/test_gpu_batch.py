@@ -222,9 +222,11 @@ def test_lockstep_autotuned_launch_shapes():
     assert dense_rows, table
     for t in dense_rows:
         assert t["chosen"]["bk"] in (32, 64) and t["chosen"]["operators_per_launch"] in (8, 16, 32)
-        assert len(t["candidates_ms"]) == 6 and all(c[2] > 0 for c in t["candidates_ms"])
-        best = min(t["candidates_ms"], key=lambda c: c[2])
-        assert [best[0], best[1]] == [t["chosen"]["bk"], t["chosen"]["operators_per_launch"]]
+        assert t["chosen"]["streams"] in (1, 4)
+        assert len(t["candidates_ms"]) == 12 and all(c[3] > 0 for c in t["candidates_ms"])
+        chosen = [c for c in t["candidates_ms"]
+                  if c[:3] == [t["chosen"]["bk"], t["chosen"]["operators_per_launch"], t["chosen"]["streams"]]]
+        assert len(chosen) == 1 and chosen[0][3] <= min(c[3] for c in t["candidates_ms"])  # the fastest
     json.dumps(table)
     for ctx in ctxs:
         ctx.close()

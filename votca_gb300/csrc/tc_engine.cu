@@ -653,10 +653,10 @@ struct GemmBuckets {
     owner[key].push_back(item);
   }
   // launches every bucket; ks[item] = K splits of that item's problem
-  void run(int *err, cudaStream_t s, std::vector<int> &ks, int group_max = 32) {
+  void run(int *err, cudaStream_t s, std::vector<int> &ks, int group_max = 32, int nstreams = 1) {
     for (auto &kv : by_shape) {
       std::vector<int> k(kv.second.size(), 0);
-      tc_gemm_grouped(kv.second, kv.first / 1000, err, s, k.data(), group_max);
+      tc_gemm_grouped(kv.second, kv.first / 1000, err, s, k.data(), group_max, nstreams);
       const auto &own = owner[kv.first];
       for (size_t i = 0; i < own.size(); ++i) ks[own[i]] = k[i];
     }
@@ -869,14 +869,14 @@ namespace {
 
 // Empirical choice of the launch shape of the grouped dense products (the dominant launch of
 // the lockstep batch): on the first product round with at least 16 operators of a tile width,
-// every candidate (K box 32 or 64 bf16 elements, 8, 16 or 32 operators per launch) runs the
-// whole round twice into scratch outputs and the second run is timed with events; the fastest
-// is kept for the process.  The candidates compute identical numbers (the same FP32 chains in
+// every candidate (K box 32 or 64 bf16 elements, 8, 16 or 32 operators per launch, the launches
+// on one stream or spread over four) runs the whole round twice into scratch outputs and the
+// second run is timed with events; the fastest is kept for the process.  The candidates compute identical numbers (the same FP32 chains in
 // the same order), so the choice affects time only.
 struct DenseTuning {
   bool done = false;
-  int bk = 64, group = 32;
-  std::vector<std::array<double, 3>> table;  // bk, group, ms
+  int bk = 64, group = 32, streams = 1;
+  std::vector<std::array<double, 4>> table;  // bk, group, streams, ms
 };
 std::mutex g_tune_mu;
 std::map<int, DenseTuning> g_dense_tuning;  // by tile width
@@ -893,11 +893,12 @@ std::string autotune_report() {
     first = false;
     out += "{\"kernel\": \"grouped dense product\", \"bn\": " + std::to_string(kv.first) +
            ", \"chosen\": {\"bk\": " + std::to_string(kv.second.bk) + ", \"operators_per_launch\": " +
-           std::to_string(kv.second.group) + "}, \"candidates_ms\": [";
+           std::to_string(kv.second.group) + ", \"streams\": " + std::to_string(kv.second.streams) +
+           "}, \"candidates_ms\": [";
     for (size_t i = 0; i < kv.second.table.size(); ++i) {
       const auto &t = kv.second.table[i];
-      char buf[96];
-      snprintf(buf, sizeof(buf), "%s[%d, %d, %.4f]", i ? ", " : "", (int)t[0], (int)t[1], t[2]);
+      char buf[112];
+      snprintf(buf, sizeof(buf), "%s[%d, %d, %d, %.4f]", i ? ", " : "", (int)t[0], (int)t[1], (int)t[2], t[3]);
       out += buf;
     }
     out += "]}";
@@ -946,13 +947,14 @@ void MixedEngine::apply_dense_grouped(const Coef &c, const std::vector<GroupedIt
     tunable = tunable && g_kacc && bn <= 64 && (bn_all == 0 || bn == bn_all);
     bn_all = bn;
   }
-  int use_bk = 0, use_group = 32;
+  int use_bk = 0, use_group = 32, use_streams = 1;
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_dense_tuning.find(bn_all);
     if (it != g_dense_tuning.end() && it->second.done) {
       use_bk = it->second.bk;
       use_group = it->second.group;
+      use_streams = it->second.streams;
       tunable = false;
     }
   }
@@ -1005,31 +1007,33 @@ void MixedEngine::apply_dense_grouped(const Coef &c, const std::vector<GroupedIt
     VGB_CUDA(cudaEventCreate(&e1));
     double best = 1e30;
     for (int bk : {32, 64})
-      for (int group : {8, 16, 32}) {
-        float ms = 0.f;
-        for (int rep = 0; rep < 2; ++rep) {
-          GemmBuckets tb;
-          build(bk, &Ys, tb);
-          VGB_CUDA(cudaEventRecord(e0, s));
-          tb.run(err, s, ks, group);
-          VGB_CUDA(cudaEventRecord(e1, s));
-          VGB_CUDA(cudaEventSynchronize(e1));
-          VGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      for (int group : {8, 16, 32})
+        for (int streams : {1, 4}) {
+          float ms = 0.f;
+          for (int rep = 0; rep < 2; ++rep) {
+            GemmBuckets tb;
+            build(bk, &Ys, tb);
+            VGB_CUDA(cudaEventRecord(e0, s));
+            tb.run(err, s, ks, group, streams);
+            VGB_CUDA(cudaEventRecord(e1, s));
+            VGB_CUDA(cudaEventSynchronize(e1));
+            VGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+          }
+          t.table.push_back({(double)bk, (double)group, (double)streams, (double)ms});
+          if (ms < best) { best = ms; t.bk = bk; t.group = group; t.streams = streams; }
         }
-        t.table.push_back({(double)bk, (double)group, (double)ms});
-        if (ms < best) { best = ms; t.bk = bk; t.group = group; }
-      }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     t.done = true;
     use_bk = t.bk;
     use_group = t.group;
+    use_streams = t.streams;
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_dense_tuning[bn_all] = t;
   }
   GemmBuckets b;
   build(use_bk, nullptr, b);
-  b.run(err, s, ks, use_group);
+  b.run(err, s, ks, use_group, use_streams);
   std::vector<ReduceJob> rj;
   for (size_t i = 0; i < n; ++i) {
     if (direct[i]) continue;

@@ -3,6 +3,7 @@
 
 #include <cuda_bf16.h>
 
+#include <map>
 #include <memory>
 #include <mutex>
 
@@ -1100,10 +1101,43 @@ int tc_gemm(const TcMat &A, const TcMat &B, const TcShape &sh, const TcEpilogue 
   return p.ksplit;
 }
 
+namespace {
+
+// Non-blocking auxiliary streams per device (created once, kept for the process): the launches
+// of one grouped product spread over them so that the tail of one launch overlaps the start of
+// the next.
+std::vector<cudaStream_t> aux_streams(int n) {
+  static std::mutex mu;
+  static std::map<int, std::vector<cudaStream_t>> pool;
+  int dev = 0;
+  VGB_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  auto &v = pool[dev];
+  while ((int)v.size() < n) {
+    cudaStream_t st;
+    VGB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    v.push_back(st);
+  }
+  return std::vector<cudaStream_t>(v.begin(), v.begin() + n);
+}
+
+}  // namespace
+
 void tc_gemm_grouped(const std::vector<const TcProblem *> &probs, int bn, int *err, cudaStream_t s,
-                     int *ksplit_out, int group_max) {
+                     int *ksplit_out, int group_max, int nstreams) {
   std::unique_ptr<GroupSrc> src(new GroupSrc());
   const int gmax = std::max(1, std::min(group_max, kGroupMax));
+  // more than one launch and several streams: launch l on stream l % nstreams, ordered after the
+  // work already on s, and s waits for all of them at the end
+  std::vector<cudaStream_t> sts;
+  cudaEvent_t fork = nullptr;
+  if (nstreams > 1 && (int64_t)probs.size() > gmax) {
+    sts = aux_streams(std::min(nstreams, 8));
+    VGB_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    VGB_CUDA(cudaEventRecord(fork, s));
+    for (cudaStream_t st : sts) VGB_CUDA(cudaStreamWaitEvent(st, fork, 0));
+  }
+  int launches = 0;
   int bk = 0;
   size_t i = 0;
   while (i < probs.size()) {
@@ -1129,7 +1163,18 @@ void tc_gemm_grouped(const std::vector<const TcProblem *> &probs, int bn, int *e
     }
     if (src->n == 0) continue;
     src->begin[src->n] = total;
-    launch_any(bn, bk, *src, total, s);
+    launch_any(bn, bk, *src, total, sts.empty() ? s : sts[launches % sts.size()]);
+    ++launches;
+  }
+  if (!sts.empty()) {
+    for (cudaStream_t st : sts) {
+      cudaEvent_t join;
+      VGB_CUDA(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
+      VGB_CUDA(cudaEventRecord(join, st));
+      VGB_CUDA(cudaStreamWaitEvent(s, join, 0));
+      VGB_CUDA(cudaEventDestroy(join));
+    }
+    VGB_CUDA(cudaEventDestroy(fork));
   }
 }
 

@@ -93,9 +93,10 @@ struct TcProblem {
 // possible: each launch walks the concatenated tile lists of up to 32 problems,
 // whose tensor maps and parameters travel in the kernel parameter space.
 // ksplit_out[i] (optional) receives problem i's K splits, as tc_gemm returns.
-// group_max: problems per launch (at most 32).
+// group_max: problems per launch (at most 32); nstreams > 1: the launches spread over that many
+// auxiliary streams (forked from and joined back into s), so that their tails overlap.
 void tc_gemm_grouped(const std::vector<const TcProblem *> &probs, int bn, int *err, cudaStream_t s,
-                     int *ksplit_out = nullptr, int group_max = 32);
+                     int *ksplit_out = nullptr, int group_max = 32, int nstreams = 1);
 
 // FP64 -> bf16 hi/lo split into a row-major padded operand out[r * ldo + c] for
 // r < rows, c < cols; the source element (r, c) is
