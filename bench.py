@@ -423,7 +423,7 @@ def reference_arm(args):
     print(json.dumps(line))
 
 
-def batched_solve(n_molecules, nthreads, roots=5, tol=1e-7, cpu=False):
+def batched_solve(n_molecules, nthreads, roots=5, tol=1e-7, cpu=False, lockstep_only=False):
     """Independent molecules of uneven shape (v ~ U{4..32}, c ~ U{32..256},
     Naux ~ U{128..1024}, Nmo = v+c+8), lowest `roots` TDA singlets each, mixed
     precision.  Timed twice: the batched solve alone (operators staged in HBM)
@@ -457,6 +457,12 @@ def batched_solve(n_molecules, nthreads, roots=5, tol=1e-7, cpu=False):
     t0 = time.perf_counter()
     ev, info, iters = ds.solve_batch(ops, roots, nthreads=0)  # lockstep, grouped launches
     t_solve = time.perf_counter() - t0
+    if lockstep_only:  # profiler workload: the cold and the warm lockstep solve only
+        for cx in ctxs:
+            cx.close()
+        return {"workload": f"batched_tda_singlet_{n_molecules}mol_roots{roots}_lockstep",
+                "first_solve_seconds": t_cold, "solve_seconds": t_solve,
+                "roots_per_s": len(ops) * roots / t_solve, "iterations_mean": float(np.mean(iters))}
     # the same molecules as independent solves on host threads (one stream each); like the
     # lockstep mode, without the FP64 polish
     ds.set_fp64_polish(False)
@@ -870,6 +876,8 @@ def main():
     ap.add_argument("--product-only", default=None, choices=["mixed", "sliced", "fp64"],
                     help="profiler workload: the Hd product of that precision, twice, at the workload shape")
     ap.add_argument("--columns", type=int, default=8, help="vectors of --product-only")
+    ap.add_argument("--batch-only", action="store_true",
+                    help="profiler workload: the cold and the warm lockstep solve of the batched set")
     ap.add_argument("--solve-only", action="store_true",
                     help="one split-precision 20-singlet solve (with its FP64 polish) at the workload shape, "
                          "after one warm-up solve, and nothing else (for profiler captures)")
@@ -878,6 +886,9 @@ def main():
         return reference_arm(args)
     if args.product_only:
         return product_only(args)
+    if args.batch_only:
+        print(json.dumps(batched_solve(args.molecules, args.batch_threads, lockstep_only=True)))
+        return None
     if args.solve_only:
         return solve_only(args)
 
