@@ -72,6 +72,13 @@ __global__ void __launch_bounds__(kThreads) tn_partial_kernel(const __grid_const
   __shared__ double sm[kTileLd * kTnCols];
   const int cols = (int)(q.m + q.p);
   const int64_t mp = q.m * q.p;
+  // Fewer outputs than threads (m p <= 128): the rows of a tile are split over S lanes of one
+  // warp per output, so that every warp of the block issues FP64 FMAs (GB300 has about 2 FP64
+  // FMA lanes per clock and SM: a block whose outputs fit in two warps would use half of them).
+  int S = 1;
+  while (S < 32 && mp * 2 * S <= kThreads) S *= 2;
+  const int sub = threadIdx.x & (S - 1);
+  const int64_t os = threadIdx.x / S;  // the output of this thread when S > 1
   double acc[kTnOut];
 #pragma unroll
   for (int k = 0; k < kTnOut; ++k) acc[k] = 0.0;
@@ -84,17 +91,32 @@ __global__ void __launch_bounds__(kThreads) tn_partial_kernel(const __grid_const
       sm[col * kTileLd + r] = v;
     }
     __syncthreads();
+    if (S > 1) {
+      if (os < mp) {
+        const double *a = sm + (os % q.m) * kTileLd, *b = sm + (q.m + os / q.m) * kTileLd;
+        double s = acc[0];
+        for (int r = sub; r < rows; r += S) s = fma(a[r], b[r], s);
+        acc[0] = s;
+      }
+    } else {
 #pragma unroll
-    for (int k = 0; k < kTnOut; ++k) {
-      const int64_t o = threadIdx.x + (int64_t)k * kThreads;
-      if (o < mp) {
-        const double *a = sm + (o % q.m) * kTileLd, *b = sm + (q.m + o / q.m) * kTileLd;
-        double s = acc[k];
-        for (int r = 0; r < rows; ++r) s = fma(a[r], b[r], s);
-        acc[k] = s;
+      for (int k = 0; k < kTnOut; ++k) {
+        const int64_t o = threadIdx.x + (int64_t)k * kThreads;
+        if (o < mp) {
+          const double *a = sm + (o % q.m) * kTileLd, *b = sm + (q.m + o / q.m) * kTileLd;
+          double s = acc[k];
+          for (int r = 0; r < rows; ++r) s = fma(a[r], b[r], s);
+          acc[k] = s;
+        }
       }
     }
     __syncthreads();
+  }
+  if (S > 1) {  // the S lanes of an output are consecutive lanes of one warp (S divides 32)
+    double v = acc[0];
+    for (int off = S / 2; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    if (sub == 0 && os < mp) q.part[blockIdx.x * mp + os] = v;
+    return;
   }
 #pragma unroll
   for (int k = 0; k < kTnOut; ++k) {
@@ -157,6 +179,7 @@ struct NormJob {
   const double *A, *B;  // B null: norms
   int64_t lda, ldb, n, p;
   double *out;
+  double *inv = nullptr;  // norms only: also 1 / norm where norm > 0, else 0
 };
 __global__ void norm_kernel(const __grid_constant__ Group<NormJob> g) {
   const NormJob q = g.j[blockIdx.y];
@@ -172,12 +195,18 @@ __global__ void norm_kernel(const __grid_constant__ Group<NormJob> g) {
     if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
     __syncthreads();
   }
-  if (threadIdx.x == 0) q.out[c] = q.B ? red[0] : sqrt(red[0]);
+  if (threadIdx.x == 0) {
+    const double r = q.B ? red[0] : sqrt(red[0]);
+    q.out[c] = r;
+    // the FP64 division runs once per column here instead of once per element of a scaling
+    if (q.inv) q.inv[c] = r > 0.0 ? 1.0 / r : 0.0;
+  }
 }
 
 // ---- elementwise column work ----
 struct ColJob {
-  int kind;  // 0: A /= norm (norm > 0); 1: A -= lam * B (residual); 2: copy B -> A;
+  int kind;  // 0: A *= 1 / norm (v holds the reciprocal norms, 0 for a zero column);
+             // 1: A -= lam * B (residual); 2: copy B -> A;
              // 3: DPR A[:, kk] = -B[:, cols[kk]] / (D - lam[kk]), non-finite -> 0
   double *A;
   const double *B, *D, *v;  // v: norms or lambdas
@@ -192,8 +221,8 @@ __global__ void col_kernel(const __grid_constant__ Group<ColJob> g) {
     const int64_t i = t % q.n, j = t / q.n;
     double *a = q.A + i + j * q.lda;
     if (q.kind == 0) {
-      const double nv = q.v[j];
-      if (nv > 0.0) *a /= nv;
+      const double iv = q.v[j];
+      if (iv > 0.0) *a *= iv;  // Eigen's normalize leaves a zero column unchanged
     } else if (q.kind == 1) {
       *a -= q.v[j] * q.B[i + j * q.ldb];
     } else if (q.kind == 2) {
@@ -272,14 +301,15 @@ __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(const __grid_constant
     if (threadIdx.x == 0) {
       double t = 0.0;
       for (int w = 0; w < kGsThreads / 32; ++w) t += red[w][0];
-      nrm = sqrt(t);
-      if (q.check && !(nrm > 1e-12 * q.norms0[range])) *q.flag = 1;
+      const double nv = sqrt(t);
+      if (q.check && !(nv > 1e-12 * q.norms0[range])) *q.flag = 1;
+      nrm = nv > 0.0 ? 1.0 / nv : 0.0;  // one FP64 division per column, not one per row
     }
     __syncthreads();
-    const double nv = nrm;
-    if (nv > 0.0) {  // Eigen's normalize leaves a zero column unchanged
+    const double iv = nrm;
+    if (iv > 0.0) {  // Eigen's normalize leaves a zero column unchanged
 #pragma unroll 4
-      for (int64_t i = threadIdx.x; i < q.n; i += kGsThreads) qj[i] /= nv;
+      for (int64_t i = threadIdx.x; i < q.n; i += kGsThreads) qj[i] *= iv;
     }
     __syncthreads();
   }
@@ -345,7 +375,7 @@ struct Mol {
   std::vector<int64_t> upd;
   std::vector<double> upd_lam;
   // device (views into the pool)
-  double *V, *AV, *D, *q, *res, *Ud, *lamd, *cbuf, *norms0, *norms, *h, *part, *Td, *eigw;
+  double *V, *AV, *D, *q, *res, *Ud, *lamd, *cbuf, *norms0, *norms, *inorms, *h, *part, *Td, *eigw;
   int *flag, *einfo;
   // packed host transfer offsets (doubles): off_in = [U (capc x needmax) | lambdas (needmax) |
   // correction columns (capc) | their lambdas (capc)] in din/hin; off_out in hout (diagonal);
@@ -578,7 +608,7 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
     M.needmax = std::min(M.capc, std::max(M.restart_size, M.size_update));
     M.chunks = ceil_div(M.n, (int64_t)kTnRows);
     M.evals.assign(neigen, 0.0);
-    pool_doubles += 2 * M.n * M.capc + 2 * M.n * M.needmax + 3 * M.capc + M.capc * M.capc +
+    pool_doubles += 2 * M.n * M.capc + 2 * M.n * M.needmax + 4 * M.capc + M.capc * M.capc +
                     M.chunks * M.capc * M.capc + 64;
     // projected matrix, Ritz coefficients and values, eigensolver scratch (device)
     pool_doubles += M.capc * M.capc + M.capc * M.needmax + M.needmax + sym_eig_work_doubles(M.capc, M.needmax) + 64;
@@ -604,6 +634,7 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
       M.res = take(M.n * M.needmax);
       M.norms0 = take(M.capc);
       M.norms = take(M.capc);
+      M.inorms = take(M.capc);
       M.h = take(M.capc + M.capc * M.capc);
       M.part = take(M.chunks * M.capc * M.capc);
       p += 64;
@@ -863,9 +894,10 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
         cj.push_back(c);
         NormJob w;
         w.A = c.A; w.B = nullptr; w.lda = M->n; w.ldb = M->n; w.n = M->n; w.p = M->nupdate; w.out = M->norms;
+        w.inv = M->inorms;
         nj.push_back(w);
         ColJob z;
-        z.kind = 0; z.A = c.A; z.B = nullptr; z.D = nullptr; z.v = M->norms; z.cols = nullptr;
+        z.kind = 0; z.A = c.A; z.B = nullptr; z.D = nullptr; z.v = M->inorms; z.cols = nullptr;
         z.lda = M->n; z.ldb = M->n; z.n = M->n; z.p = M->nupdate;
         sc.push_back(z);
       }
@@ -896,9 +928,10 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
           nn.push_back({M->V, M->h, M->n, M->ncols, M->n, M->ncols, M->nupdate, Vn, M->n, -1.0, 1.0});
           NormJob w;
           w.A = Vn; w.B = nullptr; w.lda = M->n; w.ldb = M->n; w.n = M->n; w.p = M->nupdate; w.out = M->norms;
+          w.inv = M->inorms;
           nj.push_back(w);
           ColJob z;
-          z.kind = 0; z.A = Vn; z.B = nullptr; z.D = nullptr; z.v = M->norms; z.cols = nullptr;
+          z.kind = 0; z.A = Vn; z.B = nullptr; z.D = nullptr; z.v = M->inorms; z.cols = nullptr;
           z.lda = M->n; z.ldb = M->n; z.n = M->n; z.p = M->nupdate;
           sc.push_back(z);
           if (M->nupdate > 1) {

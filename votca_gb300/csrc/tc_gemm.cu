@@ -896,6 +896,91 @@ __global__ void slice_kernel(const In in, int64_t rows, int64_t cols, const Spli
   }
 }
 
+// Single pass of the same slicing for runs of at most 1024 columns and NSL digits: a lane
+// holds its (up to) 8 groups of 4 consecutive elements of the run in registers, so every load
+// of the run is in flight at once and the input is read from memory once (the two-pass kernel
+// above re-reads the run for its digits and keeps one load per lane in flight).  The digits and
+// their bf16 bits are those of slice_kernel, element for element.
+constexpr int kRunGroups = 8;  // 8 groups x 4 elements x 32 lanes = 1024 columns per run
+template <class In, int NSL>
+__global__ void __launch_bounds__(256) slice_run_kernel(const In in, int64_t rows, int64_t cols, const SplitMap m,
+                                                        int64_t chunk, uint16_t *__restrict__ out, int64_t ldo,
+                                                        int64_t plane) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nchunks = (cols + chunk - 1) / chunk;
+  const int64_t units = rows * nchunks;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t u = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; u < units; u += nwarps) {
+    const int64_t r = u / nchunks, q = u % nchunks;
+    const int64_t rq = r / m.rdiv, rr = r % m.rdiv;
+    if (rr >= m.rlim) continue;  // uniform over the warp
+    const int64_t base = rq * m.rs1 + rr * m.rs2;
+    const int64_t c0 = q * chunk, c1 = min(cols, c0 + chunk);
+    unsigned long long w[kRunGroups][4];
+    unsigned long long mx = 0;
+#pragma unroll
+    for (int g = 0; g < kRunGroups; ++g) {
+      const int64_t c = c0 + 128 * g + 4 * lane;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) w[g][v] = 0;
+      if (c + 4 <= c1) {
+        in.load4(base + c, w[g]);
+      } else if (c < c1) {
+#pragma unroll
+        for (int v = 0; v < 3; ++v)
+          if (c + v < c1) w[g][v] = __ldg(in.p + base + c + v);
+      }
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const unsigned long long a = In::abs_word(w[g][v]);
+        mx = a > mx ? a : mx;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      const unsigned long long y = __shfl_xor_sync(0xffffffffu, mx, o);
+      mx = y > mx ? y : mx;
+    }
+    const int e = In::exponent(mx);
+    uint16_t *orow = out + r * ldo;
+#pragma unroll
+    for (int g = 0; g < kRunGroups; ++g) {
+      const int64_t c = c0 + 128 * g + 4 * lane;
+      if (c >= c1) continue;
+      unsigned long long packed[NSL];
+#pragma unroll
+      for (int sl = 0; sl < NSL; ++sl) packed[sl] = 0;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        // zero-filled words past the run's end slice to zero digits and are not stored
+        long long rem = mx != 0 ? In::fixed_word(w[g][v], e, 7 * NSL) : 0;
+#pragma unroll
+        for (int sl = 0; sl < NSL; ++sl) {
+          const int shift = 7 * (NSL - 1 - sl);
+          long long d = rem;
+          if (shift > 0) {
+            d = (rem + (1LL << (shift - 1))) >> shift;  // round half up, as digits()
+            rem -= d << shift;
+          }
+          packed[sl] |= (unsigned long long)digit_bits(d, e, sl + 1) << (16 * v);
+        }
+      }
+      if (c + 4 <= c1) {
+#pragma unroll
+        for (int sl = 0; sl < NSL; ++sl)
+          *reinterpret_cast<unsigned long long *>(orow + sl * plane + c) = packed[sl];
+      } else {
+        const int nv = (int)(c1 - c);
+#pragma unroll
+        for (int sl = 0; sl < NSL; ++sl)
+#pragma unroll
+          for (int v = 0; v < 3; ++v)
+            if (v < nv) orow[sl * plane + c + v] = (uint16_t)(packed[sl] >> (16 * v));
+      }
+    }
+  }
+}
+
 __global__ void reduce_f64_kernel(const double *__restrict__ part, int64_t M, int64_t N, int G,
                                   const TcEpilogue e) {
   const int64_t total = M * N;
@@ -1241,7 +1326,7 @@ void slice_f64(const double *x, int64_t rows, int64_t cols, const SplitMap &m, i
   const F64In in{reinterpret_cast<const unsigned long long *>(x)};
   if (m.cs == 1 && chunk % 4 == 0 && m.rs1 % 4 == 0 && m.rs2 % 4 == 0 && ldo % 4 == 0 && plane % 4 == 0 &&
       ((uintptr_t)x & 31) == 0 && ((uintptr_t)out & 7) == 0) {
-    if (nslices == 5) slice_kernel<F64In, 4, 5><<<blocks, 256, 0, s>>>(in, rows, cols, m, nslices, chunk, out, ldo, plane);
+    if (nslices == 5) slice_run_kernel<F64In, 5><<<blocks, 256, 0, s>>>(in, rows, cols, m, chunk, out, ldo, plane);
     else slice_kernel<F64In, 4, 0><<<blocks, 256, 0, s>>>(in, rows, cols, m, nslices, chunk, out, ldo, plane);
   } else {
     slice_kernel<F64In, 1, 0><<<blocks, 256, 0, s>>>(in, rows, cols, m, nslices, chunk, out, ldo, plane);
@@ -1260,7 +1345,7 @@ void slice_pairs(const float *x2, int64_t rows, int64_t cols, const SplitMap &m,
   const PairIn in{reinterpret_cast<const unsigned long long *>(x2)};
   if (m.cs == 1 && chunk % 4 == 0 && m.rs1 % 4 == 0 && m.rs2 % 4 == 0 && ldo % 4 == 0 && plane % 4 == 0 &&
       ((uintptr_t)x2 & 31) == 0 && ((uintptr_t)out & 7) == 0) {
-    if (nslices == 5) slice_kernel<PairIn, 4, 5><<<blocks, 256, 0, s>>>(in, rows, cols, m, nslices, chunk, out, ldo, plane);
+    if (nslices == 5) slice_run_kernel<PairIn, 5><<<blocks, 256, 0, s>>>(in, rows, cols, m, chunk, out, ldo, plane);
     else slice_kernel<PairIn, 4, 0><<<blocks, 256, 0, s>>>(in, rows, cols, m, nslices, chunk, out, ldo, plane);
   } else {
     slice_kernel<PairIn, 1, 0><<<blocks, 256, 0, s>>>(in, rows, cols, m, nslices, chunk, out, ldo, plane);
