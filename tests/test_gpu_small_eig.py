@@ -86,17 +86,20 @@ def test_single_job_and_errors():
         _solve([a], [34])  # more pairs than the order
 
 
-def test_davidson_shaped_problem_phase_cycles():
-    """A Ritz problem of the C1 solve's shape (m = 124, 40 wanted pairs): correct, and the SM
-    cycles of each phase reported (printed for the record)."""
+@pytest.mark.parametrize("m,nw", [(124, 40), (28, 7)])
+def test_davidson_shaped_problem_phase_cycles(m, nw):
+    """Ritz problems of the C1 solve's shape (m = 124, 40 wanted pairs; vectors of the inverse
+    iteration in global memory) and of a batched 5-root solve (m = 28, 7 pairs; in shared
+    memory): correct, and the SM cycles of each phase reported (printed for the record)."""
     rng = np.random.default_rng(9)
-    m = 124
     t = np.diag(np.sort(rng.uniform(9, 15, m))) + 1e-3 * rng.standard_normal((m, m))
     t = 0.5 * (t + t.T)
     cyc = np.zeros(4, dtype=np.int64)
-    (lam, U), = _solve([t], [40], cyc)
-    np.testing.assert_allclose(lam, np.linalg.eigvalsh(t)[:40], atol=1e-12 * 15)
-    print("phase cycles (tridiagonal, bisection, inverse iteration, back-transform):", cyc.tolist())
+    (lam, U), = _solve([t], [nw], cyc)
+    np.testing.assert_allclose(lam, np.linalg.eigvalsh(t)[:nw], atol=1e-12 * 15)
+    assert np.abs(U.T @ U - np.eye(nw)).max() <= 1e-12
+    print(f"m {m} nw {nw}: phase cycles (tridiagonal, bisection, inverse iteration, back-transform):",
+          cyc.tolist())
     assert np.all(cyc > 0)
 
 

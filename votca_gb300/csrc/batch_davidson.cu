@@ -28,12 +28,16 @@
 #include <thread>
 #include <unistd.h>
 
+#include <cooperative_groups.h>
+
 #include "small_eig.cuh"
 #include "tc_engine.cuh"
 
 namespace vgb {
 
 namespace {
+
+namespace cg = cooperative_groups;
 
 constexpr int kThreads = 256;
 constexpr int kJobs = 320;       // jobs per grouped launch: a 256-molecule step in one launch
@@ -64,7 +68,7 @@ struct TnJob {
   int64_t lda, ldb, n, m, p;
   double *part;  // [chunk][m * p]
 };
-__global__ void __launch_bounds__(kThreads) tn_partial_kernel(const __grid_constant__ Group<TnJob> g) {
+__global__ void __launch_bounds__(kThreads, 4) tn_partial_kernel(const __grid_constant__ Group<TnJob> g) {
   const TnJob q = g.j[blockIdx.y];
   const int64_t r0 = (int64_t)blockIdx.x * kTnRows;
   if (r0 >= q.n) return;
@@ -235,7 +239,7 @@ __global__ void col_kernel(const __grid_constant__ Group<ColJob> g) {
   }
 }
 
-// ---- column-wise Gram-Schmidt of Q[:, nstart:ncols] within the block, one CTA per molecule ----
+// ---- column-wise Gram-Schmidt of Q[:, nstart:ncols] within the block ----
 struct GsJob {
   double *Q;
   int64_t n, nstart, ncols;
@@ -243,18 +247,31 @@ struct GsJob {
   int check;
   int *flag;
 };
-// kGsThreads threads per molecule and rows unrolled by 4: a pass over the rows of a column is a
-// few dependent loads per thread (the kernel is bound by load latency, not by bandwidth)
-constexpr int kGsThreads = 512;
-__global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(const __grid_constant__ Group<GsJob> g) {
-  const GsJob q = g.j[blockIdx.x];
+// A cluster of kGsCluster CTAs per molecule, each owning a contiguous range of rows: the dots
+// and the norm of every column are summed over the cluster through distributed shared memory
+// (each CTA publishes its partial sums in a double-buffered slot; one cluster barrier per
+// reduction; the partials are added in rank order, so every CTA gets the same, deterministic
+// value).  With one CTA per molecule the FP64 work of the largest molecules ran on one SM (at
+// about 2 FP64 FMAs per clock) while the others idled.  Rows are unrolled by 4: a pass over
+// the rows of a column is a few dependent loads per thread.
+constexpr int kGsCluster = 4;
+constexpr int kGsThreads = 128;
+__global__ void __cluster_dims__(kGsCluster, 1, 1) __launch_bounds__(kGsThreads, 8)
+    gs_kernel(const __grid_constant__ Group<GsJob> g) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const unsigned rank = cluster.block_rank();
+  const GsJob q = g.j[blockIdx.x / kGsCluster];
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   constexpr int kMaxRange = 256;
   constexpr int kReg = 8;  // dots accumulated per pass over the rows
   __shared__ double h[kMaxRange];
   __shared__ double red[kGsThreads / 32][kReg];
+  __shared__ double part[2][kReg];  // this CTA's published partial sums
   __shared__ double nrm;
+  const int64_t per = (q.n + kGsCluster - 1) / kGsCluster;
+  const int64_t r0 = min(q.n, (int64_t)rank * per), r1 = min(q.n, r0 + per);
   const double *M = q.Q + q.nstart * q.n;
+  int buf = 0;
   for (int64_t j = q.nstart + 1; j < q.ncols; ++j) {
     const int64_t range = j - q.nstart;
     double *qj = q.Q + j * q.n;
@@ -266,7 +283,7 @@ __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(const __grid_constant
 #pragma unroll
       for (int l = 0; l < kReg; ++l) acc[l] = 0.0;
 #pragma unroll 4
-      for (int64_t i = threadIdx.x; i < q.n; i += kGsThreads) {
+      for (int64_t i = r0 + threadIdx.x; i < r1; i += kGsThreads) {
         const double x = qj[i];
 #pragma unroll
         for (int l = 0; l < kReg; ++l)
@@ -282,13 +299,20 @@ __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(const __grid_constant
       if (threadIdx.x < lc) {
         double t = 0.0;
         for (int w = 0; w < kGsThreads / 32; ++w) t += red[w][threadIdx.x];
+        part[buf][threadIdx.x] = t;
+      }
+      cluster.sync();  // every CTA's partials of this reduction are published
+      if (threadIdx.x < lc) {
+        double t = 0.0;
+        for (unsigned r = 0; r < kGsCluster; ++r) t += cluster.map_shared_rank(&part[buf][0], r)[threadIdx.x];
         h[l0 + threadIdx.x] = t;
       }
+      buf ^= 1;  // the next barrier orders these reads before the slot is written again
       __syncthreads();
     }
     double nacc = 0.0;
 #pragma unroll 4
-    for (int64_t i = threadIdx.x; i < q.n; i += kGsThreads) {
+    for (int64_t i = r0 + threadIdx.x; i < r1; i += kGsThreads) {
       double s = 0.0;
       for (int64_t l = 0; l < range; ++l) s = fma(M[l * q.n + i], h[l], s);
       const double v = qj[i] - s;
@@ -301,18 +325,26 @@ __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(const __grid_constant
     if (threadIdx.x == 0) {
       double t = 0.0;
       for (int w = 0; w < kGsThreads / 32; ++w) t += red[w][0];
+      part[buf][0] = t;
+    }
+    cluster.sync();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (unsigned r = 0; r < kGsCluster; ++r) t += cluster.map_shared_rank(&part[buf][0], r)[0];
       const double nv = sqrt(t);
-      if (q.check && !(nv > 1e-12 * q.norms0[range])) *q.flag = 1;
+      if (rank == 0 && q.check && !(nv > 1e-12 * q.norms0[range])) *q.flag = 1;
       nrm = nv > 0.0 ? 1.0 / nv : 0.0;  // one FP64 division per column, not one per row
     }
+    buf ^= 1;
     __syncthreads();
     const double iv = nrm;
     if (iv > 0.0) {  // Eigen's normalize leaves a zero column unchanged
 #pragma unroll 4
-      for (int64_t i = threadIdx.x; i < q.n; i += kGsThreads) qj[i] *= iv;
+      for (int64_t i = r0 + threadIdx.x; i < r1; i += kGsThreads) qj[i] *= iv;
     }
     __syncthreads();
   }
+  cluster.sync();  // no CTA leaves while another may still read its partial sums
 }
 
 // ---- unit vectors V[rows[j], j] = 1 ----
@@ -355,7 +387,8 @@ void launch_jobs(const std::vector<Job> &jobs, Kernel kernel, unsigned bx, bool 
   for (size_t i = 0; i < jobs.size();) {
     g->n = 0;
     for (; i < jobs.size() && g->n < kJobs; ++i) g->j[g->n++] = jobs[i];
-    const dim3 grid = grid_x_is_job ? dim3((unsigned)g->n) : dim3(bx, (unsigned)g->n);
+    // grid_x_is_job: bx consecutive CTAs (a cluster) per job along x
+    const dim3 grid = grid_x_is_job ? dim3((unsigned)g->n * bx) : dim3(bx, (unsigned)g->n);
     kernel<<<grid, threads, 0, s>>>(*g);
     VGB_LAUNCH_CHECK();
   }
@@ -946,7 +979,7 @@ void davidson_solve_batch(const std::vector<BseOperator *> &ops, const Coef &coe
         run_nn(nn, s);
         run_norms(nj, s);
         run_cols(sc, s);
-        launch_jobs(gs, gs_kernel, 1, true, s, kGsThreads);
+        launch_jobs(gs, gs_kernel, kGsCluster, true, s, kGsThreads);
       }
       for (Mol *M : ext) M->ncols += M->nupdate;
     }

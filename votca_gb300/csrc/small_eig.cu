@@ -30,9 +30,9 @@ __device__ double block_sum(double v, double *red) {
   __syncthreads();  // earlier readers of red are done
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
   __syncthreads();
-  double t = 0.0;
-  for (int w = 0; w < kEigWarps; ++w) t += red[w];  // fixed order: deterministic
-  return t;
+  // pairwise in a fixed order (deterministic): three dependent FP64 adds instead of eight
+  static_assert(kEigWarps == 8, "block_sum adds eight warp sums");
+  return ((red[0] + red[1]) + (red[2] + red[3])) + ((red[4] + red[5]) + (red[6] + red[7]));
 }
 
 __device__ double block_max(double v, double *red) {
@@ -132,7 +132,7 @@ __device__ void start_vector(double *z, int64_t m, int64_t j) {
   }
 }
 
-__global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(const __grid_constant__ SymEigGroup g) {
+__global__ void __launch_bounds__(kEigThreads, 2) sym_eig_kernel(const __grid_constant__ SymEigGroup g) {
   const SymEigJob q = g.j[blockIdx.x];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t m = q.m, nw = q.nw;
@@ -146,8 +146,16 @@ __global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(const __grid_const
   double *d = sm, *e = d + m, *tau = e + m, *vv = tau + m, *pp = vv + m, *red = pp + m;
   float *d32 = reinterpret_cast<float *>(red + 32), *e2 = d32 + m, *lam32 = e2 + m;
   int *cl = reinterpret_cast<int *>(lam32 + m);
-  double *A = (nvec + ld * m <= g.smem_doubles) ? sm + nvec : q.work;
-  double *scratch = q.work + ld * m;  // 5 m per wanted eigenvalue
+  const bool a_sm = nvec + ld * m <= g.smem_doubles;
+  double *A = a_sm ? sm + nvec : q.work;
+  // The eigenvectors of the tridiagonal and the LU factors of their inverse iterations (6 m per
+  // wanted eigenvalue) in shared memory when they fit behind A: the inverse iteration and the
+  // back-transformation are serial chains over m, and each step through global memory waits for
+  // an L2 round trip (the vectors are copied to U at the end).
+  const bool z_sm = a_sm && nvec + ld * m + 6 * m * nw <= g.smem_doubles;
+  double *Z = z_sm ? sm + nvec + ld * m : q.U;
+  const int64_t ldz = z_sm ? m : q.ldu;
+  double *scratch = z_sm ? Z + m * nw : q.work + ld * m;  // 5 m per wanted eigenvalue
 
   if (tid == 0 && q.clocks) q.clocks[0] = clock64();
   // ---- load the lower triangle ----
@@ -179,15 +187,29 @@ __global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(const __grid_const
     }
     if (tid == 0) { tau[k] = tk; e[k] = beta; d[k] = A[k + ld * k]; }
     __syncthreads();
-    // p = tau A22 v from the lower triangle
+    // p = tau A22 v from the lower triangle; four interleaved partial sums per row (a chain of
+    // dependent FP64 FMAs is the latency of this step)
     double pv_part = 0.0;
     for (int64_t i = k1 + tid; i < m; i += kEigThreads) {
-      double acc = 0.0;
-      for (int64_t j = k1; j < m; ++j) {
-        const double a = (j <= i) ? A[i + ld * j] : A[j + ld * i];
-        acc = fma(a, vv[j], acc);
+      double acc[4] = {0.0, 0.0, 0.0, 0.0};
+      int64_t j = k1;
+      for (; j + 4 <= m; j += 4) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int64_t jj = j + u;
+          const double a = (jj <= i) ? A[i + ld * jj] : A[jj + ld * i];
+          acc[u] = fma(a, vv[jj], acc[u]);
+        }
       }
-      const double p = tk * acc;
+#pragma unroll
+      for (int u = 0; u < 3; ++u) {  // at most three left
+        const int64_t jj = j + u;
+        if (jj < m) {
+          const double a = (jj <= i) ? A[i + ld * jj] : A[jj + ld * i];
+          acc[u] = fma(a, vv[jj], acc[u]);
+        }
+      }
+      const double p = tk * ((acc[0] + acc[1]) + (acc[2] + acc[3]));
       pp[i] = p;
       pv_part = fma(p, vv[i], pv_part);
     }
@@ -263,14 +285,14 @@ __global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(const __grid_const
     double *w = scratch + 5 * m * j0;  // 5 m per member, contiguous over the cluster
     double *r0 = w, *u1 = w + m, *u2 = w + 2 * m, *l = w + 3 * m, *pv = w + 4 * m;
     for (int64_t jj = j0; jj < j1; ++jj) {
-      double *z = q.U + q.ldu * jj;
+      double *z = Z + ldz * jj;
       start_vector(z, m, jj);
       tri_lu(d, e, m, (double)lam32[jj], tiny, r0, u1, u2, l, pv);
       const int steps = s == 1 ? 2 : 5;
       for (int st = 0; st < steps; ++st) {
         tri_solve(m, r0, u1, u2, l, pv, z, 1);
         for (int64_t kk = j0; kk < jj; ++kk) {  // earlier members of the cluster
-          const double *y = q.U + q.ldu * kk;
+          const double *y = Z + ldz * kk;
           double dot = 0.0;
           for (int64_t i = 0; i < m; ++i) dot = fma(y[i], z[i], dot);
           for (int64_t i = 0; i < m; ++i) z[i] = fma(-dot, y[i], z[i]);
@@ -289,7 +311,7 @@ __global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(const __grid_const
     if (s > 1) {  // Rayleigh-Ritz on the cluster: cyclic Jacobi on C = Z_c^T T Z_c
       double *C = w, *W = w + s * s, *y = w + 2 * s * s;
       for (int64_t b = 0; b < s; ++b) {
-        const double *zb = q.U + q.ldu * (j0 + b);
+        const double *zb = Z + ldz * (j0 + b);
         for (int64_t i = 0; i < m; ++i) {
           double t = d[i] * zb[i];
           if (i > 0) t = fma(e[i - 1], zb[i - 1], t);
@@ -297,7 +319,7 @@ __global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(const __grid_const
           y[i] = t;
         }
         for (int64_t a = 0; a < s; ++a) {
-          const double *za = q.U + q.ldu * (j0 + a);
+          const double *za = Z + ldz * (j0 + a);
           double t = 0.0;
           for (int64_t i = 0; i < m; ++i) t = fma(za[i], y[i], t);
           C[a + s * b] = t;
@@ -360,10 +382,10 @@ __global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(const __grid_const
       for (int64_t i = 0; i < m; ++i) {  // Z_c <- Z_c W, row by row
         for (int64_t a = 0; a < s; ++a) {
           double t = 0.0;
-          for (int64_t b = 0; b < s; ++b) t = fma(q.U[i + q.ldu * (j0 + b)], W[b + s * a], t);
+          for (int64_t b = 0; b < s; ++b) t = fma(Z[i + ldz * (j0 + b)], W[b + s * a], t);
           y[a] = t;
         }
-        for (int64_t a = 0; a < s; ++a) q.U[i + q.ldu * (j0 + a)] = y[a];
+        for (int64_t a = 0; a < s; ++a) Z[i + ldz * (j0 + a)] = y[a];
       }
     }
   }
@@ -372,7 +394,7 @@ __global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(const __grid_const
 
   // ---- 4. back-transformation U = H_0 H_1 ... H_{m-3} Z, one warp per eigenvector ----
   for (int64_t j = warp; j < nw; j += kEigWarps) {
-    double *z = q.U + q.ldu * j;
+    double *z = Z + ldz * j;
     for (int64_t k = m - 3; k >= 0; --k) {
       const double tk = tau[k];
       if (tk == 0.0) continue;
@@ -384,6 +406,8 @@ __global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(const __grid_const
     }
   }
   __syncthreads();
+  if (z_sm)
+    for (int64_t t = tid; t < m * nw; t += kEigThreads) q.U[(t % m) + q.ldu * (t / m)] = Z[t];
   if (tid == 0 && q.clocks) q.clocks[4] = clock64();
   if (tid == 0 && q.info) *q.info = 0;
 }
@@ -422,7 +446,8 @@ void sym_eig_device(const SymEigJob *jobs, int64_t njobs, cudaStream_t s) {
                   "small symmetric eigenproblem: invalid job");
       g->j[i] = jb;
       const int64_t full = eig_vec_doubles(jb.m) + eig_ld(jb.m) * jb.m;
-      need = std::max(need, full <= limit ? full : eig_vec_doubles(jb.m));
+      const int64_t with_z = full + 6 * jb.m * jb.nw;  // also the vectors of the inverse iteration
+      need = std::max(need, with_z <= limit ? with_z : full <= limit ? full : eig_vec_doubles(jb.m));
     }
     g->smem_doubles = need;
     sym_eig_kernel<<<g->n, kEigThreads, need * sizeof(double), s>>>(*g);
