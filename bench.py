@@ -1017,7 +1017,8 @@ def main():
         nprod = 4 if os.environ.get("VGB_TC_PRODUCTS") == "4" else 3
         # DRAM bytes per launch of this kernel: Mcc2 (hi+lo) read once, X read, the S intermediate
         # written; this model matches the ncu capture of the same kernel on a small case
-        # (dram__bytes_read/write.sum, see profiles/tc_gemm_hd_stage1_*.md)
+        # (dram__bytes_read.sum + dram__bytes_write.sum of the stage-1 launch at v=32, c=512,
+        # Naux=512, k=30)
         kc = -(-C // 64) * 64
         kg = -(-(NAUX * V) // 64) * 64
         per_launch_cols = K / launches_per_step
