@@ -239,7 +239,8 @@ __global__ void col_kernel(const __grid_constant__ Group<ColJob> g) {
   }
 }
 
-// ---- column-wise Gram-Schmidt of Q[:, nstart:ncols] within the block ----
+// ---- column-wise Gram-Schmidt of Q[:, nstart:ncols] within the block (the column loops of
+// DavidsonSolver::gramschmidt, davidsonsolver.cc:453-458 and 468-477) ----
 struct GsJob {
   double *Q;
   int64_t n, nstart, ncols;
