@@ -118,6 +118,9 @@ typedef struct bse_uks_options {
  * (window-local, occupied first); both share epsilon_0_inv (same auxsize).  The operator
  * acts on [x_alpha; x_beta] (alpha pairs first, pair index v * ctotal + c per channel,
  * vtotal = homo - vmin + 1, ctotal = cmax - homo); its size is the sum of the two channels.
+ * A channel without occupied (homo = vmin - 1) or virtual (homo = cmax) levels in the window
+ * carries an empty block, as the reference's setup_block (bse_operator_uks.cc:25-35): the
+ * operator is then the other channel's, without cross-spin terms (both empty: an error).
  * The returned handle serves bse_op_size / bse_op_matmul(_device) / bse_op_diagonal(_device)
  * / bse_ham_matmul / bse_davidson_solve with BSE_OPERATOR_UKS<cqp, cx, cd, cd2>
  * coefficients (ExcitonUKSOperator_TDA = 1,1,1,0; ExcitonUKSOperator_BTDA_B = 0,1,0,1;

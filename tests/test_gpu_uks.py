@@ -55,6 +55,38 @@ def test_products_and_diagonals_match_reference_loops(homos, name):
     ctx.close()
 
 
+@pytest.mark.parametrize("homos", [(5, 0), (0, 5), (5, 12)], ids=["beta_no_occupied", "alpha_no_occupied",
+                                                               "beta_no_virtual"])
+def test_empty_spin_channel(homos):
+    """A spin channel without occupied (homo = vmin - 1) or without virtual (homo = cmax) levels
+    in the BSE window carries an empty block (setup_block, bse_operator_uks.cc:25-35): every
+    preset's product and diagonal match the restated loops, a split-precision handle agrees with
+    FP64, and the TDA roots are those of the dense operator."""
+    from votca_gb300 import bse_operator_uks as bu
+    from votca_gb300.davidson import DavidsonSolver
+
+    p = UKSProblem(homos[0], homos[1], vmin=1, cmax=12, naux=17, nmo=15, seed=21)
+    ctx, orc = _setup(p)
+    assert ctx.size == orc.size == max(orc.alpha.size, orc.beta.size) > 0
+    X = np.random.default_rng(3).standard_normal((orc.size, 4))
+    for name in PRESETS:
+        op = _op(ctx, name)
+        R = orc.matmul(X, name)
+        Y = op.matmul(X)
+        assert np.linalg.norm(Y - R) <= 1e-12 * np.linalg.norm(R), name
+        np.testing.assert_allclose(op.diagonal(), orc.diagonal(name), rtol=1e-12, atol=1e-14)
+    ctxm, _ = _setup(p, precision=1)
+    Ym = _op(ctxm, "tda").matmul(X)
+    Yf = orc.matmul(X, "tda")
+    assert np.linalg.norm(Ym - Yf) <= 2e-4 * np.linalg.norm(Yf - orc.matmul(X, "qp"))
+    ds = DavidsonSolver()
+    ds.set_tolerance(1e-9)
+    lam, _ = ds.solve(bu.ExcitonUKSOperator_TDA(ctx), 3)
+    assert np.max(np.abs(lam - np.linalg.eigvalsh(orc.dense("tda"))[:3])) < 1e-9
+    ctx.close()
+    ctxm.close()
+
+
 def test_ham_product_and_dense_matrix():
     from votca_gb300 import bse_operator as bo
 
@@ -135,6 +167,10 @@ def test_errors():
         bu.GpuBSEContextUKS(p.w, mm, p.hqp_alpha, p.hqp_beta, opt)
     assert e.value.code == 1
     ctx, _ = _setup(p)
+    with pytest.raises(_lib.BSEError) as e:  # both spin channels without a BSE block
+        bu.GpuBSEContextUKS(p.w, bu.TCMatrix_gwbse_spin(bo.TCMatrix_gwbse(p.mmn_alpha), bo.TCMatrix_gwbse(p.mmn_beta)),
+                            p.hqp_alpha, p.hqp_beta, bu.BSEOperatorUKS_Options(-1, 10, 0, 0, 0, 10))
+    assert e.value.code == 1
     with pytest.raises(_lib.BSEError):  # Hd and Hd2 together
         bu.BSE_OPERATOR_UKS(ctx, 1, 1, 1, 1)
     with pytest.raises(_lib.BSEError):  # the allocation-free product is for restricted operators

@@ -9,6 +9,13 @@ namespace vgb {
 
 namespace {
 
+// A spin channel without occupied (homo = vmin - 1) or without virtual (homo = cmax) levels in
+// the BSE window carries an empty block: setup_block's size vtotal * ctotal is 0
+// (bse_operator_uks.cc:25-35), and the operator is the other channel's alone.
+bool channel_empty(const bse_uks_options &o, int64_t homo) {
+  return homo - o.vmin + 1 == 0 || o.cmax - homo == 0;
+}
+
 bse_options channel_options(const bse_uks_options &o, int64_t homo) {
   bse_options r;
   r.homo = homo;
@@ -58,14 +65,29 @@ void UksOperator::stage(const bse_mmn_desc &desc_a, const double *const *slices_
   VGB_REQUIRE(desc_a.auxsize == desc_b.auxsize, "bse_uks_op_create: alpha and beta Naux differ");
   VGB_REQUIRE(slices_a && slices_b && w && hqp_a && hqp_b, "bse_uks_op_create: null input");
   precision = prec;
-  alpha.stage(desc_a, slices_a, w, dense_w, hqp_a, ldh_a, size_a, channel_options(opt, opt.homo_alpha), prec, s);
-  beta.stage(desc_b, slices_b, w, dense_w, hqp_b, ldh_b, size_b, channel_options(opt, opt.homo_beta), prec, s);
+  const bool ea = channel_empty(opt, opt.homo_alpha), eb = channel_empty(opt, opt.homo_beta);
+  VGB_REQUIRE(!(ea && eb), "bse_uks_op_create: both spin channels have an empty BSE window");
+  for (BseOperator *ch : {&alpha, &beta}) {
+    const bool empty = ch == &alpha ? ea : eb;
+    const int64_t homo = ch == &alpha ? opt.homo_alpha : opt.homo_beta;
+    if (!empty) continue;
+    ch->vt = homo - opt.vmin + 1;
+    ch->ct = opt.cmax - homo;
+    ch->naux = desc_a.auxsize;
+    ch->dim = 0;
+    ch->precision = prec;
+  }
+  if (!ea)
+    alpha.stage(desc_a, slices_a, w, dense_w, hqp_a, ldh_a, size_a, channel_options(opt, opt.homo_alpha), prec, s);
+  if (!eb)
+    beta.stage(desc_b, slices_b, w, dense_w, hqp_b, ldh_b, size_b, channel_options(opt, opt.homo_beta), prec, s);
   dim = alpha.dim + beta.dim;
   // the cross-spin Hd2 blocks read each channel's Mmn over the other channel's ranges
   for (const bse_mmn_desc *d : {&desc_a, &desc_b}) {
     VGB_REQUIRE(opt.vmin >= d->mmin && opt.cmax <= d->mmax && opt.vmin >= d->nmin && opt.cmax <= d->nmax,
                 "bse_uks_op_create: BSE window outside an Mmn range");
   }
+  if (ea || eb) return;  // no cross-spin blocks
   const int64_t naux = alpha.naux;
   const HostMmn Ma{desc_a, slices_a}, Mb{desc_b, slices_b};
   const int64_t ca0 = opt.homo_alpha + 1, cb0 = opt.homo_beta + 1;
@@ -155,8 +177,9 @@ void UksOperator::matmul(const Coef &c, const double *X, int64_t ldx, int64_t k,
   VGB_REQUIRE(ldx >= dim && ldy >= dim, "uks matmul: leading dimension too small");
   if (k == 0) return;
   const int64_t da = alpha.dim;
-  alpha.matmul(c, X, ldx, k, Y, ldy, s);
-  beta.matmul(c, X + da, ldx, k, Y + da, ldy, s);
+  if (alpha.dim > 0) alpha.matmul(c, X, ldx, k, Y, ldy, s);
+  if (beta.dim > 0) beta.matmul(c, X + da, ldx, k, Y + da, ldy, s);
+  if (alpha.dim == 0 || beta.dim == 0) return;  // an empty channel couples to nothing
   if (c.cd != 0) {
     cross_tda(alpha, beta, -(double)c.cd, X + da, ldx, k, Y, ldy, s);
     cross_tda(beta, alpha, -(double)c.cd, X, ldx, k, Y + da, ldy, s);
@@ -168,8 +191,8 @@ void UksOperator::matmul(const Coef &c, const double *X, int64_t ldx, int64_t k,
 }
 
 void UksOperator::diagonal(const Coef &c, double *D, cudaStream_t s) {
-  alpha.diagonal(c, D, s);
-  beta.diagonal(c, D + alpha.dim, s);
+  if (alpha.dim > 0) alpha.diagonal(c, D, s);
+  if (beta.dim > 0) beta.diagonal(c, D + alpha.dim, s);
 }
 
 void UksOperator::ham_matmul(const Coef &a, const Coef &b, const double *X, int64_t ldx, int64_t k,
@@ -191,8 +214,8 @@ void UksOperator::ham_matmul(const Coef &a, const Coef &b, const double *X, int6
 }
 
 void UksOperator::check_errors(cudaStream_t s) {
-  alpha.check_errors(s);
-  beta.check_errors(s);
+  if (alpha.dim > 0) alpha.check_errors(s);
+  if (beta.dim > 0) beta.check_errors(s);
 }
 
 }  // namespace vgb
