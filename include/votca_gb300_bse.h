@@ -209,6 +209,25 @@ int bse_aux_pseudo_inv_sqrt(int64_t n, const double *V, int64_t ldv, double etol
 int bse_aux_pseudo_inv_sqrt_gwbse(int64_t n, const double *S, int64_t lds, const double *V, int64_t ldv,
                                   double etol, double *out, int64_t ldo, int64_t *removed);
 
+/* Transition dipoles of BSE states from one spin block, Orbitals::CalcFreeTransition_Dipoles +
+ * CalcCoupledTransition_Dipoles (xtp/src/libxtp/orbitals.cc:740-800 restricted singlets,
+ * :804-877 combined UKS excitons), with the AO dipole matrices supplied by the caller in place
+ * of libint2's AODipole (emultipole1 about the caller's origin):
+ *   D_i = C[:, cmin : cmin + ctotal]^T dip_i C[:, vmin : vmin + vtotal]   (i = x, y, z)
+ *   dipoles[3 s + i] (+)= prefactor sum_{v,c} (X + Y)(v ctotal + c, s) D_i(c, v)
+ *   ao_dipoles: three column-major nbf x nbf matrices back to back (x, y, z);
+ *   mo_coefficients: column-major nbf x nmo, leading dimension ldc;
+ *   X, Y: the states' vectors (vtotal ctotal rows, leading dimension ldx, nstates columns);
+ *         Y NULL for TDA states; a UKS block passes its rows of the combined vector;
+ *   prefactor: -sqrt(2) for restricted singlets, -1 for each spin block of a UKS exciton;
+ *   accumulate: 0 overwrites dipoles, 1 adds (the second spin block).
+ * FP64 GEMMs on the device.  Oscillator strengths follow as f = 2/3 Omega |d|^2
+ * (Orbitals::Oscillatorstrengths, orbitals.cc:645-673). */
+int bse_transition_dipoles(const double *ao_dipoles, int64_t nbf, const double *mo_coefficients, int64_t ldc,
+                           int64_t nmo, int64_t vmin, int64_t vtotal, int64_t cmin, int64_t ctotal,
+                           const double *X, const double *Y, int64_t ldx, int64_t nstates, double prefactor,
+                           int32_t accumulate, double *dipoles);
+
 /* A dense FP64 symmetric matrix as an operator (the reference tests'
  * HermitianBlockOperator, test_davidson.cc:265-281).  b may be NULL; when
  * given, bse_ham_* use [[a, b], [-b, -a]]. */

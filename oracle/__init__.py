@@ -11,6 +11,7 @@ reference.  The product package (votca_gb300) never imports it.
   uks_oracle.py       restated BSE_OPERATOR_UKS blocks
   threecenter_oracle.py   restated Fill3cMO and the auxiliary metrics
   gaussian_integrals.py   McMurchie-Davidson AO integrals for the golden methane case
+  orbitals_oracle.py  restated transition dipoles and oscillator strengths
 """
 from __future__ import annotations
 

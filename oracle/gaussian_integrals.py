@@ -163,6 +163,36 @@ def overlap(shells):
     return S
 
 
+def dipole(shells, origin=(0.0, 0.0, 0.0)):
+    """<mu| r_i - O_i |nu> for i = x, y, z as a (3, n, n) array: the AODipole matrices
+    (libint2 emultipole1 about the origin O, xtp/src/libxtp/libint2_calls.cc:206-214).  In the
+    Hermite expansion the Cartesian factor is (E_1 + X_PO E_0) (pi/p)^(1/2) along the dipole
+    axis and E_0 (pi/p)^(1/2) along the two others (McMurchie-Davidson, as the overlap)."""
+    O = np.asarray(origin, dtype=np.float64)
+    n = sum(s.size() for s in shells)
+    D = np.zeros((3, n, n))
+    offs = np.cumsum([0] + [s.size() for s in shells])
+    for I, sa in enumerate(shells):
+        for J, sb in enumerate(shells):
+            Q = sa.center - sb.center
+            for a, da in zip(sa.exps, sa.coefs):
+                for b, db in zip(sb.exps, sb.coefs):
+                    p = a + b
+                    P = (a * sa.center + b * sb.center) / p
+                    for ia, ca in enumerate(sa.comps):
+                        for ib, cb in enumerate(sb.comps):
+                            e0 = [_E(ca[d], cb[d], 0, Q[d], a, b) for d in range(3)]
+                            e1 = [_E(ca[d], cb[d], 1, Q[d], a, b) for d in range(3)]
+                            f = da * db * _norm(a, ca) * _norm(b, cb) * (math.pi / p) ** 1.5
+                            for k in range(3):
+                                w = e1[k] + (P[k] - O[k]) * e0[k]
+                                for d in range(3):
+                                    if d != k:
+                                        w *= e0[d]
+                                D[k, offs[I] + ia, offs[J] + ib] += f * w
+    return D
+
+
 def _eri(bra, ket, p, q, Pc, Qc):
     """sum over Hermite terms of bra (dict) and ket (dict) with the (-1)^(ket order) sign."""
     alpha = p * q / (p + q)

@@ -39,6 +39,12 @@ isApprox 1e-5):
   MOs                17x17 MO coefficients
   ref0b, ref2b, ref4b  slices m = 0, 2, 4 (8 x 17: n = 0..7 by aux) of TCMatrix_gwbse::Fill
                      over the window m 0..5, n 0..7
+Writes orbitals_osc.npz (xtp/src/tests/DataFiles/orbitals and .../aomatrix3d, methane 3-21G):
+  basis_xml, elements, xyz   the basis and geometry (orbitals/3-21G.xml, molecule.xyz)
+  MOs, spsi                  MOs3.mm and spsi_ref2.mm, the inputs of the osc_strength test
+  omega, dipoles_ref, oscs_ref  its literals (test_orbitals.cc:216-250)
+  dip_ref, dip_ref_nonzero   AODipole matrices about the origin and about dip_center_nonzero
+                             (test_aomatrix3d.cc:36-90)
 Writes aomatrix.npz (xtp/src/tests/DataFiles/aomatrix, methane 3-21G; checked by
 xtp/src/tests/test_aomatrix.cc:43-123 at isApprox 1e-5):
   overlap, coulomb                 AOOverlap / AOCoulomb matrices (overlap_ref.mm, coulomb_ref.mm)
@@ -124,7 +130,38 @@ def main():
              coulomb=read_mm_array(os.path.join(a, "coulomb_ref.mm")),
              invsqrt=read_mm_array(os.path.join(a, "coulombinvsqrt_ref.mm")),
              invsqrt_gwbse=read_mm_array(os.path.join(a, "coulombinvsqrtgw_ref.mm")))
+    write_orbitals_osc(ref, here)
     print("wrote fixtures to", here)
+
+
+def write_orbitals_osc(ref, here):
+    """orbitals_osc.npz: the inputs and golden outputs of the oscillator-strength test
+    (xtp/src/tests/test_orbitals.cc:202-256, isApprox 1e-5) and of the AO dipole matrices
+    (xtp/src/tests/test_aomatrix3d.cc:36-90, isApprox 1e-4), methane in 3-21G."""
+    o = os.path.join(ref, "xtp/src/tests/DataFiles/orbitals")
+    a = os.path.join(ref, "xtp/src/tests/DataFiles/aomatrix3d")
+    with open(os.path.join(o, "molecule.xyz")) as f:
+        lines = f.read().split("\n")
+    nat = int(lines[0])
+    atoms = [l.split() for l in lines[2:2 + nat]]
+    with open(os.path.join(o, "3-21G.xml")) as f:
+        basis_xml = f.read()
+    # the test's literals: BSE singlet energies, transition dipoles and oscillator strengths for
+    # homo = 3 (setNumberOfOccupiedLevels(4)), BSE levels 0..16, TDA
+    omega = np.array([0.107455, 0.107455, 0.107455])
+    dipoles_ref = np.array([[0.110512, 0.048776, -0.0515914],
+                            [-0.13408, 0.0969472, 0.0261392],
+                            [0.0586073, 0.121606, -0.0606862]])
+    oscs_ref = np.array([0.001236, 0.00201008, 0.00156925])
+    np.savez(os.path.join(here, "orbitals_osc.npz"),
+             basis_xml=basis_xml, elements=np.array([t[0] for t in atoms]),
+             xyz=np.array([[float(x) for x in t[1:4]] for t in atoms]),
+             MOs=read_mm_array(os.path.join(o, "MOs3.mm")),
+             spsi=read_mm_array(os.path.join(o, "spsi_ref2.mm")),
+             omega=omega, dipoles_ref=dipoles_ref, oscs_ref=oscs_ref,
+             dip_ref=np.array([read_mm_array(os.path.join(a, f"dip_ref{i}.mm")) for i in range(3)]),
+             dip_ref_nonzero=np.array([read_mm_array(os.path.join(a, f"dip_ref{i}_nonzero.mm")) for i in range(3)]),
+             dip_center_nonzero=np.array([1.71, 2.34, 3.54]))
 
 
 if __name__ == "__main__":

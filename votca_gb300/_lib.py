@@ -90,6 +90,8 @@ SIGNATURES = {
     "bse_aux_pseudo_inv_sqrt": (c_i32, [c_i64, c_dp, c_i64, ctypes.c_double, c_dp, c_i64, ctypes.POINTER(c_i64)]),
     "bse_aux_pseudo_inv_sqrt_gwbse": (c_i32, [c_i64, c_dp, c_i64, c_dp, c_i64, ctypes.c_double, c_dp, c_i64,
                                               ctypes.POINTER(c_i64)]),
+    "bse_transition_dipoles": (c_i32, [c_dp, c_i64, c_dp, c_i64, c_i64, c_i64, c_i64, c_i64, c_i64, c_dp, c_dp,
+                                       c_i64, c_i64, ctypes.c_double, c_i32, c_dp]),
     "bse_op_profile": (c_i32, [c_vp, c_i32]),
     "bse_op_profile_read": (c_i32, [c_vp, c_dp, ctypes.POINTER(c_i64), c_i32]),
     "bse_probe_fp64_tflops": (c_i32, [c_dp]),

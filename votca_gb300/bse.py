@@ -12,6 +12,10 @@
   expectation_value_operator  BSE::ExpectationValue_Operator, bse.cc:500-520
   analyze_eh_interaction      BSE::Analyze_eh_interaction, bse.cc:551-606 (with
                               ExchangePrefactor, bse.cc:136-145)
+  transition_dipoles          Orbitals::CalcCoupledTransition_Dipoles, orbitals.cc:740-877
+                              (restricted singlets; transition_dipoles_uks for UKS excitons),
+                              with caller-supplied AO dipole matrices; on the GPU
+  oscillator_strengths        Orbitals::Oscillatorstrengths, orbitals.cc:645-673
 
 The Davidson iteration itself runs on the GPU (bse_davidson_solve).
 """
@@ -190,3 +194,77 @@ def exciton_weights(homo, vmin, cmax, X, Y=None, min_print_weight=0.5):
             rows.append((int(homo - v), int(c - homo - 1), float(w[i, k])))
         out.append(rows)
     return out
+
+
+def _transition_dipoles_block(ao_dipoles, mos, vmin, vtotal, cmin, ctotal, X, Y, prefactor, out, accumulate):
+    import ctypes
+
+    from . import _lib
+
+    L = _lib.load()
+    A = np.ascontiguousarray(ao_dipoles, dtype=np.float64)
+    C = np.asfortranarray(mos, dtype=np.float64)
+    Xf = np.asfortranarray(X, dtype=np.float64)
+    Yf = None if Y is None else np.asfortranarray(Y, dtype=np.float64)
+    nbf = C.shape[0]
+    if A.shape != (3, nbf, nbf):
+        raise ValueError("transition_dipoles: ao_dipoles must be (3, nbf, nbf) with nbf = mos.shape[0]")
+    if Xf.shape[0] < vtotal * ctotal or (Yf is not None and Yf.shape != Xf.shape):
+        raise ValueError("transition_dipoles: state vectors shorter than the BSE window")
+    # each (nbf x nbf) dipole matrix column-major, the three back to back
+    Af = np.ascontiguousarray(np.transpose(A, (0, 2, 1)))
+    p = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    _lib.check(L.bse_transition_dipoles(p(Af), nbf, p(C), nbf, C.shape[1], vmin, vtotal, cmin, ctotal, p(Xf),
+                                        None if Yf is None else p(Yf), Xf.shape[0], Xf.shape[1], prefactor,
+                                        1 if accumulate else 0, p(out)))
+
+
+def transition_dipoles(ao_dipoles, mos, homo, vmin, cmax, X, Y=None):
+    """Transition dipoles (nstates x 3) of restricted BSE singlets: the interlevel dipoles
+    C_c^T dip_i C_v (CalcFreeTransition_Dipoles, orbitals.cc:740-757) contracted with each
+    state's coefficients (X + Y for full BSE; the leading vtotal * ctotal entries of each column,
+    as Eigen::Map reads them) times -sqrt(2) (orbitals.cc:763-800).  ao_dipoles: (3, nbf, nbf)
+    AODipole matrices about the caller's origin; mos: (nbf, nmo) MO coefficients."""
+    X = np.asarray(X, dtype=np.float64)
+    if X.ndim == 1:
+        X = X[:, None]
+    vtotal, ctotal = homo - vmin + 1, cmax - homo
+    out = np.zeros(3 * X.shape[1])
+    _transition_dipoles_block(ao_dipoles, mos, vmin, vtotal, homo + 1, ctotal, X, Y, -np.sqrt(2.0), out, False)
+    return out.reshape(X.shape[1], 3)
+
+
+def transition_dipoles_uks(ao_dipoles, mos_alpha, mos_beta, homo_alpha, homo_beta, vmin, cmax, X, Y=None):
+    """Transition dipoles (nstates x 3) of combined UKS excitons (orbitals.cc:804-877): the
+    alpha block of each state with the alpha orbitals plus the beta block with the beta
+    orbitals, times -1 (no sqrt(2): both spin sectors are explicit)."""
+    X = np.asarray(X, dtype=np.float64)
+    if X.ndim == 1:
+        X = X[:, None]
+    va, ca = homo_alpha - vmin + 1, cmax - homo_alpha
+    vb, cb = homo_beta - vmin + 1, cmax - homo_beta
+    if X.shape[0] != va * ca + vb * cb:
+        raise ValueError("transition_dipoles_uks: exciton vector size does not match alpha+beta sector sizes")
+    na = va * ca
+    Ya = Yb = None
+    if Y is not None:
+        Y = np.asarray(Y, dtype=np.float64).reshape(X.shape)
+        Ya, Yb = Y[:na], Y[na:]
+    out = np.zeros(3 * X.shape[1])
+    first = True
+    for mos, v, c, homo, xs, ys in ((mos_alpha, va, ca, homo_alpha, X[:na], Ya),
+                                    (mos_beta, vb, cb, homo_beta, X[na:], Yb)):
+        if v * c == 0:
+            continue
+        _transition_dipoles_block(ao_dipoles, mos, vmin, v, homo + 1, c, xs, ys, -1.0, out, not first)
+        first = False
+    return out.reshape(X.shape[1], 3)
+
+
+def oscillator_strengths(omega, dipoles):
+    """f = 2/3 Omega |d|^2 per state (Orbitals::Oscillatorstrengths, orbitals.cc:661-673),
+    Omega in Hartree and d in e bohr."""
+    d = np.asarray(dipoles, dtype=np.float64)
+    n = min(len(d), len(omega))
+    return np.sum(d[:n] ** 2, axis=1) * 2.0 / 3.0 * np.asarray(omega, dtype=np.float64)[:n]
+

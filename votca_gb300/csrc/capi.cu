@@ -560,6 +560,18 @@ int bse_aux_pseudo_inv_sqrt_gwbse(int64_t n, const double *S, int64_t lds, const
   });
 }
 
+int bse_transition_dipoles(const double *ao_dipoles, int64_t nbf, const double *mo_coefficients, int64_t ldc,
+                           int64_t nmo, int64_t vmin, int64_t vtotal, int64_t cmin, int64_t ctotal,
+                           const double *X, const double *Y, int64_t ldx, int64_t nstates, double prefactor,
+                           int32_t accumulate, double *dipoles) {
+  return guarded([&] {
+    VGB_REQUIRE(ao_dipoles && mo_coefficients && X && dipoles, "bse_transition_dipoles: null argument");
+    TmpStream ts;
+    vgb::transition_dipoles(ao_dipoles, nbf, mo_coefficients, ldc, nmo, vmin, vtotal, cmin, ctotal, X, Y, ldx,
+                            nstates, prefactor, accumulate != 0, dipoles, ts.s);
+  });
+}
+
 int bse_davidson_solve_batch(bse_handle *const *handles, int64_t nhandles, const int32_t a_coef[4],
                              const int32_t b_coef[4], const bse_davidson_options *opt,
                              int64_t neigen, double *evals, int32_t *infos, int64_t *iterations,

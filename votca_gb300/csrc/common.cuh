@@ -109,6 +109,10 @@ void mmn_multiply_right(const bse_mmn_desc &desc, double *const *slices, const d
 // Mmn producer (threecenter.cu)
 void fill_3c_mo(const bse_mmn_desc &desc, double *const *slices, const double *ao3c, int64_t nbf,
                 const double *C, int64_t ldc, int64_t nmo, cudaStream_t s);
+void transition_dipoles(const double *ao_dip, int64_t nbf, const double *C, int64_t ldc, int64_t nmo,
+                        int64_t vmin, int64_t vtotal, int64_t cmin, int64_t ctotal, const double *X,
+                        const double *Y, int64_t ldx, int64_t nstates, double prefactor, bool accumulate,
+                        double *dip, cudaStream_t s);
 void aux_pseudo_inv_sqrt(int64_t n, const double *V, int64_t ldv, double etol, double *out, int64_t ldo,
                          int64_t *removed, cudaStream_t s);
 void aux_pseudo_inv_sqrt_gwbse(int64_t n, const double *S, int64_t lds, const double *V, int64_t ldv,

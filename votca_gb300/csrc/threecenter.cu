@@ -9,6 +9,10 @@
 //                         AOCoulomb::Pseudo_InvSqrt_GWBSE (aomatrix.cc:53-86): the metric the
 //                         GW-BSE Mmn is multiplied with, (V'^-1/2 S^-1/2)^T with
 //                         V' = S^-1/2 V S^-1/2, both inverse roots over eigenvalues >= etol.
+//   transition_dipoles    Orbitals::CalcCoupledTransition_Dipoles (xtp/src/libxtp/orbitals.cc:
+//                         740-877): the AO dipole matrices (caller-supplied, like the 3c
+//                         integrals) in the MO basis of one spin block, contracted with the
+//                         BSE states.
 // The two eigenproblems are solved on the host, as the reference does (Eigen's
 // SelfAdjointEigenSolver); the matrix products run on the device.
 #include <cmath>
@@ -164,6 +168,65 @@ void fill_3c_mo(const bse_mmn_desc &desc, double *const *slices, const double *a
                                cudaMemcpyDeviceToHost, s));
     VGB_CUDA(cudaStreamSynchronize(s));  // A, T and R are reused by the next chunk
   }
+}
+
+// Transition dipoles of BSE states from one spin block (Orbitals::CalcFreeTransition_Dipoles
+// and CalcCoupledTransition_Dipoles, xtp/src/libxtp/orbitals.cc:740-800 and 804-877): the
+// interlevel dipoles D_i = C_c^T dip_i C_v (ctotal x vtotal, i = x, y, z) as two GEMMs per
+// component, then d(i, s) = prefactor sum_{v,c} (X + Y)(v ctotal + c, s) D_i(c, v) as one GEMM
+// of the flattened D (dim x 3, the pair index of the eigenvectors) with the states.
+void transition_dipoles(const double *ao_dip, int64_t nbf, const double *C, int64_t ldc, int64_t nmo,
+                        int64_t vmin, int64_t vtotal, int64_t cmin, int64_t ctotal, const double *X,
+                        const double *Y, int64_t ldx, int64_t nstates, double prefactor, bool accumulate,
+                        double *dip, cudaStream_t s) {
+  VGB_REQUIRE(ao_dip && C && X && dip, "transition_dipoles: null input");
+  VGB_REQUIRE(nbf >= 1 && ldc >= nbf && vtotal >= 0 && ctotal >= 0 && nstates >= 0, "transition_dipoles: bad sizes");
+  VGB_REQUIRE(vmin >= 0 && cmin >= 0 && vmin + vtotal <= nmo && cmin + ctotal <= nmo,
+              "transition_dipoles: BSE window outside the orbital coefficients");
+  const int64_t dim = vtotal * ctotal;
+  VGB_REQUIRE(ldx >= dim, "transition_dipoles: leading dimension of the states too small");
+  std::vector<double> out(3 * (size_t)nstates, 0.0);
+  if (dim > 0 && nstates > 0) {
+    DeviceBuffer<double> A(3 * nbf * nbf), Cv(nbf * vtotal), Cc(nbf * ctotal), T(nbf * vtotal),
+        D(dim * 3), Xd(dim * nstates), R(3 * nstates);
+    VGB_CUDA(cudaMemcpyAsync(A.get(), ao_dip, 3 * nbf * nbf * sizeof(double), cudaMemcpyHostToDevice, s));
+    VGB_CUDA(cudaMemcpy2DAsync(Cv.get(), nbf * sizeof(double), C + ldc * vmin, ldc * sizeof(double),
+                               nbf * sizeof(double), vtotal, cudaMemcpyHostToDevice, s));
+    VGB_CUDA(cudaMemcpy2DAsync(Cc.get(), nbf * sizeof(double), C + ldc * cmin, ldc * sizeof(double),
+                               nbf * sizeof(double), ctotal, cudaMemcpyHostToDevice, s));
+    VGB_CUDA(cudaMemcpy2DAsync(Xd.get(), dim * sizeof(double), X, ldx * sizeof(double), dim * sizeof(double),
+                               nstates, cudaMemcpyHostToDevice, s));
+    GemmWorkspace ws;
+    for (int i = 0; i < 3; ++i) {
+      GemmDesc g;  // T (nbf x vtotal) = dip_i C_v
+      g.M = nbf; g.N = vtotal; g.K = nbf;
+      g.A = A.get() + i * nbf * nbf; g.a_rs = 1; g.a_cs = nbf;
+      g.B = Cv.get(); g.b_rs = 1; g.b_cs = nbf;
+      g.C = T.get(); g.c_rs = 1; g.c_cs = nbf;
+      dgemm(g, s, &ws);
+      GemmDesc h;  // D_i (ctotal x vtotal, column-major: the pair index c + ctotal v) = C_c^T T
+      h.M = ctotal; h.N = vtotal; h.K = nbf;
+      h.A = Cc.get(); h.a_rs = nbf; h.a_cs = 1;
+      h.B = T.get(); h.b_rs = 1; h.b_cs = nbf;
+      h.C = D.get() + i * dim; h.c_rs = 1; h.c_cs = ctotal;
+      dgemm(h, s, &ws);
+    }
+    for (int pass = 0; pass < (Y ? 2 : 1); ++pass) {
+      if (pass == 1)  // the full-BSE states enter as X + Y (orbitals.cc:780-782)
+        VGB_CUDA(cudaMemcpy2DAsync(Xd.get(), dim * sizeof(double), Y, ldx * sizeof(double), dim * sizeof(double),
+                                   nstates, cudaMemcpyHostToDevice, s));
+      GemmDesc r;  // R (3 x nstates) += prefactor D^T (X or Y)
+      r.M = 3; r.N = nstates; r.K = dim;
+      r.A = D.get(); r.a_rs = dim; r.a_cs = 1;
+      r.B = Xd.get(); r.b_rs = 1; r.b_cs = dim;
+      r.C = R.get(); r.c_rs = 1; r.c_cs = 3;
+      r.alpha = prefactor; r.beta = pass == 0 ? 0.0 : 1.0;
+      dgemm(r, s, &ws);
+    }
+    VGB_CUDA(cudaMemcpyAsync(out.data(), R.get(), 3 * nstates * sizeof(double), cudaMemcpyDeviceToHost, s));
+    VGB_CUDA(cudaStreamSynchronize(s));
+  }
+  for (int64_t t = 0; t < 3 * nstates; ++t) dip[t] = accumulate ? dip[t] + out[t] : out[t];
 }
 
 }  // namespace vgb
