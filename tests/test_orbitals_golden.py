@@ -47,3 +47,22 @@ def test_transition_dipoles_and_oscillator_strengths_match_golden():
     # the same with the golden AO matrices in place of the oracle's integrals
     td_g = transition_dipoles(g["dip_ref"], g["MOs"], 0, 4, 4, 13, g["spsi"])
     assert np.abs(td_g - td).max() < 2e-5
+
+
+def test_host_side_of_the_dipole_api():
+    """The host arithmetic and argument checks of votca_gb300.bse (no device work): oscillator
+    strengths as the oracle's, and shape errors raised before the library is called."""
+    import pytest
+
+    from votca_gb300.bse import oscillator_strengths as osc, transition_dipoles, transition_dipoles_uks
+
+    d = np.random.default_rng(2).standard_normal((4, 3))
+    om = np.array([0.3, 0.2, 0.4, 0.5])
+    assert np.allclose(osc(om, d), oscillator_strengths(om, d), rtol=1e-15)
+    assert osc(om[:2], d).shape == (2,)  # the shorter of states and energies, as the reference
+    with pytest.raises(ValueError):  # dipole matrices not (3, nbf, nbf)
+        transition_dipoles(np.zeros((3, 4, 5)), np.eye(5), 1, 0, 4, np.zeros((6, 1)))
+    with pytest.raises(ValueError):  # states shorter than the window's pairs
+        transition_dipoles(np.zeros((3, 5, 5)), np.eye(5), 1, 0, 4, np.zeros((5, 1)))
+    with pytest.raises(ValueError):  # UKS vector size does not match the two sectors
+        transition_dipoles_uks(np.zeros((3, 5, 5)), np.eye(5), np.eye(5), 1, 0, 0, 4, np.zeros((7, 1)))
