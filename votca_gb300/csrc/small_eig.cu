@@ -146,16 +146,21 @@ __global__ void __launch_bounds__(kEigThreads, 2) sym_eig_kernel(const __grid_co
   double *d = sm, *e = d + m, *tau = e + m, *vv = tau + m, *pp = vv + m, *red = pp + m;
   float *d32 = reinterpret_cast<float *>(red + 32), *e2 = d32 + m, *lam32 = e2 + m;
   int *cl = reinterpret_cast<int *>(lam32 + m);
-  const bool a_sm = nvec + ld * m <= g.smem_doubles;
-  double *A = a_sm ? sm + nvec : q.work;
-  // The eigenvectors of the tridiagonal and the LU factors of their inverse iterations (6 m per
-  // wanted eigenvalue) in shared memory when they fit behind A: the inverse iteration and the
-  // back-transformation are serial chains over m, and each step through global memory waits for
-  // an L2 round trip (the vectors are copied to U at the end).
-  const bool z_sm = a_sm && nvec + ld * m + 6 * m * nw <= g.smem_doubles;
-  double *Z = z_sm ? sm + nvec + ld * m : q.U;
+  // Shared memory behind the vectors, in this order while it lasts: the lower triangle A, the
+  // eigenvectors of the tridiagonal (m per wanted eigenvalue), the LU factors of their inverse
+  // iterations (5 m per wanted eigenvalue); the rest in global scratch.  The inverse iteration
+  // and the back-transformation are serial chains over m, and each step through global memory
+  // waits for an L2 round trip (the vectors are copied to U at the end).
+  int64_t off = nvec;
+  const bool a_sm = off + ld * m <= g.smem_doubles;
+  double *A = a_sm ? sm + off : q.work;
+  if (a_sm) off += ld * m;
+  const bool z_sm = off + m * nw <= g.smem_doubles;
+  double *Z = z_sm ? sm + off : q.U;
   const int64_t ldz = z_sm ? m : q.ldu;
-  double *scratch = z_sm ? Z + m * nw : q.work + ld * m;  // 5 m per wanted eigenvalue
+  if (z_sm) off += m * nw;
+  const bool lu_sm = z_sm && off + 5 * m * nw <= g.smem_doubles;
+  double *scratch = lu_sm ? sm + off : q.work + ld * m;  // 5 m per wanted eigenvalue
 
   if (tid == 0 && q.clocks) q.clocks[0] = clock64();
   // ---- load the lower triangle ----
@@ -392,17 +397,51 @@ __global__ void __launch_bounds__(kEigThreads, 2) sym_eig_kernel(const __grid_co
   __syncthreads();
   if (tid == 0 && q.clocks) q.clocks[3] = clock64();
 
-  // ---- 4. back-transformation U = H_0 H_1 ... H_{m-3} Z, one warp per eigenvector ----
-  for (int64_t j = warp; j < nw; j += kEigWarps) {
-    double *z = Z + ldz * j;
-    for (int64_t k = m - 3; k >= 0; --k) {
-      const double tk = tau[k];
-      if (tk == 0.0) continue;
-      double s = 0.0;
-      for (int64_t i = k + 1 + lane; i < m; i += 32) s = fma(i == k + 1 ? 1.0 : A[i + ld * k], z[i], s);
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      const double f = tk * s;
-      for (int64_t i = k + 1 + lane; i < m; i += 32) z[i] = fma(-f, i == k + 1 ? 1.0 : A[i + ld * k], z[i]);
+  // ---- 4. back-transformation U = H_0 H_1 ... H_{m-3} Z ----
+  // Up to one vector per warp: each warp applies the reflectors to its vector (a warp reduction
+  // per reflector).  More vectors: every reflector is applied to a batch of vectors at once, G
+  // threads per vector (all threads busy), each summing every G-th row of the dot product; the
+  // G partial sums of a vector are added in a fixed order by each of its threads (no FP64
+  // shuffle tree: on GB300's narrow FP64 pipe the five butterfly levels of a warp reduction,
+  // repeated for every vector of every warp, cost more than the dot products themselves).
+  if (nw <= kEigWarps) {
+    for (int64_t j = warp; j < nw; j += kEigWarps) {
+      double *z = Z + ldz * j;
+      for (int64_t k = m - 3; k >= 0; --k) {
+        const double tk = tau[k];
+        if (tk == 0.0) continue;
+        double s = 0.0;
+        for (int64_t i = k + 1 + lane; i < m; i += 32) s = fma(i == k + 1 ? 1.0 : A[i + ld * k], z[i], s);
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        const double f = tk * s;
+        for (int64_t i = k + 1 + lane; i < m; i += 32) z[i] = fma(-f, i == k + 1 ? 1.0 : A[i + ld * k], z[i]);
+      }
+    }
+  } else {
+    __shared__ double part[kEigThreads];
+    const int G = (int)std::min<int64_t>(32, std::max<int64_t>(1, kEigThreads / nw));
+    const int per_batch = kEigThreads / G;
+    const int slot = tid / G, sub = tid % G;
+    for (int64_t j0 = 0; j0 < nw; j0 += per_batch) {
+      const int64_t j = j0 + slot;
+      const bool act = slot < per_batch && j < nw;
+      double *z = act ? Z + ldz * j : nullptr;
+      for (int64_t k = m - 3; k >= 0; --k) {
+        const double tk = tau[k];
+        if (tk == 0.0) continue;  // uniform over the block
+        double s = 0.0;
+        if (act)
+          for (int64_t i = k + 1 + sub; i < m; i += G) s = fma(i == k + 1 ? 1.0 : A[i + ld * k], z[i], s);
+        part[tid] = s;
+        __syncthreads();
+        if (act) {
+          double t = 0.0;
+          for (int p = 0; p < G; ++p) t += part[slot * G + p];
+          const double f = tk * t;
+          for (int64_t i = k + 1 + sub; i < m; i += G) z[i] = fma(-f, i == k + 1 ? 1.0 : A[i + ld * k], z[i]);
+        }
+        __syncthreads();  // part is written again for the next reflector
+      }
     }
   }
   __syncthreads();
@@ -445,9 +484,15 @@ void sym_eig_device(const SymEigJob *jobs, int64_t njobs, cudaStream_t s) {
                       jb.ldt >= jb.m && jb.work != nullptr,
                   "small symmetric eigenproblem: invalid job");
       g->j[i] = jb;
-      const int64_t full = eig_vec_doubles(jb.m) + eig_ld(jb.m) * jb.m;
-      const int64_t with_z = full + 6 * jb.m * jb.nw;  // also the vectors of the inverse iteration
-      need = std::max(need, with_z <= limit ? with_z : full <= limit ? full : eig_vec_doubles(jb.m));
+      // the vectors, then A, the inverse-iteration vectors and their LU factors while they fit
+      // (the kernel places them in the same order)
+      int64_t job_need = eig_vec_doubles(jb.m);
+      if (job_need + eig_ld(jb.m) * jb.m <= limit) job_need += eig_ld(jb.m) * jb.m;
+      if (job_need + jb.m * jb.nw <= limit) {
+        job_need += jb.m * jb.nw;
+        if (job_need + 5 * jb.m * jb.nw <= limit) job_need += 5 * jb.m * jb.nw;
+      }
+      need = std::max(need, job_need);
     }
     g->smem_doubles = need;
     sym_eig_kernel<<<g->n, kEigThreads, need * sizeof(double), s>>>(*g);
